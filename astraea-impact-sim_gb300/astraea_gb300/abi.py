@@ -1,0 +1,146 @@
+"""ctypes view of the C-ABI in include/astraea_gb300.h.
+
+The two descriptor structs mirror the engine's ParticleBuffersDevice
+(engine/types.hpp:114-161) and RadixBvhDevice (engine/sph_gravity.cuh:26-59)
+member for member; FIELDS lists the 56 particle arrays in struct order with
+their element types.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PACKAGE_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PACKAGE_DIR, "libastraea_gb300.so")
+
+# (name, numpy dtype) in ParticleBuffersDevice order.
+_F32 = np.float32
+FIELDS = [
+    ("posX", _F32), ("posY", _F32), ("posZ", _F32),
+    ("velX", _F32), ("velY", _F32), ("velZ", _F32),
+    ("velHalfX", _F32), ("velHalfY", _F32), ("velHalfZ", _F32),
+    ("accX", _F32), ("accY", _F32), ("accZ", _F32),
+    ("mass", _F32), ("h", _F32), ("h0", _F32), ("rho", _F32), ("drhoDt", _F32),
+    ("pressure", _F32), ("soundSpeed", _F32), ("u", _F32), ("duDt", _F32), ("tempK", _F32),
+    ("radPowerW", _F32),
+    ("sXX", _F32), ("sYY", _F32), ("sZZ", _F32), ("sXY", _F32), ("sXZ", _F32), ("sYZ", _F32),
+    ("dSXX", _F32), ("dSYY", _F32), ("dSZZ", _F32), ("dSXY", _F32), ("dSXZ", _F32), ("dSYZ", _F32),
+    ("damage", _F32), ("damageCbrt", _F32), ("dDamageCbrtDt", _F32), ("epsFail", _F32),
+    ("divV", _F32), ("curlVX", _F32), ("curlVY", _F32), ("curlVZ", _F32),
+    ("shepardC", _F32), ("surfFactor", _F32), ("phiGrav", _F32),
+    ("materialId", np.uint8), ("phaseId", np.uint8), ("bodyId", np.uint8),
+    ("originalId", np.uint32), ("tracerIndex", np.int32),
+    ("tracerRestRadiusPsu", _F32), ("tracerRestNormalX", _F32), ("tracerRestNormalY", _F32),
+    ("tracerRestNormalZ", _F32), ("tracerIsOcean", np.uint8),
+]
+FIELD_NAMES = [f for f, _ in FIELDS]
+FIELD_DTYPES = dict(FIELDS)
+assert len(FIELDS) == 56
+
+
+class Particles(ctypes.Structure):
+    _fields_ = [("capacity", ctypes.c_uint32), ("count", ctypes.c_uint32)] + [
+        (name, ctypes.c_void_p) for name, _ in FIELDS
+    ]
+
+
+BVH_POINTERS = [
+    "mortonCodes", "mortonCodesSorted", "indicesIn", "indicesSorted",
+    "leftChild", "rightChild", "parent", "atomicVisited",
+    "aabbMinX", "aabbMinY", "aabbMinZ", "aabbMaxX", "aabbMaxY", "aabbMaxZ",
+    "nodeMass", "comX", "comY", "comZ", "nodeMaxH",
+]
+
+
+class RadixBvh(ctypes.Structure):
+    _fields_ = (
+        [("capacity", ctypes.c_uint32)]
+        + [(name, ctypes.c_void_p) for name in BVH_POINTERS]
+        + [("cubTempStorage", ctypes.c_void_p), ("cubTempBytes", ctypes.c_size_t),
+           ("sceneBoundsOrdered", ctypes.c_void_p), ("sceneBoundsFloat", ctypes.c_void_p),
+           ("livingFlags", ctypes.c_void_p), ("nodeComMass", ctypes.c_void_p),
+           ("nodeMinExtent", ctypes.c_void_p), ("nodeMaxHPacked", ctypes.c_void_p)]
+    )
+
+
+assert ctypes.sizeof(Particles) == 8 + 56 * 8
+assert ctypes.sizeof(RadixBvh) == 8 + 19 * 8 + 8 + 8 + 6 * 8
+
+STATUS_NAMES = {0: "OK", 1: "CUDA", 2: "CAPACITY", 3: "INVALID", 4: "DEVICE_TIMEOUT", 5: "DEVICE_STATE"}
+
+DEVFLAG_LOOKBACK_TIMEOUT = 0x1
+DEVFLAG_NEIGHBOR_OVERFLOW = 0x2
+DEVFLAG_STACK_OVERFLOW = 0x4
+
+COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "pass2_pairs",
+            "pass1_pairs", "fallback_walks", "lookback_spins", "reserved"]
+
+# (symbol, argtypes) of every exported entry point, in header order.
+_P = ctypes.POINTER(Particles)
+_B = ctypes.POINTER(RadixBvh)
+_U32 = ctypes.c_uint32
+_F = ctypes.c_float
+_VP = ctypes.c_void_p
+SIGNATURES = [
+    ("astraea_gb300_last_error", [], ctypes.c_char_p),
+    ("astraea_gb300_abi_version", [], ctypes.c_int),
+    ("astraea_gb300_set_stream", [_VP], ctypes.c_int),
+    ("astraea_gb300_allocate_radix_bvh", [_B, _U32], ctypes.c_int),
+    ("astraea_gb300_free_radix_bvh", [_B], ctypes.c_int),
+    ("astraea_gb300_allocate_particle_buffers", [_P, _U32], ctypes.c_int),
+    ("astraea_gb300_free_particle_buffers", [_P], ctypes.c_int),
+    ("astraea_gb300_clear_stats", [_P], ctypes.c_int),
+    ("astraea_gb300_sort_and_build_bvh", [_P, _P, _B], ctypes.c_int),
+    ("astraea_gb300_sph_pass1_neighbors", [_P, _B], ctypes.c_int),
+    ("astraea_gb300_evaluate_eos", [_P], ctypes.c_int),
+    ("astraea_gb300_gravity_barnes_hut", [_P, _B, _F], ctypes.c_int),
+    ("astraea_gb300_sph_pass2_forces", [_P, _B], ctypes.c_int),
+    ("astraea_gb300_leapfrog_kick_half", [_P, _F, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    ("astraea_gb300_leapfrog_drift", [_P, _F, _B], ctypes.c_int),
+    ("astraea_gb300_reduce_dt_psu", [_P, _F, _F, ctypes.POINTER(_F)], ctypes.c_int),
+    ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
+    ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
+    ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),
+    ("astraea_gb300_release_scratch", [_B], ctypes.c_int),
+    ("astraea_gb300_radix_sort_pairs", [_VP, _VP, _VP, _VP, _U32, ctypes.c_int], ctypes.c_int),
+    ("astraea_gb300_read_device_status", [ctypes.POINTER(_U32), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    ("astraea_gb300_reset_device_status", [], ctypes.c_int),
+    ("astraea_gb300_set_lookback_spin_limit", [_U32], ctypes.c_int),
+    ("astraea_gb300_debug_lookback_probe", [_U32, ctypes.POINTER(_U32)], ctypes.c_int),
+]
+EXPORTED_SYMBOLS = [name for name, _, _ in SIGNATURES]
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libastraea_gb300.so (built by build_lib.py); raises when absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libastraea_gb300.so not built (%s); run __graft_entry__.build()" % p)
+    lib = ctypes.CDLL(p)
+    for name, args, res in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if lib.astraea_gb300_abi_version() != 1:
+        raise RuntimeError("ABI version mismatch")
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class AstraeaError(RuntimeError):
+    """Raised for a non-zero AstraeaStatus (the engine throws std::runtime_error)."""
+
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+def check(status):
+    if status != 0:
+        raise AstraeaError(status, load_library().astraea_gb300_last_error().decode(errors="replace"))

@@ -1,0 +1,311 @@
+"""Host-side mirror of the ASTRAEA kernel interface over the CUDA C-ABI.
+
+The functions below have the names, argument meaning and error behaviour of
+astraea::cuda::* in engine/sph_gravity.cuh:61-92 (launchSortAndBuildBvh ->
+sort_and_build_bvh, ...): they enqueue work on the CUDA stream and raise
+AstraeaError where the engine throws std::runtime_error.  Device memory is
+held in torch tensors (one per SoA field), passed to the library as the
+C descriptors of include/astraea_gb300.h.  Every call goes to
+libastraea_gb300.so; there is no other implementation behind them.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import abi
+
+_TORCH_DTYPES = {np.float32: torch.float32, np.uint8: torch.uint8, np.uint32: torch.int32, np.int32: torch.int32}
+
+
+def _torch_dtype(np_dtype):
+    return _TORCH_DTYPES[np_dtype]
+
+
+def lib():
+    return abi.load_library()
+
+
+class DeviceParticles:
+    """ParticleBuffersDevice in torch tensors (engine/types.hpp:114-161)."""
+
+    def __init__(self, capacity, device="cuda"):
+        self.capacity = int(capacity)
+        self.count = 0
+        self.device = torch.device(device)
+        self.arrays = {
+            name: torch.zeros(max(self.capacity, 1), dtype=_torch_dtype(dt), device=self.device)
+            for name, dt in abi.FIELDS
+        }
+        self.arrays["tracerIndex"].fill_(-1)
+
+    def struct(self):
+        s = abi.Particles()
+        s.capacity = self.capacity
+        s.count = self.count
+        for name in abi.FIELD_NAMES:
+            setattr(s, name, self.arrays[name].data_ptr())
+        return s
+
+    def upload(self, host, count=None):
+        """Copy host arrays (dict name -> numpy) into the first `count` slots."""
+        n = int(count if count is not None else len(host["posX"]))
+        if n > self.capacity:
+            raise abi.AstraeaError(2, "upload: count %d > capacity %d" % (n, self.capacity))
+        self.count = n
+        for name, dt in abi.FIELDS:
+            if name in host:
+                a = np.ascontiguousarray(host[name][:n]).astype(dt, copy=False)
+                if dt == np.uint32:
+                    a = a.view(np.int32)
+                self.arrays[name][:n].copy_(torch.from_numpy(a))
+
+    def download(self, fields=None):
+        out = {}
+        n = self.count
+        for name in fields or abi.FIELD_NAMES:
+            t = self.arrays[name][:n].cpu().numpy()
+            if abi.FIELD_DTYPES[name] == np.uint32:
+                t = t.view(np.uint32)
+            out[name] = t
+        return out
+
+
+def _rebind_after_swap(p, alt, sp, salt):
+    """Follow the pointer swap the library made in the structs."""
+    by_ptr = {}
+    for dp in (p, alt):
+        for name, t in dp.arrays.items():
+            by_ptr[t.data_ptr()] = t
+    for dp, s in ((p, sp), (alt, salt)):
+        for name in abi.FIELD_NAMES:
+            dp.arrays[name] = by_ptr[getattr(s, name)]
+        dp.count = s.count
+
+
+class DeviceBvh:
+    """RadixBvhDevice allocated by the library (allocateRadixBvh)."""
+
+    def __init__(self, capacity):
+        self.s = abi.RadixBvh()
+        abi.check(lib().astraea_gb300_allocate_radix_bvh(ctypes.byref(self.s), int(capacity)))
+
+    @property
+    def capacity(self):
+        return self.s.capacity
+
+    def free(self):
+        if self.s.capacity:
+            abi.check(lib().astraea_gb300_free_radix_bvh(ctypes.byref(self.s)))
+
+    def __del__(self):
+        try:
+            if self.s.capacity and abi._lib is not None:
+                abi._lib.astraea_gb300_free_radix_bvh(ctypes.byref(self.s))
+        except Exception:
+            pass
+
+
+
+class TorchBvh:
+    """RadixBvhDevice whose arrays are caller-owned torch tensors, the way
+    tests/cpp/test_gravity_sph.cpp:178-236 builds one with raw cudaMalloc.
+    packed=False leaves the packed node arrays and the scene scratch NULL,
+    like that test (the library then uses its own scratch)."""
+
+    def __init__(self, capacity, packed=True):
+        n = int(capacity)
+        nodes = 2 * n
+        dev = "cuda"
+        z = lambda k, dt: torch.zeros(max(k, 1), dtype=dt, device=dev)
+        self.t = {
+            "mortonCodes": z(n, torch.int64), "mortonCodesSorted": z(n, torch.int64),
+            "indicesIn": z(n, torch.int32), "indicesSorted": z(n, torch.int32),
+            "leftChild": z(n, torch.int32), "rightChild": z(n, torch.int32),
+            "parent": z(nodes, torch.int32), "atomicVisited": z(n, torch.int32),
+        }
+        for f in ("aabbMinX", "aabbMinY", "aabbMinZ", "aabbMaxX", "aabbMaxY", "aabbMaxZ", "nodeMass", "comX",
+                  "comY", "comZ", "nodeMaxH"):
+            self.t[f] = z(nodes, torch.float32)
+        if packed:
+            self.t["sceneBoundsOrdered"] = z(6, torch.int32)
+            self.t["sceneBoundsFloat"] = z(6, torch.float32)
+            self.t["livingFlags"] = z(2, torch.int32)
+            for f in ("nodeComMass", "nodeMinExtent", "nodeMaxHPacked"):
+                self.t[f] = z(4 * nodes, torch.float32)
+        self.s = abi.RadixBvh()
+        self.s.capacity = n
+        for name, t in self.t.items():
+            setattr(self.s, name, t.data_ptr())
+
+    @property
+    def capacity(self):
+        return self.s.capacity
+
+    def release(self):
+        if self.t:
+            abi.check(lib().astraea_gb300_release_scratch(ctypes.byref(self.s)))
+            self.t = {}
+
+    def __del__(self):
+        try:
+            if self.t and abi._lib is not None:
+                abi._lib.astraea_gb300_release_scratch(ctypes.byref(self.s))
+        except Exception:
+            pass
+
+
+# -------------------------------------------------------- engine entry points
+def clear_stats(p):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_clear_stats(ctypes.byref(s)))
+
+
+def sort_and_build_bvh(p, alt, bvh):
+    sp, salt = p.struct(), alt.struct()
+    abi.check(lib().astraea_gb300_sort_and_build_bvh(ctypes.byref(sp), ctypes.byref(salt), ctypes.byref(bvh.s)))
+    _rebind_after_swap(p, alt, sp, salt)
+
+
+def sph_pass1_neighbors(p, bvh):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_sph_pass1_neighbors(ctypes.byref(s), ctypes.byref(bvh.s)))
+
+
+def evaluate_eos(p):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_evaluate_eos(ctypes.byref(s)))
+
+
+def gravity_barnes_hut(p, bvh, theta=0.5):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_gravity_barnes_hut(ctypes.byref(s), ctypes.byref(bvh.s), float(theta)))
+
+
+def sph_pass2_forces(p, bvh):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_sph_pass2_forces(ctypes.byref(s), ctypes.byref(bvh.s)))
+
+
+def leapfrog_kick_half(p, half_dt, include_xsph=False, clamp_thermal=False):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_leapfrog_kick_half(ctypes.byref(s), float(half_dt), int(bool(include_xsph)),
+                                                     int(bool(clamp_thermal))))
+
+
+def leapfrog_drift(p, dt, bvh):
+    s = p.struct()
+    abi.check(lib().astraea_gb300_leapfrog_drift(ctypes.byref(s), float(dt), ctypes.byref(bvh.s) if bvh else None))
+
+
+def reduce_dt_psu(p, prev_dt, max_dt):
+    s = p.struct()
+    out = ctypes.c_float(0.0)
+    abi.check(lib().astraea_gb300_reduce_dt_psu(ctypes.byref(s), float(prev_dt), float(max_dt), ctypes.byref(out)))
+    return out.value
+
+
+def step(p, alt, bvh, prev_dt, max_dt, theta=0.5, out_dt_ptr=None):
+    """Fused Simulation::step kernel sequence; returns without a sync."""
+    sp, salt = p.struct(), alt.struct()
+    abi.check(lib().astraea_gb300_step(ctypes.byref(sp), ctypes.byref(salt), ctypes.byref(bvh.s), float(prev_dt),
+                                       float(max_dt), float(theta), out_dt_ptr))
+    _rebind_after_swap(p, alt, sp, salt)
+
+
+def invalidate_step_cache(bvh):
+    abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
+
+
+def reserve(bvh, capacity):
+    abi.check(lib().astraea_gb300_reserve(ctypes.byref(bvh.s), int(capacity)))
+
+
+def radix_sort_pairs(keys, vals, end_bit=64):
+    """Stable sort of (int64 keys as unsigned, int32 values) torch tensors."""
+    n = keys.numel()
+    k_in, v_in = keys.clone(), vals.clone()
+    k_out, v_out = torch.empty_like(keys), torch.empty_like(vals)
+    abi.check(lib().astraea_gb300_radix_sort_pairs(k_in.data_ptr(), k_out.data_ptr(), v_in.data_ptr(),
+                                                   v_out.data_ptr(), n, int(end_bit)))
+    return k_out, v_out
+
+
+def read_device_status():
+    flags = ctypes.c_uint32(0)
+    counters = (ctypes.c_uint64 * 8)()
+    abi.check(lib().astraea_gb300_read_device_status(ctypes.byref(flags), counters))
+    return flags.value, dict(zip(abi.COUNTERS, list(counters)))
+
+
+def reset_device_status():
+    abi.check(lib().astraea_gb300_reset_device_status())
+
+
+def set_lookback_spin_limit(limit):
+    abi.check(lib().astraea_gb300_set_lookback_spin_limit(int(limit)))
+
+
+class Simulation:
+    """Device state + step driver, the part of engine/simulation.cpp that
+    drives the hot path: upload (uploadHostStateToDevice :468-523), initial
+    forces (evaluateInitialForcesOnDevice :525-536) and step() (:1711-1753)."""
+
+    def __init__(self, capacity):
+        self.p = DeviceParticles(capacity)
+        self.alt = DeviceParticles(capacity)
+        self.bvh = DeviceBvh(capacity)
+        self.prev_dt = 0.0
+        self.sim_time = 0.0
+        self._dt_host = torch.zeros(1, dtype=torch.float32).pin_memory()
+
+    def load_state(self, host):
+        self.p.upload(host)
+        self.alt.count = self.p.count
+        for f in ("velHalfX", "velHalfY", "velHalfZ"):
+            src = "vel" + f[-1]
+            self.p.arrays[f][: self.p.count].copy_(self.p.arrays[src][: self.p.count])
+        for f in ("pressure", "soundSpeed", "phaseId"):
+            self.p.arrays[f].zero_()
+        clear_stats(self.p)
+        self.prev_dt = 0.0
+        self.sim_time = 0.0
+
+    def evaluate_initial_forces(self, theta=0.5):
+        clear_stats(self.p)
+        sort_and_build_bvh(self.p, self.alt, self.bvh)
+        sph_pass1_neighbors(self.p, self.bvh)
+        evaluate_eos(self.p)
+        gravity_barnes_hut(self.p, self.bvh, theta)
+        sph_pass2_forces(self.p, self.bvh)
+        torch.cuda.synchronize()
+
+    def step_stagewise(self, max_dt, theta=0.5):
+        """The engine's step() as the sequence of stage entry points."""
+        dt = reduce_dt_psu(self.p, self.prev_dt, max_dt)
+        self.prev_dt = dt
+        leapfrog_kick_half(self.p, 0.5 * dt, True, False)
+        leapfrog_drift(self.p, dt, self.bvh)
+        sort_and_build_bvh(self.p, self.alt, self.bvh)
+        sph_pass1_neighbors(self.p, self.bvh)
+        evaluate_eos(self.p)
+        gravity_barnes_hut(self.p, self.bvh, theta)
+        sph_pass2_forces(self.p, self.bvh)
+        leapfrog_kick_half(self.p, 0.5 * dt, False, False)
+        evaluate_eos(self.p)
+        self.sim_time += dt
+        return dt
+
+    def step(self, max_dt, theta=0.5, sync=True):
+        """Fused step; dt stays on the device.  Returns dt when sync."""
+        step(self.p, self.alt, self.bvh, self.prev_dt, max_dt, theta, self._dt_host.data_ptr())
+        if sync:
+            torch.cuda.synchronize()
+            dt = float(self._dt_host[0])
+            self.prev_dt = dt
+            self.sim_time += dt
+            return dt
+        return None
+
+    def state(self, fields=None):
+        return self.p.download(fields)

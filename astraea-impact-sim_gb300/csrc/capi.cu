@@ -1,0 +1,680 @@
+// capi.cu -- the C-ABI of include/astraea_gb300.h: allocation, the stage
+// entry points that replace astraea::cuda::launch* (engine/sph_gravity.cu:
+// 1796-2161), the fused step, and library-owned scratch.
+//
+// Scratch ("workspace") lives with the BVH it serves: it is keyed by the
+// BVH's leftChild device pointer and created on the first build.  It holds
+// the packed leaf / node records the tree walks read, the neighbour lists,
+// the onesweep scratch and a few device words (bounds, living flags, dt).
+// Nothing is allocated per step; astraea_gb300_reserve allocates everything
+// ahead of time for callers that capture steps in a CUDA graph.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+
+#include "kernels.h"
+
+using namespace astraea_gb300;
+
+namespace {
+
+thread_local std::string g_lastError;
+std::atomic<cudaStream_t> g_stream{nullptr};
+std::atomic<uint32_t> g_spinLimit{1u << 22};
+std::mutex g_mutex;
+
+AstraeaStatus fail(AstraeaStatus s, const std::string& msg) {
+    g_lastError = msg;
+    return s;
+}
+
+#define AG_CUDA(expr)                                                                                     \
+    do {                                                                                                  \
+        const cudaError_t agErr = (expr);                                                                 \
+        if (agErr != cudaSuccess)                                                                         \
+            return fail(ASTRAEA_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(agErr));        \
+    } while (0)
+
+cudaStream_t stream() { return g_stream.load(); }
+
+int currentDevice() {
+    int d = 0;
+    cudaGetDevice(&d);
+    return d;
+}
+
+int smCount() {
+    static int cache[64] = {};
+    const int d = currentDevice();
+    if (d >= 0 && d < 64 && cache[d] > 0) return cache[d];
+    int s = 0;
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, d);
+    if (s <= 0) s = 1;
+    if (d >= 0 && d < 64) cache[d] = s;
+    return s;
+}
+
+// ------------------------------------------------------- per-device state
+struct DeviceState {
+    DevStatus* status = nullptr;   // device (flags, dt word, counters)
+    uint32_t* hostWord = nullptr;  // pinned, 4 words
+    uint32_t* zeroWords = nullptr; // device, 8 zero words (absent living flags)
+};
+std::map<int, DeviceState> g_devices;
+
+AstraeaStatus deviceState(DeviceState** out) {
+    const int d = currentDevice();
+    auto it = g_devices.find(d);
+    if (it == g_devices.end()) {
+        DeviceState s;
+        AG_CUDA(cudaMalloc(&s.status, sizeof(DevStatus)));
+        AG_CUDA(cudaMemset(s.status, 0, sizeof(DevStatus)));
+        AG_CUDA(cudaMallocHost(&s.hostWord, 4 * sizeof(uint32_t)));
+        AG_CUDA(cudaMalloc(&s.zeroWords, 8 * sizeof(uint32_t)));
+        AG_CUDA(cudaMemset(s.zeroWords, 0, 8 * sizeof(uint32_t)));
+        it = g_devices.emplace(d, s).first;
+    }
+    *out = &it->second;
+    return ASTRAEA_OK;
+}
+
+// ------------------------------------------------------------- workspace
+struct Workspace {
+    int device = 0;
+    Work w{};
+    uint32_t capacity = 0;
+    void* block = nullptr;         // one allocation for all arrays
+    float* dtSlots = nullptr;      // 2 floats (inside block)
+    uint32_t* rawMin = nullptr;    // 2 words (inside block)
+    bool treeBuilt = false;        // node records hold a tree built here
+    uint32_t builtN = 0;           // particle count of that tree
+    bool stepCacheValid = false;   // neighbour lists + device dt valid for the next fused step
+    const void* stepToken = nullptr;
+    uint32_t stepCount = 0;
+    int parity = 0;
+};
+std::map<std::pair<int, const void*>, Workspace*> g_work;
+
+uint32_t maxNeighbors() {
+    static uint32_t v = [] {
+        const char* e = std::getenv("ASTRAEA_GB300_MAX_NEIGHBORS");
+        long x = e ? std::strtol(e, nullptr, 10) : 192;
+        if (x < 32) x = 32;
+        if (x > 4096) x = 4096;
+        return static_cast<uint32_t>((x + 3) & ~3L);
+    }();
+    return v;
+}
+
+size_t alignUp(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    const size_t C = std::max<uint32_t>(capacity, 2u);
+    const uint32_t maxNbr = maxNeighbors();
+    uint32_t maxTiles = 0;
+    const size_t sortWords = sortScratchWords(static_cast<uint32_t>(C), &maxTiles);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { const size_t o = off; off += alignUp(bytes); return o; };
+    const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 80);
+    const size_t oNode = take(C * 64), oMom = take(C * 32), oDrift = take(C * 16);
+    const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
+    const size_t oSort = take(sortWords * 4), oDt = take(64);
+    void* block = nullptr;
+    AG_CUDA(cudaMalloc(&block, off));
+    char* b = static_cast<char*>(block);
+    if (ws->block) cudaFree(ws->block);
+    ws->block = block;
+    ws->capacity = static_cast<uint32_t>(C);
+    ws->device = currentDevice();
+    Work& w = ws->w;
+    w.capacity = static_cast<uint32_t>(C);
+    w.maxNbr = maxNbr;
+    w.leafPM = reinterpret_cast<float4*>(b + oPM);
+    w.leafAux = reinterpret_cast<float4*>(b + oAux);
+    w.velRho = reinterpret_cast<float4*>(b + oVR);
+    w.rec2 = reinterpret_cast<float4*>(b + oRec);
+    w.node = reinterpret_cast<float4*>(b + oNode);
+    w.nodeMom = reinterpret_cast<NodeMom*>(b + oMom);
+    w.driftPos = reinterpret_cast<float4*>(b + oDrift);
+    w.nbrCount = reinterpret_cast<uint32_t*>(b + oCnt);
+    w.nbrList = reinterpret_cast<uint32_t*>(b + oList);
+    w.words = reinterpret_cast<uint32_t*>(b + oWords);
+    w.sortScratch = reinterpret_cast<uint32_t*>(b + oSort);
+    w.sortScratchWords = sortWords;
+    w.sortMaxTiles = maxTiles;
+    w.status = ds->status;
+    ws->dtSlots = reinterpret_cast<float*>(b + oDt);
+    ws->rawMin = reinterpret_cast<uint32_t*>(b + oDt + 16);
+    AG_CUDA(cudaMemset(w.words, 0, kWCount * 4));
+    AG_CUDA(cudaMemset(b + oDt, 0, 64));
+    ws->treeBuilt = false;
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+// Workspace of a BVH; created (or grown) when `create`.
+AstraeaStatus workspaceFor(const AstraeaRadixBvh* bvh, uint32_t need, bool create, Workspace** out) {
+    if (bvh == nullptr || bvh->leftChild == nullptr) return fail(ASTRAEA_ERR_INVALID, "BVH descriptor has no leftChild array");
+    std::lock_guard<std::mutex> lock(g_mutex);
+    const auto key = std::make_pair(currentDevice(), static_cast<const void*>(bvh->leftChild));
+    auto it = g_work.find(key);
+    if (it == g_work.end()) {
+        if (!create) return fail(ASTRAEA_ERR_INVALID, "BVH was not built by astraea_gb300_sort_and_build_bvh");
+        Workspace* ws = new Workspace();
+        const AstraeaStatus s = allocWorkspace(ws, need);
+        if (s != ASTRAEA_OK) { delete ws; return s; }
+        it = g_work.emplace(key, ws).first;
+    } else if (it->second->capacity < need) {
+        if (!create) return fail(ASTRAEA_ERR_CAPACITY, "workspace smaller than particle count");
+        const AstraeaStatus s = allocWorkspace(it->second, need);
+        if (s != ASTRAEA_OK) return s;
+    }
+    *out = it->second;
+    return ASTRAEA_OK;
+}
+
+void dropWorkspace(const void* leftChild) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    for (auto it = g_work.begin(); it != g_work.end(); ++it) {
+        if (it->first.second == leftChild) {
+            cudaFree(it->second->block);
+            delete it->second;
+            g_work.erase(it);
+            return;
+        }
+    }
+}
+
+template <typename T>
+cudaError_t allocArr(T*& p, size_t count) {
+    p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+}
+template <typename T>
+void freeArr(T*& p) {
+    if (p) { cudaFree(p); p = nullptr; }
+}
+
+#define AG_ALL_PARTICLE_ARRAYS(X)                                                                          \
+    X(posX) X(posY) X(posZ) X(velX) X(velY) X(velZ) X(velHalfX) X(velHalfY) X(velHalfZ) X(accX) X(accY)     \
+        X(accZ) X(mass) X(h) X(h0) X(rho) X(drhoDt) X(pressure) X(soundSpeed) X(u) X(duDt) X(tempK)         \
+            X(radPowerW) X(sXX) X(sYY) X(sZZ) X(sXY) X(sXZ) X(sYZ) X(dSXX) X(dSYY) X(dSZZ) X(dSXY) X(dSXZ)   \
+                X(dSYZ) X(damage) X(damageCbrt) X(dDamageCbrtDt) X(epsFail) X(divV) X(curlVX) X(curlVY)     \
+                    X(curlVZ) X(shepardC) X(surfFactor) X(phiGrav) X(materialId) X(phaseId) X(bodyId)      \
+                        X(originalId) X(tracerIndex) X(tracerRestRadiusPsu) X(tracerRestNormalX)           \
+                            X(tracerRestNormalY) X(tracerRestNormalZ) X(tracerIsOcean)
+
+void swapParticlePointers(AstraeaParticles& a, AstraeaParticles& b) {   // sph_gravity.cu:1745-1784
+#define AG_SWAP(f) std::swap(a.f, b.f);
+    AG_ALL_PARTICLE_ARRAYS(AG_SWAP)
+#undef AG_SWAP
+}
+
+AstraeaStatus checkLaunch(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) return fail(ASTRAEA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return ASTRAEA_OK;
+}
+#define AG_LAUNCH(expr)                                              \
+    do {                                                             \
+        const AstraeaStatus agS = checkLaunch((expr), #expr);        \
+        if (agS != ASTRAEA_OK) return agS;                           \
+    } while (0)
+
+uint32_t* livingPtr(const AstraeaRadixBvh* bvh, Workspace* ws) {
+    return (bvh->livingFlags != nullptr) ? bvh->livingFlags : ws->w.words + kWLiving;
+}
+
+// Sort + permutation + Karras + refit shared by the stage call and the step.
+AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh, Workspace* ws,
+                        const float4* driftPos, bool allFields) {
+    const uint32_t n = p->count;
+    cudaStream_t st = stream();
+    Work& w = ws->w;
+    uint32_t* living = livingPtr(bvh, ws);
+    if (living != w.words + kWLiving) AG_CUDA(cudaMemsetAsync(living, 0, 2 * sizeof(uint32_t), st));
+    MortonSource ms{};
+    if (driftPos != nullptr) {
+        ms.xyz = driftPos;
+    } else {
+        ms.x = p->posX; ms.y = p->posY; ms.z = p->posZ;
+    }
+    ms.boundsOrdered = w.words + kWBounds;
+    ms.boundsFloatOut = bvh->sceneBoundsFloat;
+    bool inA = true;
+    // keys/values start in the *Sorted arrays; after an even number of passes
+    // the sorted pairs are back there.
+    AG_LAUNCH(radixSortPairs(bvh->mortonCodesSorted, bvh->indicesSorted, bvh->mortonCodes, bvh->indicesIn, n, 63,
+                             w.sortScratch, w.sortScratchWords, w.sortMaxTiles, w.status, g_spinLimit.load(),
+                             KeySource::MortonFromPositions, &ms, &inA, st));
+    if (!inA) {
+        AG_CUDA(cudaMemcpyAsync(bvh->mortonCodesSorted, bvh->mortonCodes, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        AG_CUDA(cudaMemcpyAsync(bvh->indicesSorted, bvh->indicesIn, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    }
+    if (bvh->sceneBoundsOrdered != nullptr)
+        AG_CUDA(cudaMemcpyAsync(bvh->sceneBoundsOrdered, w.words + kWBounds, 6 * sizeof(uint32_t),
+                                cudaMemcpyDeviceToDevice, st));
+    AG_LAUNCH(launchPermuteLeavesKarras(*p, *alt, *bvh, driftPos, w, n, living, allFields, st));
+    swapParticlePointers(*p, *alt);
+    alt->count = p->count;
+    AG_LAUNCH(launchRefit(*bvh, w, n, st));
+    ws->treeBuilt = true;
+    ws->builtN = n;
+    return ASTRAEA_OK;
+}
+
+// Workspace holding a tree built here for exactly n particles.
+AstraeaStatus builtWorkspace(const AstraeaRadixBvh* bvh, uint32_t n, Workspace** out) {
+    AstraeaStatus s = workspaceFor(bvh, n, false, out);
+    if (s != ASTRAEA_OK) return s;
+    if (!(*out)->treeBuilt || (*out)->builtN != n)
+        return fail(ASTRAEA_ERR_INVALID, "BVH holds no tree built by astraea_gb300_sort_and_build_bvh for this count");
+    return ASTRAEA_OK;
+}
+
+float hostClampDt(uint32_t bits, float prevDt, float maxDt) {   // sph_gravity.cu:2137-2160
+    const float floorDt = fminf(1.0e-5f, maxDt);
+    const float upper = (prevDt > 0.0f) ? fminf(prevDt * 1.15f, maxDt) : maxDt;
+    float raw = 0.0f;
+    std::memcpy(&raw, &bits, sizeof(float));
+    if (bits == 0x7f7f7f7fu || !std::isfinite(raw) || raw <= 0.0f) raw = upper;
+    return fminf(upper, fmaxf(floorDt, raw));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* astraea_gb300_last_error(void) { return g_lastError.c_str(); }
+int astraea_gb300_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
+
+AstraeaStatus astraea_gb300_set_stream(void* s) {
+    g_stream.store(static_cast<cudaStream_t>(s));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_set_lookback_spin_limit(uint32_t limit) {
+    g_spinLimit.store(limit == 0u ? (1u << 22) : limit);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_read_device_status(uint32_t* flags, uint64_t* counters8) {
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    DevStatus h{};
+    AG_CUDA(cudaStreamSynchronize(stream()));
+    AG_CUDA(cudaMemcpy(&h, ds->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    if (flags) *flags = h.flags;
+    if (counters8)
+        for (int k = 0; k < kCntCount; ++k) counters8[k] = h.counters[k];
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_reset_device_status(void) {
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    AG_CUDA(cudaMemsetAsync(ds->status, 0, sizeof(DevStatus), stream()));
+    return ASTRAEA_OK;
+}
+
+// ------------------------------------------------------------ allocation
+AstraeaStatus astraea_gb300_allocate_radix_bvh(AstraeaRadixBvh* bvh, uint32_t capacity) {
+    if (bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null BVH");
+    AstraeaStatus s = astraea_gb300_free_radix_bvh(bvh);
+    if (s != ASTRAEA_OK) return s;
+    if (capacity == 0u) return ASTRAEA_OK;
+    const size_t nodes = 2u * static_cast<size_t>(capacity) - 1u;       // sph_gravity.cu:1812-1842
+    const size_t internal = (capacity > 1u) ? static_cast<size_t>(capacity - 1u) : 1u;
+    AG_CUDA(allocArr(bvh->mortonCodes, capacity));
+    AG_CUDA(allocArr(bvh->mortonCodesSorted, capacity));
+    AG_CUDA(allocArr(bvh->indicesIn, capacity));
+    AG_CUDA(allocArr(bvh->indicesSorted, capacity));
+    AG_CUDA(allocArr(bvh->leftChild, internal));
+    AG_CUDA(allocArr(bvh->rightChild, internal));
+    AG_CUDA(allocArr(bvh->parent, nodes));
+    AG_CUDA(allocArr(bvh->atomicVisited, internal));
+    AG_CUDA(allocArr(bvh->aabbMinX, nodes)); AG_CUDA(allocArr(bvh->aabbMinY, nodes)); AG_CUDA(allocArr(bvh->aabbMinZ, nodes));
+    AG_CUDA(allocArr(bvh->aabbMaxX, nodes)); AG_CUDA(allocArr(bvh->aabbMaxY, nodes)); AG_CUDA(allocArr(bvh->aabbMaxZ, nodes));
+    AG_CUDA(allocArr(bvh->nodeMass, nodes));
+    AG_CUDA(allocArr(bvh->comX, nodes)); AG_CUDA(allocArr(bvh->comY, nodes)); AG_CUDA(allocArr(bvh->comZ, nodes));
+    AG_CUDA(allocArr(bvh->nodeMaxH, nodes));
+    AG_CUDA(allocArr(bvh->sceneBoundsOrdered, 6));
+    AG_CUDA(allocArr(bvh->sceneBoundsFloat, 6));
+    AG_CUDA(allocArr(bvh->livingFlags, 2));
+    AG_CUDA(allocArr(bvh->nodeComMass, nodes));
+    AG_CUDA(allocArr(bvh->nodeMinExtent, nodes));
+    AG_CUDA(allocArr(bvh->nodeMaxHPacked, nodes));
+    AG_CUDA(cudaMemset(bvh->livingFlags, 0, 2 * sizeof(uint32_t)));
+    bvh->cubTempStorage = nullptr;
+    bvh->cubTempBytes = 0;
+    bvh->capacity = capacity;
+    Workspace* ws = nullptr;
+    return workspaceFor(bvh, capacity, true, &ws);
+}
+
+AstraeaStatus astraea_gb300_free_radix_bvh(AstraeaRadixBvh* bvh) {
+    if (bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null BVH");
+    if (bvh->leftChild != nullptr) dropWorkspace(bvh->leftChild);
+    freeArr(bvh->mortonCodes); freeArr(bvh->mortonCodesSorted); freeArr(bvh->indicesIn); freeArr(bvh->indicesSorted);
+    freeArr(bvh->leftChild); freeArr(bvh->rightChild); freeArr(bvh->parent); freeArr(bvh->atomicVisited);
+    freeArr(bvh->aabbMinX); freeArr(bvh->aabbMinY); freeArr(bvh->aabbMinZ);
+    freeArr(bvh->aabbMaxX); freeArr(bvh->aabbMaxY); freeArr(bvh->aabbMaxZ);
+    freeArr(bvh->nodeMass); freeArr(bvh->comX); freeArr(bvh->comY); freeArr(bvh->comZ); freeArr(bvh->nodeMaxH);
+    freeArr(bvh->sceneBoundsOrdered); freeArr(bvh->sceneBoundsFloat); freeArr(bvh->livingFlags);
+    freeArr(bvh->nodeComMass); freeArr(bvh->nodeMinExtent); freeArr(bvh->nodeMaxHPacked);
+    if (bvh->cubTempStorage) { cudaFree(bvh->cubTempStorage); bvh->cubTempStorage = nullptr; }
+    bvh->cubTempBytes = 0;
+    bvh->capacity = 0;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_allocate_particle_buffers(AstraeaParticles* p, uint32_t capacity) {
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    astraea_gb300_free_particle_buffers(p);
+    if (capacity == 0u) return ASTRAEA_OK;
+#define AG_ALLOC(f) AG_CUDA(allocArr(p->f, capacity));
+    AG_ALL_PARTICLE_ARRAYS(AG_ALLOC)
+#undef AG_ALLOC
+    p->capacity = capacity;
+    p->count = 0;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_free_particle_buffers(AstraeaParticles* p) {
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+#define AG_FREE(f) freeArr(p->f);
+    AG_ALL_PARTICLE_ARRAYS(AG_FREE)
+#undef AG_FREE
+    p->capacity = 0;
+    p->count = 0;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_reserve(const AstraeaRadixBvh* bvh, uint32_t capacity) {
+    Workspace* ws = nullptr;
+    AstraeaStatus s = workspaceFor(bvh, capacity, true, &ws);
+    if (s != ASTRAEA_OK) return s;
+    DeviceState* ds = nullptr;
+    return deviceState(&ds);
+}
+
+AstraeaStatus astraea_gb300_release_scratch(const AstraeaRadixBvh* bvh) {
+    if (bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null BVH");
+    if (bvh->leftChild != nullptr) dropWorkspace(bvh->leftChild);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_invalidate_step_cache(const AstraeaRadixBvh* bvh) {
+    Workspace* ws = nullptr;
+    AstraeaStatus s = workspaceFor(bvh, 0, false, &ws);
+    if (s != ASTRAEA_OK) return ASTRAEA_OK;   // nothing cached
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+// ---------------------------------------------------------------- stages
+AstraeaStatus astraea_gb300_clear_stats(AstraeaParticles* p) {
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    if (p->count == 0u) return ASTRAEA_OK;
+    AG_LAUNCH(launchClearStats(*p, p->count, stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_sort_and_build_bvh(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh) {
+    if (p == nullptr || alt == nullptr || bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null descriptor");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    if (bvh->capacity < n || alt->capacity < n)                            // sph_gravity.cu:2001-2003
+        return fail(ASTRAEA_ERR_CAPACITY, "launchSortAndBuildBvh: device buffers capacity < particle count");
+    Workspace* ws = nullptr;
+    AstraeaStatus s = workspaceFor(bvh, std::max(bvh->capacity, n), true, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (bvh->livingFlags == nullptr) bvh->livingFlags = ws->w.words + kWLiving;   // sph_gravity.cu:2008-2011
+    AG_LAUNCH(launchInitBounds(ws->w.words, stream()));
+    AG_LAUNCH(launchBounds(*p, n, ws->w.words, smCount(), stream()));
+    s = buildTree(p, alt, bvh, ws, nullptr, true);
+    if (s != ASTRAEA_OK) return s;
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_sph_pass1_neighbors(AstraeaParticles* p, const AstraeaRadixBvh* bvh) {
+    if (p == nullptr || bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null descriptor");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, true, st));
+    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st));
+    AG_LAUNCH(launchPass1(*p, ws->w, n, st));
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_evaluate_eos(AstraeaParticles* p) {
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    if (p->count == 0u) return ASTRAEA_OK;
+    AG_LAUNCH(launchEos(*p, nullptr, p->count, stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta) {
+    if (p == nullptr || bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null descriptor");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
+    AG_LAUNCH(launchGravity(*p, ws->w, n, theta, smCount(), stream()));
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_sph_pass2_forces(AstraeaParticles* p, const AstraeaRadixBvh* bvh) {
+    if (p == nullptr || bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null descriptor");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    DeviceState* ds = nullptr;
+    s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, true, st));
+    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st));
+    AG_LAUNCH(launchPackPass2Records(*p, ws->w, n, st));
+    const uint32_t* living = (bvh->livingFlags != nullptr) ? bvh->livingFlags : ds->zeroWords;   // :2104
+    AG_LAUNCH(launchPass2(*p, ws->w, n, living, st));
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_leapfrog_kick_half(AstraeaParticles* p, float halfDtPsu, int includeXsph,
+                                               int clampThermal) {
+    (void)includeXsph;   // unused by the engine kernel too (sph_gravity.cu:1297)
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    if (p->count == 0u) return ASTRAEA_OK;
+    KickArgs a{};
+    a.halfDtHost = halfDtPsu;
+    a.dtMode = 0;
+    a.clampThermal = clampThermal != 0;
+    AG_LAUNCH(launchKick(*p, p->count, a, stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_leapfrog_drift(AstraeaParticles* p, float dtPsu, const AstraeaRadixBvh* bvh) {
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    cudaStream_t st = stream();
+    const bool useBvh = bvh != nullptr && bvh->capacity >= n && bvh->leftChild != nullptr &&   // :2127
+                        bvh->rightChild != nullptr && n >= 2u;
+    if (!useBvh) {
+        AG_LAUNCH(launchDriftPlain(*p, n, dtPsu, st));
+        return ASTRAEA_OK;
+    }
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, true, st));
+    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st));
+    AG_LAUNCH(launchDrift(*p, ws->w, n, nullptr, dtPsu, true, false, nullptr, st));
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevDtPsu, float maxDtPsu, float* outDt) {
+    if (p == nullptr || outDt == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const float upper = (prevDtPsu > 0.0f) ? fminf(prevDtPsu * 1.15f, maxDtPsu) : maxDtPsu;
+    if (p->count == 0u) { *outDt = upper; return ASTRAEA_OK; }
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    uint32_t* dtWord = &ds->status->dtBits;
+    AG_CUDA(cudaMemsetAsync(dtWord, 0x7f, sizeof(uint32_t), st));       // sph_gravity.cu:2146
+    AG_LAUNCH(launchReduceDt(*p, p->count, dtWord, smCount(), st));
+    // flags + dt bits in one copy: the blocking read the engine does anyway
+    AG_CUDA(cudaMemcpyAsync(ds->hostWord, ds->status, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AG_CUDA(cudaStreamSynchronize(st));
+    if (ds->hostWord[0] & kFlagLookbackTimeout)
+        return fail(ASTRAEA_ERR_DEVICE_TIMEOUT, "a radix-sort look-back wait timed out; results since the last status "
+                                                "reset are invalid (astraea_gb300_reset_device_status clears it)");
+    *outDt = hostClampDt(ds->hostWord[1], prevDtPsu, maxDtPsu);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult) {
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    uint32_t* words = ds->zeroWords;   // words[0]: never written by anyone; words[4]: result
+    AG_LAUNCH(launchLookbackProbe(words, ds->status, spinLimit, words + 4, st));
+    AG_CUDA(cudaMemcpyAsync(ds->hostWord, words + 4, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AG_CUDA(cudaStreamSynchronize(st));
+    if (outResult) *outResult = ds->hostWord[0];
+    return (ds->hostWord[0] == 2u) ? ASTRAEA_ERR_DEVICE_TIMEOUT : ASTRAEA_OK;
+}
+
+// -------------------------------------------------------------- fused step
+AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh, float prevDtPsu,
+                                 float maxDtPsu, float theta, float* outDtPsu) {
+    if (p == nullptr || alt == nullptr || bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null descriptor");
+    const uint32_t n = p->count;
+    if (n == 0u) return fail(ASTRAEA_ERR_INVALID, "step called with no particles");
+    if (bvh->capacity < n || alt->capacity < n)
+        return fail(ASTRAEA_ERR_CAPACITY, "step: device buffers capacity < particle count");
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK)
+        return fail(ASTRAEA_ERR_INVALID, "step: build the tree once with astraea_gb300_sort_and_build_bvh first");
+    cudaStream_t st = stream();
+    Work& w = ws->w;
+    const int sms = smCount();
+    int q = ws->parity;
+    const bool useBvh = bvh->leftChild != nullptr && bvh->rightChild != nullptr && n >= 2u;
+    const bool cacheOk = ws->stepCacheValid && ws->stepToken == static_cast<const void*>(p->posX);
+    if (!cacheOk) {
+        // Device dt state from the caller's previous dt and the current state.
+        float slots[2] = {0.0f, 0.0f};
+        slots[q] = prevDtPsu;
+        AG_CUDA(cudaMemcpyAsync(ws->dtSlots, slots, sizeof(slots), cudaMemcpyHostToDevice, st));
+        AG_CUDA(cudaMemsetAsync(ws->rawMin + q, 0x7f, sizeof(uint32_t), st));
+        AG_LAUNCH(launchReduceDt(*p, n, ws->rawMin + q, sms, st));
+        AG_LAUNCH(launchRefreshLeaves(*p, w, n, false, st));
+        if (useBvh) AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
+        AG_CUDA(cudaStreamSynchronize(st));   // slots[] is a stack array
+    }
+    // 1. opening half kick; dt resolved on the device
+    KickArgs k1{};
+    k1.dtMode = 1;
+    k1.rawMinIn = ws->rawMin + q;
+    k1.dtSlots = ws->dtSlots;
+    k1.parity = q;
+    k1.maxDt = maxDtPsu;
+    k1.resetWord = ws->rawMin + (q ^ 1);
+    k1.boundsWordsInit = w.words;
+    k1.velRhoOut = w.velRho;
+    AG_LAUNCH(launchKick(*p, n, k1, st));
+    // 2. XSPH drift on the previous step's neighbour lists -> scratch positions + bounds
+    AG_LAUNCH(launchDrift(*p, w, n, ws->dtSlots + (q ^ 1), 0.0f, useBvh, true, w.words, st));
+    // 3. sort + permutation (live fields) + Karras + refit
+    s = buildTree(p, alt, bvh, ws, w.driftPos, false);
+    if (s != ASTRAEA_OK) return s;
+    // 4. neighbour lists for pass 1, pass 2 and the next drift
+    AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
+    AG_LAUNCH(launchPass1(*p, w, n, st));
+    AG_LAUNCH(launchEos(*p, &w, n, st));
+    AG_LAUNCH(launchGravity(*p, w, n, theta, sms, st));
+    AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));
+    // 5. closing half kick + EOS + next dt minimum
+    KickArgs k2{};
+    k2.dtMode = 2;
+    k2.dtSlots = ws->dtSlots;
+    k2.parity = q;
+    k2.withEos = true;
+    k2.rawMinOut = ws->rawMin + (q ^ 1);
+    AG_LAUNCH(launchKick(*p, n, k2, st));
+    if (outDtPsu != nullptr)
+        AG_CUDA(cudaMemcpyAsync(outDtPsu, ws->dtSlots + (q ^ 1), sizeof(float), cudaMemcpyDeviceToHost, st));
+    ws->parity = q ^ 1;
+    ws->stepCacheValid = true;
+    ws->stepToken = static_cast<const void*>(p->posX);
+    ws->stepCount += 1;
+    return ASTRAEA_OK;
+}
+
+// ------------------------------------------------------------ radix sort
+AstraeaStatus astraea_gb300_radix_sort_pairs(uint64_t* keysIn, uint64_t* keysOut, uint32_t* valsIn,
+                                             uint32_t* valsOut, uint32_t n, int endBit) {
+    if (n == 0u) return ASTRAEA_OK;
+    if (!keysIn || !keysOut || !valsIn || !valsOut || endBit < 1 || endBit > 64)
+        return fail(ASTRAEA_ERR_INVALID, "radix_sort_pairs: bad argument");
+    static std::map<int, std::pair<uint32_t*, size_t>> scratch;
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    uint32_t maxTiles = 0;
+    const size_t words = sortScratchWords(n, &maxTiles);
+    uint32_t* buf = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        auto& e = scratch[currentDevice()];
+        if (e.second < words) {
+            if (e.first) cudaFree(e.first);
+            e.first = nullptr;
+            e.second = 0;
+            AG_CUDA(cudaMalloc(&e.first, words * sizeof(uint32_t)));
+            e.second = words;
+        }
+        buf = e.first;
+    }
+    cudaStream_t st = stream();
+    bool inA = true;
+    AG_LAUNCH(radixSortPairs(keysIn, valsIn, keysOut, valsOut, n, endBit, buf, words, maxTiles, ds->status,
+                             g_spinLimit.load(), KeySource::Array, nullptr, &inA, st));
+    if (inA) {
+        AG_CUDA(cudaMemcpyAsync(keysOut, keysIn, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        AG_CUDA(cudaMemcpyAsync(valsOut, valsIn, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    }
+    return ASTRAEA_OK;
+}
+
+}  // extern "C"

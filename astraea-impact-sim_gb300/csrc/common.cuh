@@ -1,0 +1,378 @@
+// common.cuh -- shared device definitions of the GB300 ASTRAEA physics path.
+//
+// Constants and small device functions used by every kernel.  Formulas cite
+// the reference kernel they restate (engine/sph_gravity.cu, engine/eos.cu of
+// Ananasjik/astraea-impact-sim).  Data layout (HBM, per particle / per node):
+//
+//   leafPM  [N]   float4 {x, y, z, m}            sorted positions + mass
+//   leafAux [N]   float4 {Hs, eps, 2h, 0}        Hs = search radius (below)
+//   velRho  [N]   float4 {vx, vy, vz, rho}       neighbour velocity + density
+//   rec2    [5N]  float4 x5 per particle          pass-2 neighbour record
+//   node    [4(N-1)] float4 x4 per internal node:
+//        r0 {comX, comY, comZ, mass}
+//        r1 {dNode, left (int bits), right (int bits), maxHs}
+//        r2 {minX, minY, minZ, maxH}             maxH = max 2h (engine field)
+//        r3 {maxX, maxY, maxZ, 0}
+//   nodeMom [N-1] NodeMom {sum m x, sum m y, sum m z, sum m}  FP64 refit
+//
+// Search radius: pass 1 (engine/sph_gravity.cu:713) needs r < 2 h_old,
+// pass 2 and the next drift (:1071, :1439) need r < max(2 h_i, 2 h_j) with
+// h_new = clamp(h_old * f, 0.35 h0, 6 h0), f in [0.92, 1.08] (:785-787).
+// Hs = 2 max(1.09 h_old, 0.351 h0) bounds every one of those radii, so one
+// neighbour list per step, built against r < max(Hs_i, Hs_j), holds the
+// exact neighbour set of all three passes (each pass re-applies its own
+// exact test in FP32, in the reference's order of operations).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace astraea_gb300 {
+
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr float kGPsuF = 66.7430f;        // engine/units.hpp:27
+constexpr int kWarp = 32;
+constexpr int kTreeStack = 128;           // per-thread DFS fallback stack
+
+// Device status word flags (mirrors include/astraea_gb300.h).
+constexpr uint32_t kFlagLookbackTimeout = 0x1u;
+constexpr uint32_t kFlagNeighborOverflow = 0x2u;
+constexpr uint32_t kFlagStackOverflow = 0x4u;
+
+// Counters in DevStatus::counters.
+enum Counter : int {
+    kCntGravityInteractions = 0,   // particle-node + particle-particle evaluations
+    kCntGravityNodeTests = 1,      // internal nodes tested by the group walk
+    kCntNeighborEntries = 2,       // neighbour-list entries written
+    kCntPass2Pairs = 3,            // in-range pairs of SPH pass 2
+    kCntPass1Pairs = 4,            // in-range pairs of SPH pass 1
+    kCntFallbackWalks = 5,         // particles served by the per-thread walk
+    kCntLookbackSpins = 6,
+    kCntCount = 8
+};
+
+struct DevStatus {
+    unsigned int flags;
+    unsigned int dtBits;     // raw dt minimum of launchReduceDtPsu
+    unsigned long long counters[kCntCount];
+};
+
+// ------------------------------------------------------------------ bits ---
+__device__ __forceinline__ uint32_t orderedFromFloat(float f) {   // sph_gravity.cu:140-144
+    const uint32_t u = __float_as_uint(f);
+    return u ^ (static_cast<uint32_t>(-static_cast<int32_t>(u >> 31)) | 0x80000000u);
+}
+__device__ __forceinline__ float floatFromOrdered(uint32_t u) {   // sph_gravity.cu:146-149
+    return __uint_as_float(u ^ (((u >> 31) - 1u) | 0x80000000u));
+}
+// Interleave the low 21 bits of v two zero bits apart (Morton spreading).
+__device__ __forceinline__ uint64_t spreadBits21(uint64_t v) {
+    v &= 0x1fffffULL;
+    v = (v | (v << 32)) & 0x001f00000000ffffULL;
+    v = (v | (v << 16)) & 0x001f0000ff0000ffULL;
+    v = (v | (v << 8)) & 0x100f00f00f00f00fULL;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
+    v = (v | (v << 2)) & 0x1249249249249249ULL;
+    return v;
+}
+
+// Squared length with explicit IEEE rounding and no multiply-add fusion:
+// ((dx*dx + dy*dy) + dz*dz).  Range and acceptance tests use this form so a
+// pair's in/out decision is bit-identical to the oracle.
+__device__ __forceinline__ float len2Exact(float dx, float dy, float dz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+__device__ __forceinline__ float pointBoxDist2(float px, float py, float pz, float mnx, float mny, float mnz,
+                                               float mxx, float mxy, float mxz) {
+    const float dx = fmaxf(0.0f, fmaxf(__fsub_rn(mnx, px), __fsub_rn(px, mxx)));
+    const float dy = fmaxf(0.0f, fmaxf(__fsub_rn(mny, py), __fsub_rn(py, mxy)));
+    const float dz = fmaxf(0.0f, fmaxf(__fsub_rn(mnz, pz), __fsub_rn(pz, mxz)));
+    return len2Exact(dx, dy, dz);
+}
+
+// ---------------------------------------------------------- SPH kernels ---
+// Wendland C2 in 3-D with support H (sph_gravity.cu:199-208).
+__device__ __forceinline__ float wendlandC2(float r, float H) {
+    if (r >= H || H <= 0.0f) return 0.0f;
+    const float q = r / H;
+    const float omq = 1.0f - q;
+    const float omq2 = omq * omq;
+    const float norm = 21.0f / (2.0f * kPiF * H * H * H);
+    return norm * omq2 * omq2 * (1.0f + 4.0f * q);
+}
+// g with grad_i W(r_i - r_j, H) = g (r_i - r_j) (sph_gravity.cu:211-220).
+__device__ __forceinline__ float wendlandC2Grad(float r, float H) {
+    if (r >= H || H <= 0.0f) return 0.0f;
+    const float q = r / H;
+    const float omq = 1.0f - q;
+    const float H2 = H * H;
+    const float H5 = H2 * H2 * H;
+    return -(210.0f / (kPiF * H5)) * omq * omq * omq;
+}
+// Balsara switch (sph_gravity.cu:222-228).
+__device__ __forceinline__ float balsaraSwitch(float divV, float cx, float cy, float cz, float cs, float h) {
+    const float ad = fabsf(divV);
+    const float ac = sqrtf(cx * cx + cy * cy + cz * cz);
+    const float den = ad + ac + 1.0e-4f * fmaxf(cs, 0.05f) / fmaxf(h, 1.0e-6f);
+    return ad / fmaxf(den, 1.0e-30f);
+}
+// Largest principal stress of (-P I + S), S traceless (sph_gravity.cu:230-254):
+// trigonometric solution of the deviatoric cubic.
+__device__ __forceinline__ float maxPrincipalStress(float P, float xx, float yy, float zz, float xy, float xz,
+                                                    float yz) {
+    const float p2 = xx * xx + yy * yy + zz * zz + 2.0f * (xy * xy + xz * xz + yz * yz);
+    if (p2 <= 1.0e-24f) return -P;
+    const float q = sqrtf(p2 * (1.0f / 6.0f));
+    const float iq = 1.0f / q;
+    const float bxx = xx * iq, byy = yy * iq, bzz = zz * iq, bxy = xy * iq, bxz = xz * iq, byz = yz * iq;
+    const float det = bxx * (byy * bzz - byz * byz) - bxy * (bxy * bzz - byz * bxz) + bxz * (bxy * byz - byy * bxz);
+    const float r = fminf(1.0f, fmaxf(-1.0f, 0.5f * det));
+    const float phi = acosf(r) * (1.0f / 3.0f);
+    return -P + 2.0f * q * cosf(phi);
+}
+__device__ __forceinline__ float effectivePressure(float P, uint8_t phase) {   // sph_gravity.cu:965-969
+    return (phase != 0u) ? fmaxf(P, 0.0f) : P;
+}
+
+// ------------------------------------------------------ material tables ---
+// Strength constants (sph_gravity.cu:35-73) and EOS parameters
+// (eos.cu:10-116) in PSU (P in TPa, u in MJ/kg, rho in 1e6 kg/m^3).
+struct MatConst {
+    // strength
+    float muShear, tMelt, bulkK, yieldY0;
+    // EOS (FP32 path)
+    float rho0, a, b, A, B, E0, Eiv, Ecv, alpha, beta;
+    float cv;              // MJ/(kg K)
+    float cvTrefHi, cvTrefLo;   // cv * tRef as a float pair (hi + lo)
+    float cMinCondensed;   // max(0.05, sqrt(A / rho0))
+    float rho0KgTimes08;   // 0.8 * rho0 in kg/m^3 (vapour test)
+    float u0Ref;           // cv * 300 K (sph_gravity.cu:27-33)
+    float kH2, gamma;      // HydrogenHelium polytrope + ideal gas
+};
+
+// Compile-time construction of the table from the published SI constants of
+// engine/eos.cu:10-116 and engine/sph_gravity.cu:35-73.
+constexpr double cxSqrt(double x) {
+    double r = x > 1.0 ? x : 1.0;
+    for (int i = 0; i < 200; ++i) r = 0.5 * (r + x / r);
+    return r;
+}
+constexpr MatConst makeMat(double rho0Kg, double a, double b, double APa, double BPa, double E0, double Eiv,
+                           double Ecv, double alpha, double beta, double cvSI, double tMelt, double tRef,
+                           double muPa, double bulkPa, double y0Pa, double kH2, double gamma) {
+    const double cv = cvSI / 1.0e6;
+    const double cvTref = cv * tRef;
+    const float hi = static_cast<float>(cvTref);
+    const double rho0 = rho0Kg / 1.0e6;
+    const double A = APa / 1.0e12;
+    const double cMin = (A > 0.0) ? cxSqrt(A / rho0) : 0.0;
+    return MatConst{static_cast<float>(muPa / 1.0e12), static_cast<float>(tMelt), static_cast<float>(bulkPa / 1.0e12),
+                    static_cast<float>(y0Pa / 1.0e12), static_cast<float>(rho0), static_cast<float>(a),
+                    static_cast<float>(b), static_cast<float>(A), static_cast<float>(BPa / 1.0e12),
+                    static_cast<float>(E0 / 1.0e6), static_cast<float>(Eiv / 1.0e6), static_cast<float>(Ecv / 1.0e6),
+                    static_cast<float>(alpha), static_cast<float>(beta), static_cast<float>(cv), hi,
+                    static_cast<float>(cvTref - static_cast<double>(hi)),
+                    static_cast<float>(cMin > 0.05 ? cMin : 0.05), static_cast<float>(0.8 * rho0Kg),
+                    static_cast<float>((cvSI * 300.0) / 1.0e6), static_cast<float>(kH2), static_cast<float>(gamma)};
+}
+// Strength columns (mu, T_melt, K, Y0) of the HydrogenHelium row are zero in
+// engine/sph_gravity.cu:64-65, which disables the strength model for gas.
+static __constant__ MatConst c_mat[5] = {
+    makeMat(7800.0, 0.5, 1.5, 1.28e11, 1.05e11, 9.50e6, 2.40e6, 8.67e6, 5.0, 5.0, 449.0, 1811.0, 293.0, 7.70e10,
+            1.28e11, 6.80e8, 0.0, 1.0),
+    makeMat(2680.0, 0.5, 1.3, 1.80e10, 1.80e10, 1.60e7, 3.50e6, 1.80e7, 5.0, 5.0, 790.0, 1600.0, 293.0, 2.20e10,
+            1.80e10, 3.50e9, 0.0, 1.0),
+    makeMat(1000.0, 0.7, 0.15, 2.18e9, 1.325e10, 7.00e6, 4.19e5, 2.68e6, 10.0, 5.0, 4184.0, 273.15, 273.15, 3.50e9,
+            2.18e9, 1.00e7, 0.0, 1.0),
+    makeMat(0.178, 0.4, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 8260.0, 0.0, 0.0, 0.0, 0.0, 0.0, 2.08e5, 1.4),
+    makeMat(2000.0, 0.5, 1.3, 1.20e10, 1.20e10, 1.60e7, 3.50e6, 1.80e7, 5.0, 5.0, 800.0, 1500.0, 293.0, 8.00e9,
+            1.20e10, 5.00e7, 0.0, 1.0),
+};
+
+__device__ __forceinline__ int matIndex(uint8_t m) { return (m <= 4u) ? static_cast<int>(m) : 1; }
+
+// ---------------------------------------------------------------- EOS -----
+// FP32 evaluation of engine/eos.cu:283-388.  The reference evaluates in FP64;
+// here every cancellation-prone quantity is formed without loss:
+//   mu = (rho - rho0)/rho0 (exact difference when rho is within 2x of rho0),
+//   cold energy by its Taylor series for mu < 0.1,
+//   the thermal excess u - cv T_ref with cv T_ref split into a float pair.
+struct EosOut { float P, cs, T; uint8_t phase; };
+
+__device__ __forceinline__ float coldEnergyF32(int mi, float rho) {
+    const MatConst& c = c_mat[mi];
+    rho = fmaxf(rho, 0.0f);
+    if (mi == 3) return c.kH2 * rho;
+    if (!(rho > c.rho0)) return 0.0f;
+    const float mu = (rho - c.rho0) / c.rho0;
+    float ta, tb;
+    if (mu < 0.1f) {
+        // termA = sum_{k>=2} (-1)^k (k-1)/k mu^k ; termB = sum_{k>=3} (-1)^(k+1) (k-2)/k mu^k
+        float sa = 0.0f, sb = 0.0f;
+#pragma unroll
+        for (int k = 16; k >= 2; --k) {
+            const float ca = ((k & 1) ? -1.0f : 1.0f) * static_cast<float>(k - 1) / static_cast<float>(k);
+            const float cb = (k >= 3) ? (((k & 1) ? 1.0f : -1.0f) * static_cast<float>(k - 2) / static_cast<float>(k)) : 0.0f;
+            sa = sa * mu + ca;
+            sb = sb * mu + cb;
+        }
+        ta = sa * mu * mu;
+        tb = sb * mu * mu;
+    } else {
+        const float eta = 1.0f + mu;
+        const float le = log1pf(mu);
+        ta = le - (mu / eta);
+        tb = (mu * (2.0f + mu)) / eta - 2.0f * le;
+    }
+    return (c.A * ta + c.B * tb) / c.rho0;
+}
+
+struct PD { float p, dpr, dpu; bool tension; };
+
+__device__ __forceinline__ PD tillotsonCompressedF32(const MatConst& c, float rho, float eta, float mu, float uE,
+                                                     float dmg) {
+    const float bEff = (mu >= 0.0f) ? c.B : 0.0f;
+    const float den = c.E0 * eta * eta;
+    const float ratio = (den > 1.0e-30f) ? (uE / den) : 1.0e30f;
+    const float iw = 1.0f / (ratio + 1.0f);
+    const float wm1w2 = (ratio > 1.0e15f) ? 0.0f : (ratio * iw * iw);
+    PD r;
+    r.p = (c.a + c.b * iw) * rho * uE + c.A * mu + bEff * mu * mu;
+    r.dpr = (c.a + c.b * iw) * uE + 2.0f * c.b * uE * wm1w2 + (c.A + 2.0f * bEff * mu) / c.rho0;
+    r.dpu = (c.a + c.b * iw * iw) * rho;
+    r.tension = false;
+    if (r.p < 0.0f && dmg > 0.0f) {
+        const float keep = 1.0f - dmg;
+        r.p *= keep; r.dpr *= keep; r.dpu *= keep;
+        r.tension = true;
+    }
+    return r;
+}
+
+__device__ __forceinline__ PD tillotsonExpandedF32(const MatConst& c, float rho, float eta, float mu, float uE) {
+    const float x = (c.rho0 - rho) / rho;          // 1/eta - 1, formed without cancellation
+    const float ax2 = c.alpha * x * x;
+    const float bx = c.beta * x;
+    const float eA = (ax2 < 700.0f) ? expf(-ax2) : 0.0f;
+    PD r;
+    r.tension = false;
+    if (eA == 0.0f) {
+        r.p = c.a * rho * uE; r.dpr = c.a * uE; r.dpu = c.a * rho;
+        return r;
+    }
+    const float eB = (bx < 700.0f) ? expf(-bx) : 0.0f;
+    const float den = c.E0 * eta * eta;
+    const float ratio = (den > 1.0e-30f) ? (uE / den) : 1.0e30f;
+    const float iw = 1.0f / (ratio + 1.0f);
+    const float wm1w2 = (ratio > 1.0e15f) ? 0.0f : (ratio * iw * iw);
+    const float ideal = c.a * rho * uE;
+    const float inner = (c.b * rho * uE * iw) + c.A * mu * eB;
+    const float pe = ideal + inner * eA;
+    const float r0r2 = c.rho0 / (rho * rho);
+    const float expDrho = (eB > 0.0f) ? ((c.A / c.rho0 + c.A * mu * c.beta * r0r2) * eB) : 0.0f;
+    r.p = pe;
+    r.dpr = c.a * uE + eA * (c.b * uE * iw + 2.0f * c.b * uE * wm1w2 + expDrho) + 2.0f * c.alpha * x * r0r2 * (pe - ideal);
+    r.dpu = (c.a + c.b * eA * iw * iw) * rho;
+    return r;
+}
+
+__device__ __forceinline__ uint8_t classifyPhaseF32(int mi, const MatConst& c, float rho, float u, float T) {
+    if (mi == 3) return (T > 10000.0f) ? 3u : 5u;                 // eos.cu:235-238
+    const float rhoKg = rho * 1.0e6f;
+    if (mi == 2) {                                               // eos.cu:243-254
+        if (T > 15000.0f) return 3u;
+        if (u >= c.Ecv || (T > 647.0f && rhoKg < 322.0f)) return 2u;
+        if (T >= 273.15f) return 4u;
+        return 0u;
+    }
+    if (T > 12000.0f) return 3u;                                 // eos.cu:257-266
+    if (u >= c.Ecv && rhoKg < c.rho0KgTimes08) return 2u;
+    if (T >= c.tMelt) return 1u;
+    return 0u;
+}
+
+__device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, float u, float dIn) {
+    const int mi = matIndex(matRaw);
+    const MatConst& c = c_mat[mi];
+    const float rho = fmaxf(rhoIn, 1.0e-12f);
+    const float dmg = fminf(fmaxf(dIn, 0.0f), 1.0f);
+    EosOut o;
+    if (mi == 3) {                                               // eos.cu:328-340
+        const float uTh = fmaxf(0.0f, u - c.kH2 * rho);
+        const float T = fmaxf(3.0f, uTh / c.cv);
+        const float P = c.kH2 * rho * rho + (c.gamma - 1.0f) * rho * uTh;
+        const float cs2 = 2.0f * c.kH2 * rho + c.gamma * (c.gamma - 1.0f) * uTh;
+        o.P = P; o.cs = fmaxf(0.05f, sqrtf(fmaxf(0.0f, cs2))); o.T = T;
+        o.phase = classifyPhaseF32(mi, c, rho, u, T);
+        return o;
+    }
+    const float mu = (rho - c.rho0) / c.rho0;
+    const float eta = rho / c.rho0;
+    const float uCold = coldEnergyF32(mi, rho);
+    const float T = fmaxf(3.0f, (u - uCold) / c.cv);
+    const float excess = ((u - c.cvTrefHi) - c.cvTrefLo) - uCold;
+    const float uE = uCold + fmaxf(0.0f, excess);
+    PD r;
+    if (mu >= 0.0f || uE < c.Eiv) {
+        r = tillotsonCompressedF32(c, rho, eta, mu, uE, dmg);
+    } else if (uE >= c.Ecv) {
+        r = tillotsonExpandedF32(c, rho, eta, mu, uE);
+    } else {
+        const PD pc = tillotsonCompressedF32(c, rho, eta, mu, uE, dmg);
+        const PD pe = tillotsonExpandedF32(c, rho, eta, mu, uE);
+        const float den = fmaxf(1.0e-30f, c.Ecv - c.Eiv);
+        const float f = fminf(fmaxf((uE - c.Eiv) / den, 0.0f), 1.0f);
+        r.p = (1.0f - f) * pc.p + f * pe.p;
+        r.dpr = (1.0f - f) * pc.dpr + f * pe.dpr;
+        r.dpu = (1.0f - f) * pc.dpu + f * pe.dpu + (pe.p - pc.p) / den;
+        r.tension = pc.tension;
+    }
+    const float cs2 = r.dpr + (r.p / (rho * rho)) * r.dpu;
+    const bool condensed = (mu >= 0.0f) || (uE < c.Eiv && rho >= 0.9f * c.rho0 && !r.tension);
+    const float cMin = condensed ? c.cMinCondensed : 0.05f;
+    o.P = r.p;
+    o.cs = fmaxf(cMin, sqrtf(fmaxf(0.0f, cs2)));
+    o.T = T;
+    o.phase = classifyPhaseF32(mi, c, rho, u, T);
+    return o;
+}
+
+// FP64 mass moments of one internal node (32 bytes, 16-byte aligned).
+struct __align__(16) NodeMom {
+    double sx, sy, sz, m;
+};
+
+// ----------------------------------------------------------- workspace ---
+// Device pointers of the library-owned scratch of one BVH (see capi.cu).
+struct Work {
+    uint32_t capacity;
+    uint32_t maxNbr;
+    float4* leafPM;
+    float4* leafAux;
+    float4* velRho;
+    float4* rec2;
+    float4* node;          // 4 x float4 per internal node
+    NodeMom* nodeMom;
+    float4* driftPos;      // {x, y, z, 0} after the drift
+    uint32_t* nbrCount;
+    uint32_t* nbrList;     // particle-major, maxNbr per particle
+    uint32_t* words;       // small words, see WordIndex
+    uint32_t* sortScratch; // histograms + look-back + tile counters
+    size_t sortScratchWords;
+    uint32_t sortMaxTiles;
+    DevStatus* status;
+};
+
+// Indices into Work::words.
+enum WordIndex : int {
+    kWBounds = 0,        // 6 ordered-uint bounds (min xyz, max xyz)
+    kWLiving = 6,        // 2 living flags
+    kWDtMin = 8,         // 2 dt-min bit words (step parity)
+    kWDtState = 10,      // 2 float dt slots (step parity)
+    kWGroupCounter = 12, // persistent-grid work counter (gravity)
+    kWNbrCounter = 13,   // persistent-grid work counter (neighbour build)
+    kWBoundsF = 16,      // 6 floats: decoded bounds
+    kWCount = 32
+};
+
+}  // namespace astraea_gb300

@@ -1,0 +1,103 @@
+// kernels.h -- launchers of every kernel of the library (host side) and the
+// small device helpers more than one translation unit inlines.
+#pragma once
+
+#include "internal.h"
+
+namespace astraea_gb300 {
+
+// ------------------------------------------------------ device helpers ---
+__device__ __forceinline__ float warpMinF(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warpMaxF(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Reduce each thread's partial AABB over the block and merge it into the
+// ordered-uint bound words with atomics (engine/sph_gravity.cu:300-324).
+// Every thread of the block must call it.
+__device__ __forceinline__ void blockBoundsToWords(const float* mn, const float* mx, uint32_t* words) {
+    __shared__ float sMin[3][32], sMax[3][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = warpMinF(mn[k]), b = warpMaxF(mx[k]);
+        if (lane == 0) { sMin[k][warp] = a; sMax[k][warp] = b; }
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float a = (lane < nw) ? sMin[k][lane] : 1.0e30f;
+            float b = (lane < nw) ? sMax[k][lane] : -1.0e30f;
+            a = warpMinF(a);
+            b = warpMaxF(b);
+            if (lane == 0) {
+                atomicMin(&words[kWBounds + k], orderedFromFloat(a));
+                atomicMax(&words[kWBounds + 3 + k], orderedFromFloat(b));
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ build.cu ---
+cudaError_t launchInitBounds(uint32_t* words, cudaStream_t st);
+cudaError_t launchBounds(const AstraeaParticles& p, uint32_t n, uint32_t* words, int sms, cudaStream_t st);
+cudaError_t launchPermuteLeavesKarras(const AstraeaParticles& p, const AstraeaParticles& alt,
+                                      const AstraeaRadixBvh& bvh, const float4* posSrc, const Work& w, uint32_t n,
+                                      uint32_t* livingFlags, bool allFields, cudaStream_t st);
+cudaError_t launchRefreshLeaves(const AstraeaParticles& p, const Work& w, uint32_t n, bool withVelRho,
+                                cudaStream_t st);
+cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, cudaStream_t st);
+
+// ---------------------------------------------------------- gravity.cu ---
+cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, int sms,
+                          cudaStream_t st);
+
+// -------------------------------------------------------------- sph.cu ---
+cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st);
+cudaError_t launchPass1(const AstraeaParticles& p, const Work& w, uint32_t n, cudaStream_t st);
+cudaError_t launchPass2(const AstraeaParticles& p, const Work& w, uint32_t n, const uint32_t* livingFlags,
+                        cudaStream_t st);
+// XSPH drift; new positions go to w.driftPos when toScratch, else back into
+// p.pos (after all neighbours were read).  Also merges the new positions'
+// AABB into the bound words when boundsWords != nullptr.
+cudaError_t launchDrift(const AstraeaParticles& p, const Work& w, uint32_t n, const float* dtDev, float dtHost,
+                        bool useList, bool toScratch, uint32_t* boundsWords, cudaStream_t st);
+
+// -------------------------------------------------------- integrate.cu ---
+cudaError_t launchClearStats(const AstraeaParticles& p, uint32_t n, cudaStream_t st);
+// EOS; when w != nullptr also writes the pass-2 neighbour records.
+cudaError_t launchEos(const AstraeaParticles& p, const Work* w, uint32_t n, cudaStream_t st);
+// Half kick.  dtMode 0: halfDt = halfDtHost.  dtMode 1 (opening kick of a
+// fused step): dt = clamp of the raw minimum *rawMinIn against the previous
+// dt dtSlots[parity] (the host clamp of launchReduceDtPsu), written to
+// dtSlots[parity ^ 1].  dtMode 2 (closing kick): dt = dtSlots[parity ^ 1].
+struct KickArgs {
+    float halfDtHost;
+    int dtMode;
+    bool clampThermal;
+    bool withEos;              // evaluate the EOS on the kicked state (fused)
+    const uint32_t* rawMinIn;  // raw dt minimum bits (device), dtMode 1
+    float* dtSlots;            // 2 floats indexed by step parity
+    int parity;
+    float maxDt;
+    uint32_t* rawMinOut;       // when non-null: reduce the next dt minimum into it
+    uint32_t* resetWord;       // when non-null: block 0 writes 0x7f7f7f7f here
+    uint32_t* boundsWordsInit; // when non-null: block 0 re-arms bounds + living flags
+    float4* velRhoOut;         // when non-null: write {v, rho} records
+};
+cudaError_t launchKick(const AstraeaParticles& p, uint32_t n, const KickArgs& a, cudaStream_t st);
+cudaError_t launchReduceDt(const AstraeaParticles& p, uint32_t n, uint32_t* rawMinOut, int sms, cudaStream_t st);
+// Pass-2 records from the current SoA, without evaluating the EOS.
+cudaError_t launchPackPass2Records(const AstraeaParticles& p, const Work& w, uint32_t n, cudaStream_t st);
+// x += dt v without XSPH (drift without a tree, sph_gravity.cu:1484-1488).
+cudaError_t launchDriftPlain(const AstraeaParticles& p, uint32_t n, float dt, cudaStream_t st);
+
+}  // namespace astraea_gb300

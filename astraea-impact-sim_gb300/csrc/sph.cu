@@ -1,0 +1,531 @@
+// sph.cu -- neighbour lists, SPH pass 1 / pass 2 and the XSPH drift (sm_103a).
+//
+// Restates sphPass1Kernel (engine/sph_gravity.cu:645-788), sphPass2Kernel
+// (:965-1287) and leapfrogDriftKernel (:1376-1489).  The engine walks the
+// tree three times per step with one particle per lane; a lane's pair body
+// only runs when that lane is in range, so most lanes idle.  Here:
+//   * one group walk per step (buildNeighborsKernel) writes, for every
+//     particle, the list of j with r_ij < max(Hs_i, Hs_j) -- a superset of the
+//     pass-1, pass-2 and next-drift neighbour sets (see common.cuh);
+//   * pass 1, pass 2 and the drift run one thread per particle over its own
+//     list, re-applying the engine's exact FP32 range test, so every lane
+//     works on its own pairs;
+//   * neighbour data is read from packed float4 records (positions + mass,
+//     velocity + density, and a five-float4 pass-2 record written by the EOS
+//     kernel), one 16-byte load per group of fields instead of one gather per
+//     field.
+// A particle whose list overflowed the per-particle capacity is served by a
+// per-thread depth-first walk with the same superset test (rare path).
+#include "kernels.h"
+
+namespace astraea_gb300 {
+namespace {
+
+constexpr int kNbWarps = 4;
+constexpr int kNbStack = 1024;
+constexpr int kNbList = 64;
+
+struct NbWarpSmem {
+    int stack[kNbStack];
+    float4 cand[kNbList];    // {x, y, z, Hs}
+    int candIdx[kNbList];
+    float4 gpos[32];         // {x, y, z, Hs}
+};
+
+__device__ __forceinline__ uint32_t laneMaskLt() {
+    uint32_t m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, uint32_t n, uint32_t numGroups,
+                                                                      uint32_t* groupCounter) {
+    __shared__ NbWarpSmem smem[kNbWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    NbWarpSmem& S = smem[warp];
+    unsigned long long nEntries = 0;
+    bool overflow = false, stackOverflow = false;
+    const uint32_t maxNbr = w.maxNbr;
+
+    if (n < 2u) {
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            w.nbrCount[i] = 0u;
+        return;
+    }
+    const float4 rootR1 = __ldg(&w.node[1]);
+    const int rootL = __float_as_int(rootR1.y), rootR = __float_as_int(rootR1.z);
+
+    for (;;) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(groupCounter, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= numGroups) break;
+        const uint32_t i = g * 32u + static_cast<uint32_t>(lane);
+        const bool active = i < n;
+        const int act = static_cast<int>(min(32u, n - g * 32u));
+        float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
+        float Hs = 0.0f;
+        if (active) {
+            me = __ldg(&w.leafPM[i]);
+            Hs = __ldg(&w.leafAux[i]).x;
+        }
+        S.gpos[lane] = make_float4(me.x, me.y, me.z, Hs);
+        const float gminx = warpMinF(active ? me.x : 3.0e38f), gmaxx = warpMaxF(active ? me.x : -3.0e38f);
+        const float gminy = warpMinF(active ? me.y : 3.0e38f), gmaxy = warpMaxF(active ? me.y : -3.0e38f);
+        const float gminz = warpMinF(active ? me.z : 3.0e38f), gmaxz = warpMaxF(active ? me.z : -3.0e38f);
+        const float gHs = warpMaxF(Hs);
+        if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
+        int sp = 2, cCount = 0;
+        uint32_t cnt = 0, rounds = 0;
+        uint32_t* myList = w.nbrList + static_cast<size_t>(active ? i : 0u) * maxNbr;
+        __syncwarp();
+
+        auto flush = [&](int base, int num) {
+            if (active) {
+                for (int e = 0; e < num; ++e) {
+                    const float4 q = S.cand[base + e];
+                    const int j = S.candIdx[base + e];
+                    const float r2 = len2Exact(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z));
+                    const float R = fmaxf(Hs, q.w);
+                    if (j != static_cast<int>(i) && r2 < __fmul_rn(R, R)) {
+                        if (cnt < maxNbr) myList[cnt] = static_cast<uint32_t>(j);
+                        ++cnt;
+                    }
+                }
+            }
+        };
+
+        while (sp > 0) {
+            if (++rounds > 2u * n + 64u) {     // only reachable on a corrupted tree
+                stackOverflow = true;
+                break;
+            }
+            const int take = min(sp, 32);
+            const int c = (lane < take) ? S.stack[sp - take + lane] : 0;
+            sp -= take;
+            __syncwarp();
+            const bool has = lane < take && c >= -static_cast<int>(n) && c < static_cast<int>(n) - 1;
+            const bool isLeaf = has && c < 0;
+            bool open = false;
+            int cl = 0, cr = 0;
+            if (has && c >= 0) {
+                const float4* rec = w.node + 4 * static_cast<size_t>(c);
+                const float4 r1 = __ldg(&rec[1]);
+                const float4 bmin = __ldg(&rec[2]);
+                const float4 bmax = __ldg(&rec[3]);
+                cl = __float_as_int(r1.y);
+                cr = __float_as_int(r1.z);
+                // box-box distance bounds every member's point-box distance
+                const float dx = fmaxf(0.0f, fmaxf(bmin.x - gmaxx, gminx - bmax.x));
+                const float dy = fmaxf(0.0f, fmaxf(bmin.y - gmaxy, gminy - bmax.y));
+                const float dz = fmaxf(0.0f, fmaxf(bmin.z - gmaxz, gminz - bmax.z));
+                const float Rg = fmaxf(gHs, r1.w);
+                if (dx * dx + dy * dy + dz * dz <= Rg * Rg * 1.00001f) {
+                    for (int q = 0; q < act; ++q) {
+                        const float4 pq = S.gpos[q];
+                        const float R = fmaxf(pq.w, r1.w);
+                        if (pointBoxDist2(pq.x, pq.y, pq.z, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <=
+                            R * R * 1.00001f) {
+                            open = true;
+                            break;
+                        }
+                    }
+                }
+            }
+            unsigned openMask = __ballot_sync(0xffffffffu, open);
+            if (sp + 2 * __popc(openMask) > kNbStack) {
+                stackOverflow = true;     // cannot happen for trees of depth < 32
+                openMask = 0u;
+                open = false;
+            }
+            if (open) {
+                const int pos = sp + 2 * __popc(openMask & laneMaskLt());
+                S.stack[pos] = cl;
+                S.stack[pos + 1] = cr;
+            }
+            sp += 2 * __popc(openMask);
+            const unsigned leafMask = __ballot_sync(0xffffffffu, isLeaf);
+            if (isLeaf) {
+                const int j = ~c;
+                const float4 pm = __ldg(&w.leafPM[j]);
+                const float hsj = __ldg(&w.leafAux[j]).x;
+                const int slot = cCount + __popc(leafMask & laneMaskLt());
+                S.cand[slot] = make_float4(pm.x, pm.y, pm.z, hsj);
+                S.candIdx[slot] = j;
+            }
+            cCount += __popc(leafMask);
+            __syncwarp();
+            if (cCount >= 32) {
+                cCount -= 32;
+                flush(cCount, 32);
+                __syncwarp();
+            }
+        }
+        flush(0, cCount);
+        if (active) {
+            w.nbrCount[i] = cnt;
+            if (cnt > maxNbr) overflow = true;
+        }
+        nEntries += cnt;
+        __syncwarp();
+    }
+    const unsigned long long tot = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(nEntries & 0xffffffffu));
+    const bool anyOver = __any_sync(0xffffffffu, overflow);
+    if (lane == 0) {
+        atomicAdd(&w.status->counters[kCntNeighborEntries], tot);
+        if (anyOver) atomicOr(&w.status->flags, kFlagNeighborOverflow);
+        if (stackOverflow) atomicOr(&w.status->flags, kFlagStackOverflow);
+    }
+}
+
+// Visit every j of particle i's superset list; when the list overflowed,
+// walk the tree depth-first with the same superset test instead.
+template <class F>
+__device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& f) {
+    const uint32_t c = __ldg(&w.nbrCount[i]);
+    if (c <= w.maxNbr) {
+        const uint32_t* list = w.nbrList + static_cast<size_t>(i) * w.maxNbr;
+        uint32_t k = 0;
+        for (; k + 4 <= c; k += 4) {
+            const uint4 q = __ldg(reinterpret_cast<const uint4*>(list + k));
+            f(q.x); f(q.y); f(q.z); f(q.w);
+        }
+        for (; k < c; ++k) f(__ldg(&list[k]));
+        return;
+    }
+    atomicAdd(&w.status->counters[kCntFallbackWalks], 1ull);
+    const float4 me = __ldg(&w.leafPM[i]);
+    const float Hs = __ldg(&w.leafAux[i]).x;
+    int stack[kTreeStack];
+    int sp = 0;
+    const float4 rootR1 = __ldg(&w.node[1]);
+    stack[sp++] = __float_as_int(rootR1.y);
+    stack[sp++] = __float_as_int(rootR1.z);
+    const int nInt = static_cast<int>(w.capacity);
+    uint32_t iters = 0;
+    while (sp > 0) {
+        const int c2 = stack[--sp];
+        if (++iters > 4u * w.capacity + 64u || c2 < -nInt || c2 >= nInt - 1) {   // corrupted tree only
+            atomicOr(&w.status->flags, kFlagStackOverflow);
+            break;
+        }
+        if (c2 < 0) {
+            const uint32_t j = static_cast<uint32_t>(~c2);
+            if (j == i) continue;
+            const float4 q = __ldg(&w.leafPM[j]);
+            const float R = fmaxf(Hs, __ldg(&w.leafAux[j]).x);
+            if (len2Exact(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z)) < __fmul_rn(R, R)) f(j);
+            continue;
+        }
+        const float4* rec = w.node + 4 * static_cast<size_t>(c2);
+        const float4 r1 = __ldg(&rec[1]);
+        const float4 bmin = __ldg(&rec[2]);
+        const float4 bmax = __ldg(&rec[3]);
+        const float R = fmaxf(Hs, r1.w);
+        if (pointBoxDist2(me.x, me.y, me.z, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <= R * R * 1.00001f) {
+            if (sp + 2 <= kTreeStack) {
+                stack[sp++] = __float_as_int(r1.y);
+                stack[sp++] = __float_as_int(r1.z);
+            } else {
+                atomicOr(&w.status->flags, kFlagStackOverflow);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- pass 1 ---
+__global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 me = __ldg(&w.leafPM[i]);
+    const float4 vr = __ldg(&w.velRho[i]);
+    const float mi = me.w;
+    const float hi = fmaxf(__ldg(&p.h[i]), 1.0e-6f);
+    const float h0i = fmaxf(__ldg(&p.h0[i]), 1.0e-6f);
+    const float rhoI = fmaxf(vr.w, 1.0e-9f);
+    const float Hi = 2.0f * hi;
+    const float Hi2 = __fmul_rn(Hi, Hi);
+    const float w0 = 21.0f / (2.0f * kPiF * Hi * Hi * Hi);
+    float shep = (mi / rhoI) * w0;
+    int ngb = 1;
+    float nsX = 0.f, nsY = 0.f, nsZ = 0.f;
+    float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
+    if (n >= 2u) {
+        forEachCandidate(w, i, [&](uint32_t j) {
+            const float4 q = __ldg(&w.leafPM[j]);
+            const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
+            const float r2 = len2Exact(dx, dy, dz);
+            if (!(r2 < Hi2)) return;                       // sph_gravity.cu:713
+            ++ngb;
+            const float4 vj = __ldg(&w.velRho[j]);
+            const float r = sqrtf(r2);
+            const float volJ = q.w / fmaxf(vj.w, 1.0e-9f);
+            const float wij = wendlandC2(r, Hi);
+            shep += volJ * wij;
+            nsX -= volJ * dx * wij;
+            nsY -= volJ * dy * wij;
+            nsZ -= volJ * dz * wij;
+            const float gc = wendlandC2Grad(r, Hi);
+            const float gx = gc * dx, gy = gc * dy, gz = gc * dz;
+            const float dvx = vj.x - vr.x, dvy = vj.y - vr.y, dvz = vj.z - vr.z;
+            gXX += volJ * dvx * gx; gXY += volJ * dvx * gy; gXZ += volJ * dvx * gz;
+            gYX += volJ * dvy * gx; gYY += volJ * dvy * gy; gYZ += volJ * dvy * gz;
+            gZX += volJ * dvz * gx; gZY += volJ * dvz * gy; gZZ += volJ * dvz * gz;
+        });
+    }
+    p.shepardC[i] = shep;                                   // sph_gravity.cu:772-787
+    const float normNs = sqrtf(nsX * nsX + nsY * nsY + nsZ * nsZ);
+    float fs = fminf(1.0f, fmaxf(0.0f, 1.6f * fmaxf(1.0f - shep, normNs / hi) - 0.15f));
+    if (ngb <= 2) fs = 1.0f;
+    p.surfFactor[i] = fs;
+    p.divV[i] = gXX + gYY + gZZ;
+    p.curlVX[i] = gZY - gYZ;
+    p.curlVY[i] = gXZ - gZX;
+    p.curlVZ[i] = gYX - gXY;
+    const float ratio = 56.0f / static_cast<float>(ngb);
+    const float factor = fminf(1.08f, fmaxf(0.92f, cbrtf(ratio)));
+    p.h[i] = fminf(6.0f * h0i, fmaxf(0.35f * h0i, hi * factor));
+}
+
+// ---------------------------------------------------------------- pass 2 ---
+// Pass-2 record (written by the EOS kernel), 5 float4 per particle:
+//   q0 {x, y, z, h}   q1 {vx, vy, vz, m}   q2 {rho, P_eff, cs, f_Balsara}
+//   q3 {sXX, sYY, sZZ, sXY}   q4 {sXZ, sYZ, material, 0}
+// with h, rho, cs already clamped as the engine clamps them on load.
+__global__ void __launch_bounds__(128) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
+                                                   const uint32_t* livingFlags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* R = w.rec2;
+    const float4 a0 = __ldg(&R[5 * i + 0]);
+    const float4 a1 = __ldg(&R[5 * i + 1]);
+    const float4 a2 = __ldg(&R[5 * i + 2]);
+    const float4 a3 = __ldg(&R[5 * i + 3]);
+    const float4 a4 = __ldg(&R[5 * i + 4]);
+    const float xi = a0.x, yi = a0.y, zi = a0.z, hi = a0.w, Hi = 2.0f * hi;
+    const float vxi = a1.x, vyi = a1.y, vzi = a1.z, mi = a1.w;
+    const float rhoI = a2.x, pI = a2.y, csI = a2.z, fBalI = a2.w;
+    const float sXXi = a3.x, sYYi = a3.y, sZZi = a3.z, sXYi = a3.w, sXZi = a4.x, sYZi = a4.y;
+    const int matI = __float_as_int(a4.z);
+    const float invRhoI2 = 1.0f / (rhoI * rhoI);
+    const float Ri = (pI < 0.0f) ? (0.3f * (-pI) * invRhoI2) : 0.0f;
+    const float pOverRho2I = pI * invRhoI2;
+    const float tempI = __ldg(&p.tempK[i]);
+    const float damI = __ldg(&p.damage[i]);
+    const float fSurf = __ldg(&p.surfFactor[i]);
+
+    float axS = 0.f, ayS = 0.f, azS = 0.f, drC = 0.f, drD = 0.f, duP = 0.f, duAv = 0.f, duT = 0.f, duS = 0.f;
+    float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
+    unsigned pairs = 0;
+    if (n >= 2u) {
+        forEachCandidate(w, i, [&](uint32_t j) {
+            const float4 b0 = __ldg(&R[5 * j + 0]);
+            const float dx = __fsub_rn(xi, b0.x), dy = __fsub_rn(yi, b0.y), dz = __fsub_rn(zi, b0.z);
+            const float r2 = len2Exact(dx, dy, dz);
+            const float hj = b0.w, Hj = 2.0f * hj;
+            const float Hm = fmaxf(Hi, Hj);
+            if (!(r2 < __fmul_rn(Hm, Hm))) return;          // sph_gravity.cu:1071
+            ++pairs;
+            const float4 b1 = __ldg(&R[5 * j + 1]);
+            const float4 b2 = __ldg(&R[5 * j + 2]);
+            const float4 b3 = __ldg(&R[5 * j + 3]);
+            const float4 b4 = __ldg(&R[5 * j + 4]);
+            const float mj = b1.w, rhoJ = b2.x, pJ = b2.y, csJ = b2.z, fBalJ = b2.w;
+            const float dvx = vxi - b1.x, dvy = vyi - b1.y, dvz = vzi - b1.z;
+            const float vDotR = dvx * dx + dvy * dy + dvz * dz;
+            const float r = sqrtf(r2);
+            const float gI = wendlandC2Grad(r, Hi), gJ = wendlandC2Grad(r, Hj);
+            const float gb = 0.5f * (gI + gJ);
+            const float gx = gb * dx, gy = gb * dy, gz = gb * dz;
+            const float invRhoJ2 = 1.0f / (rhoJ * rhoJ);
+            const float vDotG = dvx * gx + dvy * gy + dvz * gz;
+            const float volJ = mj / rhoJ;
+            drC += volJ * vDotG;                               // continuity (:1114)
+            if (__float_as_int(b4.z) == matI) {                // delta-SPH diffusion (:1115-1119)
+                const float rDotG = -(dx * gx + dy * gy + dz * gz);
+                const float dd = r2 + 0.01f * Hi * Hi;
+                drD += volJ * (2.0f * (rhoJ - rhoI) / dd) * rDotG;
+            }
+            float piIJ = 0.0f;                                 // Monaghan AV x Balsara (:1121-1128)
+            if (vDotR < 0.0f) {
+                const float hB = 0.5f * (hi + hj), cB = 0.5f * (csI + csJ), rB = 0.5f * (rhoI + rhoJ);
+                const float muIJ = (hB * vDotR) / (r2 + 0.01f * hB * hB);
+                piIJ = ((-1.0f * cB * muIJ + 2.0f * muIJ * muIJ) / rB) * (0.5f * (fBalI + fBalJ));
+            }
+            float tens = 0.0f;                                 // tensile correction (:1130-1142)
+            const float Rj = (pJ < 0.0f) ? (0.3f * (-pJ) * invRhoJ2) : 0.0f;
+            if (Ri + Rj > 0.0f) {
+                const float Hb = 0.5f * (Hi + Hj);
+                if (r < Hb) {
+                    const float qb = r / Hb, om = 1.0f - qb, om2 = om * om;
+                    const float fr = (om2 * om2 * (1.0f + 4.0f * qb)) * (1.0f / 0.6328125f);
+                    const float fr2 = fr * fr;
+                    tens = (Ri + Rj) * (fr2 * fr2);
+                }
+            }
+            const float iso = -mj * ((pOverRho2I + pJ * invRhoJ2) + piIJ + tens);
+            axS += iso * gx; ayS += iso * gy; azS += iso * gz;
+            duP += mj * vDotG;
+            duAv += 0.5f * mj * piIJ * vDotG;
+            duT += 0.5f * mj * tens * vDotG;
+            const float tXX = sXXi * invRhoI2 + b3.x * invRhoJ2, tYY = sYYi * invRhoI2 + b3.y * invRhoJ2;
+            const float tZZ = sZZi * invRhoI2 + b3.z * invRhoJ2, tXY = sXYi * invRhoI2 + b3.w * invRhoJ2;
+            const float tXZ = sXZi * invRhoI2 + b4.x * invRhoJ2, tYZ = sYZi * invRhoI2 + b4.y * invRhoJ2;
+            axS += mj * (tXX * gx + tXY * gy + tXZ * gz);      // deviatoric stress (:1161-1163)
+            ayS += mj * (tXY * gx + tYY * gy + tYZ * gz);
+            azS += mj * (tXZ * gx + tYZ * gy + tZZ * gz);
+            const float wx = -dvx, wy = -dvy, wz = -dvz;
+            duS += mj * ((sXXi * wx + sXYi * wy + sXZi * wz) * gx + (sXYi * wx + sYYi * wy + sYZi * wz) * gy +
+                         (sXZi * wx + sYZi * wy + sZZi * wz) * gz);
+            const float gxi = gI * dx, gyi = gI * dy, gzi = gI * dz;   // velocity gradient (:1173-1179)
+            gXX += volJ * wx * gxi; gXY += volJ * wx * gyi; gXZ += volJ * wx * gzi;
+            gYX += volJ * wy * gxi; gYY += volJ * wy * gyi; gYZ += volJ * wy * gzi;
+            gZX += volJ * wz * gxi; gZY += volJ * wz * gyi; gZZ += volJ * wz * gzi;
+        });
+    }
+    p.accX[i] += axS;                                          // sph_gravity.cu:1213-1218
+    p.accY[i] += ayS;
+    p.accZ[i] += azS;
+    const float diffMask = (__ldg(&p.shepardC[i]) > 0.85f) ? (1.0f - fSurf) : 0.0f;
+    p.drhoDt[i] = rhoI * drC + 0.05f * Hi * csI * diffMask * drD;
+    const float duStress = invRhoI2 * duS;
+
+    // Surface radiative cooling (sph_gravity.cu:1222-1235), in FP32: every
+    // quantity stays far inside the float range (area <~1e13 m^2, T^4 <~1e20).
+    const bool livingIntact = livingFlags[1] != 0u;
+    const float tAmb = (livingIntact && __ldg(&p.bodyId[i]) == 0u && damI < 0.8f) ? 255.0f : 3.0f;
+    const float mSi = fmaxf(mi * 1.0e24f, 1.0f);
+    const float rhoSi = fmaxf(rhoI * 1.0e6f, 1.0e-3f);
+    const float rP = cbrtf((3.0f * mSi) / (4.0f * kPiF * rhoSi));
+    const float area = kPiF * rP * rP;
+    const float T4 = tempI * tempI * tempI * tempI;
+    const float Ta4 = tAmb * tAmb * tAmb * tAmb;
+    const float dT4 = fmaxf(0.0f, T4 - Ta4);
+    const float pRad = fSurf * 0.9f * 5.670374419e-8f * area * dT4;
+    p.radPowerW[i] = pRad;
+    const float duRad = -pRad / (fmaxf(mi, 1.0e-30f) * 1.0e27f);
+    p.duDt[i] = pOverRho2I * duP + duAv + duT + duStress + duRad;
+
+    // Jaumann stress rate + Grady-Kipp damage (sph_gravity.cu:1239-1286).
+    const MatConst& st = c_mat[matIndex(static_cast<uint8_t>(matI))];
+    if (st.muShear <= 0.0f || st.tMelt <= 0.0f) {
+        p.dSXX[i] = 0.f; p.dSYY[i] = 0.f; p.dSZZ[i] = 0.f; p.dSXY[i] = 0.f; p.dSXZ[i] = 0.f; p.dSYZ[i] = 0.f;
+        p.dDamageCbrtDt[i] = 0.0f;
+        return;
+    }
+    const float tNorm = tempI / st.tMelt;
+    const float soft = fmaxf(0.0f, 1.0f - tNorm * tNorm);
+    const float muEff = (1.0f - damI) * st.muShear * soft;
+    const float tr3 = (gXX + gYY + gZZ) * (1.0f / 3.0f);
+    const float eXX = gXX - tr3, eYY = gYY - tr3, eZZ = gZZ - tr3;
+    const float eXY = 0.5f * (gXY + gYX), eXZ = 0.5f * (gXZ + gZX), eYZ = 0.5f * (gYZ + gZY);
+    const float rXY = 0.5f * (gXY - gYX), rXZ = 0.5f * (gXZ - gZX), rYZ = 0.5f * (gYZ - gZY);
+    const float rYX = -rXY, rZX = -rXZ, rZY = -rYZ;
+    p.dSXX[i] = 2.0f * muEff * eXX + 2.0f * (sXYi * rXY + sXZi * rXZ);
+    p.dSYY[i] = 2.0f * muEff * eYY + 2.0f * (sXYi * rYX + sYZi * rYZ);
+    p.dSZZ[i] = 2.0f * muEff * eZZ + 2.0f * (sXZi * rZX + sYZi * rZY);
+    p.dSXY[i] = 2.0f * muEff * eXY + sXXi * rYX + sXZi * rYZ + sYYi * rXY + sYZi * rXZ;
+    p.dSXZ[i] = 2.0f * muEff * eXZ + sXXi * rZX + sXYi * rZY + sZZi * rXZ + sYZi * rXY;
+    p.dSYZ[i] = 2.0f * muEff * eYZ + sXYi * rZX + sYYi * rZY + sXZi * rYX + sZZi * rYZ;
+    if (tempI < st.tMelt && damI < 1.0f) {
+        const float sigmaMax = maxPrincipalStress(pI, sXXi, sYYi, sZZi, sXYi, sXZi, sYZi);
+        const float stiff = fmaxf(st.bulkK + (4.0f / 3.0f) * st.muShear, 1.0e-12f);
+        const float epsT = fmaxf(0.0f, sigmaMax) / stiff;
+        const float epsF = fmaxf(__ldg(&p.epsFail[i]), 1.0e-8f);
+        const float cCrack = fmaxf(csI, sqrtf((st.bulkK + (4.0f / 3.0f) * st.muShear) / rhoI));
+        p.dDamageCbrtDt[i] = (epsT > epsF) ? (0.4f * cCrack / hi) : 0.0f;
+    } else {
+        p.dDamageCbrtDt[i] = 0.0f;
+    }
+    (void)pairs;
+}
+
+// ----------------------------------------------------------------- drift ---
+// XSPH position update (sph_gravity.cu:1376-1489).  Neighbour positions come
+// from the leaf records (the positions before this drift), so no thread reads
+// a position another thread is moving.  The position add is done in FP64.
+__global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, uint32_t n, const float* dtDev,
+                                                   float dtHost, bool useList, bool toScratch,
+                                                   uint32_t* boundsWords) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float mn[3] = {1.0e30f, 1.0e30f, 1.0e30f}, mx[3] = {-1.0e30f, -1.0e30f, -1.0e30f};
+    if (i < n) {
+        const float dt = (dtDev != nullptr) ? *dtDev : dtHost;
+        const float4 me = __ldg(&w.leafPM[i]);
+        const float4 vr = __ldg(&w.velRho[i]);
+        const float hi = fmaxf(__ldg(&p.h[i]), 1.0e-6f);
+        const float Hi = 2.0f * hi;
+        const float rhoI = fmaxf(vr.w, 1.0e-9f);
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        if (useList && n >= 2u) {
+            forEachCandidate(w, i, [&](uint32_t j) {
+                const float4 q = __ldg(&w.leafPM[j]);
+                const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
+                const float r2 = len2Exact(dx, dy, dz);
+                const float Hj = 2.0f * fmaxf(__ldg(&p.h[j]), 1.0e-6f);
+                const float Hm = fmaxf(Hi, Hj);
+                if (!(r2 < __fmul_rn(Hm, Hm))) return;
+                const float4 vj = __ldg(&w.velRho[j]);
+                const float r = sqrtf(r2);
+                const float wb = 0.5f * (wendlandC2(r, Hi) + wendlandC2(r, Hj));
+                const float rb = 0.5f * (rhoI + fmaxf(vj.w, 1.0e-9f));
+                const float co = (q.w / rb) * wb;
+                sx += co * (vj.x - vr.x);
+                sy += co * (vj.y - vr.y);
+                sz += co * (vj.z - vr.z);
+            });
+        }
+        const double d = static_cast<double>(dt);
+        const float nx = static_cast<float>(static_cast<double>(me.x) + d * (static_cast<double>(vr.x) + 0.25 * static_cast<double>(sx)));
+        const float ny = static_cast<float>(static_cast<double>(me.y) + d * (static_cast<double>(vr.y) + 0.25 * static_cast<double>(sy)));
+        const float nz = static_cast<float>(static_cast<double>(me.z) + d * (static_cast<double>(vr.z) + 0.25 * static_cast<double>(sz)));
+        if (toScratch) {
+            w.driftPos[i] = make_float4(nx, ny, nz, 0.0f);
+        } else {
+            p.posX[i] = nx; p.posY[i] = ny; p.posZ[i] = nz;
+        }
+        mn[0] = mx[0] = nx; mn[1] = mx[1] = ny; mn[2] = mx[2] = nz;
+    }
+    if (boundsWords != nullptr) blockBoundsToWords(mn, mx, boundsWords);
+}
+
+inline unsigned gridFor(uint32_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
+
+}  // namespace
+
+cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t groups = (n + 31u) / 32u;
+    uint32_t* counter = w.words + kWNbrCounter;
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    int perSm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, buildNeighborsKernel, kNbWarps * 32, 0);
+    if (e != cudaSuccess) return e;
+    const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(std::max(1, perSm) * sms),
+                                               (groups + kNbWarps - 1) / kNbWarps);
+    buildNeighborsKernel<<<blocks, kNbWarps * 32, 0, st>>>(w, n, groups, counter);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPass1(const AstraeaParticles& p, const Work& w, uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    pass1Kernel<<<gridFor(n, 128), 128, 0, st>>>(p, w, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPass2(const AstraeaParticles& p, const Work& w, uint32_t n, const uint32_t* livingFlags,
+                        cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    pass2Kernel<<<gridFor(n, 128), 128, 0, st>>>(p, w, n, livingFlags);
+    return cudaGetLastError();
+}
+
+cudaError_t launchDrift(const AstraeaParticles& p, const Work& w, uint32_t n, const float* dtDev, float dtHost,
+                        bool useList, bool toScratch, uint32_t* boundsWords, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    driftKernel<<<gridFor(n, 128), 128, 0, st>>>(p, w, n, dtDev, dtHost, useList, toScratch, boundsWords);
+    return cudaGetLastError();
+}
+
+}  // namespace astraea_gb300

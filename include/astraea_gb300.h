@@ -1,0 +1,235 @@
+/*
+ * astraea_gb300.h -- C-ABI of the GB300-native ASTRAEA per-step physics path.
+ *
+ * Every entry point here replaces one function of the ASTRAEA engine's kernel
+ * interface `astraea::cuda::*` declared in engine/sph_gravity.cuh:61-92 and
+ * implemented in engine/sph_gravity.cu.  The structs mirror the engine's
+ * particle SoA descriptor `astraea::ParticleBuffersDevice`
+ * (engine/types.hpp:114-161) and `astraea::cuda::RadixBvhDevice`
+ * (engine/sph_gravity.cuh:26-59) field for field, so a caller can pass the
+ * engine's own structs by pointer (the C++ shim in
+ * astraea-impact-sim_gb300/csrc/shim does exactly that).
+ *
+ * Conventions
+ *   - Every function returns an AstraeaStatus; 0 is success.  On failure
+ *     astraea_gb300_last_error() returns a message (thread-local).
+ *   - Work is enqueued on the stream set by astraea_gb300_set_stream
+ *     (default: the legacy default stream, as the engine uses).
+ *   - count == 0 is a no-op for every launch, as in the engine.
+ *   - Pointers are device pointers unless a parameter says "host".
+ */
+#ifndef ASTRAEA_GB300_H
+#define ASTRAEA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASTRAEA_GB300_ABI_VERSION 1
+
+typedef enum AstraeaStatus {
+    ASTRAEA_OK = 0,
+    ASTRAEA_ERR_CUDA = 1,          /* a CUDA runtime call failed */
+    ASTRAEA_ERR_CAPACITY = 2,      /* buffers smaller than the particle count */
+    ASTRAEA_ERR_INVALID = 3,       /* bad argument (null pointer, bad size) */
+    ASTRAEA_ERR_DEVICE_TIMEOUT = 4,/* a bounded device-side wait gave up */
+    ASTRAEA_ERR_DEVICE_STATE = 5   /* device status word reported a fault */
+} AstraeaStatus;
+
+typedef struct AstraeaFloat4 { float x, y, z, w; } AstraeaFloat4;
+
+/* Particle SoA; same member order and types as ParticleBuffersDevice
+ * (engine/types.hpp:114-161): 2 x u32 then 56 device pointers. */
+typedef struct AstraeaParticles {
+    uint32_t capacity;
+    uint32_t count;
+    float* posX;      float* posY;      float* posZ;
+    float* velX;      float* velY;      float* velZ;
+    float* velHalfX;  float* velHalfY;  float* velHalfZ;
+    float* accX;      float* accY;      float* accZ;
+    float* mass;
+    float* h;
+    float* h0;
+    float* rho;
+    float* drhoDt;
+    float* pressure;
+    float* soundSpeed;
+    float* u;
+    float* duDt;
+    float* tempK;
+    float* radPowerW;
+    float* sXX; float* sYY; float* sZZ;
+    float* sXY; float* sXZ; float* sYZ;
+    float* dSXX; float* dSYY; float* dSZZ;
+    float* dSXY; float* dSXZ; float* dSYZ;
+    float* damage;
+    float* damageCbrt;
+    float* dDamageCbrtDt;
+    float* epsFail;
+    float* divV;
+    float* curlVX; float* curlVY; float* curlVZ;
+    float* shepardC;
+    float* surfFactor;
+    float* phiGrav;
+    uint8_t*  materialId;
+    uint8_t*  phaseId;
+    uint8_t*  bodyId;
+    uint32_t* originalId;
+    int32_t*  tracerIndex;
+    float* tracerRestRadiusPsu;
+    float* tracerRestNormalX;
+    float* tracerRestNormalY;
+    float* tracerRestNormalZ;
+    uint8_t* tracerIsOcean;
+} AstraeaParticles;
+
+/* Linear BVH descriptor; same member order and types as RadixBvhDevice
+ * (engine/sph_gravity.cuh:26-59).  Internal nodes are [0, N-2], leaves are
+ * node-array entries [N-1, 2N-2]; a child value < 0 encodes leaf ~child. */
+typedef struct AstraeaRadixBvh {
+    uint32_t  capacity;
+    uint64_t* mortonCodes;
+    uint64_t* mortonCodesSorted;
+    uint32_t* indicesIn;
+    uint32_t* indicesSorted;
+    int32_t*  leftChild;
+    int32_t*  rightChild;
+    int32_t*  parent;
+    uint32_t* atomicVisited;
+    float* aabbMinX; float* aabbMinY; float* aabbMinZ;
+    float* aabbMaxX; float* aabbMaxY; float* aabbMaxZ;
+    float* nodeMass;
+    float* comX; float* comY; float* comZ;
+    float* nodeMaxH;
+    void*  cubTempStorage;   /* unused by this library; kept for layout */
+    size_t cubTempBytes;     /* unused by this library; kept for layout */
+    uint32_t* sceneBoundsOrdered;
+    float*    sceneBoundsFloat;
+    uint32_t* livingFlags;
+    AstraeaFloat4* nodeComMass;     /* {comX, comY, comZ, mass}  */
+    AstraeaFloat4* nodeMinExtent;   /* {minX, minY, minZ, dNode} */
+    AstraeaFloat4* nodeMaxHPacked;  /* {maxX, maxY, maxZ, maxH}  */
+} AstraeaRadixBvh;
+
+/* ---- library / runtime ------------------------------------------------ */
+
+/* Thread-local message for the last non-OK status (never NULL). */
+const char* astraea_gb300_last_error(void);
+/* ABI version of the loaded library (ASTRAEA_GB300_ABI_VERSION). */
+int astraea_gb300_abi_version(void);
+/* Stream for all subsequent launches from any thread (a cudaStream_t, or
+ * NULL for the legacy default stream, which is the engine's behaviour). */
+AstraeaStatus astraea_gb300_set_stream(void* stream);
+
+/* ---- allocation (engine/sph_gravity.cu:1806-1984) ---------------------- */
+
+/* Replaces allocateRadixBvh (engine/sph_gravity.cu:1806-1855). */
+AstraeaStatus astraea_gb300_allocate_radix_bvh(AstraeaRadixBvh* bvh, uint32_t capacity);
+/* Replaces freeRadixBvh (engine/sph_gravity.cu:1857-1893). */
+AstraeaStatus astraea_gb300_free_radix_bvh(AstraeaRadixBvh* bvh);
+/* Replaces allocateParticleBuffers (engine/sph_gravity.cu:1895-1941). */
+AstraeaStatus astraea_gb300_allocate_particle_buffers(AstraeaParticles* p, uint32_t capacity);
+/* Replaces freeParticleBuffers (engine/sph_gravity.cu:1943-1984). */
+AstraeaStatus astraea_gb300_free_particle_buffers(AstraeaParticles* p);
+
+/* ---- the per-step stages (engine/sph_gravity.cu:1988-2161) -------------- */
+
+/* Replaces launchClearStats (engine/sph_gravity.cu:1988-1994). */
+AstraeaStatus astraea_gb300_clear_stats(AstraeaParticles* p);
+/* Replaces launchSortAndBuildBvh (engine/sph_gravity.cu:1996-2061): scene
+ * AABB, 63-bit Morton codes, stable radix sort (value = original index),
+ * 56-field permutation into alt, pointer swap p<->alt (both structs are
+ * modified), Karras LBVH, bottom-up refit. */
+AstraeaStatus astraea_gb300_sort_and_build_bvh(AstraeaParticles* p, AstraeaParticles* alt,
+                                               AstraeaRadixBvh* bvh);
+/* Replaces launchSphPass1Neighbors (engine/sph_gravity.cu:2063-2074). */
+AstraeaStatus astraea_gb300_sph_pass1_neighbors(AstraeaParticles* p, const AstraeaRadixBvh* bvh);
+/* Replaces launchEvaluateEos (engine/sph_gravity.cu:2076-2083). */
+AstraeaStatus astraea_gb300_evaluate_eos(AstraeaParticles* p);
+/* Replaces launchGravityBarnesHut (engine/sph_gravity.cu:2085-2097). */
+AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const AstraeaRadixBvh* bvh,
+                                               float theta);
+/* Replaces launchSphPass2Forces (engine/sph_gravity.cu:2099-2111). */
+AstraeaStatus astraea_gb300_sph_pass2_forces(AstraeaParticles* p, const AstraeaRadixBvh* bvh);
+/* Replaces launchLeapfrogKickHalf (engine/sph_gravity.cu:2113-2120). */
+AstraeaStatus astraea_gb300_leapfrog_kick_half(AstraeaParticles* p, float halfDtPsu,
+                                               int includeXsph, int clampThermal);
+/* Replaces launchLeapfrogDrift (engine/sph_gravity.cu:2122-2134).  Unlike the
+ * engine kernel (which reads neighbour positions while other threads move
+ * them), neighbours are read from the pre-drift positions. */
+AstraeaStatus astraea_gb300_leapfrog_drift(AstraeaParticles* p, float dtPsu,
+                                           const AstraeaRadixBvh* bvh);
+/* Replaces launchReduceDtPsu (engine/sph_gravity.cu:2136-2161); blocks until
+ * the result is on the host and writes it to *outDtPsu (host pointer).  Also
+ * returns ASTRAEA_ERR_DEVICE_TIMEOUT when a bounded device wait gave up since
+ * the last astraea_gb300_reset_device_status. */
+AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevDtPsu,
+                                          float maxDtPsu, float* outDtPsu);
+
+/* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
+
+/* One Simulation::step() kernel sequence (engine/simulation.cpp:1711-1753):
+ * reduce-dt, kick(dt/2), drift, sort+build, pass 1, EOS, gravity(theta),
+ * pass 2, kick(dt/2), EOS -- with dt kept on the device (no host round
+ * trip) and one neighbour list per step shared by pass 1, pass 2 and the
+ * next step's drift.  The previous step's dt is kept on the device between
+ * calls on the same BVH; prevDtPsu is used only when no such state exists
+ * (first call, or after astraea_gb300_invalidate_step_cache), exactly as the
+ * engine passes Simulation::prevDtPsu to launchReduceDtPsu.  *outDtPsu (host,
+ * may be NULL) receives this step's dt once the stream reaches the end of the
+ * step (pinned memory: asynchronous; pageable memory: the copy blocks).
+ * Needs one astraea_gb300_sort_and_build_bvh on this BVH beforehand (the
+ * engine's evaluateInitialForcesOnDevice does that).  Fields the engine's
+ * permutation moves but the step recomputes before reading (forces, rates,
+ * EOS outputs, pass-1 outputs) are not moved.  After writing positions or h
+ * from outside the library between steps, call
+ * astraea_gb300_invalidate_step_cache. */
+AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh,
+                                 float prevDtPsu, float maxDtPsu, float theta, float* outDtPsu);
+/* Forget the neighbour lists and device-side dt kept between fused steps. */
+AstraeaStatus astraea_gb300_invalidate_step_cache(const AstraeaRadixBvh* bvh);
+/* Pre-allocate every library-owned scratch buffer for `capacity` particles on
+ * the current device, so later calls allocate nothing (stream capture). */
+AstraeaStatus astraea_gb300_reserve(const AstraeaRadixBvh* bvh, uint32_t capacity);
+
+/* Release the library scratch kept for this BVH (its neighbour lists and
+ * packed node records) without touching the BVH's own arrays; for callers
+ * that allocate and free the BVH arrays themselves.  No engine counterpart
+ * (the engine's fallback scratch lives until process exit). */
+AstraeaStatus astraea_gb300_release_scratch(const AstraeaRadixBvh* bvh);
+
+/* ---- library primitives and diagnostics --------------------------------- */
+
+/* Stable LSD radix sort of (u64 key, u32 value) pairs over key bits
+ * [0, endBit), endBit <= 64; the call site it replaces is
+ * cub::DeviceRadixSort::SortPairs in engine/sph_gravity.cu:2029-2046.
+ * keysIn/valsIn are used as ping-pong buffers and are clobbered; the sorted
+ * pairs land in keysOut/valsOut. */
+AstraeaStatus astraea_gb300_radix_sort_pairs(uint64_t* keysIn, uint64_t* keysOut,
+                                             uint32_t* valsIn, uint32_t* valsOut,
+                                             uint32_t n, int endBit);
+/* Device status word (bit flags, see ASTRAEA_DEVFLAG_*) and counters
+ * accumulated since the last reset; host pointers, 8 x u64 counters. */
+#define ASTRAEA_DEVFLAG_LOOKBACK_TIMEOUT   0x1u
+#define ASTRAEA_DEVFLAG_NEIGHBOR_OVERFLOW  0x2u
+#define ASTRAEA_DEVFLAG_STACK_OVERFLOW     0x4u
+#define ASTRAEA_DEVFLAG_GROUP_FALLBACK     0x8u
+AstraeaStatus astraea_gb300_read_device_status(uint32_t* outFlags, uint64_t* outCounters8);
+AstraeaStatus astraea_gb300_reset_device_status(void);
+/* Test hook: lower the onesweep look-back spin limit (0 restores default). */
+AstraeaStatus astraea_gb300_set_lookback_spin_limit(uint32_t limit);
+/* Failure-detection probe: runs the onesweep look-back wait on a status word
+ * that nothing publishes, with the given spin limit.  The wait must give up:
+ * returns ASTRAEA_ERR_DEVICE_TIMEOUT, *outResult = 2 and sets
+ * ASTRAEA_DEVFLAG_LOOKBACK_TIMEOUT in the device status (no GPU fault, the
+ * context stays usable).  No engine counterpart. */
+AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASTRAEA_GB300_H */

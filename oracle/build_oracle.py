@@ -1,0 +1,66 @@
+"""Build recipe for the oracle (TEST INFRASTRUCTURE ONLY).
+
+* oracle/_build/liboracle.so -- the CPU restatement in oracle/oracle.cpp,
+  compiled with OpenMP and with multiply-add contraction off
+  (-ffp-contract=off) so its float arithmetic rounds like the reference
+  expressions it restates, on x86_64 and aarch64 alike.
+* oracle/_ref/libref_eos.so -- the reference's own engine/eos.cu compiled as
+  host C++ from the reference checkout where it lies (only when that checkout
+  exists; it is absent on GPU machines, which use the committed golden
+  vectors instead).  Nothing of the reference is copied into this tree.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+REFERENCE_ENGINE = os.environ.get("ASTRAEA_REFERENCE_ENGINE", "/root/reference/engine")
+
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def _run(cmd):
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), res.stdout, res.stderr))
+
+
+def _stale(out, srcs):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_oracle(force=False):
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "liboracle.so")
+    srcs = [os.path.join(HERE, "oracle.cpp"), os.path.join(ROOT, "include", "astraea_gb300.h")]
+    if force or _stale(out, srcs):
+        tmp = out + ".tmp%d" % os.getpid()
+        _run(["g++"] + CXXFLAGS + ["-fopenmp", "-I", os.path.join(ROOT, "include"), srcs[0], "-o", tmp])
+        os.replace(tmp, out)
+    return out
+
+
+def build_reference_eos(force=False):
+    """Compile the reference EOS as host C++; returns the path or None."""
+    eos_cu = os.path.join(REFERENCE_ENGINE, "eos.cu")
+    if not os.path.exists(eos_cu):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libref_eos.so")
+    shim = os.path.join(HERE, "ref_eos_capi.cpp")
+    if force or _stale(out, [eos_cu, shim]):
+        tmp = out + ".tmp%d" % os.getpid()
+        _run(["g++"] + CXXFLAGS + ["-I", REFERENCE_ENGINE, "-x", "c++", eos_cu, "-x", "none", shim, "-o", tmp])
+        os.replace(tmp, out)
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="--force" in sys.argv))
+    print(build_reference_eos(force="--force" in sys.argv))

@@ -1,0 +1,1073 @@
+// oracle.cpp -- CPU restatement of the ASTRAEA per-step physics path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the GB300 kernels
+// and the CPU baseline timed by bench.py; nothing in the product library links
+// or calls it.  It restates engine/sph_gravity.cu (the reference kernels) and
+// engine/eos.cu (the reference EOS) of Ananasjik/astraea-impact-sim function by
+// function, keeping the reference's floating-point expression order, its
+// warp-wide traversal semantics (groups of 32 consecutive sorted particles,
+// a node is opened for the whole group if any member needs it), and its
+// per-lane summation order (depth-first, left child first).  Compile with
+// -ffp-contract=off so no multiply-add is fused.
+//
+// Extra "truth" entry points evaluate the same physics in FP64: a direct-sum
+// gravity (the N^2 check of tests/cpp/test_gravity_sph.cpp:366-378) and the
+// SPH passes instantiated with double arithmetic.
+//
+// The particle and BVH descriptors are the C-ABI structs of
+// include/astraea_gb300.h, here holding HOST pointers.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "astraea_gb300.h"
+
+namespace {
+
+constexpr int kGroup = 32;            // warp width of the reference traversal
+constexpr int kStackSize = 192;       // engine/sph_gravity.cu:22
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr double kPiD = 3.14159265358979323846;
+constexpr float kGPsuF = 66.7430f;    // engine/units.hpp:27 (float of G_PSU)
+constexpr double kGPsuD = 6.67430e-11 * 1.0e24 * 1.0e3 * 1.0e3 / (1.0e6 * 1.0e6 * 1.0e6);
+constexpr double kSigmaSB = 5.670374419e-8;   // engine/units.hpp:6
+
+// ---------------------------------------------------------------- EOS ----
+// Restates engine/eos.cu.  Table values are the published constants in
+// engine/eos.cu:10-116 (Tillotson 1962 / Melosh 1989, Benz & Asphaug 1999,
+// Allen 1967, polytrope n=1, Jutzi 2008).
+struct MatParams {
+    double rho0, a, b, A, B, E0, Eiv, Ecv, alpha, beta, cv, tMelt, tRef, mu, Y0, epsFailMin, kH2, gamma;
+};
+const MatParams kMat[5] = {
+    {7800.0, 0.5, 1.5, 1.28e11, 1.05e11, 9.50e6, 2.40e6, 8.67e6, 5.0, 5.0, 449.0, 1811.0, 293.0, 7.70e10, 6.80e8, 1.0e-3, 0.0, 1.0},
+    {2680.0, 0.5, 1.3, 1.80e10, 1.80e10, 1.60e7, 3.50e6, 1.80e7, 5.0, 5.0, 790.0, 1600.0, 293.0, 2.20e10, 3.50e9, 1.0e-4, 0.0, 1.0},
+    {1000.0, 0.7, 0.15, 2.18e9, 1.325e10, 7.00e6, 4.19e5, 2.68e6, 10.0, 5.0, 4184.0, 273.15, 273.15, 3.50e9, 1.00e7, 5.0e-4, 0.0, 1.0},
+    {0.178, 0.4, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 8260.0, 0.0, 0.0, 0.0, 0.0, 1.0, 2.08e5, 1.4},
+    {2000.0, 0.5, 1.3, 1.20e10, 1.20e10, 1.60e7, 3.50e6, 1.80e7, 5.0, 5.0, 800.0, 1500.0, 293.0, 8.00e9, 5.00e7, 5.0e-5, 0.0, 1.0},
+};
+constexpr int kHH = 3;
+
+inline int matIndex(int m) { return (m < 0 || m > 4) ? 1 : m; }   // eos.cu:271-275
+
+// engine/eos.cu:283-318
+double coldEnergy(int mat, double rho) {
+    const MatParams& p = kMat[matIndex(mat)];
+    rho = rho > 0.0 ? rho : 0.0;
+    if (matIndex(mat) == kHH) return p.kH2 * rho;
+    const double rho0 = p.rho0 / 1.0e6;
+    const double eta = rho / rho0;
+    if (eta <= 1.0) return 0.0;
+    const double mu = eta - 1.0;
+    const double A = p.A / 1.0e12, B = p.B / 1.0e12;
+    double ta, tb;
+    if (mu < 1.0e-5) {
+        const double m2 = mu * mu, m3 = m2 * mu, m4 = m3 * mu, m5 = m4 * mu;
+        ta = 0.5 * m2 - (2.0 / 3.0) * m3 + 0.75 * m4 - 0.8 * m5;
+        tb = (1.0 / 3.0) * m3 - 0.5 * m4 + 0.6 * m5;
+    } else {
+        const double le = std::log1p(mu);
+        ta = le - (mu / eta);
+        tb = (mu * (2.0 + mu)) / eta - 2.0 * le;
+    }
+    return (A * ta + B * tb) / rho0;
+}
+
+struct PDeriv { double p, dpdrho, dpdu; bool damagedTension; };
+
+// engine/eos.cu:136-176 (compressed / cold branch)
+PDeriv tillotsonCompressed(const MatParams& p, double rho, double rho0, double eta, double mu, double uE, double dmg) {
+    const double A = p.A / 1.0e12, B = p.B / 1.0e12, E0 = p.E0 / 1.0e6;
+    const double bEff = (mu >= 0.0) ? B : 0.0;
+    const double den = E0 * eta * eta;
+    const double ratio = (den > 1.0e-30) ? (uE / den) : 1.0e30;
+    const double w = ratio + 1.0;
+    const double iw = 1.0 / w;
+    const double wm1w2 = (ratio > 1.0e15) ? 0.0 : (ratio * iw * iw);
+    PDeriv r;
+    r.p = (p.a + p.b * iw) * rho * uE + A * mu + bEff * mu * mu;
+    r.dpdrho = (p.a + p.b * iw) * uE + 2.0 * p.b * uE * wm1w2 + (A + 2.0 * bEff * mu) / rho0;
+    r.dpdu = (p.a + p.b * iw * iw) * rho;
+    r.damagedTension = false;
+    if (r.p < 0.0 && dmg > 0.0) {
+        const double keep = 1.0 - dmg;
+        r.p *= keep; r.dpdrho *= keep; r.dpdu *= keep;
+        r.damagedTension = true;
+    }
+    return r;
+}
+
+// engine/eos.cu:178-227 (expanded / hot branch)
+PDeriv tillotsonExpanded(const MatParams& p, double rho, double rho0, double eta, double mu, double uE) {
+    const double A = p.A / 1.0e12, E0 = p.E0 / 1.0e6;
+    const double x = 1.0 / eta - 1.0;
+    const double ax2 = p.alpha * x * x;
+    const double bx = p.beta * x;
+    const double eA = (ax2 < 700.0) ? std::exp(-ax2) : 0.0;
+    PDeriv r;
+    r.damagedTension = false;
+    if (eA == 0.0) {
+        r.p = p.a * rho * uE; r.dpdrho = p.a * uE; r.dpdu = p.a * rho;
+        return r;
+    }
+    const double eB = (bx < 700.0) ? std::exp(-bx) : 0.0;
+    const double den = E0 * eta * eta;
+    const double ratio = (den > 1.0e-30) ? (uE / den) : 1.0e30;
+    const double w = ratio + 1.0;
+    const double iw = 1.0 / w;
+    const double wm1w2 = (ratio > 1.0e15) ? 0.0 : (ratio * iw * iw);
+    const double ideal = p.a * rho * uE;
+    const double inner = (p.b * rho * uE * iw) + A * mu * eB;
+    const double pe = ideal + inner * eA;
+    const double r0r2 = rho0 / (rho * rho);
+    const double expDrho = (eB > 0.0) ? ((A / rho0 + A * mu * p.beta * r0r2) * eB) : 0.0;
+    r.p = pe;
+    r.dpdrho = p.a * uE + eA * (p.b * uE * iw + 2.0 * p.b * uE * wm1w2 + expDrho) + 2.0 * p.alpha * x * r0r2 * (pe - ideal);
+    r.dpdu = (p.a + p.b * eA * iw * iw) * rho;
+    return r;
+}
+
+// engine/eos.cu:229-267
+uint8_t phaseOf(int mat, const MatParams& p, double rho, double u, double T) {
+    mat = matIndex(mat);
+    if (mat == kHH) return (T > 10000.0) ? 3 : 5;
+    const double rhoKg = rho * 1.0e6;
+    const double ecv = p.Ecv / 1.0e6;
+    if (mat == 2) {
+        if (T > 15000.0) return 3;
+        if (u >= ecv || (T > 647.0 && rhoKg < 322.0)) return 2;
+        if (T >= 273.15) return 4;
+        return 0;
+    }
+    if (T > 12000.0) return 3;
+    if (u >= ecv && rhoKg < 0.8 * p.rho0) return 2;
+    if (T >= p.tMelt) return 1;
+    return 0;
+}
+
+struct EosOut { float p, cs, T; uint8_t phase; };
+
+// engine/eos.cu:320-388
+EosOut evaluateEos(int mat, float rhoIn, float uIn, float dIn) {
+    const int mi = matIndex(mat);
+    const MatParams& p = kMat[mi];
+    const double rho = std::max(static_cast<double>(rhoIn), 1.0e-12);
+    const double u = static_cast<double>(uIn);
+    double dmg = static_cast<double>(dIn);
+    dmg = dmg < 0.0 ? 0.0 : (dmg > 1.0 ? 1.0 : dmg);
+    const double cv = p.cv / 1.0e6;
+    const double uCold = coldEnergy(mi, rho);
+    if (mi == kHH) {
+        const double uTh = std::max(0.0, u - uCold);
+        const double T = std::max(3.0, uTh / cv);
+        const double P = p.kH2 * rho * rho + (p.gamma - 1.0) * rho * uTh;
+        const double cs2 = 2.0 * p.kH2 * rho + p.gamma * (p.gamma - 1.0) * uTh;
+        const double cs = std::max(0.05, std::sqrt(std::max(0.0, cs2)));
+        return {static_cast<float>(P), static_cast<float>(cs), static_cast<float>(T), phaseOf(mi, p, rho, u, T)};
+    }
+    const double rho0 = p.rho0 / 1.0e6;
+    const double eta = rho / rho0;
+    const double mu = eta - 1.0;
+    const double T = std::max(3.0, (u - uCold) / cv);
+    const double uE = uCold + std::max(0.0, u - uCold - cv * p.tRef);
+    const double Eiv = p.Eiv / 1.0e6, Ecv = p.Ecv / 1.0e6, A = p.A / 1.0e12;
+    PDeriv r;
+    if (eta >= 1.0 || uE < Eiv) {
+        r = tillotsonCompressed(p, rho, rho0, eta, mu, uE, dmg);
+    } else if (uE >= Ecv) {
+        r = tillotsonExpanded(p, rho, rho0, eta, mu, uE);
+    } else {
+        const PDeriv c = tillotsonCompressed(p, rho, rho0, eta, mu, uE, dmg);
+        const PDeriv e = tillotsonExpanded(p, rho, rho0, eta, mu, uE);
+        const double den = std::max(1.0e-30, Ecv - Eiv);
+        double f = (uE - Eiv) / den;
+        f = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
+        r.p = (1.0 - f) * c.p + f * e.p;
+        r.dpdrho = (1.0 - f) * c.dpdrho + f * e.dpdrho;
+        r.dpdu = (1.0 - f) * c.dpdu + f * e.dpdu + (e.p - c.p) / den;
+        r.damagedTension = c.damagedTension;
+    }
+    const double cs2 = r.dpdrho + (r.p / (rho * rho)) * r.dpdu;
+    const bool condensed = (eta >= 1.0) || (uE < Eiv && rho >= 0.9 * rho0 && !r.damagedTension);
+    const double cMin = condensed ? std::max(0.05, std::sqrt(A / rho0)) : 0.05;
+    const double cs = std::max(cMin, std::sqrt(std::max(0.0, cs2)));
+    return {static_cast<float>(r.p), static_cast<float>(cs), static_cast<float>(T), phaseOf(mi, p, rho, u, T)};
+}
+
+// --------------------------------------------------- kernel constants ----
+// engine/sph_gravity.cu:27-73: u_ref = cv * 300 K, and the strength table.
+inline float u0RefPsu(int m) { return static_cast<float>((kMat[matIndex(m)].cv * 300.0) / 1.0e6); }
+struct Strength { float mu, tMelt, K, Y0; };
+inline Strength strengthOf(int m) {
+    switch (matIndex(m)) {
+        case 0: return {static_cast<float>(7.70e10 / 1e12), 1811.0f, static_cast<float>(1.28e11 / 1e12), static_cast<float>(6.80e8 / 1e12)};
+        case 1: return {static_cast<float>(2.20e10 / 1e12), 1600.0f, static_cast<float>(1.80e10 / 1e12), static_cast<float>(3.50e9 / 1e12)};
+        case 2: return {static_cast<float>(3.50e9 / 1e12), 273.15f, static_cast<float>(2.18e9 / 1e12), static_cast<float>(1.00e7 / 1e12)};
+        case 3: return {0.0f, 0.0f, 0.0f, 0.0f};
+        default: return {static_cast<float>(8.00e9 / 1e12), 1500.0f, static_cast<float>(1.20e10 / 1e12), static_cast<float>(5.00e7 / 1e12)};
+    }
+}
+
+// ------------------------------------------------------ small helpers ----
+inline uint32_t toOrdered(float f) {
+    uint32_t u; std::memcpy(&u, &f, 4);
+    const uint32_t mask = static_cast<uint32_t>(-static_cast<int32_t>(u >> 31)) | 0x80000000u;
+    return u ^ mask;
+}
+inline float fromOrdered(uint32_t u) {
+    const uint32_t mask = ((u >> 31) - 1u) | 0x80000000u;
+    u ^= mask; float f; std::memcpy(&f, &u, 4); return f;
+}
+inline uint64_t spread21(uint64_t v) {   // bit interleave, engine/sph_gravity.cu:151-159
+    v &= 0x1fffffULL;
+    v = (v | (v << 32)) & 0x001f00000000ffffULL;
+    v = (v | (v << 16)) & 0x001f0000ff0000ffULL;
+    v = (v | (v << 8)) & 0x100f00f00f00f00fULL;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
+    v = (v | (v << 2)) & 0x1249249249249249ULL;
+    return v;
+}
+inline int clz64(uint64_t x) { return x ? __builtin_clzll(x) : 64; }
+inline int clz32(uint32_t x) { return x ? __builtin_clz(x) : 32; }
+
+template <typename R> inline R wendland(R r, R H) {      // sph_gravity.cu:199-208
+    if (r >= H || H <= R(0)) return R(0);
+    const R q = r / H, omq = R(1) - q, omq2 = omq * omq;
+    const R norm = R(21) / (R(2) * R(kPiD) * H * H * H);
+    return norm * omq2 * omq2 * (R(1) + R(4) * q);
+}
+template <> inline float wendland<float>(float r, float H) {
+    if (r >= H || H <= 0.0f) return 0.0f;
+    const float q = r / H, omq = 1.0f - q, omq2 = omq * omq;
+    const float norm = 21.0f / (2.0f * kPiF * H * H * H);
+    return norm * omq2 * omq2 * (1.0f + 4.0f * q);
+}
+template <typename R> inline R wendlandGrad(R r, R H) {  // sph_gravity.cu:211-220
+    if (r >= H || H <= R(0)) return R(0);
+    const R q = r / H, omq = R(1) - q, H2 = H * H, H5 = H2 * H2 * H;
+    return -(R(210) / (R(kPiD) * H5)) * omq * omq * omq;
+}
+template <> inline float wendlandGrad<float>(float r, float H) {
+    if (r >= H || H <= 0.0f) return 0.0f;
+    const float q = r / H, omq = 1.0f - q, H2 = H * H, H5 = H2 * H2 * H;
+    return -(210.0f / (kPiF * H5)) * omq * omq * omq;
+}
+template <typename R> inline R balsara(R div, R cx, R cy, R cz, R cs, R h) {  // :222-228
+    const R ad = std::fabs(div);
+    const R ac = std::sqrt(cx * cx + cy * cy + cz * cz);
+    const R den = ad + ac + R(1.0e-4f) * std::max(cs, R(0.05f)) / std::max(h, R(1.0e-6f));
+    return ad / std::max(den, R(1.0e-30f));
+}
+inline float maxPrincipal(float P, float xx, float yy, float zz, float xy, float xz, float yz) {  // :230-254
+    const float p2 = xx * xx + yy * yy + zz * zz + 2.0f * (xy * xy + xz * xz + yz * yz);
+    if (p2 <= 1.0e-24f) return -P;
+    const float q = std::sqrt(p2 * (1.0f / 6.0f));
+    const float iq = 1.0f / q;
+    const float bxx = xx * iq, byy = yy * iq, bzz = zz * iq, bxy = xy * iq, bxz = xz * iq, byz = yz * iq;
+    const float det = bxx * (byy * bzz - byz * byz) - bxy * (bxy * bzz - byz * bxz) + bxz * (bxy * byz - byy * bxz);
+    const float r = std::min(1.0f, std::max(-1.0f, 0.5f * det));
+    const float phi = std::acos(r) * (1.0f / 3.0f);
+    return -P + 2.0f * q * std::cos(phi);
+}
+inline float pointBoxDist2(float px, float py, float pz, float mnx, float mny, float mnz, float mxx, float mxy, float mxz) {
+    const float dx = std::max(0.0f, std::max(mnx - px, px - mxx));
+    const float dy = std::max(0.0f, std::max(mny - py, py - mxy));
+    const float dz = std::max(0.0f, std::max(mnz - pz, pz - mxz));
+    return dx * dx + dy * dy + dz * dz;
+}
+inline float effPressure(float P, uint8_t phase) { return phase != 0 ? std::max(P, 0.0f) : P; }
+
+struct NodeBox { float mnx, mny, mnz, mxx, mxy, mxz, maxH, dNode, cx, cy, cz, m; };
+inline NodeBox nodeBox(const AstraeaRadixBvh& b, int c) {
+    NodeBox o;
+    o.mnx = b.aabbMinX[c]; o.mny = b.aabbMinY[c]; o.mnz = b.aabbMinZ[c];
+    o.mxx = b.aabbMaxX[c]; o.mxy = b.aabbMaxY[c]; o.mxz = b.aabbMaxZ[c];
+    o.maxH = b.nodeMaxH[c];
+    o.dNode = std::max(o.mxx - o.mnx, std::max(o.mxy - o.mny, o.mxz - o.mnz));
+    o.cx = b.comX[c]; o.cy = b.comY[c]; o.cz = b.comZ[c]; o.m = b.nodeMass[c];
+    return o;
+}
+
+int numGroups(uint32_t n) { return static_cast<int>((n + kGroup - 1) / kGroup); }
+
+// Depth-first walk shared by the SPH-style traversals: `open(c)` decides
+// whether the group descends into internal node c; `leaf(j)` visits particle
+// j.  The stack discipline (pop, left child then right child, push opened
+// internal children, drop pushes past kStackSize) is that of the reference
+// warp loops, e.g. engine/sph_gravity.cu:687-766.
+template <class Open, class Leaf>
+void walkGroup(const AstraeaRadixBvh& b, Open open, Leaf leaf) {
+    int stack[kStackSize];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        const int ch[2] = {b.leftChild[node], b.rightChild[node]};
+        for (int k = 0; k < 2; ++k) {
+            const int c = ch[k];
+            if (c < 0) {
+                leaf(static_cast<uint32_t>(~c));
+            } else if (open(c) && sp < kStackSize) {
+                stack[sp++] = c;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------- EOS API
+void oracle_eos_batch(uint32_t n, const uint8_t* mat, const float* rho, const float* u, const float* dmg,
+                      float* P, float* cs, float* T, uint8_t* phase) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) {
+        const EosOut r = evaluateEos(mat[i], rho[i], u[i], dmg[i]);
+        P[i] = r.p; cs[i] = r.cs; T[i] = r.T; phase[i] = r.phase;
+    }
+}
+double oracle_cold_energy(int mat, double rho) { return coldEnergy(mat, rho); }
+
+// --------------------------------------------------------- clear stats ----
+// engine/sph_gravity.cu:624-641
+void oracle_clear_stats(AstraeaParticles* p) {
+    for (uint32_t i = 0; i < p->count; ++i) {
+        p->accX[i] = p->accY[i] = p->accZ[i] = 0.0f;
+        p->drhoDt[i] = 0.0f; p->duDt[i] = 0.0f; p->radPowerW[i] = 0.0f;
+        p->dSXX[i] = p->dSYY[i] = p->dSZZ[i] = p->dSXY[i] = p->dSXZ[i] = p->dSYZ[i] = 0.0f;
+        p->dDamageCbrtDt[i] = 0.0f; p->divV[i] = 0.0f;
+        p->curlVX[i] = p->curlVY[i] = p->curlVZ[i] = 0.0f;
+        p->shepardC[i] = 1.0f; p->surfFactor[i] = 0.0f; p->phiGrav[i] = 0.0f;
+    }
+}
+
+// ------------------------------------------------------ bounds + Morton ----
+// engine/sph_gravity.cu:258-361 (min/max are order independent, so a serial
+// scan gives the same bounds as the block reduction + ordered-uint atomics).
+void oracle_scene_bounds(uint32_t n, const float* x, const float* y, const float* z, float* out6) {
+    uint32_t o[6] = {toOrdered(1.0e30f), toOrdered(1.0e30f), toOrdered(1.0e30f),
+                     toOrdered(-1.0e30f), toOrdered(-1.0e30f), toOrdered(-1.0e30f)};
+    float mn[3] = {1.0e30f, 1.0e30f, 1.0e30f}, mx[3] = {-1.0e30f, -1.0e30f, -1.0e30f};
+    for (uint32_t i = 0; i < n; ++i) {
+        mn[0] = std::fmin(mn[0], x[i]); mx[0] = std::fmax(mx[0], x[i]);
+        mn[1] = std::fmin(mn[1], y[i]); mx[1] = std::fmax(mx[1], y[i]);
+        mn[2] = std::fmin(mn[2], z[i]); mx[2] = std::fmax(mx[2], z[i]);
+    }
+    for (int k = 0; k < 3; ++k) {
+        o[k] = std::min(o[k], toOrdered(mn[k]));
+        o[3 + k] = std::max(o[3 + k], toOrdered(mx[k]));
+    }
+    for (int k = 0; k < 6; ++k) out6[k] = fromOrdered(o[k]);
+}
+
+void oracle_morton(uint32_t n, const float* x, const float* y, const float* z, const float* b6, uint64_t* codes) {
+    const float minX = b6[0], minY = b6[1], minZ = b6[2];
+    const float sx = b6[3] - minX, sy = b6[4] - minY, sz = b6[5] - minZ;
+    const float ix = (sx > 1.0e-6f) ? (2097151.0f / sx) : 0.0f;
+    const float iy = (sy > 1.0e-6f) ? (2097151.0f / sy) : 0.0f;
+    const float iz = (sz > 1.0e-6f) ? (2097151.0f / sz) : 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float fx = std::fmin(std::fmax((x[i] - minX) * ix, 0.0f), 2097151.0f);
+        const float fy = std::fmin(std::fmax((y[i] - minY) * iy, 0.0f), 2097151.0f);
+        const float fz = std::fmin(std::fmax((z[i] - minZ) * iz, 0.0f), 2097151.0f);
+        const uint64_t qx = static_cast<uint32_t>(fx), qy = static_cast<uint32_t>(fy), qz = static_cast<uint32_t>(fz);
+        codes[i] = (spread21(qx) << 2) | (spread21(qy) << 1) | spread21(qz);
+    }
+}
+
+// Stable sort by key (ties keep ascending input index), the semantics of
+// cub::DeviceRadixSort::SortPairs over bits [0, 63) used at
+// engine/sph_gravity.cu:2042-2046 (all Morton codes are < 2^63).
+void oracle_sort_pairs(uint32_t n, const uint64_t* keys, uint64_t* keysSorted, uint32_t* perm) {
+    std::vector<uint32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b]; });
+    for (uint32_t i = 0; i < n; ++i) { perm[i] = idx[i]; keysSorted[i] = keys[idx[i]]; }
+}
+
+// Karras 2012 binary radix tree, engine/sph_gravity.cu:173-187 + 477-528.
+static inline int deltaK(const uint64_t* c, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    if (c[i] != c[j]) return clz64(c[i] ^ c[j]);
+    return 64 + clz32(static_cast<uint32_t>(i) ^ static_cast<uint32_t>(j));
+}
+void oracle_karras(uint32_t nU, const uint64_t* codes, int32_t* left, int32_t* right, int32_t* parent) {
+    const int n = static_cast<int>(nU);
+    if (n == 1) { parent[0] = -1; return; }
+    for (int i = 0; i + 1 < n; ++i) {
+        const int d = (deltaK(codes, n, i, i + 1) - deltaK(codes, n, i, i - 1) >= 0) ? 1 : -1;
+        const int dMin = deltaK(codes, n, i, i - d);
+        int lmax = 2;
+        while (deltaK(codes, n, i, i + lmax * d) > dMin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (deltaK(codes, n, i, i + (l + t) * d) > dMin) l += t;
+        const int j = i + l * d;
+        const int dNode = deltaK(codes, n, i, j);
+        int s = 0, t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (deltaK(codes, n, i, i + (s + t) * d) > dNode) s += t;
+        } while (t > 1);
+        const int g = i + s * d + ((d < 0) ? d : 0);
+        const int first = std::min(i, j), last = std::max(i, j);
+        left[i] = (first == g) ? ~g : g;
+        right[i] = (last == g + 1) ? ~(g + 1) : (g + 1);
+        parent[(first == g) ? (n - 1 + g) : g] = i;
+        parent[(last == g + 1) ? (n - 1 + g + 1) : (g + 1)] = i;
+    }
+    parent[0] = -1;
+}
+
+// engine/sph_gravity.cu:363-430 (gather) + 1745-1784 (pointer swap).
+#define ORACLE_FIELDS_F32(X) X(posX) X(posY) X(posZ) X(velX) X(velY) X(velZ) X(velHalfX) X(velHalfY) X(velHalfZ) \
+    X(accX) X(accY) X(accZ) X(mass) X(h) X(h0) X(rho) X(drhoDt) X(pressure) X(soundSpeed) X(u) X(duDt) X(tempK)     \
+    X(radPowerW) X(sXX) X(sYY) X(sZZ) X(sXY) X(sXZ) X(sYZ) X(dSXX) X(dSYY) X(dSZZ) X(dSXY) X(dSXZ) X(dSYZ)          \
+    X(damage) X(damageCbrt) X(dDamageCbrtDt) X(epsFail) X(divV) X(curlVX) X(curlVY) X(curlVZ) X(shepardC)          \
+    X(surfFactor) X(phiGrav) X(tracerRestRadiusPsu) X(tracerRestNormalX) X(tracerRestNormalY) X(tracerRestNormalZ)
+#define ORACLE_FIELDS_OTHER(X) X(materialId) X(phaseId) X(bodyId) X(originalId) X(tracerIndex) X(tracerIsOcean)
+
+void oracle_permute_swap(AstraeaParticles* p, AstraeaParticles* alt, const uint32_t* perm) {
+    const uint32_t n = p->count;
+#define GATHER(f) for (uint32_t i = 0; i < n; ++i) alt->f[i] = p->f[perm[i]];
+    ORACLE_FIELDS_F32(GATHER) ORACLE_FIELDS_OTHER(GATHER)
+#undef GATHER
+#define SWAP(f) std::swap(p->f, alt->f);
+    ORACLE_FIELDS_F32(SWAP) ORACLE_FIELDS_OTHER(SWAP)
+#undef SWAP
+    alt->count = p->count;
+}
+
+// Leaf init + bottom-up refit in FP32, engine/sph_gravity.cu:440-475, 531-620.
+// A serial post-order pass computes exactly what the atomic second-arrival
+// scheme computes (each node combines its two finished children once).
+void oracle_refit(const AstraeaParticles* p, AstraeaRadixBvh* b, uint32_t* livingFlags) {
+    const uint32_t n = p->count;
+    livingFlags[0] = livingFlags[1] = 0u;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t L = n - 1 + i;
+        const float x = p->posX[i], y = p->posY[i], z = p->posZ[i], m = p->mass[i], H = 2.0f * p->h[i];
+        b->aabbMinX[L] = b->aabbMaxX[L] = x; b->aabbMinY[L] = b->aabbMaxY[L] = y; b->aabbMinZ[L] = b->aabbMaxZ[L] = z;
+        b->nodeMass[L] = m; b->comX[L] = x; b->comY[L] = y; b->comZ[L] = z; b->nodeMaxH[L] = H;
+        if (p->tracerIndex[i] >= 0) {
+            livingFlags[0] = 1u;
+            if (p->damage[i] < 0.8f) livingFlags[1] = 1u;
+        }
+    }
+    if (n < 2) return;
+    // iterative post-order over internal nodes
+    std::vector<int> order;
+    order.reserve(n);
+    std::vector<int> st;
+    st.push_back(0);
+    while (!st.empty()) {
+        const int v = st.back(); st.pop_back();
+        order.push_back(v);
+        if (b->leftChild[v] >= 0) st.push_back(b->leftChild[v]);
+        if (b->rightChild[v] >= 0) st.push_back(b->rightChild[v]);
+    }
+    for (auto it = order.rbegin(); it != order.rend(); ++it) {
+        const int v = *it;
+        const int lc = b->leftChild[v], rc = b->rightChild[v];
+        const int l = lc < 0 ? static_cast<int>(n - 1) + ~lc : lc;
+        const int r = rc < 0 ? static_cast<int>(n - 1) + ~rc : rc;
+        const float mnx = std::fmin(b->aabbMinX[l], b->aabbMinX[r]);
+        const float mny = std::fmin(b->aabbMinY[l], b->aabbMinY[r]);
+        const float mnz = std::fmin(b->aabbMinZ[l], b->aabbMinZ[r]);
+        const float mxx = std::fmax(b->aabbMaxX[l], b->aabbMaxX[r]);
+        const float mxy = std::fmax(b->aabbMaxY[l], b->aabbMaxY[r]);
+        const float mxz = std::fmax(b->aabbMaxZ[l], b->aabbMaxZ[r]);
+        const float mh = std::fmax(b->nodeMaxH[l], b->nodeMaxH[r]);
+        const float ml = b->nodeMass[l], mr = b->nodeMass[r], ms = ml + mr;
+        float cx, cy, cz;
+        if (ms > 0.0f) {
+            const float im = 1.0f / ms;
+            cx = (ml * b->comX[l] + mr * b->comX[r]) * im;
+            cy = (ml * b->comY[l] + mr * b->comY[r]) * im;
+            cz = (ml * b->comZ[l] + mr * b->comZ[r]) * im;
+        } else {
+            cx = 0.5f * (b->comX[l] + b->comX[r]);
+            cy = 0.5f * (b->comY[l] + b->comY[r]);
+            cz = 0.5f * (b->comZ[l] + b->comZ[r]);
+        }
+        b->aabbMinX[v] = mnx; b->aabbMinY[v] = mny; b->aabbMinZ[v] = mnz;
+        b->aabbMaxX[v] = mxx; b->aabbMaxY[v] = mxy; b->aabbMaxZ[v] = mxz;
+        b->nodeMaxH[v] = mh; b->nodeMass[v] = ms; b->comX[v] = cx; b->comY[v] = cy; b->comZ[v] = cz;
+    }
+}
+
+// Whole launchSortAndBuildBvh (engine/sph_gravity.cu:1996-2061) on host
+// arrays; bvh must hold host arrays of the reference sizes.
+void oracle_sort_and_build(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* b, float* bounds6Out) {
+    const uint32_t n = p->count;
+    if (n == 0) return;
+    float b6[6];
+    oracle_scene_bounds(n, p->posX, p->posY, p->posZ, b6);
+    if (bounds6Out) std::memcpy(bounds6Out, b6, sizeof(b6));
+    oracle_morton(n, p->posX, p->posY, p->posZ, b6, b->mortonCodes);
+    for (uint32_t i = 0; i < n; ++i) b->indicesIn[i] = i;
+    oracle_sort_pairs(n, b->mortonCodes, b->mortonCodesSorted, b->indicesSorted);
+    oracle_permute_swap(p, alt, b->indicesSorted);
+    oracle_karras(n, b->mortonCodesSorted, b->leftChild, b->rightChild, b->parent);
+    uint32_t lf[2];
+    oracle_refit(p, b, lf);
+    if (b->livingFlags) { b->livingFlags[0] = lf[0]; b->livingFlags[1] = lf[1]; }
+}
+
+// ------------------------------------------------------------ SPH pass 1 ----
+// engine/sph_gravity.cu:645-788, instantiated in float (reference) or double.
+}  // extern "C"
+template <typename R>
+static void pass1Impl(AstraeaParticles* p, const AstraeaRadixBvh* b) {
+    const uint32_t n = p->count;
+    const int G = numGroups(n);
+    std::vector<float> hNew(n);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int g = 0; g < G; ++g) {
+        const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
+        const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
+        R xi[kGroup], yi[kGroup], zi[kGroup], vx[kGroup], vy[kGroup], vz[kGroup], hi[kGroup], h0i[kGroup], Hi[kGroup], Hi2[kGroup];
+        R shep[kGroup], nsX[kGroup] = {}, nsY[kGroup] = {}, nsZ[kGroup] = {};
+        R gg[kGroup][9] = {};
+        int cnt[kGroup];
+        float Hi2f[kGroup], xf[kGroup], yf[kGroup], zf[kGroup];
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            xi[l] = p->posX[i]; yi[l] = p->posY[i]; zi[l] = p->posZ[i];
+            xf[l] = p->posX[i]; yf[l] = p->posY[i]; zf[l] = p->posZ[i];
+            vx[l] = p->velX[i]; vy[l] = p->velY[i]; vz[l] = p->velZ[i];
+            const float hf = std::fmax(p->h[i], 1.0e-6f);
+            const float Hf = 2.0f * hf;
+            hi[l] = hf; h0i[l] = std::fmax(p->h0[i], 1.0e-6f);
+            Hi[l] = Hf; Hi2f[l] = Hf * Hf; Hi2[l] = R(Hi2f[l]);
+            const R mi = p->mass[i], rhoI = std::fmax(p->rho[i], 1.0e-9f);
+            const R w0 = R(21) / (R(2) * R(kPiD) * Hi[l] * Hi[l] * Hi[l]);
+            shep[l] = (sizeof(R) == 4) ? R((static_cast<float>(mi) / static_cast<float>(rhoI)) * (21.0f / (2.0f * kPiF * Hf * Hf * Hf)))
+                                       : (mi / rhoI) * w0;
+            cnt[l] = 1;
+        }
+        if (n >= 2) {
+            walkGroup(*b,
+                [&](int c) {
+                    for (int l = 0; l < act; ++l)
+                        if (pointBoxDist2(xf[l], yf[l], zf[l], b->aabbMinX[c], b->aabbMinY[c], b->aabbMinZ[c],
+                                          b->aabbMaxX[c], b->aabbMaxY[c], b->aabbMaxZ[c]) <= Hi2f[l])
+                            return true;
+                    return false;
+                },
+                [&](uint32_t j) {
+                    const float pxj = p->posX[j], pyj = p->posY[j], pzj = p->posZ[j];
+                    for (int l = 0; l < act; ++l) {
+                        const uint32_t i = i0 + l;
+                        const float dxf = xf[l] - pxj, dyf = yf[l] - pyj, dzf = zf[l] - pzj;
+                        const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+                        if (j == i || !(r2f < Hi2f[l])) continue;
+                        ++cnt[l];
+                        const R dx = xi[l] - R(pxj), dy = yi[l] - R(pyj), dz = zi[l] - R(pzj);
+                        const R r2 = (sizeof(R) == 4) ? R(r2f) : dx * dx + dy * dy + dz * dz;
+                        const R r = std::sqrt(r2);
+                        const R vol = R(p->mass[j]) / R(std::fmax(p->rho[j], 1.0e-9f));
+                        const R w = wendland<R>(r, Hi[l]);
+                        shep[l] += vol * w;
+                        nsX[l] -= vol * dx * w; nsY[l] -= vol * dy * w; nsZ[l] -= vol * dz * w;
+                        const R gc = wendlandGrad<R>(r, Hi[l]);
+                        const R gx = gc * dx, gy = gc * dy, gz = gc * dz;
+                        const R dvx = R(p->velX[j]) - vx[l], dvy = R(p->velY[j]) - vy[l], dvz = R(p->velZ[j]) - vz[l];
+                        R* G9 = gg[l];
+                        G9[0] += vol * dvx * gx; G9[1] += vol * dvx * gy; G9[2] += vol * dvx * gz;
+                        G9[3] += vol * dvy * gx; G9[4] += vol * dvy * gy; G9[5] += vol * dvy * gz;
+                        G9[6] += vol * dvz * gx; G9[7] += vol * dvz * gy; G9[8] += vol * dvz * gz;
+                    }
+                });
+        }
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            p->shepardC[i] = static_cast<float>(shep[l]);
+            const R nn = std::sqrt(nsX[l] * nsX[l] + nsY[l] * nsY[l] + nsZ[l] * nsZ[l]);
+            R fs = std::min(R(1), std::max(R(0), R(1.6f) * std::max(R(1) - shep[l], nn / hi[l]) - R(0.15f)));
+            if (cnt[l] <= 2) fs = R(1);
+            p->surfFactor[i] = static_cast<float>(fs);
+            const R* G9 = gg[l];
+            p->divV[i] = static_cast<float>(G9[0] + G9[4] + G9[8]);
+            p->curlVX[i] = static_cast<float>(G9[7] - G9[5]);
+            p->curlVY[i] = static_cast<float>(G9[2] - G9[6]);
+            p->curlVZ[i] = static_cast<float>(G9[3] - G9[1]);
+            const float ratio = 56.0f / static_cast<float>(cnt[l]);
+            const float fac = std::fmin(1.08f, std::fmax(0.92f, std::cbrt(ratio)));
+            hNew[i] = std::fmin(6.0f * static_cast<float>(h0i[l]), std::fmax(0.35f * static_cast<float>(h0i[l]), static_cast<float>(hi[l]) * fac));
+        }
+    }
+    for (uint32_t i = 0; i < n; ++i) p->h[i] = hNew[i];
+}
+extern "C" {
+void oracle_sph_pass1(AstraeaParticles* p, const AstraeaRadixBvh* b) { if (p->count) pass1Impl<float>(p, b); }
+void oracle_sph_pass1_f64(AstraeaParticles* p, const AstraeaRadixBvh* b) { if (p->count) pass1Impl<double>(p, b); }
+
+void oracle_evaluate_eos(AstraeaParticles* p) {
+    oracle_eos_batch(p->count, p->materialId, p->rho, p->u, p->damage, p->pressure, p->soundSpeed, p->tempK, p->phaseId);
+}
+
+// --------------------------------------------------------- Barnes-Hut ----
+// engine/sph_gravity.cu:810-961 (float), per group of 32.
+void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, uint64_t* interactionsOut) {
+    const uint32_t n = p->count;
+    if (n == 0) return;
+    if (n == 1) { p->accX[0] = p->accY[0] = p->accZ[0] = p->phiGrav[0] = 0.0f; return; }
+    const float th = std::fmax(0.0f, theta);
+    const float theta2 = th * th;
+    const bool checkInside = theta2 > 0.333333f;
+    const int G = numGroups(n);
+    uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : total)
+    for (int g = 0; g < G; ++g) {
+        const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
+        const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
+        float xi[kGroup], yi[kGroup], zi[kGroup], eI[kGroup], eI2[kGroup];
+        float ax[kGroup] = {}, ay[kGroup] = {}, az[kGroup] = {}, ph[kGroup] = {};
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            xi[l] = p->posX[i]; yi[l] = p->posY[i]; zi[l] = p->posZ[i];
+            eI[l] = 0.8f * std::fmax(p->h0[i], 1.0e-6f); eI2[l] = eI[l] * eI[l];
+        }
+        int stack[kStackSize];
+        int sp = 0;
+        stack[sp++] = 0;
+        float dxs[kGroup], dys[kGroup], dzs[kGroup], r2s[kGroup];
+        while (sp > 0) {
+            const int node = stack[--sp];
+            const int ch[2] = {b->leftChild[node], b->rightChild[node]};
+            for (int k = 0; k < 2; ++k) {
+                const int c = ch[k];
+                if (c < 0) {
+                    const uint32_t j = static_cast<uint32_t>(~c);
+                    const float pxj = p->posX[j], pyj = p->posY[j], pzj = p->posZ[j], mj = p->mass[j];
+                    const float eJ = 0.8f * std::fmax(p->h0[j], 1.0e-6f);
+                    for (int l = 0; l < act; ++l) {
+                        if (i0 + l == j) continue;
+                        const float dx = xi[l] - pxj, dy = yi[l] - pyj, dz = zi[l] - pzj;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float eij = 0.5f * (eI[l] + eJ);
+                        const float den = r2 + eij * eij + 1.0e-20f;
+                        const float iR = 1.0f / std::sqrt(den);
+                        const float iR3 = iR * iR * iR;
+                        const float f = -kGPsuF * mj * iR3;
+                        ax[l] += f * dx; ay[l] += f * dy; az[l] += f * dz;
+                        ph[l] -= kGPsuF * mj * iR;
+                        ++total;
+                    }
+                } else {
+                    const NodeBox nb = nodeBox(*b, c);
+                    bool anyOpen = false;
+                    for (int l = 0; l < act; ++l) {
+                        const float dx = xi[l] - nb.cx, dy = yi[l] - nb.cy, dz = zi[l] - nb.cz;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        dxs[l] = dx; dys[l] = dy; dzs[l] = dz; r2s[l] = r2;
+                        bool acc = (nb.dNode * nb.dNode < theta2 * r2) && (r2 > 1.0e-20f);
+                        if (acc && checkInside && xi[l] >= nb.mnx && xi[l] <= nb.mxx && yi[l] >= nb.mny &&
+                            yi[l] <= nb.mxy && zi[l] >= nb.mnz && zi[l] <= nb.mxz)
+                            acc = false;
+                        if (!acc) anyOpen = true;
+                    }
+                    if (!anyOpen || sp >= kStackSize) {
+                        for (int l = 0; l < act; ++l) {
+                            const float den = r2s[l] + eI2[l] + 1.0e-20f;
+                            const float iR = 1.0f / std::sqrt(den);
+                            const float iR3 = iR * iR * iR;
+                            const float f = -kGPsuF * nb.m * iR3;
+                            ax[l] += f * dxs[l]; ay[l] += f * dys[l]; az[l] += f * dzs[l];
+                            ph[l] -= kGPsuF * nb.m * iR;
+                            ++total;
+                        }
+                    } else {
+                        stack[sp++] = c;
+                    }
+                }
+            }
+        }
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            p->accX[i] = ax[l]; p->accY[i] = ay[l]; p->accZ[i] = az[l]; p->phiGrav[i] = ph[l];
+        }
+    }
+    if (interactionsOut) *interactionsOut = total;
+}
+
+// FP64 direct sum with eps_ij = (eps_i + eps_j)/2, eps = 0.8 h0, for the
+// listed targets (tests/cpp/test_gravity_sph.cpp:359-379 criterion).
+void oracle_direct_gravity_f64(uint32_t n, const float* x, const float* y, const float* z, const float* m,
+                               const float* h0, uint32_t nt, const uint32_t* targets, double* acc3, double* phi) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t t = 0; t < static_cast<int64_t>(nt); ++t) {
+        const uint32_t i = targets[t];
+        const double xi = x[i], yi = y[i], zi = z[i], ei = 0.8 * static_cast<double>(h0[i]);
+        double ax = 0, ay = 0, az = 0, ph = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const double dx = xi - x[j], dy = yi - y[j], dz = zi - z[j];
+            const double e = 0.5 * (ei + 0.8 * static_cast<double>(h0[j]));
+            const double d2 = dx * dx + dy * dy + dz * dz + e * e;
+            const double inv = 1.0 / std::sqrt(d2);
+            const double f = -kGPsuD * m[j] * inv * inv * inv;
+            ax += f * dx; ay += f * dy; az += f * dz; ph -= kGPsuD * m[j] * inv;
+        }
+        acc3[3 * t] = ax; acc3[3 * t + 1] = ay; acc3[3 * t + 2] = az;
+        if (phi) phi[t] = ph;
+    }
+}
+
+// ------------------------------------------------------------ SPH pass 2 ----
+// engine/sph_gravity.cu:965-1287.
+}  // extern "C"
+template <typename R>
+static void pass2Impl(AstraeaParticles* p, const AstraeaRadixBvh* b) {
+    const uint32_t n = p->count;
+    const int G = numGroups(n);
+    const bool livingIntact = b->livingFlags ? (b->livingFlags[1] != 0u) : false;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int g = 0; g < G; ++g) {
+        const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
+        const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
+        struct Lane {
+            float xf, yf, zf, Hf, hf;
+            R x, y, z, vx, vy, vz, m, h, H, rho, iRho2, P, cs, T, dmg, fs, fBal, Ri, pOr2;
+            R s[6];
+            uint8_t mat;
+            R ax, ay, az, drC, drD, duP, duAv, duT, duS, g[9];
+        } L[kGroup];
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            Lane& q = L[l];
+            std::memset(&q, 0, sizeof(Lane));
+            q.xf = p->posX[i]; q.yf = p->posY[i]; q.zf = p->posZ[i];
+            q.x = q.xf; q.y = q.yf; q.z = q.zf;
+            q.vx = p->velX[i]; q.vy = p->velY[i]; q.vz = p->velZ[i];
+            q.m = p->mass[i];
+            q.hf = std::fmax(p->h[i], 1.0e-6f); q.Hf = 2.0f * q.hf;
+            q.h = q.hf; q.H = q.Hf;
+            const float rhof = std::fmax(p->rho[i], 1.0e-9f);
+            q.rho = rhof;
+            q.iRho2 = R(1) / (q.rho * q.rho);
+            q.P = effPressure(p->pressure[i], p->phaseId[i]);
+            q.cs = std::fmax(p->soundSpeed[i], 0.05f);
+            q.T = p->tempK[i]; q.dmg = p->damage[i]; q.fs = p->surfFactor[i]; q.mat = p->materialId[i];
+            q.s[0] = p->sXX[i]; q.s[1] = p->sYY[i]; q.s[2] = p->sZZ[i]; q.s[3] = p->sXY[i]; q.s[4] = p->sXZ[i]; q.s[5] = p->sYZ[i];
+            q.fBal = balsara<R>(p->divV[i], p->curlVX[i], p->curlVY[i], p->curlVZ[i], q.cs, q.h);
+            q.Ri = (q.P < R(0)) ? (R(0.3f) * (-q.P) * q.iRho2) : R(0);
+            q.pOr2 = q.P * q.iRho2;
+        }
+        if (n >= 2) {
+            walkGroup(*b,
+                [&](int c) {
+                    for (int l = 0; l < act; ++l) {
+                        const float rad = std::fmax(L[l].Hf, 1.09f * b->nodeMaxH[c]);
+                        if (pointBoxDist2(L[l].xf, L[l].yf, L[l].zf, b->aabbMinX[c], b->aabbMinY[c], b->aabbMinZ[c],
+                                          b->aabbMaxX[c], b->aabbMaxY[c], b->aabbMaxZ[c]) <= rad * rad)
+                            return true;
+                    }
+                    return false;
+                },
+                [&](uint32_t j) {
+                    const float pxj = p->posX[j], pyj = p->posY[j], pzj = p->posZ[j];
+                    const float hjf = std::fmax(p->h[j], 1.0e-6f), Hjf = 2.0f * hjf;
+                    bool bal = false;
+                    R fBalJ = 0;
+                    for (int l = 0; l < act; ++l) {
+                        const uint32_t i = i0 + l;
+                        Lane& q = L[l];
+                        const float dxf = q.xf - pxj, dyf = q.yf - pyj, dzf = q.zf - pzj;
+                        const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+                        const float Hmf = std::fmax(q.Hf, Hjf);
+                        if (j == i || !(r2f < Hmf * Hmf)) continue;
+                        const R dx = q.x - R(pxj), dy = q.y - R(pyj), dz = q.z - R(pzj);
+                        const R r2 = (sizeof(R) == 4) ? R(r2f) : dx * dx + dy * dy + dz * dz;
+                        const R hj = hjf, Hj = Hjf, mj = p->mass[j];
+                        const R rhoJ = std::fmax(p->rho[j], 1.0e-9f);
+                        const R pJ = effPressure(p->pressure[j], p->phaseId[j]);
+                        const R csJ = std::fmax(p->soundSpeed[j], 0.05f);
+                        const R dvx = q.vx - R(p->velX[j]), dvy = q.vy - R(p->velY[j]), dvz = q.vz - R(p->velZ[j]);
+                        const R vDotR = dvx * dx + dvy * dy + dvz * dz;
+                        if (vDotR < R(0) && !bal) {
+                            fBalJ = balsara<R>(p->divV[j], p->curlVX[j], p->curlVY[j], p->curlVZ[j], csJ, hj);
+                            bal = true;
+                        }
+                        const R r = std::sqrt(r2);
+                        const R gI = wendlandGrad<R>(r, q.H), gJ = wendlandGrad<R>(r, Hj);
+                        const R gb = R(0.5f) * (gI + gJ);
+                        const R gx = gb * dx, gy = gb * dy, gz = gb * dz;
+                        const R iRhoJ2 = R(1) / (rhoJ * rhoJ);
+                        const R vDotG = dvx * gx + dvy * gy + dvz * gz;
+                        q.drC += (mj / rhoJ) * vDotG;
+                        if (p->materialId[j] == q.mat) {
+                            const R rDotG = -(dx * gx + dy * gy + dz * gz);
+                            const R dd = r2 + R(0.01f) * q.H * q.H;
+                            q.drD += (mj / rhoJ) * (R(2) * (rhoJ - q.rho) / dd) * rDotG;
+                        }
+                        R pi = 0;
+                        if (vDotR < R(0)) {
+                            const R hB = R(0.5f) * (q.h + hj), cB = R(0.5f) * (q.cs + csJ), rB = R(0.5f) * (q.rho + rhoJ);
+                            const R muIJ = (hB * vDotR) / (r2 + R(0.01f) * hB * hB);
+                            pi = ((R(-1) * cB * muIJ + R(2) * muIJ * muIJ) / rB) * (R(0.5f) * (q.fBal + fBalJ));
+                        }
+                        R tens = 0;
+                        const R Rj = (pJ < R(0)) ? (R(0.3f) * (-pJ) * iRhoJ2) : R(0);
+                        if (q.Ri + Rj > R(0)) {
+                            const R Hb = R(0.5f) * (q.H + Hj);
+                            if (r < Hb) {
+                                const R qb = r / Hb, om = R(1) - qb, om2 = om * om;
+                                const R fr = (om2 * om2 * (R(1) + R(4) * qb)) * (R(1) / R(0.6328125f));
+                                const R fr2 = fr * fr;
+                                tens = (q.Ri + Rj) * (fr2 * fr2);
+                            }
+                        }
+                        const R pT = q.pOr2 + pJ * iRhoJ2;
+                        const R iso = -mj * (pT + pi + tens);
+                        q.ax += iso * gx; q.ay += iso * gy; q.az += iso * gz;
+                        q.duP += mj * vDotG;
+                        q.duAv += R(0.5f) * mj * pi * vDotG;
+                        q.duT += R(0.5f) * mj * tens * vDotG;
+                        const R sj[6] = {R(p->sXX[j]), R(p->sYY[j]), R(p->sZZ[j]), R(p->sXY[j]), R(p->sXZ[j]), R(p->sYZ[j])};
+                        const R tXX = q.s[0] * q.iRho2 + sj[0] * iRhoJ2, tYY = q.s[1] * q.iRho2 + sj[1] * iRhoJ2;
+                        const R tZZ = q.s[2] * q.iRho2 + sj[2] * iRhoJ2, tXY = q.s[3] * q.iRho2 + sj[3] * iRhoJ2;
+                        const R tXZ = q.s[4] * q.iRho2 + sj[4] * iRhoJ2, tYZ = q.s[5] * q.iRho2 + sj[5] * iRhoJ2;
+                        q.ax += mj * (tXX * gx + tXY * gy + tXZ * gz);
+                        q.ay += mj * (tXY * gx + tYY * gy + tYZ * gz);
+                        q.az += mj * (tXZ * gx + tYZ * gy + tZZ * gz);
+                        const R wx = -dvx, wy = -dvy, wz = -dvz;
+                        q.duS += mj * ((q.s[0] * wx + q.s[3] * wy + q.s[4] * wz) * gx +
+                                       (q.s[3] * wx + q.s[1] * wy + q.s[5] * wz) * gy +
+                                       (q.s[4] * wx + q.s[5] * wy + q.s[2] * wz) * gz);
+                        const R vol = mj / rhoJ;
+                        const R gxi = gI * dx, gyi = gI * dy, gzi = gI * dz;
+                        q.g[0] += vol * wx * gxi; q.g[1] += vol * wx * gyi; q.g[2] += vol * wx * gzi;
+                        q.g[3] += vol * wy * gxi; q.g[4] += vol * wy * gyi; q.g[5] += vol * wy * gzi;
+                        q.g[6] += vol * wz * gxi; q.g[7] += vol * wz * gyi; q.g[8] += vol * wz * gzi;
+                    }
+                });
+        }
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            Lane& q = L[l];
+            p->accX[i] += static_cast<float>(q.ax);
+            p->accY[i] += static_cast<float>(q.ay);
+            p->accZ[i] += static_cast<float>(q.az);
+            const R mask = (p->shepardC[i] > 0.85f) ? (R(1) - q.fs) : R(0);
+            p->drhoDt[i] = static_cast<float>(q.rho * q.drC + R(0.05f) * q.H * q.cs * mask * q.drD);
+            const R duStress = q.iRho2 * q.duS;
+            // FP64 radiative cooling epilogue, engine/sph_gravity.cu:1222-1235
+            const double tAmb = (livingIntact && p->bodyId[i] == 0u && p->damage[i] < 0.8f) ? 255.0 : 3.0;
+            const double mSi = std::fmax(static_cast<double>(p->mass[i]) * 1.0e24, 1.0);
+            const double rhoSi = std::fmax(static_cast<double>(static_cast<float>(q.rho)) * 1.0e6, 1.0e-3);
+            const double rP = std::cbrt((3.0 * mSi) / (4.0 * kPiD * rhoSi));
+            const double area = kPiD * rP * rP;
+            const double T = static_cast<double>(p->tempK[i]);
+            const double T4 = T * T * T * T, Ta4 = tAmb * tAmb * tAmb * tAmb;
+            const double dT4 = std::fmax(0.0, T4 - Ta4);
+            const double pRad = static_cast<double>(p->surfFactor[i]) * 0.9 * kSigmaSB * area * dT4;
+            p->radPowerW[i] = static_cast<float>(pRad);
+            const float duRad = static_cast<float>(-pRad / (std::fmax(static_cast<double>(p->mass[i]), 1.0e-30) * 1.0e27));
+            p->duDt[i] = static_cast<float>(q.pOr2 * q.duP + q.duAv + q.duT + duStress + R(duRad));
+            const Strength st = strengthOf(q.mat);
+            if (st.mu <= 0.0f || st.tMelt <= 0.0f) {
+                p->dSXX[i] = p->dSYY[i] = p->dSZZ[i] = p->dSXY[i] = p->dSXZ[i] = p->dSYZ[i] = 0.0f;
+                p->dDamageCbrtDt[i] = 0.0f;
+                continue;
+            }
+            const R tN = q.T / R(st.tMelt);
+            const R soft = std::max(R(0), R(1) - tN * tN);
+            const R muE = (R(1) - q.dmg) * R(st.mu) * soft;
+            const R* g = q.g;
+            const R tr3 = (g[0] + g[4] + g[8]) * (R(1) / R(3));
+            const R eXX = g[0] - tr3, eYY = g[4] - tr3, eZZ = g[8] - tr3;
+            const R eXY = R(0.5f) * (g[1] + g[3]), eXZ = R(0.5f) * (g[2] + g[6]), eYZ = R(0.5f) * (g[5] + g[7]);
+            const R rXY = R(0.5f) * (g[1] - g[3]), rXZ = R(0.5f) * (g[2] - g[6]), rYZ = R(0.5f) * (g[5] - g[7]);
+            const R rYX = -rXY, rZX = -rXZ, rZY = -rYZ;
+            const R* s = q.s;  // xx yy zz xy xz yz
+            p->dSXX[i] = static_cast<float>(R(2) * muE * eXX + R(2) * (s[3] * rXY + s[4] * rXZ));
+            p->dSYY[i] = static_cast<float>(R(2) * muE * eYY + R(2) * (s[3] * rYX + s[5] * rYZ));
+            p->dSZZ[i] = static_cast<float>(R(2) * muE * eZZ + R(2) * (s[4] * rZX + s[5] * rZY));
+            p->dSXY[i] = static_cast<float>(R(2) * muE * eXY + s[0] * rYX + s[4] * rYZ + s[1] * rXY + s[5] * rXZ);
+            p->dSXZ[i] = static_cast<float>(R(2) * muE * eXZ + s[0] * rZX + s[3] * rZY + s[2] * rXZ + s[5] * rXY);
+            p->dSYZ[i] = static_cast<float>(R(2) * muE * eYZ + s[3] * rZX + s[1] * rZY + s[4] * rYX + s[2] * rYZ);
+            const float Tf = p->tempK[i], Df = p->damage[i];
+            if (Tf < st.tMelt && Df < 1.0f) {
+                const float Pf = static_cast<float>(q.P);
+                const float sig = maxPrincipal(Pf, p->sXX[i], p->sYY[i], p->sZZ[i], p->sXY[i], p->sXZ[i], p->sYZ[i]);
+                const float stiff = std::fmax(st.K + (4.0f / 3.0f) * st.mu, 1.0e-12f);
+                const float eT = std::fmax(0.0f, sig) / stiff;
+                const float eF = std::fmax(p->epsFail[i], 1.0e-8f);
+                const float rhof = std::fmax(p->rho[i], 1.0e-9f);
+                const float cC = std::fmax(std::fmax(p->soundSpeed[i], 0.05f), std::sqrt((st.K + (4.0f / 3.0f) * st.mu) / rhof));
+                p->dDamageCbrtDt[i] = (eT > eF) ? (0.4f * cC / q.hf) : 0.0f;
+            } else {
+                p->dDamageCbrtDt[i] = 0.0f;
+            }
+        }
+    }
+}
+extern "C" {
+void oracle_sph_pass2(AstraeaParticles* p, const AstraeaRadixBvh* b) { if (p->count) pass2Impl<float>(p, b); }
+void oracle_sph_pass2_f64(AstraeaParticles* p, const AstraeaRadixBvh* b) { if (p->count) pass2Impl<double>(p, b); }
+
+// ------------------------------------------------------------ KDK kick ----
+// engine/sph_gravity.cu:1291-1374.
+void oracle_kick_half(AstraeaParticles* p, float hdt, int clampThermal) {
+    const uint32_t n = p->count;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < static_cast<int64_t>(n); ++ii) {
+        const uint32_t i = static_cast<uint32_t>(ii);
+        const float vx = p->velX[i] + hdt * p->accX[i];
+        const float vy = p->velY[i] + hdt * p->accY[i];
+        const float vz = p->velZ[i] + hdt * p->accZ[i];
+        p->velX[i] = vx; p->velY[i] = vy; p->velZ[i] = vz;
+        p->velHalfX[i] = vx; p->velHalfY[i] = vy; p->velHalfZ[i] = vz;
+        const float rhoN = std::fmax(p->rho[i] + hdt * p->drhoDt[i], 1.0e-9f);
+        p->rho[i] = rhoN;
+        const int m = matIndex(p->materialId[i]);
+        const Strength st = strengthOf(m);
+        float uN = p->u[i] + hdt * p->duDt[i];
+        if (clampThermal) {
+            const double uMin = coldEnergy(m, static_cast<double>(rhoN)) + 3.0 * (kMat[m].cv / 1.0e6);
+            uN = std::fmax(uN, static_cast<float>(uMin));
+        } else {
+            uN = std::fmax(uN, 0.0f);
+        }
+        p->u[i] = uN;
+        float dc = p->damageCbrt[i] + hdt * p->dDamageCbrtDt[i];
+        dc = std::fmin(1.0f, std::fmax(p->damageCbrt[i], dc));
+        const float D = dc * dc * dc;
+        p->damageCbrt[i] = dc; p->damage[i] = D;
+        if (clampThermal) {
+            const EosOut e = evaluateEos(m, rhoN, uN, D);
+            p->pressure[i] = e.p; p->soundSpeed[i] = e.cs; p->tempK[i] = e.T; p->phaseId[i] = e.phase;
+        }
+        if (st.mu <= 0.0f || st.tMelt <= 0.0f || p->tempK[i] >= st.tMelt) {
+            p->sXX[i] = p->sYY[i] = p->sZZ[i] = p->sXY[i] = p->sXZ[i] = p->sYZ[i] = 0.0f;
+            continue;
+        }
+        float sxx = p->sXX[i] + hdt * p->dSXX[i], syy = p->sYY[i] + hdt * p->dSYY[i], szz = p->sZZ[i] + hdt * p->dSZZ[i];
+        const float sxy = p->sXY[i] + hdt * p->dSXY[i], sxz = p->sXZ[i] + hdt * p->dSXZ[i], syz = p->sYZ[i] + hdt * p->dSYZ[i];
+        const float tr3 = (sxx + syy + szz) * (1.0f / 3.0f);
+        sxx -= tr3; syy -= tr3; szz -= tr3;
+        const float tR = p->tempK[i] / st.tMelt;
+        const float yI = (1.0f - D) * st.Y0 * std::fmax(0.0f, 1.0f - tR);
+        const float yF = D * std::fmin(st.Y0, 0.6f * std::fmax(0.0f, p->pressure[i]));
+        const float Y = std::fmax(yI, yF);
+        const float j2 = 0.5f * (sxx * sxx + syy * syy + szz * szz + 2.0f * (sxy * sxy + sxz * sxz + syz * syz));
+        const float eq = std::sqrt(3.0f * j2 + 1.0e-30f);
+        const float sc = (Y <= 0.0f) ? 0.0f : std::fmin(1.0f, Y / eq);
+        p->sXX[i] = sxx * sc; p->sYY[i] = syy * sc; p->sZZ[i] = szz * sc;
+        p->sXY[i] = sxy * sc; p->sXZ[i] = sxz * sc; p->sYZ[i] = syz * sc;
+    }
+}
+
+// ------------------------------------------------------------ XSPH drift ----
+// engine/sph_gravity.cu:1376-1489, with neighbours read from the pre-drift
+// positions (the reference kernel reads them while other threads write).
+void oracle_drift(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int useBvh) {
+    const uint32_t n = p->count;
+    std::vector<float> nx(n), ny(n), nz(n);
+    const int G = numGroups(n);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int g = 0; g < G; ++g) {
+        const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
+        const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
+        float xi[kGroup], yi[kGroup], zi[kGroup], vxi[kGroup], vyi[kGroup], vzi[kGroup], Hi[kGroup], rhoI[kGroup];
+        float sx[kGroup] = {}, sy[kGroup] = {}, sz[kGroup] = {};
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            xi[l] = p->posX[i]; yi[l] = p->posY[i]; zi[l] = p->posZ[i];
+            vxi[l] = p->velX[i]; vyi[l] = p->velY[i]; vzi[l] = p->velZ[i];
+            Hi[l] = 2.0f * std::fmax(p->h[i], 1.0e-6f); rhoI[l] = std::fmax(p->rho[i], 1.0e-9f);
+        }
+        if (useBvh && n >= 2) {
+            walkGroup(*b,
+                [&](int c) {
+                    for (int l = 0; l < act; ++l) {
+                        const float rad = std::fmax(Hi[l], 1.09f * b->nodeMaxH[c]);
+                        if (pointBoxDist2(xi[l], yi[l], zi[l], b->aabbMinX[c], b->aabbMinY[c], b->aabbMinZ[c],
+                                          b->aabbMaxX[c], b->aabbMaxY[c], b->aabbMaxZ[c]) <= rad * rad)
+                            return true;
+                    }
+                    return false;
+                },
+                [&](uint32_t j) {
+                    const float pxj = p->posX[j], pyj = p->posY[j], pzj = p->posZ[j];
+                    const float Hj = 2.0f * std::fmax(p->h[j], 1.0e-6f);
+                    for (int l = 0; l < act; ++l) {
+                        if (i0 + l == j) continue;
+                        const float dx = xi[l] - pxj, dy = yi[l] - pyj, dz = zi[l] - pzj;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float Hm = std::fmax(Hi[l], Hj);
+                        if (!(r2 < Hm * Hm)) continue;
+                        const float r = std::sqrt(r2);
+                        const float wb = 0.5f * (wendland<float>(r, Hi[l]) + wendland<float>(r, Hj));
+                        const float rb = 0.5f * (rhoI[l] + std::fmax(p->rho[j], 1.0e-9f));
+                        const float co = (p->mass[j] / rb) * wb;
+                        sx[l] += co * (p->velX[j] - vxi[l]);
+                        sy[l] += co * (p->velY[j] - vyi[l]);
+                        sz[l] += co * (p->velZ[j] - vzi[l]);
+                    }
+                });
+        }
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            nx[i] = xi[l] + dt * (vxi[l] + 0.25f * sx[l]);
+            ny[i] = yi[l] + dt * (vyi[l] + 0.25f * sy[l]);
+            nz[i] = zi[l] + dt * (vzi[l] + 0.25f * sz[l]);
+        }
+    }
+    std::memcpy(p->posX, nx.data(), n * 4); std::memcpy(p->posY, ny.data(), n * 4); std::memcpy(p->posZ, nz.data(), n * 4);
+}
+
+// --------------------------------------------------------------- dt ----
+// engine/sph_gravity.cu:1493-1550 + host clamp 2136-2161.
+float oracle_reduce_dt(const AstraeaParticles* p, float prevDt, float maxDt, float* rawMinOut) {
+    const float floorDt = std::fmin(1.0e-5f, maxDt);
+    const float upper = (prevDt > 0.0f) ? std::fmin(prevDt * 1.15f, maxDt) : maxDt;
+    const uint32_t n = p->count;
+    if (n == 0) return upper;
+    float mn = 1.0e30f;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float hi = std::fmax(p->h[i], 1.0e-6f), cs = std::fmax(p->soundSpeed[i], 0.05f);
+        const float v = std::sqrt(p->velX[i] * p->velX[i] + p->velY[i] * p->velY[i] + p->velZ[i] * p->velZ[i]);
+        const float dtC = 0.25f * hi / (2.2f * cs + v + 1.0e-6f);
+        const float a = std::sqrt(p->accX[i] * p->accX[i] + p->accY[i] * p->accY[i] + p->accZ[i] * p->accZ[i]);
+        const float dtA = 0.25f * std::sqrt(hi / (a + 1.0e-8f));
+        const int m = matIndex(p->materialId[i]);
+        const float uI = std::fmax(p->u[i], 0.0f);
+        const float uS = std::fmax(uI, u0RefPsu(m));
+        const float dtT = 0.20f * (uI + 0.01f * uS) / (std::fabs(p->duDt[i]) + 1.0e-8f);
+        const float d = std::fmin(dtC, std::fmin(dtA, dtT));
+        if (std::isfinite(d) && d > 0.0f) mn = std::fmin(mn, d);
+    }
+    if (rawMinOut) *rawMinOut = mn;
+    float raw = mn;
+    if (!(std::isfinite(raw) && raw > 0.0f) || raw >= 1.0e30f) raw = upper;
+    return std::fmin(upper, std::fmax(floorDt, raw));
+}
+
+// ------------------------------------------------------------ full step ----
+// engine/simulation.cpp:1711-1753 kernel sequence.
+float oracle_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* b, float prevDt, float maxDt,
+                  float theta) {
+    const float dt = oracle_reduce_dt(p, prevDt, maxDt, nullptr);
+    oracle_kick_half(p, 0.5f * dt, 0);
+    const int useBvh = (b->capacity >= p->count && b->leftChild != nullptr && p->count >= 2u) ? 1 : 0;
+    oracle_drift(p, dt, b, useBvh);
+    oracle_sort_and_build(p, alt, b, nullptr);
+    oracle_sph_pass1(p, b);
+    oracle_evaluate_eos(p);
+    oracle_gravity(p, b, theta, nullptr);
+    oracle_sph_pass2(p, b);
+    oracle_kick_half(p, 0.5f * dt, 0);
+    oracle_evaluate_eos(p);
+    return dt;
+}
+
+int oracle_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,291 @@
+"""Python driver of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/_build/liboracle.so (oracle/oracle.cpp, built by
+oracle/build_oracle.py) and runs the reference algorithm on host numpy
+particle states.  Used by tests/ as the checker, by __graft_entry__.smoke()
+and by bench.py's CPU baseline; never by the product library.
+
+A host state is a dict field -> numpy array with the ParticleBuffersDevice
+field names (astraea_gb300.abi.FIELDS).  The BVH is a dict of numpy arrays
+sized like the engine allocates them (engine/sph_gravity.cu:1812-1842).
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "astraea-impact-sim_gb300"))
+from astraea_gb300 import abi  # noqa: E402  (struct layout of include/astraea_gb300.h)
+
+_lib = None
+_ref = None
+
+
+def load(build=True):
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        if build or not os.path.exists(path):
+            sys.path.insert(0, HERE)
+            import build_oracle
+            path = build_oracle.build_oracle()
+        _lib = ctypes.CDLL(path)
+        P, B = ctypes.POINTER(abi.Particles), ctypes.POINTER(abi.RadixBvh)
+        vp, u32, f = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float
+        sig = {
+            "oracle_eos_batch": [u32, vp, vp, vp, vp, vp, vp, vp, vp],
+            "oracle_clear_stats": [P],
+            "oracle_scene_bounds": [u32, vp, vp, vp, vp],
+            "oracle_morton": [u32, vp, vp, vp, vp, vp],
+            "oracle_sort_pairs": [u32, vp, vp, vp],
+            "oracle_karras": [u32, vp, vp, vp, vp],
+            "oracle_sort_and_build": [P, P, B, vp],
+            "oracle_sph_pass1": [P, B],
+            "oracle_sph_pass1_f64": [P, B],
+            "oracle_evaluate_eos": [P],
+            "oracle_gravity": [P, B, f, vp],
+            "oracle_direct_gravity_f64": [u32, vp, vp, vp, vp, vp, u32, vp, vp, vp],
+            "oracle_sph_pass2": [P, B],
+            "oracle_sph_pass2_f64": [P, B],
+            "oracle_kick_half": [P, f, ctypes.c_int],
+            "oracle_drift": [P, f, B, ctypes.c_int],
+            "oracle_reduce_dt": [P, f, f, vp],
+            "oracle_step": [P, P, B, f, f, f],
+        }
+        for name, args in sig.items():
+            getattr(_lib, name).argtypes = args
+        _lib.oracle_reduce_dt.restype = f
+        _lib.oracle_step.restype = f
+        _lib.oracle_cold_energy.restype = ctypes.c_double
+        _lib.oracle_cold_energy.argtypes = [ctypes.c_int, ctypes.c_double]
+    return _lib
+
+
+def load_reference_eos():
+    """The reference's own eos.cu built as host C++ (None where absent)."""
+    global _ref
+    if _ref is None:
+        path = os.path.join(HERE, "_ref", "libref_eos.so")
+        if not os.path.exists(path):
+            sys.path.insert(0, HERE)
+            import build_oracle
+            path = build_oracle.build_reference_eos()
+        if path is None or not os.path.exists(path):
+            return None
+        try:
+            _ref = ctypes.CDLL(path)
+        except OSError:
+            return None
+        vp, u32 = ctypes.c_void_p, ctypes.c_uint32
+        _ref.ref_eos_batch.argtypes = [u32, vp, vp, vp, vp, vp, vp, vp, vp]
+        _ref.ref_cold_energy.argtypes = [ctypes.c_int, ctypes.c_double]
+        _ref.ref_cold_energy.restype = ctypes.c_double
+    return _ref
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class HostParticles:
+    """Owns numpy arrays and a ctypes Particles struct pointing at them."""
+
+    def __init__(self, state, capacity=None):
+        n = len(state["posX"])
+        cap = max(capacity or n, 1)
+        self.arrays = {}
+        for name, dt in abi.FIELDS:
+            a = np.zeros(cap, dtype=dt)
+            if name in state:
+                a[:n] = state[name][:n]
+            elif name == "tracerIndex":
+                a[:] = -1
+            self.arrays[name] = a
+        self.count = n
+        self.capacity = cap
+
+    def struct(self):
+        s = abi.Particles()
+        s.capacity, s.count = self.capacity, self.count
+        for name in abi.FIELD_NAMES:
+            setattr(s, name, self.arrays[name].ctypes.data)
+        return s
+
+    def rebind(self, s, by_ptr):
+        self.arrays = {name: by_ptr[getattr(s, name)] for name in abi.FIELD_NAMES}
+        self.count = s.count
+
+    def state(self):
+        return {k: v[: self.count].copy() for k, v in self.arrays.items()}
+
+
+class HostBvh:
+    def __init__(self, capacity):
+        n = max(int(capacity), 1)
+        nodes = 2 * n - 1
+        self.a = {
+            "mortonCodes": np.zeros(n, np.uint64), "mortonCodesSorted": np.zeros(n, np.uint64),
+            "indicesIn": np.zeros(n, np.uint32), "indicesSorted": np.zeros(n, np.uint32),
+            "leftChild": np.zeros(n, np.int32), "rightChild": np.zeros(n, np.int32),
+            "parent": np.zeros(nodes, np.int32), "atomicVisited": np.zeros(n, np.uint32),
+            "livingFlags": np.zeros(2, np.uint32), "sceneBoundsFloat": np.zeros(6, np.float32),
+        }
+        for f in ("aabbMinX", "aabbMinY", "aabbMinZ", "aabbMaxX", "aabbMaxY", "aabbMaxZ", "nodeMass", "comX",
+                  "comY", "comZ", "nodeMaxH"):
+            self.a[f] = np.zeros(nodes, np.float32)
+        self.s = abi.RadixBvh()
+        self.s.capacity = n
+        for k, v in self.a.items():
+            setattr(self.s, k, v.ctypes.data)
+
+
+class Oracle:
+    """Stage-by-stage CPU restatement on one host state (p, alt, bvh)."""
+
+    def __init__(self, state, capacity=None):
+        self.lib = load()
+        self.p = HostParticles(state, capacity)
+        self.alt = HostParticles({"posX": np.zeros(0, np.float32)}, self.p.capacity)
+        self.alt.count = self.p.count
+        self.bvh = HostBvh(self.p.capacity)
+        self.bounds = np.zeros(6, np.float32)
+        self.prev_dt = 0.0
+
+    def _pp(self):
+        return self.p.struct(), self.alt.struct()
+
+    def clear_stats(self):
+        s = self.p.struct()
+        self.lib.oracle_clear_stats(ctypes.byref(s))
+
+    def sort_and_build(self):
+        sp, sa = self._pp()
+        self.lib.oracle_sort_and_build(ctypes.byref(sp), ctypes.byref(sa), ctypes.byref(self.bvh.s), _ptr(self.bounds))
+        by_ptr = {}
+        for hp in (self.p, self.alt):
+            for a in hp.arrays.values():
+                by_ptr[a.ctypes.data] = a
+        self.p.rebind(sp, by_ptr)
+        self.alt.rebind(sa, by_ptr)
+
+    def pass1(self, f64=False):
+        s = self.p.struct()
+        (self.lib.oracle_sph_pass1_f64 if f64 else self.lib.oracle_sph_pass1)(ctypes.byref(s), ctypes.byref(self.bvh.s))
+
+    def eos(self):
+        s = self.p.struct()
+        self.lib.oracle_evaluate_eos(ctypes.byref(s))
+
+    def gravity(self, theta=0.5):
+        s = self.p.struct()
+        cnt = np.zeros(1, np.uint64)
+        self.lib.oracle_gravity(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(cnt))
+        return int(cnt[0])
+
+    def pass2(self, f64=False):
+        s = self.p.struct()
+        (self.lib.oracle_sph_pass2_f64 if f64 else self.lib.oracle_sph_pass2)(ctypes.byref(s), ctypes.byref(self.bvh.s))
+
+    def kick(self, half_dt, clamp_thermal=False):
+        s = self.p.struct()
+        self.lib.oracle_kick_half(ctypes.byref(s), float(half_dt), int(bool(clamp_thermal)))
+
+    def drift(self, dt):
+        s = self.p.struct()
+        use = 1 if self.p.count >= 2 else 0
+        self.lib.oracle_drift(ctypes.byref(s), float(dt), ctypes.byref(self.bvh.s), use)
+
+    def reduce_dt(self, prev_dt, max_dt):
+        s = self.p.struct()
+        raw = np.zeros(1, np.float32)
+        dt = self.lib.oracle_reduce_dt(ctypes.byref(s), float(prev_dt), float(max_dt), _ptr(raw))
+        return float(dt), float(raw[0])
+
+    def initial_forces(self, theta=0.5):
+        self.clear_stats()
+        self.sort_and_build()
+        self.pass1()
+        self.eos()
+        self.gravity(theta)
+        self.pass2()
+
+    def step(self, max_dt, theta=0.5):
+        dt, _ = self.reduce_dt(self.prev_dt, max_dt)
+        self.prev_dt = dt
+        self.kick(0.5 * dt)
+        self.drift(dt)
+        self.sort_and_build()
+        self.pass1()
+        self.eos()
+        self.gravity(theta)
+        self.pass2()
+        self.kick(0.5 * dt)
+        self.eos()
+        return dt
+
+    def state(self):
+        return self.p.state()
+
+
+def eos_batch(mat, rho, u, dmg, reference=False):
+    """(P, cs, T, phase) of the oracle EOS, or of the reference's own when
+    reference=True (None if that library is unavailable)."""
+    lib = load_reference_eos() if reference else load()
+    if lib is None:
+        return None
+    n = len(rho)
+    mat = np.ascontiguousarray(mat, np.uint8)
+    rho = np.ascontiguousarray(rho, np.float32)
+    u = np.ascontiguousarray(u, np.float32)
+    dmg = np.ascontiguousarray(dmg, np.float32)
+    P, cs, T = (np.zeros(n, np.float32) for _ in range(3))
+    ph = np.zeros(n, np.uint8)
+    fn = lib.ref_eos_batch if reference else lib.oracle_eos_batch
+    fn(n, _ptr(mat), _ptr(rho), _ptr(u), _ptr(dmg), _ptr(P), _ptr(cs), _ptr(T), _ptr(ph))
+    return P, cs, T, ph
+
+
+def direct_gravity_f64(state, targets):
+    lib = load()
+    n = len(state["posX"])
+    t = np.ascontiguousarray(targets, np.uint32)
+    acc = np.zeros((len(t), 3), np.float64)
+    phi = np.zeros(len(t), np.float64)
+    arrs = [np.ascontiguousarray(state[k], np.float32) for k in ("posX", "posY", "posZ", "mass", "h0")]
+    lib.oracle_direct_gravity_f64(n, *[_ptr(a) for a in arrs], len(t), _ptr(t), _ptr(acc), _ptr(phi))
+    return acc, phi
+
+
+def sort_pairs(keys):
+    lib = load()
+    keys = np.ascontiguousarray(keys, np.uint64)
+    n = len(keys)
+    ks = np.zeros(n, np.uint64)
+    perm = np.zeros(n, np.uint32)
+    lib.oracle_sort_pairs(n, _ptr(keys), _ptr(ks), _ptr(perm))
+    return ks, perm
+
+
+def morton(x, y, z):
+    lib = load()
+    x, y, z = (np.ascontiguousarray(a, np.float32) for a in (x, y, z))
+    n = len(x)
+    b = np.zeros(6, np.float32)
+    lib.oracle_scene_bounds(n, _ptr(x), _ptr(y), _ptr(z), _ptr(b))
+    codes = np.zeros(n, np.uint64)
+    lib.oracle_morton(n, _ptr(x), _ptr(y), _ptr(z), _ptr(b), _ptr(codes))
+    return codes, b
+
+
+def karras(codes_sorted):
+    lib = load()
+    c = np.ascontiguousarray(codes_sorted, np.uint64)
+    n = len(c)
+    left = np.zeros(max(n - 1, 1), np.int32)
+    right = np.zeros(max(n - 1, 1), np.int32)
+    parent = np.zeros(2 * n - 1, np.int32)
+    lib.oracle_karras(n, _ptr(c), _ptr(left), _ptr(right), _ptr(parent))
+    return left, right, parent

@@ -1,0 +1,262 @@
+"""GB300 kernels against the oracle, stage by stage, through the C-ABI.
+
+Inputs are the seeded scenes of astraea_gb300.scenarios; both sides start
+from the same host state.  Integer and index results (Morton codes, sorted
+permutation, tree topology, dt) must be bit-identical; floating-point fields
+must agree within a norm-relative RMS of 1e-5 (the parity bound for
+accelerations, densities, du/dt and stress rates).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from astraea_gb300 import abi, engine, scenarios
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def c1_state(n_t=12288, n_i=4096, seed=42):
+    st, _ = scenarios.two_granite_spheres(n_target=n_t, n_impactor=n_i, seed=seed)
+    return st
+
+
+def gpu_setup(st, packed=True):
+    n = len(st["posX"])
+    p, alt = engine.DeviceParticles(n), engine.DeviceParticles(n)
+    p.upload(st)
+    alt.count = n
+    bvh = engine.TorchBvh(n, packed=packed)
+    return p, alt, bvh
+
+
+def tnp(t, n, dtype=None):
+    a = t[:n].cpu().numpy()
+    return a.view(dtype) if dtype is not None else a
+
+
+def report(tag, gpu, cpu, fields):
+    errs = {f: rel_rms(gpu[f], cpu[f]) for f in fields}
+    print("%s %s" % (tag, " ".join("%s=%.2e" % kv for kv in errs.items())))
+    return errs
+
+
+@pytest.mark.parametrize("packed", [True, False])
+def test_sort_and_build_bit_exact(packed):
+    st = c1_state()
+    n = len(st["posX"])
+    p, alt, bvh = gpu_setup(st, packed)
+    engine.sort_and_build_bvh(p, alt, bvh)
+    torch.cuda.synchronize()
+    o = oracle.Oracle(st)
+    o.sort_and_build()
+    b = o.bvh.a
+    assert np.array_equal(tnp(bvh.t["mortonCodesSorted"], n, np.uint64), b["mortonCodesSorted"])
+    assert np.array_equal(tnp(bvh.t["indicesSorted"], n, np.uint32), b["indicesSorted"])
+    assert np.array_equal(tnp(bvh.t["leftChild"], n - 1), b["leftChild"][: n - 1])
+    assert np.array_equal(tnp(bvh.t["rightChild"], n - 1), b["rightChild"][: n - 1])
+    assert np.array_equal(tnp(bvh.t["parent"], 2 * n - 1), b["parent"])
+    g, c = p.download(), o.state()
+    for f in abi.FIELD_NAMES:                      # 56-field permutation, bit for bit
+        assert np.array_equal(g[f], c[f]), f
+    for f in ("aabbMinX", "aabbMinY", "aabbMinZ", "aabbMaxX", "aabbMaxY", "aabbMaxZ", "nodeMaxH"):
+        assert np.array_equal(tnp(bvh.t[f], 2 * n - 1), b[f]), f
+    for f in ("nodeMass", "comX", "comY", "comZ"):  # FP64 moments vs FP32 refit
+        assert rel_rms(tnp(bvh.t[f], 2 * n - 1), b[f]) < 1e-6, f
+    if packed:
+        assert np.array_equal(tnp(bvh.t["sceneBoundsFloat"], 6), o.bounds)
+        ncm = tnp(bvh.t["nodeComMass"], 4 * (2 * n - 1)).reshape(-1, 4)
+        assert rel_rms(ncm[:, 3], b["nodeMass"]) < 1e-6
+
+
+@pytest.mark.parametrize("n,end_bit", [(1, 64), (5, 64), (4096, 63), (4097, 64), (300001, 64), (1 << 20, 63)])
+def test_radix_sort_pairs_stable(n, end_bit):
+    rng = np.random.Generator(np.random.PCG64(n))
+    hi = rng.integers(0, 7, n).astype(np.uint64) << np.uint64(min(end_bit, 63) - 3)
+    keys = (hi | rng.integers(0, 1 << 20, n).astype(np.uint64) * np.uint64(rng.integers(0, 2, n) == 1)).astype(np.uint64)
+    if end_bit == 64:
+        keys |= (rng.integers(0, 2, n).astype(np.uint64) << np.uint64(63))
+    vals = np.arange(n, dtype=np.uint32)
+    kt = torch.from_numpy(keys.view(np.int64)).cuda()
+    vt = torch.from_numpy(vals.view(np.int32)).cuda()
+    ks, vs = engine.radix_sort_pairs(kt, vt, end_bit)
+    torch.cuda.synchronize()
+    mask = np.uint64((1 << end_bit) - 1) if end_bit < 64 else np.uint64(0xFFFFFFFFFFFFFFFF)
+    order = np.argsort(keys & mask, kind="stable")
+    assert np.array_equal(vs.cpu().numpy().view(np.uint32), vals[order])
+    assert np.array_equal(ks.cpu().numpy().view(np.uint64), keys[order])
+
+
+def test_pass1_eos_gravity_pass2_parity():
+    st = c1_state()
+    p, alt, bvh = gpu_setup(st)
+    o = oracle.Oracle(st)
+    engine.clear_stats(p)
+    o.clear_stats()
+    engine.sort_and_build_bvh(p, alt, bvh)
+    o.sort_and_build()
+    engine.sph_pass1_neighbors(p, bvh)
+    o.pass1()
+    g, c = p.download(), o.state()
+    e = report("pass1", g, c, ["h", "shepardC", "surfFactor", "divV", "curlVX", "curlVY", "curlVZ"])
+    assert max(e.values()) < TOL
+    engine.evaluate_eos(p)
+    o.eos()
+    g, c = p.download(), o.state()
+    e = report("eos", g, c, ["pressure", "soundSpeed", "tempK"])
+    assert max(e.values()) < TOL
+    assert np.mean(g["phaseId"] == c["phaseId"]) > 0.999
+    engine.gravity_barnes_hut(p, bvh, 0.5)
+    o.gravity(0.5)
+    g, c = p.download(), o.state()
+    e = report("gravity", g, c, ["accX", "accY", "accZ", "phiGrav"])
+    assert max(e.values()) < TOL
+    engine.sph_pass2_forces(p, bvh)
+    o.pass2()
+    g, c = p.download(), o.state()
+    e = report("pass2", g, c, ["accX", "accY", "accZ", "drhoDt", "duDt", "radPowerW", "dSXX", "dSYY", "dSZZ",
+                               "dSXY", "dSXZ", "dSYZ", "dDamageCbrtDt"])
+    assert max(e.values()) < TOL
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_gravity_parity_and_ac3_error(theta):
+    a, _ = scenarios._layered_body(2048, 6.417e-1, 0.3, 2200.0, 0, np.random.Generator(np.random.PCG64(42)))
+    b, _ = scenarios._layered_body(2048, 3.3011e-1, 0.6, 3200.0, 1, np.random.Generator(np.random.PCG64(43)))
+    a["posX"] -= np.float32(12.0)
+    b["posX"] += np.float32(12.0)
+    st = {k: np.concatenate([a[k], b[k]]) for k in a}
+    st["originalId"] = np.arange(4096, dtype=np.uint32)
+    p, alt, bvh = gpu_setup(st, packed=False)
+    engine.sort_and_build_bvh(p, alt, bvh)
+    engine.gravity_barnes_hut(p, bvh, theta)
+    o = oracle.Oracle(st)
+    o.sort_and_build()
+    o.gravity(theta)
+    g, c = p.download(), o.state()
+    e = report("gravity theta=%.1f" % theta, g, c, ["accX", "accY", "accZ", "phiGrav"])
+    assert max(e.values()) < TOL
+    acc, _ = oracle.direct_gravity_f64(g, np.arange(4096))
+    bh = np.stack([g["accX"], g["accY"], g["accZ"]], 1).astype(np.float64)
+    err = np.linalg.norm(bh - acc, axis=1) / np.linalg.norm(acc, axis=1)
+    print("AC-3 theta=%.1f median %.4f p99 %.4f" % (theta, np.median(err), np.sort(err)[int(0.99 * 4095)]))
+    if theta == 0.5:
+        assert np.median(err) < 0.015 and np.sort(err)[int(0.99 * 4095)] < 0.05
+
+
+def test_kick_drift_dt_parity():
+    st = c1_state()
+    p, alt, bvh = gpu_setup(st)
+    o = oracle.Oracle(st)
+    engine.clear_stats(p); o.clear_stats()
+    engine.sort_and_build_bvh(p, alt, bvh); o.sort_and_build()
+    engine.sph_pass1_neighbors(p, bvh); o.pass1()
+    engine.evaluate_eos(p); o.eos()
+    engine.gravity_barnes_hut(p, bvh); o.gravity()
+    engine.sph_pass2_forces(p, bvh); o.pass2()
+    dt_g = engine.reduce_dt_psu(p, 0.0, 5e-3)
+    dt_c, _ = o.reduce_dt(0.0, 5e-3)
+    print("dt gpu %.9g oracle %.9g" % (dt_g, dt_c))
+    engine.leapfrog_kick_half(p, 0.5 * dt_c, True, False)
+    o.kick(0.5 * dt_c)
+    g, c = p.download(), o.state()
+    e = report("kick", g, c, ["velX", "velY", "velZ", "rho", "u", "sXX", "sXY", "damage"])
+    assert max(e.values()) < TOL
+    engine.leapfrog_drift(p, dt_c, bvh)
+    o.drift(dt_c)
+    g, c = p.download(), o.state()
+    e = report("drift", g, c, ["posX", "posY", "posZ"])
+    assert max(e.values()) < 1e-6
+    # the GPU dt candidate uses the same IEEE operations: identical minimum
+    assert abs(dt_g - dt_c) <= 2e-7 * dt_c
+
+
+def test_fused_step_matches_stagewise_and_oracle():
+    st = c1_state(3072, 1024, seed=7)
+    sim_f = engine.Simulation(len(st["posX"]))
+    sim_s = engine.Simulation(len(st["posX"]))
+    for s in (sim_f, sim_s):
+        s.load_state(st)
+        s.evaluate_initial_forces()
+    o = oracle.Oracle(st)
+    o.initial_forces()
+    for k in range(4):
+        dt_f = sim_f.step(5e-3)
+        dt_s = sim_s.step_stagewise(5e-3)
+        dt_o = o.step(5e-3)
+        print("step %d dt fused %.9g stagewise %.9g oracle %.9g" % (k, dt_f, dt_s, dt_o))
+        assert abs(dt_f - dt_s) <= 1e-6 * dt_s and abs(dt_f - dt_o) <= 1e-5 * dt_o
+    gf, gs, c = sim_f.state(), sim_s.state(), o.state()
+    fields = ["posX", "posY", "posZ", "velX", "velY", "velZ", "rho", "u", "h", "accX", "accY", "accZ", "duDt",
+              "drhoDt", "pressure", "phiGrav"]
+    ef = report("fused-vs-oracle", gf, c, fields)
+    es = report("stagewise-vs-oracle", gs, c, fields)
+    report("fused-vs-stagewise", gf, gs, fields)
+    assert max(ef.values()) < 1e-4 and max(es.values()) < 1e-4
+    assert np.array_equal(gf["originalId"], gs["originalId"])
+
+
+@pytest.mark.parametrize("n", [1, 2, 33])
+def test_small_counts(n):
+    st = c1_state()
+    small = {k: v[:n].copy() for k, v in st.items()}
+    small["originalId"] = np.arange(n, dtype=np.uint32)
+    p, alt, bvh = gpu_setup(small)
+    o = oracle.Oracle(small)
+    engine.clear_stats(p); o.clear_stats()
+    engine.sort_and_build_bvh(p, alt, bvh); o.sort_and_build()
+    engine.sph_pass1_neighbors(p, bvh); o.pass1()
+    engine.evaluate_eos(p); o.eos()
+    engine.gravity_barnes_hut(p, bvh); o.gravity()
+    engine.sph_pass2_forces(p, bvh); o.pass2()
+    g, c = p.download(), o.state()
+    assert np.array_equal(g["originalId"], c["originalId"])
+    for f in ("h", "surfFactor", "accX", "phiGrav", "duDt"):
+        assert rel_rms(g[f], c[f]) < TOL or np.allclose(g[f], c[f], atol=1e-12), f
+
+
+def test_coincident_particles_tie_break():
+    n = 500
+    st = c1_state()
+    small = {k: v[:n].copy() for k, v in st.items()}
+    small["posX"][:250] = small["posX"][0]
+    small["posY"][:250] = small["posY"][0]
+    small["posZ"][:250] = small["posZ"][0]
+    small["originalId"] = np.arange(n, dtype=np.uint32)
+    p, alt, bvh = gpu_setup(small)
+    engine.sort_and_build_bvh(p, alt, bvh)
+    o = oracle.Oracle(small)
+    o.sort_and_build()
+    torch.cuda.synchronize()
+    assert np.array_equal(tnp(bvh.t["indicesSorted"], n, np.uint32), o.bvh.a["indicesSorted"])
+    assert np.array_equal(tnp(bvh.t["leftChild"], n - 1), o.bvh.a["leftChild"][: n - 1])
+
+
+def test_lookback_wait_gives_up_and_reports():
+    engine.reset_device_status()
+    out = ctypes.c_uint32(0)
+    rc = abi.load_library().astraea_gb300_debug_lookback_probe(1000, ctypes.byref(out))
+    assert rc == 4 and out.value == 2
+    flags, _ = engine.read_device_status()
+    assert flags & abi.DEVFLAG_LOOKBACK_TIMEOUT
+    # the context stays usable; the blocking dt call reports the timeout
+    st = c1_state(64, 32)
+    p, alt, bvh = gpu_setup(st)
+    with pytest.raises(abi.AstraeaError) as ei:
+        engine.reduce_dt_psu(p, 0.0, 1e-3)
+    assert ei.value.status == 4
+    engine.reset_device_status()
+    assert engine.reduce_dt_psu(p, 0.0, 1e-3) > 0.0
+
+
+def test_capacity_error_like_engine():
+    st = c1_state(64, 32)
+    p, alt, bvh = gpu_setup(st)
+    small = engine.TorchBvh(16)
+    with pytest.raises(abi.AstraeaError) as ei:
+        engine.sort_and_build_bvh(p, alt, small)
+    assert ei.value.status == 2
