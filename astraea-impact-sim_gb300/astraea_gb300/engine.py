@@ -238,6 +238,12 @@ def read_device_status():
     return flags.value, dict(zip(abi.COUNTERS, list(counters)))
 
 
+def measure_fp32_tflops():
+    out = ctypes.c_float(0.0)
+    abi.check(lib().astraea_gb300_measure_fp32_tflops(ctypes.byref(out)))
+    return out.value
+
+
 def reset_device_status():
     abi.check(lib().astraea_gb300_reset_device_status())
 

@@ -593,14 +593,10 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     const bool cacheOk = ws->stepCacheValid && ws->stepToken == static_cast<const void*>(p->posX);
     if (!cacheOk) {
         // Device dt state from the caller's previous dt and the current state.
-        float slots[2] = {0.0f, 0.0f};
-        slots[q] = prevDtPsu;
-        AG_CUDA(cudaMemcpyAsync(ws->dtSlots, slots, sizeof(slots), cudaMemcpyHostToDevice, st));
-        AG_CUDA(cudaMemsetAsync(ws->rawMin + q, 0x7f, sizeof(uint32_t), st));
+        AG_LAUNCH(launchSetDtSlots(ws->dtSlots, q, prevDtPsu, ws->rawMin, st));
         AG_LAUNCH(launchReduceDt(*p, n, ws->rawMin + q, sms, st));
         AG_LAUNCH(launchRefreshLeaves(*p, w, n, false, st));
         if (useBvh) AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
-        AG_CUDA(cudaStreamSynchronize(st));   // slots[] is a stack array
     }
     // 1. opening half kick; dt resolved on the device
     KickArgs k1{};
@@ -638,6 +634,12 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     ws->stepCacheValid = true;
     ws->stepToken = static_cast<const void*>(p->posX);
     ws->stepCount += 1;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_measure_fp32_tflops(float* outTflops) {
+    if (outTflops == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    AG_LAUNCH(measureFp32Tflops(smCount(), outTflops, stream()));
     return ASTRAEA_OK;
 }
 

@@ -142,6 +142,7 @@ struct MatConst {
     float muShear, tMelt, bulkK, yieldY0;
     // EOS (FP32 path)
     float rho0, a, b, A, B, E0, Eiv, Ecv, alpha, beta;
+    float rho0Lo;          // rho0 (double) - rho0 (float): the pair carries rho0 exactly
     float cv;              // MJ/(kg K)
     float cvTrefHi, cvTrefLo;   // cv * tRef as a float pair (hi + lo)
     float cMinCondensed;   // max(0.05, sqrt(A / rho0))
@@ -170,7 +171,8 @@ constexpr MatConst makeMat(double rho0Kg, double a, double b, double APa, double
                     static_cast<float>(y0Pa / 1.0e12), static_cast<float>(rho0), static_cast<float>(a),
                     static_cast<float>(b), static_cast<float>(A), static_cast<float>(BPa / 1.0e12),
                     static_cast<float>(E0 / 1.0e6), static_cast<float>(Eiv / 1.0e6), static_cast<float>(Ecv / 1.0e6),
-                    static_cast<float>(alpha), static_cast<float>(beta), static_cast<float>(cv), hi,
+                    static_cast<float>(alpha), static_cast<float>(beta),
+                    static_cast<float>(rho0 - static_cast<double>(static_cast<float>(rho0))), static_cast<float>(cv), hi,
                     static_cast<float>(cvTref - static_cast<double>(hi)),
                     static_cast<float>(cMin > 0.05 ? cMin : 0.05), static_cast<float>(0.8 * rho0Kg),
                     static_cast<float>((cvSI * 300.0) / 1.0e6), static_cast<float>(kH2), static_cast<float>(gamma)};
@@ -194,7 +196,10 @@ __device__ __forceinline__ int matIndex(uint8_t m) { return (m <= 4u) ? static_c
 // ---------------------------------------------------------------- EOS -----
 // FP32 evaluation of engine/eos.cu:283-388.  The reference evaluates in FP64;
 // here every cancellation-prone quantity is formed without loss:
-//   mu = (rho - rho0)/rho0 (exact difference when rho is within 2x of rho0),
+//   mu = ((rho - rho0_hi) - rho0_lo)/rho0 with rho0 = rho0_hi + rho0_lo the
+//     FP64 reference density split into two floats (the difference is exact
+//     when rho is within 2x of rho0, and the float rounding of rho0 itself,
+//     ~3e-8 relative, does not leak into mu),
 //   cold energy by its Taylor series for mu < 0.1,
 //   the thermal excess u - cv T_ref with cv T_ref split into a float pair.
 struct EosOut { float P, cs, T; uint8_t phase; };
@@ -203,8 +208,8 @@ __device__ __forceinline__ float coldEnergyF32(int mi, float rho) {
     const MatConst& c = c_mat[mi];
     rho = fmaxf(rho, 0.0f);
     if (mi == 3) return c.kH2 * rho;
-    if (!(rho > c.rho0)) return 0.0f;
-    const float mu = (rho - c.rho0) / c.rho0;
+    const float mu = ((rho - c.rho0) - c.rho0Lo) / c.rho0;
+    if (!(mu > 0.0f)) return 0.0f;
     float ta, tb;
     if (mu < 0.1f) {
         // termA = sum_{k>=2} (-1)^k (k-1)/k mu^k ; termB = sum_{k>=3} (-1)^(k+1) (k-2)/k mu^k
@@ -250,7 +255,7 @@ __device__ __forceinline__ PD tillotsonCompressedF32(const MatConst& c, float rh
 }
 
 __device__ __forceinline__ PD tillotsonExpandedF32(const MatConst& c, float rho, float eta, float mu, float uE) {
-    const float x = (c.rho0 - rho) / rho;          // 1/eta - 1, formed without cancellation
+    const float x = -mu / eta;                     // 1/eta - 1, formed without cancellation
     const float ax2 = c.alpha * x * x;
     const float bx = c.beta * x;
     const float eA = (ax2 < 700.0f) ? expf(-ax2) : 0.0f;
@@ -306,8 +311,8 @@ __device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, fl
         o.phase = classifyPhaseF32(mi, c, rho, u, T);
         return o;
     }
-    const float mu = (rho - c.rho0) / c.rho0;
-    const float eta = rho / c.rho0;
+    const float mu = ((rho - c.rho0) - c.rho0Lo) / c.rho0;   // additive uses
+    const float eta = rho / c.rho0;                           // multiplicative uses
     const float uCold = coldEnergyF32(mi, rho);
     const float T = fmaxf(3.0f, (u - uCold) / c.cv);
     const float excess = ((u - c.cvTrefHi) - c.cvTrefLo) - uCold;

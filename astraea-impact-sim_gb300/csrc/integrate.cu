@@ -197,6 +197,14 @@ __global__ void __launch_bounds__(256) driftPlainKernel(AstraeaParticles p, uint
     p.posZ[i] = static_cast<float>(static_cast<double>(p.posZ[i]) + d * static_cast<double>(p.velZ[i]));
 }
 
+__global__ void setDtSlotsKernel(float* slots, int parity, float prevDt, uint32_t* rawMin) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        slots[parity] = prevDt;
+        slots[parity ^ 1] = 0.0f;
+        rawMin[parity] = 0x7f7f7f7fu;
+    }
+}
+
 __global__ void __launch_bounds__(256) reduceDtKernel(AstraeaParticles p, uint32_t n, uint32_t* out) {
     float m = 1.0e30f;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -252,6 +260,11 @@ cudaError_t launchPackPass2Records(const AstraeaParticles& p, const Work& w, uin
 cudaError_t launchDriftPlain(const AstraeaParticles& p, uint32_t n, float dt, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     driftPlainKernel<<<gridFor(n, 256), 256, 0, st>>>(p, n, dt);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSetDtSlots(float* slots, int parity, float prevDt, uint32_t* rawMin, cudaStream_t st) {
+    setDtSlotsKernel<<<1, 32, 0, st>>>(slots, parity, prevDt, rawMin);
     return cudaGetLastError();
 }
 

@@ -95,9 +95,15 @@ struct KickArgs {
 };
 cudaError_t launchKick(const AstraeaParticles& p, uint32_t n, const KickArgs& a, cudaStream_t st);
 cudaError_t launchReduceDt(const AstraeaParticles& p, uint32_t n, uint32_t* rawMinOut, int sms, cudaStream_t st);
+// Arm the fused step's device dt state: slots[parity] = prevDt, raw minimum
+// word of this parity reset for a fresh reduction.
+cudaError_t launchSetDtSlots(float* slots, int parity, float prevDt, uint32_t* rawMin, cudaStream_t st);
 // Pass-2 records from the current SoA, without evaluating the EOS.
 cudaError_t launchPackPass2Records(const AstraeaParticles& p, const Work& w, uint32_t n, cudaStream_t st);
 // x += dt v without XSPH (drift without a tree, sph_gravity.cu:1484-1488).
 cudaError_t launchDriftPlain(const AstraeaParticles& p, uint32_t n, float dt, cudaStream_t st);
+
+// -------------------------------------------------------------- diag.cu ---
+cudaError_t measureFp32Tflops(int sms, float* tflops, cudaStream_t st);
 
 }  // namespace astraea_gb300

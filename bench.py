@@ -1,0 +1,399 @@
+#!/usr/bin/env python
+"""Throughput of the per-step physics path on GB300: particle-steps/s.
+
+Workload (--n, default 1,000,000): a differentiated Earth-Theia-like impact,
+800k-particle target + 200k impactor, Iron core 30 % of mass + Granite
+mantle, radial density from a 1-D hydrostatic integration, mass ratio 0.1,
+1.1 v_esc at 45 degrees, strength and damage on, plain Barnes-Hut at
+theta = 0.5 (seeded synthetic bodies; no dataset exists for this).
+
+A step is one Simulation::step kernel sequence (reduce-dt, kick, drift,
+sort + tree build, SPH pass 1, EOS, gravity, SPH pass 2, kick, EOS) on the
+whole particle set, through the library's fused C-ABI step.
+
+  value      N * steps / device time of the timed steps, inputs resident
+  e2e        same metric through the C-ABI with host buffers: every step
+             uploads the step's input fields from pinned host memory,
+             steps, and reads back the fields the engine's telemetry reads
+  roofline   the gravity kernel (dominant): 23 FLOP per evaluated pair
+             interaction (device counter) / CUDA-event launch time, against
+             the FP32 FMA throughput measured in this process
+  cpu_baseline  the CPU restatement of the reference algorithm (oracle/) on
+             the host cores, on a bounded sample of the same step
+
+--impl reference prints the CPU reference arm (the oracle port) on the same
+workload and metric.  Under torchrun each rank runs an independent replica
+(the path has no cross-GPU exchange; "replicas only"); value aggregates all
+ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "astraea-impact-sim_gb300"))
+
+METRIC = "particle-steps/s at N=1M, learned-θ vs plain BH at equal force error"
+UNIT = "particle-steps/s"
+FLOP_PER_INTERACTION = 23        # 20 force + 3 potential (rsqrt counted once)
+KERNELS_PER_STEP = 19            # kick, drift, histogram, 8 onesweep, permute, refit,
+                                 # neighbour lists, pass 1, EOS, gravity, pass 2, kick
+# Fields a fused step reads (uploaded every e2e step) and the fields the
+# engine's per-step telemetry reads back (engine/simulation.cpp:948-1000).
+E2E_IN = ["posX", "posY", "posZ", "velX", "velY", "velZ", "accX", "accY", "accZ", "mass", "h", "h0", "rho",
+          "drhoDt", "pressure", "soundSpeed", "u", "duDt", "tempK", "sXX", "sYY", "sZZ", "sXY", "sXZ", "sYZ",
+          "dSXX", "dSYY", "dSZZ", "dSXY", "dSXZ", "dSYZ", "damage", "damageCbrt", "dDamageCbrtDt", "epsFail",
+          "materialId", "phaseId", "bodyId", "originalId", "tracerIndex"]
+E2E_OUT = ["posX", "posY", "posZ", "velX", "velY", "velZ", "mass", "rho", "u", "phiGrav", "tempK", "pressure",
+           "radPowerW", "damage", "bodyId", "materialId", "originalId"]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--max-dt-sec", type=float, default=5.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
+    return ap.parse_args()
+
+
+def workload_config(n, theta):
+    return {
+        "workload": "differentiated Earth-Theia-like impact, N=%d (target %d + impactor %d), Iron core 30%% "
+                    "+ Granite mantle, hydrostatic radial density, mass ratio 0.1, 1.1 v_esc at 45 deg, strength "
+                    "+ damage on" % (n, n - int(round(0.2 * n)), int(round(0.2 * n))),
+        "n_particles": n,
+        "traversal": "plain Barnes-Hut theta=%.2f (learned far-field correction not built)" % theta,
+        "max_dt_psu": None,
+        "l2": "inputs larger than L2: particle SoA %.0f MB + tree/neighbour scratch ~%.0f MB (L2 129 MB)"
+              % (2 * n * 212 / 1e6, n * 1.15e3 / 1e6),
+        "parallelism": "replicas only (one independent simulation per GPU)",
+    }
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from astraea_gb300 import engine, scenarios
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n = args.n
+    max_dt = max(1.0e-5, args.max_dt_sec) / 1.0e3
+    st, info = scenarios.differentiated_impact(n_total=n, seed=42 + rank)
+    sim = engine.Simulation(n)
+    sim.load_state(st)
+    engine.reserve(sim.bvh, n)
+    sim.evaluate_initial_forces(args.theta)
+    for _ in range(max(args.warmup, 0)):
+        sim.step(max_dt, args.theta)
+    torch.cuda.synchronize()
+
+    # ---- timed region: fused steps, state resident in HBM
+    engine.reset_device_status()
+    dt_host = torch.zeros(1, dtype=torch.float32).pin_memory()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    prev = sim.prev_dt
+    for _ in range(args.steps):
+        engine.step(sim.p, sim.alt, sim.bvh, prev, max_dt, args.theta, dt_host.data_ptr())
+    e1.record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    flags, counters = engine.read_device_status()
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * n * args.steps / (ms_max / 1.0e3)
+    sim.prev_dt = float(dt_host[0])
+
+    # ---- dominant kernel: gravity, timed standalone on the current tree
+    reps = 5
+    engine.gravity_barnes_hut(sim.p, sim.bvh, args.theta)
+    torch.cuda.synchronize()
+    engine.reset_device_status()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(reps):
+        engine.gravity_barnes_hut(sim.p, sim.bvh, args.theta)
+    g1.record()
+    torch.cuda.synchronize()
+    _, gc = engine.read_device_status()
+    grav_ms = g0.elapsed_time(g1) / reps
+    inter = gc["gravity_interactions"] / reps
+    fp32_peak = engine.measure_fp32_tflops()
+    achieved = FLOP_PER_INTERACTION * inter / (grav_ms * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "gravity_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tr = json.load(open(tpath))
+            traffic = tr.get("bytes_per_particle") and tr["bytes_per_particle"] * n
+        except ValueError:
+            traffic = None
+
+    # ---- force error of the plain path vs an FP64 direct sum (sampled targets)
+    err_rms = force_error_fp64(sim, engine, torch, np, samples=1024)
+
+    # ---- e2e through the C-ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sim, engine, torch, args, max_dt, world, dist)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 in drift, refit moments)",
+        "data": "synthetic (seeded hydrostatic bodies)",
+        "config": workload_config(n, args.theta),
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "clocks": clk,
+        "roofline": {"kernel": "gravity (Barnes-Hut group walk + pair evaluation)", "bound": "fp32",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if fp32_peak else None, "traffic": traffic,
+                     "peak_source": "measured in-process (FP32 FMA kernel); bf16/HBM peaks of "
+                                    "MEASURED_PEAKS.json do not bound this kernel",
+                     "interactions_per_launch": inter, "launch_ms": grav_ms},
+        "step_hbm": step_hbm_roofline(n, ms_max / args.steps),
+        "force_error_rms_vs_fp64": err_rms,
+        "device_flags": flags,
+        "e2e": e2e,
+    }
+    out["config"]["max_dt_psu"] = max_dt
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(st, args, max_dt)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def step_hbm_roofline(n, ms):
+    """Compulsory bytes per particle-step of the reference SoA (1.58 KB, the
+    per-stage sum of the engine's reads/writes) against measured HBM."""
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        peak = 6800.0
+    achieved = 1580.0 * n / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "bytes_per_particle_step": 1580.0}
+
+
+def force_error_fp64(sim, engine, torch, np, samples=1024):
+    """RMS of |a - a_FP64| / |a_FP64| over sampled targets; the FP64 direct sum
+    (eps_ij softening, G_PSU) runs on the GPU in torch float64."""
+    engine.gravity_barnes_hut(sim.p, sim.bvh, 0.5)
+    torch.cuda.synchronize()
+    n = sim.p.count
+    A = sim.p.arrays
+    g = torch.Generator(device="cpu").manual_seed(1234)
+    tgt = torch.randperm(n, generator=g)[:samples].cuda()
+    pos = torch.stack([A["posX"][:n], A["posY"][:n], A["posZ"][:n]], 1).double()
+    m = A["mass"][:n].double()
+    eps = 0.8 * torch.clamp(A["h0"][:n].double(), min=1e-6)
+    G = 6.67430e-11 * 1e24 * 1e6 / 1e18
+    acc = torch.zeros(samples, 3, dtype=torch.float64, device="cuda")
+    pt, et = pos[tgt], eps[tgt]
+    for s0 in range(0, n, 1 << 16):
+        s1 = min(n, s0 + (1 << 16))
+        d = pt[:, None, :] - pos[None, s0:s1, :]
+        e = 0.5 * (et[:, None] + eps[None, s0:s1])
+        r2 = (d * d).sum(-1) + e * e
+        w = m[None, s0:s1] * r2.rsqrt() ** 3
+        idx = torch.arange(s0, s1, device="cuda")
+        w = torch.where(tgt[:, None] == idx[None, :], torch.zeros_like(w), w)
+        acc -= G * (w[:, :, None] * d).sum(1)
+    bh = torch.stack([A["accX"][:n][tgt], A["accY"][:n][tgt], A["accZ"][:n][tgt]], 1).double()
+    rel = (bh - acc).norm(dim=1) / acc.norm(dim=1)
+    return float(torch.sqrt((rel * rel).mean()))
+
+
+def run_e2e(sim, engine, torch, args, max_dt, world, dist):
+    n = sim.p.count
+    host_in = {f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in E2E_IN}
+    host_out = {f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in E2E_OUT}
+    for f in E2E_IN:
+        host_in[f].copy_(sim.p.arrays[f][:n])
+    dt_host = torch.zeros(1, dtype=torch.float32).pin_memory()
+    bi = sum(t.numel() * t.element_size() for t in host_in.values())
+    bo = sum(t.numel() * t.element_size() for t in host_out.values()) + 4
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        for f in E2E_IN:
+            sim.p.arrays[f][:n].copy_(host_in[f], non_blocking=True)
+        engine.invalidate_step_cache(sim.bvh)
+        engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, args.theta, dt_host.data_ptr())
+        for f in E2E_OUT:
+            host_out[f].copy_(sim.p.arrays[f][:n], non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return {"value": world * n * args.steps / (float(t.item()) / 1e3), "unit": UNIT,
+            "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
+            "note": "every step: H2D of the step's input fields from pinned memory, fused step (step cache "
+                    "invalidated: neighbour lists and dt recomputed from the uploaded state), D2H of the "
+                    "engine telemetry fields and dt"}
+
+
+# ------------------------------------------------------------- CPU arm
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    return oracle
+
+
+def cpu_sampled_step_rate(st, stride, max_dt, steps=1, warmup=0):
+    """Particle-steps/s of the oracle (the reference algorithm restated for the
+    CPU, OpenMP over all host cores) on the full workload, with the four
+    tree-walking stages run on every stride-th group and their time scaled by
+    stride; the O(N) stages (sort, permutation, tree build, EOS, kicks, dt)
+    run in full.  Returns (rate, seconds of CPU work spent, detail)."""
+    oracle = _oracle()
+    o = oracle.Oracle(st)
+    oracle.set_group_stride(stride)
+    t_all = time.perf_counter()
+    o.initial_forces()
+    walk, full = 0.0, 0.0
+    for k in range(warmup + steps):
+        t = {}
+        c = time.perf_counter()
+        dt, _ = o.reduce_dt(o.prev_dt, max_dt); o.prev_dt = dt
+        o.kick(0.5 * dt); t["kick1"] = time.perf_counter() - c; c = time.perf_counter()
+        o.drift(dt); t["drift"] = time.perf_counter() - c; c = time.perf_counter()
+        o.sort_and_build(); t["build"] = time.perf_counter() - c; c = time.perf_counter()
+        o.pass1(); t["pass1"] = time.perf_counter() - c; c = time.perf_counter()
+        o.eos(); t["eos"] = time.perf_counter() - c; c = time.perf_counter()
+        o.gravity(); t["gravity"] = time.perf_counter() - c; c = time.perf_counter()
+        o.pass2(); t["pass2"] = time.perf_counter() - c; c = time.perf_counter()
+        o.kick(0.5 * dt); o.eos(); t["kick2"] = time.perf_counter() - c
+        if k >= warmup:
+            walk += t["drift"] + t["pass1"] + t["gravity"] + t["pass2"]
+            full += t["kick1"] + t["build"] + t["eos"] + t["kick2"]
+    oracle.set_group_stride(1)
+    per_step = (full + stride * walk) / steps
+    n = len(st["posX"])
+    return n / per_step, time.perf_counter() - t_all, {"walk_s": walk / steps, "linear_s": full / steps}
+
+
+def cpu_baseline(st, args, max_dt):
+    n = len(st["posX"])
+    stride = args.cpu_stride or 2
+    rate, spent, det = cpu_sampled_step_rate(st, stride, max_dt, steps=1)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "1 step of the same N=%d workload: tree walks (drift, pass 1, gravity, pass 2) on every "
+                      "%d-th group of 32, time scaled by %d; sort/permute/build/EOS/kicks/dt in full (%.1f s "
+                      "of CPU work)" % (n, stride, stride, spent)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from astraea_gb300 import scenarios
+    n = args.n
+    max_dt = max(1.0e-5, args.max_dt_sec) / 1.0e3
+    st, _ = scenarios.differentiated_impact(n_total=n, seed=42)
+    stride = args.cpu_stride or 4
+    rate, spent, det = cpu_sampled_step_rate(st, stride, max_dt, steps=max(args.steps, 1), warmup=max(args.warmup, 0))
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = ("%d warm-up + %d timed steps of the N=%d workload on the CPU restatement of the reference kernels "
+              "(the reference has no CPU kernels of its own): tree walks on every %d-th group of 32, scaled by %d"
+              % (args.warmup, args.steps, n, stride, stride))
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": n / rate * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (reference kernels restated; FP64 EOS)", "data": "synthetic",
+        "config": workload_config(n, args.theta),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "detail": det, "cpu_seconds": spent,
+    }))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)

@@ -218,6 +218,10 @@ AstraeaStatus astraea_gb300_radix_sort_pairs(uint64_t* keysIn, uint64_t* keysOut
 #define ASTRAEA_DEVFLAG_STACK_OVERFLOW     0x4u
 #define ASTRAEA_DEVFLAG_GROUP_FALLBACK     0x8u
 AstraeaStatus astraea_gb300_read_device_status(uint32_t* outFlags, uint64_t* outCounters8);
+/* Measured FP32 FMA throughput of the current device in TFLOP/s (the
+ * denominator of the gravity kernel's roofline).  Blocks; no engine
+ * counterpart. */
+AstraeaStatus astraea_gb300_measure_fp32_tflops(float* outTflops);
 AstraeaStatus astraea_gb300_reset_device_status(void);
 /* Test hook: lower the onesweep look-back spin limit (0 restores default). */
 AstraeaStatus astraea_gb300_set_lookback_spin_limit(uint32_t limit);

@@ -293,6 +293,11 @@ inline NodeBox nodeBox(const AstraeaRadixBvh& b, int c) {
 
 int numGroups(uint32_t n) { return static_cast<int>((n + kGroup - 1) / kGroup); }
 
+// Timing sample for the CPU baseline: tree-walking stages visit only groups
+// g with g % g_groupStride == 0 (1 = all groups, the normal checker mode).
+int g_groupStride = 1;
+inline bool skipGroup(int g) { return g_groupStride > 1 && (g % g_groupStride) != 0; }
+
 // Depth-first walk shared by the SPH-style traversals: `open(c)` decides
 // whether the group descends into internal node c; `leaf(j)` visits particle
 // j.  The stack discipline (pop, left child then right child, push opened
@@ -525,9 +530,10 @@ template <typename R>
 static void pass1Impl(AstraeaParticles* p, const AstraeaRadixBvh* b) {
     const uint32_t n = p->count;
     const int G = numGroups(n);
-    std::vector<float> hNew(n);
+    std::vector<float> hNew(p->h, p->h + n);   // groups skipped by a timing sample keep h
 #pragma omp parallel for schedule(dynamic, 4)
     for (int g = 0; g < G; ++g) {
+        if (skipGroup(g)) continue;
         const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
         const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
         R xi[kGroup], yi[kGroup], zi[kGroup], vx[kGroup], vy[kGroup], vz[kGroup], hi[kGroup], h0i[kGroup], Hi[kGroup], Hi2[kGroup];
@@ -624,6 +630,7 @@ void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, 
     uint64_t total = 0;
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : total)
     for (int g = 0; g < G; ++g) {
+        if (skipGroup(g)) continue;
         const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
         const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
         float xi[kGroup], yi[kGroup], zi[kGroup], eI[kGroup], eI2[kGroup];
@@ -729,6 +736,7 @@ static void pass2Impl(AstraeaParticles* p, const AstraeaRadixBvh* b) {
     const bool livingIntact = b->livingFlags ? (b->livingFlags[1] != 0u) : false;
 #pragma omp parallel for schedule(dynamic, 4)
     for (int g = 0; g < G; ++g) {
+        if (skipGroup(g)) continue;
         const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
         const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
         struct Lane {
@@ -969,10 +977,11 @@ void oracle_kick_half(AstraeaParticles* p, float hdt, int clampThermal) {
 // positions (the reference kernel reads them while other threads write).
 void oracle_drift(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int useBvh) {
     const uint32_t n = p->count;
-    std::vector<float> nx(n), ny(n), nz(n);
+    std::vector<float> nx(p->posX, p->posX + n), ny(p->posY, p->posY + n), nz(p->posZ, p->posZ + n);
     const int G = numGroups(n);
 #pragma omp parallel for schedule(dynamic, 4)
     for (int g = 0; g < G; ++g) {
+        if (skipGroup(g)) continue;
         const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
         const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
         float xi[kGroup], yi[kGroup], zi[kGroup], vxi[kGroup], vyi[kGroup], vzi[kGroup], Hi[kGroup], rhoI[kGroup];
@@ -1069,5 +1078,6 @@ float oracle_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* b
 }
 
 int oracle_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
+void oracle_set_group_stride(int k) { g_groupStride = k < 1 ? 1 : k; }
 
 }  // extern "C"

@@ -59,6 +59,7 @@ def load(build=True):
             getattr(_lib, name).argtypes = args
         _lib.oracle_reduce_dt.restype = f
         _lib.oracle_step.restype = f
+        _lib.oracle_set_group_stride.argtypes = [ctypes.c_int]
         _lib.oracle_cold_energy.restype = ctypes.c_double
         _lib.oracle_cold_energy.argtypes = [ctypes.c_int, ctypes.c_double]
     return _lib
@@ -228,6 +229,11 @@ class Oracle:
 
     def state(self):
         return self.p.state()
+
+
+def set_group_stride(k):
+    """Tree-walking stages visit every k-th group only (CPU timing sample)."""
+    load().oracle_set_group_stride(int(k))
 
 
 def eos_batch(mat, rho, u, dmg, reference=False):

@@ -123,6 +123,24 @@ def test_pass1_eos_gravity_pass2_parity():
     assert max(e.values()) < TOL
 
 
+def test_eos_kernel_vs_reference_golden(golden_dir):
+    """The FP32 EOS kernel against the reference's own FP64 EOS outputs."""
+    g = np.load(golden_dir + "/eos_reference.npz")
+    n = len(g["rho"])
+    st = scenarios.empty_state(n)
+    st["materialId"][:], st["rho"][:], st["u"][:], st["damage"][:] = g["mat"], g["rho"], g["u"], g["dmg"]
+    p = engine.DeviceParticles(n)
+    p.upload(st)
+    engine.evaluate_eos(p)
+    out = p.download(["pressure", "soundSpeed", "tempK", "phaseId"])
+    for m in range(5):
+        sel = g["mat"] == m
+        e = {k: rel_rms(out[f][sel], g[k][sel]) for f, k in (("pressure", "P"), ("soundSpeed", "cs"), ("tempK", "T"))}
+        agree = np.mean(out["phaseId"][sel] == g["phase"][sel])
+        print("eos material %d %s phase-agree %.5f" % (m, " ".join("%s=%.2e" % kv for kv in e.items()), agree))
+        assert max(e.values()) < TOL and agree > 0.995
+
+
 @pytest.mark.parametrize("theta", [0.5, 0.7])
 def test_gravity_parity_and_ac3_error(theta):
     a, _ = scenarios._layered_body(2048, 6.417e-1, 0.3, 2200.0, 0, np.random.Generator(np.random.PCG64(42)))
