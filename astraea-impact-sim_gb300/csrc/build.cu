@@ -204,8 +204,11 @@ __device__ __forceinline__ ChildData loadChild(const Work& w, int c, int n) {
 __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, uint32_t n) {
     const uint32_t leafIdx = blockIdx.x * blockDim.x + threadIdx.x;
     if (leafIdx >= n || n < 2u) return;
-    int curr = static_cast<int>((n - 1u) + leafIdx);
-    int pNode = __ldcg(&bvh.parent[curr]);
+    // The data of the node this thread just finished stays in registers; at
+    // each level only the sibling is loaded (the engine reloads both children).
+    int curr = ~static_cast<int>(leafIdx);          // child reference of the leaf
+    ChildData mine = loadChild(w, curr, static_cast<int>(n));
+    int pNode = __ldcg(&bvh.parent[(n - 1u) + leafIdx]);
     // A radix tree over 63-bit keys + 32-bit index ties is at most 96 deep;
     // the bound only matters for a tree built from a failed sort.
     for (int level = 0; pNode >= 0; ++level) {
@@ -213,52 +216,57 @@ __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, 
             atomicOr(&w.status->flags, kFlagStackOverflow);
             return;
         }
+        // loads that do not depend on the arrival order, issued before the atomic
+        const int lc = __ldcg(&bvh.leftChild[pNode]);
+        const int rc = __ldcg(&bvh.rightChild[pNode]);
+        const int grand = __ldcg(&bvh.parent[pNode]);
         __threadfence();
         if (atomicAdd(&bvh.atomicVisited[pNode], 1u) == 0u) return;   // first arrival stops
         __threadfence();
-        const int lc = __ldcg(&bvh.leftChild[pNode]);
-        const int rc = __ldcg(&bvh.rightChild[pNode]);
-        const ChildData L = loadChild(w, lc, static_cast<int>(n));
-        const ChildData R = loadChild(w, rc, static_cast<int>(n));
-        const float mnx = fminf(L.mnx, R.mnx), mny = fminf(L.mny, R.mny), mnz = fminf(L.mnz, R.mnz);
-        const float mxx = fmaxf(L.mxx, R.mxx), mxy = fmaxf(L.mxy, R.mxy), mxz = fmaxf(L.mxz, R.mxz);
-        const float maxH = fmaxf(L.maxH, R.maxH);
-        const float maxHs = fmaxf(L.maxHs, R.maxHs);
-        const NodeMom mom{L.mom.sx + R.mom.sx, L.mom.sy + R.mom.sy, L.mom.sz + R.mom.sz, L.mom.m + R.mom.m};
-        float cx, cy, cz;
-        if (mom.m > 0.0) {
-            const double im = 1.0 / mom.m;
-            cx = static_cast<float>(mom.sx * im);
-            cy = static_cast<float>(mom.sy * im);
-            cz = static_cast<float>(mom.sz * im);
+        const bool fromLeft = (lc == curr);
+        const ChildData other = loadChild(w, fromLeft ? rc : lc, static_cast<int>(n));
+        const ChildData& L = fromLeft ? mine : other;
+        const ChildData& R = fromLeft ? other : mine;
+        ChildData out;
+        out.mnx = fminf(L.mnx, R.mnx); out.mny = fminf(L.mny, R.mny); out.mnz = fminf(L.mnz, R.mnz);
+        out.mxx = fmaxf(L.mxx, R.mxx); out.mxy = fmaxf(L.mxy, R.mxy); out.mxz = fmaxf(L.mxz, R.mxz);
+        out.maxH = fmaxf(L.maxH, R.maxH);
+        out.maxHs = fmaxf(L.maxHs, R.maxHs);
+        out.mom = NodeMom{L.mom.sx + R.mom.sx, L.mom.sy + R.mom.sy, L.mom.sz + R.mom.sz, L.mom.m + R.mom.m};
+        if (out.mom.m > 0.0) {
+            const double im = 1.0 / out.mom.m;
+            out.cx = static_cast<float>(out.mom.sx * im);
+            out.cy = static_cast<float>(out.mom.sy * im);
+            out.cz = static_cast<float>(out.mom.sz * im);
         } else {                                   // massless subtree (sph_gravity.cu:591-595)
-            cx = 0.5f * (L.cx + R.cx);
-            cy = 0.5f * (L.cy + R.cy);
-            cz = 0.5f * (L.cz + R.cz);
+            out.cx = 0.5f * (L.cx + R.cx);
+            out.cy = 0.5f * (L.cy + R.cy);
+            out.cz = 0.5f * (L.cz + R.cz);
         }
-        const float mSum = static_cast<float>(mom.m);
-        const float dNode = fmaxf(mxx - mnx, fmaxf(mxy - mny, mxz - mnz));
+        const float mSum = static_cast<float>(out.mom.m);
+        const float dNode = fmaxf(out.mxx - out.mnx, fmaxf(out.mxy - out.mny, out.mxz - out.mnz));
         float4* rec = w.node + 4 * static_cast<size_t>(pNode);
-        __stcg(&rec[0], make_float4(cx, cy, cz, mSum));
-        __stcg(&rec[1], make_float4(dNode, __int_as_float(lc), __int_as_float(rc), maxHs));
-        __stcg(&rec[2], make_float4(mnx, mny, mnz, maxH));
-        __stcg(&rec[3], make_float4(mxx, mxy, mxz, 0.0f));
+        __stcg(&rec[0], make_float4(out.cx, out.cy, out.cz, mSum));
+        __stcg(&rec[1], make_float4(dNode, __int_as_float(lc), __int_as_float(rc), out.maxHs));
+        __stcg(&rec[2], make_float4(out.mnx, out.mny, out.mnz, out.maxH));
+        __stcg(&rec[3], make_float4(out.mxx, out.mxy, out.mxz, 0.0f));
         double2* mp = reinterpret_cast<double2*>(w.nodeMom + pNode);
-        __stcg(&mp[0], make_double2(mom.sx, mom.sy));
-        __stcg(&mp[1], make_double2(mom.sz, mom.m));
+        __stcg(&mp[0], make_double2(out.mom.sx, out.mom.sy));
+        __stcg(&mp[1], make_double2(out.mom.sz, out.mom.m));
         if (bvh.aabbMinX != nullptr) {
-            bvh.aabbMinX[pNode] = mnx; bvh.aabbMinY[pNode] = mny; bvh.aabbMinZ[pNode] = mnz;
-            bvh.aabbMaxX[pNode] = mxx; bvh.aabbMaxY[pNode] = mxy; bvh.aabbMaxZ[pNode] = mxz;
-            bvh.nodeMaxH[pNode] = maxH; bvh.nodeMass[pNode] = mSum;
-            bvh.comX[pNode] = cx; bvh.comY[pNode] = cy; bvh.comZ[pNode] = cz;
+            bvh.aabbMinX[pNode] = out.mnx; bvh.aabbMinY[pNode] = out.mny; bvh.aabbMinZ[pNode] = out.mnz;
+            bvh.aabbMaxX[pNode] = out.mxx; bvh.aabbMaxY[pNode] = out.mxy; bvh.aabbMaxZ[pNode] = out.mxz;
+            bvh.nodeMaxH[pNode] = out.maxH; bvh.nodeMass[pNode] = mSum;
+            bvh.comX[pNode] = out.cx; bvh.comY[pNode] = out.cy; bvh.comZ[pNode] = out.cz;
         }
         if (bvh.nodeComMass != nullptr) {
-            bvh.nodeComMass[pNode] = AstraeaFloat4{cx, cy, cz, mSum};
-            bvh.nodeMinExtent[pNode] = AstraeaFloat4{mnx, mny, mnz, dNode};
-            bvh.nodeMaxHPacked[pNode] = AstraeaFloat4{mxx, mxy, mxz, maxH};
+            bvh.nodeComMass[pNode] = AstraeaFloat4{out.cx, out.cy, out.cz, mSum};
+            bvh.nodeMinExtent[pNode] = AstraeaFloat4{out.mnx, out.mny, out.mnz, dNode};
+            bvh.nodeMaxHPacked[pNode] = AstraeaFloat4{out.mxx, out.mxy, out.mxz, out.maxH};
         }
+        mine = out;
         curr = pNode;
-        pNode = __ldcg(&bvh.parent[curr]);
+        pNode = grand;
     }
 }
 

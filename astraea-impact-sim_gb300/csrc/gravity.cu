@@ -9,9 +9,11 @@
 // particle-particle with eps_ij = (eps_i + eps_j)/2, monopoles with eps_i.
 //
 // GB300 restructuring (same sets, different schedule):
-//   * the group walk is node-parallel: up to 32 pending nodes are tested at
-//     once, one per lane, against the group (a sound group-box bound accepts
-//     most far nodes with one test, the rest are tested member by member);
+//   * the group walk is node-parallel: up to 32 pending nodes are loaded at
+//     once, one per lane; a sound group-box bound accepts most far nodes, an
+//     exact test of one representative member opens most near ones, and the
+//     few undecided nodes are tested by all 32 members at once (one node per
+//     warp iteration, one vote), so no lane loops over the group alone;
 //   * accepted monopoles and reached leaves are appended to two per-warp
 //     interaction lists in shared memory; every 32 entries the warp evaluates
 //     them with each lane summing its own particle's force from broadcast
@@ -31,13 +33,25 @@ struct GravWarpSmem {
     float4 mlist[kGravList];   // {comX, comY, comZ, G*mass}
     float4 plist[kGravList];   // {x, y, z, G*m}
     float2 paux[kGravList];    // {eps_j, j (int bits)}
-    float4 gpos[32];           // group members {x, y, z, 0}
 };
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
     uint32_t m;
     asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
+}
+
+// The engine's per-member acceptance test (sph_gravity.cu:914-929) with
+// explicit IEEE rounding: dNode^2 < theta^2 r^2, r^2 > 1e-20 and, when
+// checkInside, the member outside the node box.
+__device__ __forceinline__ bool acceptsMember(float px, float py, float pz, float4 com, float dd, float theta2,
+                                              bool checkInside, float4 bmin, float4 bmax) {
+    const float r2 = len2Exact(__fsub_rn(px, com.x), __fsub_rn(py, com.y), __fsub_rn(pz, com.z));
+    bool ok = (dd < __fmul_rn(theta2, r2)) && (r2 > 1.0e-20f);
+    if (ok && checkInside && px >= bmin.x && px <= bmax.x && py >= bmin.y && py <= bmax.y && pz >= bmin.z &&
+        pz <= bmax.z)
+        ok = false;
+    return ok;
 }
 
 struct Accum {
@@ -119,10 +133,22 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         }
         const float xi = me.x, yi = me.y, zi = me.z;
         const float epsI2 = epsI * epsI;
-        S.gpos[lane] = make_float4(xi, yi, zi, 0.0f);
         const float gminx = warpMinF(active ? xi : 3.0e38f), gmaxx = warpMaxF(active ? xi : -3.0e38f);
         const float gminy = warpMinF(active ? yi : 3.0e38f), gmaxy = warpMaxF(active ? yi : -3.0e38f);
         const float gminz = warpMinF(active ? zi : 3.0e38f), gmaxz = warpMaxF(active ? zi : -3.0e38f);
+        // representative member: the one nearest the group-box centre
+        const float cxg = 0.5f * (gminx + gmaxx), cyg = 0.5f * (gminy + gmaxy), czg = 0.5f * (gminz + gmaxz);
+        float dc = active ? (xi - cxg) * (xi - cxg) + (yi - cyg) * (yi - cyg) + (zi - czg) * (zi - czg) : 3.0e38f;
+        int best = lane;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float od = __shfl_xor_sync(0xffffffffu, dc, o);
+            const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+            if (od < dc || (od == dc && ob < best)) { dc = od; best = ob; }
+        }
+        const float repx = __shfl_sync(0xffffffffu, xi, best);
+        const float repy = __shfl_sync(0xffffffffu, yi, best);
+        const float repz = __shfl_sync(0xffffffffu, zi, best);
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, mCount = 0, pCount = 0;
         uint32_t rounds = 0;
@@ -146,14 +172,16 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             bool accept = false;
             float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             int cl = 0, cr = 0;
+            bool undecided = false;
+            float dd = 0.0f;
+            float4 bmin = make_float4(0.f, 0.f, 0.f, 0.f), bmax = bmin;
             if (isNode) {
                 const float4* rec = w.node + 4 * static_cast<size_t>(c);
                 r0 = __ldg(&rec[0]);
                 const float4 r1 = __ldg(&rec[1]);
                 cl = __float_as_int(r1.y);
                 cr = __float_as_int(r1.z);
-                const float dd = __fmul_rn(r1.x, r1.x);
-                float4 bmin = make_float4(0.f, 0.f, 0.f, 0.f), bmax = bmin;
+                dd = __fmul_rn(r1.x, r1.x);
                 bool disjoint = true;
                 if (checkInside) {
                     bmin = __ldg(&rec[2]);
@@ -161,27 +189,39 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                     disjoint = bmax.x < gminx || bmin.x > gmaxx || bmax.y < gminy || bmin.y > gmaxy ||
                                bmax.z < gminz || bmin.z > gmaxz;
                 }
-                // Sound group test: every member lies in the group box, so its
-                // distance to the COM is at least the box distance D; the 1e-5
-                // margin covers the rounding of both computations.
+                // (1) Sound group test: every member lies in the group box, so
+                // its distance to the COM is at least the box distance D; the
+                // 1e-5 margin covers the rounding of both computations.
                 const float bx = fmaxf(0.0f, fmaxf(gminx - r0.x, r0.x - gmaxx));
                 const float by = fmaxf(0.0f, fmaxf(gminy - r0.y, r0.y - gmaxy));
                 const float bz = fmaxf(0.0f, fmaxf(gminz - r0.z, r0.z - gmaxz));
                 const float D2 = bx * bx + by * by + bz * bz;
                 if (disjoint && D2 > 2.0e-20f && dd < theta2 * D2 * 0.99999f) {
                     accept = true;
+                } else if (!acceptsMember(repx, repy, repz, r0, dd, theta2, checkInside, bmin, bmax)) {
+                    accept = false;   // (2) one member (the representative) already opens it
                 } else {
-                    accept = true;
-                    for (int q = 0; q < act; ++q) {
-                        const float4 pq = S.gpos[q];
-                        const float r2 = len2Exact(__fsub_rn(pq.x, r0.x), __fsub_rn(pq.y, r0.y), __fsub_rn(pq.z, r0.z));
-                        bool ok = (dd < __fmul_rn(theta2, r2)) && (r2 > 1.0e-20f);
-                        if (ok && checkInside && pq.x >= bmin.x && pq.x <= bmax.x && pq.y >= bmin.y &&
-                            pq.y <= bmax.y && pq.z >= bmin.z && pq.z <= bmax.z)
-                            ok = false;
-                        if (!ok) { accept = false; break; }
-                    }
+                    undecided = true; // (3) decided below by the whole group
                 }
+            }
+            // (3) exact test of each undecided node by all members at once
+            unsigned und = __ballot_sync(0xffffffffu, undecided);
+            while (und) {
+                const int k = __ffs(und) - 1;
+                und &= und - 1;
+                float4 q = make_float4(__shfl_sync(0xffffffffu, r0.x, k), __shfl_sync(0xffffffffu, r0.y, k),
+                                       __shfl_sync(0xffffffffu, r0.z, k), 0.0f);
+                const float ddk = __shfl_sync(0xffffffffu, dd, k);
+                float4 mn = bmin, mx = bmax;
+                if (checkInside) {
+                    mn = make_float4(__shfl_sync(0xffffffffu, bmin.x, k), __shfl_sync(0xffffffffu, bmin.y, k),
+                                     __shfl_sync(0xffffffffu, bmin.z, k), 0.0f);
+                    mx = make_float4(__shfl_sync(0xffffffffu, bmax.x, k), __shfl_sync(0xffffffffu, bmax.y, k),
+                                     __shfl_sync(0xffffffffu, bmax.z, k), 0.0f);
+                }
+                const bool ok = !active || acceptsMember(xi, yi, zi, q, ddk, theta2, checkInside, mn, mx);
+                const bool all = __all_sync(0xffffffffu, ok);
+                if (lane == k) accept = all;
             }
             bool open = isNode && !accept;
             unsigned openMask = __ballot_sync(0xffffffffu, open);

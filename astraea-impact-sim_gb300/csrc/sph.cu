@@ -29,7 +29,6 @@ struct NbWarpSmem {
     int stack[kNbStack];
     float4 cand[kNbList];    // {x, y, z, Hs}
     int candIdx[kNbList];
-    float4 gpos[32];         // {x, y, z, Hs}
 };
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
@@ -69,11 +68,23 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
             me = __ldg(&w.leafPM[i]);
             Hs = __ldg(&w.leafAux[i]).x;
         }
-        S.gpos[lane] = make_float4(me.x, me.y, me.z, Hs);
         const float gminx = warpMinF(active ? me.x : 3.0e38f), gmaxx = warpMaxF(active ? me.x : -3.0e38f);
         const float gminy = warpMinF(active ? me.y : 3.0e38f), gmaxy = warpMaxF(active ? me.y : -3.0e38f);
         const float gminz = warpMinF(active ? me.z : 3.0e38f), gmaxz = warpMaxF(active ? me.z : -3.0e38f);
         const float gHs = warpMaxF(Hs);
+        // representative member: the one nearest the group-box centre
+        const float cxg = 0.5f * (gminx + gmaxx), cyg = 0.5f * (gminy + gmaxy), czg = 0.5f * (gminz + gmaxz);
+        float dc = active ? (me.x - cxg) * (me.x - cxg) + (me.y - cyg) * (me.y - cyg) + (me.z - czg) * (me.z - czg)
+                          : 3.0e38f;
+        int best = lane;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float od = __shfl_xor_sync(0xffffffffu, dc, o);
+            const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+            if (od < dc || (od == dc && ob < best)) { dc = od; best = ob; }
+        }
+        const float repx = __shfl_sync(0xffffffffu, me.x, best), repy = __shfl_sync(0xffffffffu, me.y, best);
+        const float repz = __shfl_sync(0xffffffffu, me.z, best), repHs = __shfl_sync(0xffffffffu, Hs, best);
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, cCount = 0;
         uint32_t cnt = 0, rounds = 0;
@@ -108,29 +119,44 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
             const bool isLeaf = has && c < 0;
             bool open = false;
             int cl = 0, cr = 0;
+            bool undecided = false;
+            float4 bmin = make_float4(0.f, 0.f, 0.f, 0.f), bmax = bmin;
+            float nodeHs = 0.0f;
             if (has && c >= 0) {
                 const float4* rec = w.node + 4 * static_cast<size_t>(c);
                 const float4 r1 = __ldg(&rec[1]);
-                const float4 bmin = __ldg(&rec[2]);
-                const float4 bmax = __ldg(&rec[3]);
+                bmin = __ldg(&rec[2]);
+                bmax = __ldg(&rec[3]);
                 cl = __float_as_int(r1.y);
                 cr = __float_as_int(r1.z);
-                // box-box distance bounds every member's point-box distance
+                nodeHs = r1.w;
+                // (1) box-box distance bounds every member's point-box distance
                 const float dx = fmaxf(0.0f, fmaxf(bmin.x - gmaxx, gminx - bmax.x));
                 const float dy = fmaxf(0.0f, fmaxf(bmin.y - gmaxy, gminy - bmax.y));
                 const float dz = fmaxf(0.0f, fmaxf(bmin.z - gmaxz, gminz - bmax.z));
-                const float Rg = fmaxf(gHs, r1.w);
+                const float Rg = fmaxf(gHs, nodeHs);
                 if (dx * dx + dy * dy + dz * dz <= Rg * Rg * 1.00001f) {
-                    for (int q = 0; q < act; ++q) {
-                        const float4 pq = S.gpos[q];
-                        const float R = fmaxf(pq.w, r1.w);
-                        if (pointBoxDist2(pq.x, pq.y, pq.z, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <=
-                            R * R * 1.00001f) {
-                            open = true;
-                            break;
-                        }
-                    }
+                    // (2) one member in range opens it; (3) otherwise the group decides
+                    const float R = fmaxf(repHs, nodeHs);
+                    if (pointBoxDist2(repx, repy, repz, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <=
+                        R * R * 1.00001f)
+                        open = true;
+                    else
+                        undecided = true;
                 }
+            }
+            unsigned und = __ballot_sync(0xffffffffu, undecided);
+            while (und) {
+                const int k = __ffs(und) - 1;
+                und &= und - 1;
+                const float mnx = __shfl_sync(0xffffffffu, bmin.x, k), mny = __shfl_sync(0xffffffffu, bmin.y, k);
+                const float mnz = __shfl_sync(0xffffffffu, bmin.z, k), mxx = __shfl_sync(0xffffffffu, bmax.x, k);
+                const float mxy = __shfl_sync(0xffffffffu, bmax.y, k), mxz = __shfl_sync(0xffffffffu, bmax.z, k);
+                const float hk = __shfl_sync(0xffffffffu, nodeHs, k);
+                const float R = fmaxf(Hs, hk);
+                const bool near = active && pointBoxDist2(me.x, me.y, me.z, mnx, mny, mnz, mxx, mxy, mxz) <= R * R * 1.00001f;
+                const bool any = __any_sync(0xffffffffu, near);
+                if (lane == k) open = any;
             }
             unsigned openMask = __ballot_sync(0xffffffffu, open);
             if (sp + 2 * __popc(openMask) > kNbStack) {
