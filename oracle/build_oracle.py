@@ -61,6 +61,25 @@ def build_reference_eos(force=False):
     return out
 
 
+def build_reference_cubin(force=False):
+    """The reference kernels (engine/eos.cu + engine/sph_gravity.cu) as one
+    sm_100 cubin, from the checkout where they lie; None where absent."""
+    srcs = [os.path.join(REFERENCE_ENGINE, f) for f in ("eos.cu", "sph_gravity.cu", "sph_gravity.cuh", "eos.hpp")]
+    if not all(os.path.exists(x) for x in srcs):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "ref_kernels_sm100.cubin")
+    shim = os.path.join(HERE, "ref_cubin.cu")
+    if force or _stale(out, srcs + [shim]):
+        tmp = out + ".tmp%d" % os.getpid()
+        _run(["nvcc", "-cubin", "-arch=sm_100", "-O3", "--expt-relaxed-constexpr", "-std=c++20",
+              "-I", REFERENCE_ENGINE, shim, "-o", tmp])
+        os.replace(tmp, out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_reference_eos(force="--force" in sys.argv))
+    print(build_reference_cubin(force="--force" in sys.argv))

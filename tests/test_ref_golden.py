@@ -1,0 +1,141 @@
+"""Stage outputs of the reference's own CUDA kernels (the engine's
+sph_gravity.cu + eos.cu compiled for sm_100 and run on a GB300 by
+oracle/ref_gpu.py) on the two-sphere scene of 3,072 + 1,024 particles,
+committed as tests/golden/ref_stages.npz.
+
+The oracle (CPU) and the GB300 library (GPU) each run the same stage
+sequence from the same input and are compared stage by stage: integer and
+index results bit for bit, floating-point fields within a norm-relative RMS
+of 1e-5.  The reference's drift reads neighbour positions other threads are
+moving (engine/sph_gravity.cu:1430-1432 vs 1485-1487), so its positions after
+the drift carry that race; they are compared to 1e-6.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from astraea_gb300 import abi, engine
+from conftest import rel_rms
+
+STAGES = ["pass1", "eos", "gravity", "pass2"]
+FIELDS = {
+    "pass1": ["h", "shepardC", "surfFactor", "divV", "curlVX", "curlVY", "curlVZ"],
+    "eos": ["pressure", "soundSpeed", "tempK"],
+    "gravity": ["accX", "accY", "accZ", "phiGrav"],
+    "pass2": ["accX", "accY", "accZ", "drhoDt", "duDt", "radPowerW", "dSXX", "dSYY", "dSZZ", "dSXY", "dSXZ", "dSYZ"],
+    "kick": ["velX", "velY", "velZ", "rho", "u", "sXX", "sXY", "damage"],
+}
+
+
+@pytest.fixture(scope="module")
+def ref(golden_dir):
+    return np.load(golden_dir + "/ref_stages.npz")
+
+
+def inputs(ref):
+    return {k[len("input_"):]: ref[k] for k in ref.files if k.startswith("input_")}
+
+
+def check_stage(tag, got, ref, stage, tol=1e-5):
+    errs = {f: rel_rms(got[f], ref[stage + "_" + f]) for f in FIELDS[stage]}
+    print("%s %s %s" % (tag, stage, " ".join("%s=%.2e" % kv for kv in errs.items())))
+    assert max(errs.values()) < tol, (stage, errs)
+
+
+def check_build(got_state, codes, perm, left, right, parent, ref):
+    n = len(ref["build_codes"])
+    assert np.array_equal(codes[:n], ref["build_codes"])
+    assert np.array_equal(perm[:n], ref["build_perm"])
+    assert np.array_equal(left[: n - 1], ref["build_left"])
+    assert np.array_equal(right[: n - 1], ref["build_right"])
+    assert np.array_equal(parent[: 2 * n - 1], ref["build_parent"])
+    for f in ("posX", "posY", "posZ", "velX", "mass", "h", "originalId"):
+        assert np.array_equal(got_state[f], ref["build_" + f]), f
+
+
+def test_oracle_matches_reference_kernels(ref):
+    o = oracle.Oracle(inputs(ref))
+    o.clear_stats()
+    o.sort_and_build()
+    b = o.bvh.a
+    check_build(o.state(), b["mortonCodesSorted"], b["indicesSorted"], b["leftChild"], b["rightChild"], b["parent"], ref)
+    for f in ("aabbMinX", "aabbMaxX", "nodeMaxH"):
+        assert np.array_equal(b[f], ref["build_node_" + f]), f
+    for f in ("nodeMass", "comX", "comY", "comZ"):
+        assert rel_rms(b[f], ref["build_node_" + f]) < 1e-6, f
+    for stage, fn in (("pass1", o.pass1), ("eos", o.eos), ("gravity", o.gravity), ("pass2", o.pass2)):
+        fn()
+        check_stage("oracle", o.state(), ref, stage)
+    dt, _ = o.reduce_dt(0.0, 5.0e-3)
+    assert dt == float(ref["dt"][0])
+    o.kick(0.5 * dt)
+    check_stage("oracle", o.state(), ref, "kick")
+    o.drift(dt)
+    s = o.state()
+    for f in ("posX", "posY", "posZ"):
+        assert rel_rms(s[f], ref["drift_" + f]) < 1e-6, f
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("packed", [True, False])
+def test_library_matches_reference_kernels(ref, packed):
+    st = inputs(ref)
+    n = len(st["posX"])
+    p, alt = engine.DeviceParticles(n), engine.DeviceParticles(n)
+    p.upload(st)
+    alt.count = n
+    bvh = engine.TorchBvh(n, packed=packed)
+    engine.clear_stats(p)
+    engine.sort_and_build_bvh(p, alt, bvh)
+    torch.cuda.synchronize()
+    t = lambda name, k, dt=None: bvh.t[name][:k].cpu().numpy().view(dt) if dt else bvh.t[name][:k].cpu().numpy()
+    check_build(p.download(), t("mortonCodesSorted", n, np.uint64), t("indicesSorted", n, np.uint32),
+                t("leftChild", n - 1), t("rightChild", n - 1), t("parent", 2 * n - 1), ref)
+    for f in ("nodeMass", "comX", "comY", "comZ"):
+        assert rel_rms(t(f, 2 * n - 1), ref["build_node_" + f]) < 1e-6, f
+    for stage, fn in (("pass1", lambda: engine.sph_pass1_neighbors(p, bvh)), ("eos", lambda: engine.evaluate_eos(p)),
+                      ("gravity", lambda: engine.gravity_barnes_hut(p, bvh, 0.5)),
+                      ("pass2", lambda: engine.sph_pass2_forces(p, bvh))):
+        fn()
+        check_stage("gb300", p.download(), ref, stage)
+    dt = engine.reduce_dt_psu(p, 0.0, 5.0e-3)
+    assert abs(dt - float(ref["dt"][0])) <= 2e-7 * dt
+    engine.leapfrog_kick_half(p, 0.5 * dt, True, False)
+    check_stage("gb300", p.download(), ref, "kick")
+    engine.leapfrog_drift(p, dt, bvh)
+    s = p.download()
+    for f in ("posX", "posY", "posZ"):
+        assert rel_rms(s[f], ref["drift_" + f]) < 1e-6, f
+
+
+@pytest.mark.gpu
+def test_fused_steps_track_reference_kernels(ref):
+    """Two more full steps after the drift above, fused path vs the
+    reference's own step sequence (trajectory-level, so the bound is 1e-4:
+    the reference's drift race and summation order both enter)."""
+    st = inputs(ref)
+    sim = engine.Simulation(len(st["posX"]))
+    sim.load_state(st)
+    sim.evaluate_initial_forces()
+    dt0 = engine.reduce_dt_psu(sim.p, 0.0, 5.0e-3)
+    engine.leapfrog_kick_half(sim.p, 0.5 * dt0, True, False)
+    engine.leapfrog_drift(sim.p, dt0, sim.bvh)
+    engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+    engine.sph_pass1_neighbors(sim.p, sim.bvh)
+    engine.evaluate_eos(sim.p)
+    engine.gravity_barnes_hut(sim.p, sim.bvh, 0.5)
+    engine.sph_pass2_forces(sim.p, sim.bvh)
+    engine.leapfrog_kick_half(sim.p, 0.5 * dt0, False, False)
+    engine.evaluate_eos(sim.p)
+    sim.prev_dt = dt0
+    engine.invalidate_step_cache(sim.bvh)
+    for _ in range(2):
+        sim.step(5.0e-3)
+    g = sim.state()
+    assert abs(sim.prev_dt - float(ref["steps_dt"][0])) <= 1e-5 * sim.prev_dt
+    assert np.array_equal(g["originalId"], ref["steps_originalId"])
+    errs = {f: rel_rms(g[f], ref["steps_" + f]) for f in ("posX", "posY", "posZ", "velX", "velY", "velZ", "rho", "u",
+                                                          "h", "accX", "accY", "accZ")}
+    print("fused-vs-reference-kernels " + " ".join("%s=%.2e" % kv for kv in errs.items()))
+    assert max(errs.values()) < 1e-4
