@@ -103,6 +103,7 @@ SIGNATURES = [
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),
     ("astraea_gb300_release_scratch", [_B], ctypes.c_int),
     ("astraea_gb300_radix_sort_pairs", [_VP, _VP, _VP, _VP, _U32, ctypes.c_int], ctypes.c_int),
+    ("astraea_gb300_radix_sort_pairs_noalloc", [_VP, _VP, _VP, _VP, _U32, ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_read_device_status", [ctypes.POINTER(_U32), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     ("astraea_gb300_reset_device_status", [], ctypes.c_int),
     ("astraea_gb300_measure_fp32_tflops", [ctypes.POINTER(_F)], ctypes.c_int),

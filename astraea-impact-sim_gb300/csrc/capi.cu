@@ -293,6 +293,13 @@ float hostClampDt(uint32_t bits, float prevDt, float maxDt) {   // sph_gravity.c
 
 }  // namespace
 
+// Accessors for the other translation units of the library (noalloc.cu).
+namespace astraea_gb300 {
+cudaStream_t capiStream() { return stream(); }
+void capiSetLastError(const std::string& msg) { g_lastError = msg; }
+uint32_t capiSpinLimit() { return g_spinLimit.load(); }
+}  // namespace astraea_gb300
+
 extern "C" {
 
 const char* astraea_gb300_last_error(void) { return g_lastError.c_str(); }

@@ -211,6 +211,17 @@ AstraeaStatus astraea_gb300_release_scratch(const AstraeaRadixBvh* bvh);
 AstraeaStatus astraea_gb300_radix_sort_pairs(uint64_t* keysIn, uint64_t* keysOut,
                                              uint32_t* valsIn, uint32_t* valsOut,
                                              uint32_t n, int endBit);
+/* The same sort for callers that cannot allocate device memory (an arena or
+ * pool owns all of it, or the host forbids allocation after start-up): its
+ * scratch is a fixed ~2.1 MB array inside the library image, so the call
+ * makes no cudaMalloc/cudaFree.  At most 1,048,576 keys (else
+ * ASTRAEA_ERR_CAPACITY).  The first call on a device looks up the array's
+ * address (once per device; make it before any stream capture).  Calls share
+ * the array: calls whose GPU work overlaps race on it.  No counterpart in the
+ * reference. */
+AstraeaStatus astraea_gb300_radix_sort_pairs_noalloc(uint64_t* keysIn, uint64_t* keysOut,
+                                                     uint32_t* valsIn, uint32_t* valsOut,
+                                                     uint32_t n, int endBit);
 /* Device status word (bit flags, see ASTRAEA_DEVFLAG_*) and counters
  * accumulated since the last reset; host pointers, 8 x u64 counters. */
 #define ASTRAEA_DEVFLAG_LOOKBACK_TIMEOUT   0x1u
