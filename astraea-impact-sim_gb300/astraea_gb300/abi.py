@@ -73,7 +73,7 @@ DEVFLAG_NEIGHBOR_OVERFLOW = 0x2
 DEVFLAG_STACK_OVERFLOW = 0x4
 
 COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "pass2_pairs",
-            "pass1_pairs", "fallback_walks", "lookback_spins", "reserved"]
+            "pass1_pairs", "fallback_walks", "neighbor_candidates", "gravity_undecided"]
 
 # (symbol, argtypes) of every exported entry point, in header order.
 _P = ctypes.POINTER(Particles)

@@ -47,7 +47,8 @@ enum Counter : int {
     kCntPass2Pairs = 3,            // in-range pairs of SPH pass 2
     kCntPass1Pairs = 4,            // in-range pairs of SPH pass 1
     kCntFallbackWalks = 5,         // particles served by the per-thread walk
-    kCntLookbackSpins = 6,
+    kCntNeighborCandidates = 6,    // leaves tested by the neighbour build (after the group-box filter)
+    kCntGravityUndecided = 7,      // nodes the whole group had to test in the gravity walk
     kCntCount = 8
 };
 

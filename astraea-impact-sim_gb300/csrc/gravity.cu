@@ -32,7 +32,7 @@ struct GravWarpSmem {
     int stack[kGravStack];
     float4 mlist[kGravList];   // {comX, comY, comZ, G*mass}
     float4 plist[kGravList];   // {x, y, z, G*m}
-    float2 paux[kGravList];    // {eps_j, j (int bits)}
+    float2 paux[kGravList];    // {eps_j / 2, j (int bits)}
 };
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
@@ -59,6 +59,8 @@ struct Accum {
 };
 
 // Monopole terms: f = -G m / (r^2 + eps_i^2 + 1e-20)^(3/2) (sph_gravity.cu:935-942).
+// epsI2 arrives with the 1e-20 already added: eps >= 8e-7, so 1e-20 is below
+// half an ulp of eps^2 and both orders of the two additions round alike.
 __device__ __forceinline__ void evalMonopoles(const float4* list, int cnt, float xi, float yi, float zi, float epsI2,
                                               Accum& a) {
 #pragma unroll 4
@@ -66,7 +68,7 @@ __device__ __forceinline__ void evalMonopoles(const float4* list, int cnt, float
         const float4 q = list[e];
         const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float inv = rsqrtf((r2 + epsI2) + 1.0e-20f);
+        const float inv = rsqrtf(r2 + epsI2);
         const float inv3 = inv * inv * inv;
         const float f = -q.w * inv3;
         a.ax += f * dx;
@@ -76,7 +78,8 @@ __device__ __forceinline__ void evalMonopoles(const float4* list, int cnt, float
     }
 }
 
-// Particle-particle terms with eps_ij (sph_gravity.cu:875-889).
+// Particle-particle terms with eps_ij = (eps_i + eps_j)/2 (sph_gravity.cu:875-889);
+// the list carries eps_j/2.
 __device__ __forceinline__ void evalParticles(const float4* list, const float2* aux, int cnt, float xi, float yi,
                                               float zi, float epsI, int self, Accum& a, uint32_t& nSelf) {
 #pragma unroll 4
@@ -85,8 +88,8 @@ __device__ __forceinline__ void evalParticles(const float4* list, const float2* 
         const float2 x2 = aux[e];
         const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float eij = 0.5f * (epsI + x2.x);
-        const float inv = rsqrtf((r2 + eij * eij) + 1.0e-20f);
+        const float eij = fmaf(0.5f, epsI, x2.x);
+        const float inv = rsqrtf(fmaf(eij, eij, r2));
         const float inv3 = inv * inv * inv;
         const bool isSelf = __float_as_int(x2.y) == self;
         const float gm = isSelf ? 0.0f : q.w;
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
     __shared__ GravWarpSmem smem[kGravWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GravWarpSmem& S = smem[warp];
-    unsigned long long nInter = 0, nTests = 0;
+    unsigned long long nInter = 0, nTests = 0, nUndecided = 0;
     bool overflowed = false;
 
     if (n == 1u) {                                   // sph_gravity.cu:824-832
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             epsI = __ldg(&w.leafAux[i]).y;
         }
         const float xi = me.x, yi = me.y, zi = me.z;
-        const float epsI2 = epsI * epsI;
+        const float epsI2 = epsI * epsI + 1.0e-20f;
         const float gminx = warpMinF(active ? xi : 3.0e38f), gmaxx = warpMaxF(active ? xi : -3.0e38f);
         const float gminy = warpMinF(active ? yi : 3.0e38f), gmaxy = warpMaxF(active ? yi : -3.0e38f);
         const float gminz = warpMinF(active ? zi : 3.0e38f), gmaxz = warpMaxF(active ? zi : -3.0e38f);
@@ -206,6 +209,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             }
             // (3) exact test of each undecided node by all members at once
             unsigned und = __ballot_sync(0xffffffffu, undecided);
+            nUndecided += __popc(und);
             while (und) {
                 const int k = __ffs(und) - 1;
                 und &= und - 1;
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 const float ej = __ldg(&w.leafAux[j]).y;
                 const int slot = pCount + __popc(leafMask & laneMaskLt());
                 S.plist[slot] = make_float4(pm.x, pm.y, pm.z, kGPsuF * pm.w);
-                S.paux[slot] = make_float2(ej, __int_as_float(j));
+                S.paux[slot] = make_float2(0.5f * ej, __int_as_float(j));
             }
             pCount += __popc(leafMask);
             nTests += __popc(__ballot_sync(0xffffffffu, isNode));
@@ -284,6 +288,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         DevStatus* st = reinterpret_cast<DevStatus*>(w.status);
         atomicAdd(&st->counters[kCntGravityInteractions], nInter);
         atomicAdd(&st->counters[kCntGravityNodeTests], nTests);
+        atomicAdd(&st->counters[kCntGravityUndecided], nUndecided);
         if (overflowed) atomicOr(&st->flags, kFlagStackOverflow);
     }
 }

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
     __shared__ NbWarpSmem smem[kNbWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     NbWarpSmem& S = smem[warp];
-    unsigned long long nEntries = 0;
+    unsigned long long nEntries = 0, nCand = 0;
     bool overflow = false, stackOverflow = false;
     const uint32_t maxNbr = w.maxNbr;
 
@@ -91,17 +91,21 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
         uint32_t* myList = w.nbrList + static_cast<size_t>(active ? i : 0u) * maxNbr;
         __syncwarp();
 
+        auto put = [&](uint32_t j) {
+            if (cnt < maxNbr) myList[cnt] = j;
+            ++cnt;
+        };
+        // Superset test r < max(Hs_i, Hs_j) in plain FMA arithmetic: every
+        // pass re-tests its own radius exactly, and Hs exceeds those radii by
+        // 0.9 %, far more than any rounding difference.
         auto flush = [&](int base, int num) {
             if (active) {
                 for (int e = 0; e < num; ++e) {
                     const float4 q = S.cand[base + e];
                     const int j = S.candIdx[base + e];
-                    const float r2 = len2Exact(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z));
+                    const float dx = me.x - q.x, dy = me.y - q.y, dz = me.z - q.z;
                     const float R = fmaxf(Hs, q.w);
-                    if (j != static_cast<int>(i) && r2 < __fmul_rn(R, R)) {
-                        if (cnt < maxNbr) myList[cnt] = static_cast<uint32_t>(j);
-                        ++cnt;
-                    }
+                    if (dx * dx + dy * dy + dz * dz < R * R && j != static_cast<int>(i)) put(static_cast<uint32_t>(j));
                 }
             }
         };
@@ -170,16 +174,27 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
                 S.stack[pos + 1] = cr;
             }
             sp += 2 * __popc(openMask);
-            const unsigned leafMask = __ballot_sync(0xffffffffu, isLeaf);
+            // A leaf becomes a candidate only if it can reach the group box.
+            float4 pm = make_float4(0.f, 0.f, 0.f, 0.f);
+            float hsj = 0.0f;
+            bool keep = false;
             if (isLeaf) {
-                const int j = ~c;
-                const float4 pm = __ldg(&w.leafPM[j]);
-                const float hsj = __ldg(&w.leafAux[j]).x;
+                pm = __ldg(&w.leafPM[~c]);
+                hsj = __ldg(&w.leafAux[~c]).x;
+                const float dx = fmaxf(0.0f, fmaxf(gminx - pm.x, pm.x - gmaxx));
+                const float dy = fmaxf(0.0f, fmaxf(gminy - pm.y, pm.y - gmaxy));
+                const float dz = fmaxf(0.0f, fmaxf(gminz - pm.z, pm.z - gmaxz));
+                const float R = fmaxf(gHs, hsj);
+                keep = dx * dx + dy * dy + dz * dz <= R * R * 1.00001f;
+            }
+            const unsigned leafMask = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
                 const int slot = cCount + __popc(leafMask & laneMaskLt());
                 S.cand[slot] = make_float4(pm.x, pm.y, pm.z, hsj);
-                S.candIdx[slot] = j;
+                S.candIdx[slot] = ~c;
             }
             cCount += __popc(leafMask);
+            nCand += __popc(leafMask);
             __syncwarp();
             if (cCount >= 32) {
                 cCount -= 32;
@@ -199,6 +214,7 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
     const bool anyOver = __any_sync(0xffffffffu, overflow);
     if (lane == 0) {
         atomicAdd(&w.status->counters[kCntNeighborEntries], tot);
+        atomicAdd(&w.status->counters[kCntNeighborCandidates], nCand);
         if (anyOver) atomicOr(&w.status->flags, kFlagNeighborOverflow);
         if (stackOverflow) atomicOr(&w.status->flags, kFlagStackOverflow);
     }
@@ -259,6 +275,29 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
     }
 }
 
+// Same candidate set as forEachCandidate, with each candidate's first record
+// loaded by `load(j)` for four list entries before any `body(j, rec)` runs,
+// so four independent gathers are in flight per thread.
+template <class L, class B>
+__device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32_t i, L&& load, B&& body) {
+    const uint32_t c = __ldg(&w.nbrCount[i]);
+    if (c <= w.maxNbr) {
+        const uint32_t* list = w.nbrList + static_cast<size_t>(i) * w.maxNbr;
+        uint32_t k = 0;
+        for (; k + 4 <= c; k += 4) {
+            const uint4 q = __ldg(reinterpret_cast<const uint4*>(list + k));
+            const float4 r0 = load(q.x), r1 = load(q.y), r2 = load(q.z), r3 = load(q.w);
+            body(q.x, r0); body(q.y, r1); body(q.z, r2); body(q.w, r3);
+        }
+        for (; k < c; ++k) {
+            const uint32_t j = __ldg(&list[k]);
+            body(j, load(j));
+        }
+        return;
+    }
+    forEachCandidate(w, i, [&](uint32_t j) { body(j, load(j)); });
+}
+
 // ---------------------------------------------------------------- pass 1 ---
 __global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -277,8 +316,7 @@ __global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, u
     float nsX = 0.f, nsY = 0.f, nsZ = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
     if (n >= 2u) {
-        forEachCandidate(w, i, [&](uint32_t j) {
-            const float4 q = __ldg(&w.leafPM[j]);
+        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&w.leafPM[j]); }, [&](uint32_t j, float4 q) {
             const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
             const float r2 = len2Exact(dx, dy, dz);
             if (!(r2 < Hi2)) return;                       // sph_gravity.cu:713
@@ -318,7 +356,7 @@ __global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, u
 //   q0 {x, y, z, h}   q1 {vx, vy, vz, m}   q2 {rho, P_eff, cs, f_Balsara}
 //   q3 {sXX, sYY, sZZ, sXY}   q4 {sXZ, sYZ, material, 0}
 // with h, rho, cs already clamped as the engine clamps them on load.
-__global__ void __launch_bounds__(128) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
+__global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
                                                    const uint32_t* livingFlags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -344,8 +382,7 @@ __global__ void __launch_bounds__(128) pass2Kernel(AstraeaParticles p, Work w, u
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
     unsigned pairs = 0;
     if (n >= 2u) {
-        forEachCandidate(w, i, [&](uint32_t j) {
-            const float4 b0 = __ldg(&R[5 * j + 0]);
+        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&R[5 * j + 0]); }, [&](uint32_t j, float4 b0) {
             const float dx = __fsub_rn(xi, b0.x), dy = __fsub_rn(yi, b0.y), dz = __fsub_rn(zi, b0.z);
             const float r2 = len2Exact(dx, dy, dz);
             const float hj = b0.w, Hj = 2.0f * hj;
@@ -484,8 +521,7 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
         const float rhoI = fmaxf(vr.w, 1.0e-9f);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         if (useList && n >= 2u) {
-            forEachCandidate(w, i, [&](uint32_t j) {
-                const float4 q = __ldg(&w.leafPM[j]);
+            forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&w.leafPM[j]); }, [&](uint32_t j, float4 q) {
                 const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
                 const float r2 = len2Exact(dx, dy, dz);
                 const float Hj = 2.0f * fmaxf(__ldg(&p.h[j]), 1.0e-6f);
