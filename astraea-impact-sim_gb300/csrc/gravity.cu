@@ -17,7 +17,8 @@
 //   * accepted monopoles and reached leaves are appended to two per-warp
 //     interaction lists in shared memory; every 32 entries the warp evaluates
 //     them with each lane summing its own particle's force from broadcast
-//     shared-memory reads (pure FP32 FMA + one rsqrt per pair);
+//     shared-memory reads, two entries per instruction on the packed FP32
+//     pipes (add/mul/fma.rn.f32x2) plus one rsqrt per pair;
 //   * a persistent grid pulls groups from an atomic counter.
 #include "kernels.h"
 
@@ -28,11 +29,15 @@ constexpr int kGravWarps = 4;
 constexpr int kGravStack = 1024;
 constexpr int kGravList = 64;
 
-struct GravWarpSmem {
+// Interaction lists are stored pair-interleaved so that one 16-byte shared
+// load yields packed (entry 2k, entry 2k+1) operands for the f32x2 pipes:
+// mlist[8k..8k+7] = {xA, xB, yA, yB, zA, zB, -GmA, -GmB}; plist likewise,
+// with peps[2k..2k+1] = {eps_jA / 2, eps_jB / 2}.
+struct __align__(16) GravWarpSmem {
     int stack[kGravStack];
-    float4 mlist[kGravList];   // {comX, comY, comZ, G*mass}
-    float4 plist[kGravList];   // {x, y, z, G*m}
-    float2 paux[kGravList];    // {eps_j / 2, j (int bits)}
+    float mlist[8 * (kGravList / 2)];
+    float plist[8 * (kGravList / 2)];
+    float peps[kGravList];
 };
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
@@ -54,52 +59,81 @@ __device__ __forceinline__ bool acceptsMember(float px, float py, float pz, floa
     return ok;
 }
 
-struct Accum {
-    float ax, ay, az, phi;
+// ---- packed FP32 pairs (lo = entry 2k, hi = entry 2k+1) -------------------
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pack2(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) { f2 r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) { f2 r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { f2 r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r; }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ f2 rsqrt2(f2 v) {
+    float a, b;
+    unpack2(v, a, b);
+    return pack2(rsqrtf(a), rsqrtf(b));
+}
+
+struct Accum2 {
+    f2 ax, ay, az, phi;   // two partial sums each (even / odd entries)
 };
 
-// Monopole terms: f = -G m / (r^2 + eps_i^2 + 1e-20)^(3/2) (sph_gravity.cu:935-942).
-// epsI2 arrives with the 1e-20 already added: eps >= 8e-7, so 1e-20 is below
-// half an ulp of eps^2 and both orders of the two additions round alike.
-__device__ __forceinline__ void evalMonopoles(const float4* list, int cnt, float xi, float yi, float zi, float epsI2,
-                                              Accum& a) {
-#pragma unroll 4
-    for (int e = 0; e < cnt; ++e) {
-        const float4 q = list[e];
-        const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        const float inv = rsqrtf(r2 + epsI2);
-        const float inv3 = inv * inv * inv;
-        const float f = -q.w * inv3;
-        a.ax += f * dx;
-        a.ay += f * dy;
-        a.az += f * dz;
-        a.phi -= q.w * inv;
+// Monopole terms: f = -G m / (r^2 + eps_i^2 + 1e-20)^(3/2) (sph_gravity.cu:935-942),
+// two entries per instruction.  `pairs` pairs starting at list pair `first`.
+// E2 = packed eps_i^2 + 1e-20 (eps >= 8e-7, so 1e-20 is below half an ulp of
+// eps^2 and the order of the two additions does not matter).
+__device__ __forceinline__ void evalMonopoles2(const float* list, int first, int pairs, f2 X, f2 Y, f2 Z, f2 E2,
+                                               Accum2& a) {
+#pragma unroll 2
+    for (int k = first; k < first + pairs; ++k) {
+        const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(list + 8 * k);       // (x), (y)
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(list + 8 * k + 4);   // (z), (-Gm)
+        const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
+        const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const f2 inv = rsqrt2(add2(r2, E2));
+        const f2 f = mul2(v.y, mul2(inv, mul2(inv, inv)));
+        a.ax = fma2(f, dx, a.ax);
+        a.ay = fma2(f, dy, a.ay);
+        a.az = fma2(f, dz, a.az);
+        a.phi = fma2(v.y, inv, a.phi);
     }
 }
 
-// Particle-particle terms with eps_ij = (eps_i + eps_j)/2 (sph_gravity.cu:875-889);
-// the list carries eps_j/2.
-__device__ __forceinline__ void evalParticles(const float4* list, const float2* aux, int cnt, float xi, float yi,
-                                              float zi, float epsI, int self, Accum& a, uint32_t& nSelf) {
-#pragma unroll 4
-    for (int e = 0; e < cnt; ++e) {
-        const float4 q = list[e];
-        const float2 x2 = aux[e];
-        const float dx = xi - q.x, dy = yi - q.y, dz = zi - q.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        const float eij = fmaf(0.5f, epsI, x2.x);
-        const float inv = rsqrtf(fmaf(eij, eij, r2));
-        const float inv3 = inv * inv * inv;
-        const bool isSelf = __float_as_int(x2.y) == self;
-        const float gm = isSelf ? 0.0f : q.w;
-        nSelf += isSelf ? 1u : 0u;
-        const float f = -gm * inv3;
-        a.ax += f * dx;
-        a.ay += f * dy;
-        a.az += f * dz;
-        a.phi -= gm * inv;
+// Particle-particle terms with eps_ij = (eps_i + eps_j)/2 (sph_gravity.cu:875-889).
+// The list includes the particle itself; its term adds exactly zero force
+// (dx = dy = dz = 0) and a potential the caller subtracts again.
+__device__ __forceinline__ void evalParticles2(const float* list, const float* peps, int first, int pairs, f2 X,
+                                               f2 Y, f2 Z, f2 HE, Accum2& a) {
+#pragma unroll 2
+    for (int k = first; k < first + pairs; ++k) {
+        const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(list + 8 * k);
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(list + 8 * k + 4);
+        const f2 ej = *reinterpret_cast<const f2*>(peps + 2 * k);
+        const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
+        const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const f2 eij = add2(HE, ej);
+        const f2 inv = rsqrt2(fma2(eij, eij, r2));
+        const f2 f = mul2(v.y, mul2(inv, mul2(inv, inv)));
+        a.ax = fma2(f, dx, a.ax);
+        a.ay = fma2(f, dy, a.ay);
+        a.az = fma2(f, dz, a.az);
+        a.phi = fma2(v.y, inv, a.phi);
     }
+}
+
+// Store entry `slot` of a pair-interleaved list.
+__device__ __forceinline__ void putEntry(float* list, int slot, float x, float y, float z, float w) {
+    float* b = list + 8 * (slot >> 1) + (slot & 1);
+    b[0] = x; b[2] = y; b[4] = z; b[6] = w;
 }
 
 __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
@@ -155,8 +189,11 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, mCount = 0, pCount = 0;
         uint32_t rounds = 0;
-        Accum acc{0.0f, 0.0f, 0.0f, 0.0f};
-        uint32_t nSelf = 0;
+        const f2 X = pack2(xi, xi), Y = pack2(yi, yi), Z = pack2(zi, zi);
+        const f2 E2 = pack2(epsI2, epsI2), HE = pack2(0.5f * epsI, 0.5f * epsI);
+        Accum2 acc{0ull, 0ull, 0ull, 0ull};
+        const uint32_t base = g * 32u;
+        unsigned selfSeen = 0u;   // bit l: member l met its own leaf
         __syncwarp();
 
         while (sp > 0) {
@@ -243,45 +280,74 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             }
             sp += 2 * __popc(openMask);
             const unsigned accMask = __ballot_sync(0xffffffffu, accept);
-            if (accept) S.mlist[mCount + __popc(accMask & laneMaskLt())] = make_float4(r0.x, r0.y, r0.z, kGPsuF * r0.w);
+            if (accept) putEntry(S.mlist, mCount + __popc(accMask & laneMaskLt()), r0.x, r0.y, r0.z, -kGPsuF * r0.w);
             mCount += __popc(accMask);
             const unsigned leafMask = __ballot_sync(0xffffffffu, isLeaf);
+            unsigned selfBit = 0u;
             if (isLeaf) {
                 const int j = ~c;
                 const float4 pm = __ldg(&w.leafPM[j]);
                 const float ej = __ldg(&w.leafAux[j]).y;
                 const int slot = pCount + __popc(leafMask & laneMaskLt());
-                S.plist[slot] = make_float4(pm.x, pm.y, pm.z, kGPsuF * pm.w);
-                S.paux[slot] = make_float2(0.5f * ej, __int_as_float(j));
+                putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);
+                S.peps[slot] = 0.5f * ej;
+                const uint32_t rel = static_cast<uint32_t>(j) - base;
+                if (rel < 32u) selfBit = 1u << rel;
             }
+            selfSeen |= __reduce_or_sync(0xffffffffu, selfBit);
             pCount += __popc(leafMask);
             nTests += __popc(__ballot_sync(0xffffffffu, isNode));
             __syncwarp();
-            if (mCount >= 32) {
-                mCount -= 32;
-                if (active) evalMonopoles(S.mlist + mCount, 32, xi, yi, zi, epsI2, acc);
+            if (mCount >= 32) {                 // evaluate entries 0..31, move the rest down
+                if (active) evalMonopoles2(S.mlist, 0, 16, X, Y, Z, E2, acc);
                 nInter += static_cast<unsigned long long>(act) * 32u;
+                __syncwarp();
+                mCount -= 32;
+                if (lane < mCount) {
+                    const float* src = S.mlist + 8 * (16 + (lane >> 1)) + (lane & 1);
+                    putEntry(S.mlist, lane, src[0], src[2], src[4], src[6]);
+                }
                 __syncwarp();
             }
             if (pCount >= 32) {
-                pCount -= 32;
-                if (active) evalParticles(S.plist + pCount, S.paux + pCount, 32, xi, yi, zi, epsI, static_cast<int>(i), acc, nSelf);
+                if (active) evalParticles2(S.plist, S.peps, 0, 16, X, Y, Z, HE, acc);
                 nInter += static_cast<unsigned long long>(act) * 32u;
+                __syncwarp();
+                pCount -= 32;
+                if (lane < pCount) {
+                    const float* src = S.plist + 8 * (16 + (lane >> 1)) + (lane & 1);
+                    putEntry(S.plist, lane, src[0], src[2], src[4], src[6]);
+                    S.peps[lane] = S.peps[32 + lane];
+                }
                 __syncwarp();
             }
         }
+        // odd tails: pad with a massless entry (adds exactly zero)
+        if (lane == 0) {
+            if (mCount & 1) putEntry(S.mlist, mCount, 0.0f, 0.0f, 0.0f, 0.0f);
+            if (pCount & 1) { putEntry(S.plist, pCount, 0.0f, 0.0f, 0.0f, 0.0f); S.peps[pCount] = 0.0f; }
+        }
+        __syncwarp();
         if (active) {
-            evalMonopoles(S.mlist, mCount, xi, yi, zi, epsI2, acc);
-            evalParticles(S.plist, S.paux, pCount, xi, yi, zi, epsI, static_cast<int>(i), acc, nSelf);
-            p.accX[i] = acc.ax;
-            p.accY[i] = acc.ay;
-            p.accZ[i] = acc.az;
-            p.phiGrav[i] = acc.phi;
+            evalMonopoles2(S.mlist, 0, (mCount + 1) >> 1, X, Y, Z, E2, acc);
+            evalParticles2(S.plist, S.peps, 0, (pCount + 1) >> 1, X, Y, Z, HE, acc);
+            float a0, a1, b0, b1, c0, c1, d0, d1;
+            unpack2(acc.ax, a0, a1);
+            unpack2(acc.ay, b0, b1);
+            unpack2(acc.az, c0, c1);
+            unpack2(acc.phi, d0, d1);
+            float phi = d0 + d1;
+            if (selfSeen & (1u << lane)) {
+                // the self term added to phi: -G m_i / sqrt(eps_i^2), exactly as evaluated
+                phi -= (-kGPsuF * me.w) * rsqrtf(__fmul_rn(epsI, epsI));
+            }
+            p.accX[i] = a0 + a1;
+            p.accY[i] = b0 + b1;
+            p.accZ[i] = c0 + c1;
+            p.phiGrav[i] = phi;
         }
         nInter += static_cast<unsigned long long>(act) * static_cast<unsigned>(mCount + pCount);
-        // nSelf: every active lane met itself once among the leaves.
-        const unsigned selfTotal = __reduce_add_sync(0xffffffffu, nSelf);
-        if (lane == 0) nInter -= selfTotal;
+        if (lane == 0) nInter -= static_cast<unsigned long long>(__popc(selfSeen));
         __syncwarp();
     }
     if (lane == 0) {
