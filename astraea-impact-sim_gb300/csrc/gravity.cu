@@ -10,10 +10,14 @@
 //
 // GB300 restructuring (same sets, different schedule):
 //   * the group walk is node-parallel: up to 32 pending nodes are loaded at
-//     once, one per lane; a sound group-box bound accepts most far nodes, an
-//     exact test of one representative member opens most near ones, and the
-//     few undecided nodes are tested by all 32 members at once (one node per
-//     warp iteration, one vote), so no lane loops over the group alone;
+//     once, one per lane, and decided by three tests of increasing cost:
+//     (1) a sound lower bound on every member's distance to the node's COM
+//     (the larger of the group-box distance and the distance to the group's
+//     26-direction bounding polytope) accepts most far nodes; (2) the exact
+//     test of the member that lies furthest towards the node (looked up per
+//     group for 26 directions) opens most near ones; (3) the few nodes still
+//     undecided are tested by all 32 members at once, one node per warp
+//     iteration from a shared-memory list, so no lane loops over the group;
 //   * accepted monopoles and reached leaves are appended to two per-warp
 //     interaction lists in shared memory; every 32 entries the warp evaluates
 //     them with each lane summing its own particle's force from broadcast
@@ -33,11 +37,21 @@ constexpr int kGravList = 64;
 // load yields packed (entry 2k, entry 2k+1) operands for the f32x2 pipes:
 // mlist[8k..8k+7] = {xA, xB, yA, yB, zA, zB, -GmA, -GmB}; plist likewise,
 // with peps[2k..2k+1] = {eps_jA / 2, eps_jB / 2}.
+// dirPos[k] (k = 9 (sx + 1) + 3 (sy + 1) + (sz + 1), s in {-1, 0, 1}): the
+// member with the largest projection on the unit direction s / |s| (first
+// member on ties) and, in .w, that projection measured from the group-box
+// centre.  und[] holds the compacted undecided nodes of one walk round; the
+// same storage holds the member positions while dirPos is computed.
+template <bool kInside>
 struct __align__(16) GravWarpSmem {
     int stack[kGravStack];
     float mlist[8 * (kGravList / 2)];
     float plist[8 * (kGravList / 2)];
     float peps[kGravList];
+    float4 dirPos[27];
+    float4 und[32];                    // {com.x, com.y, com.z, dNode^2}
+    float4 undMin[kInside ? 32 : 1];
+    float4 undMax[kInside ? 32 : 1];
 };
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
@@ -136,12 +150,16 @@ __device__ __forceinline__ void putEntry(float* list, int slot, float x, float y
     b[0] = x; b[2] = y; b[4] = z; b[6] = w;
 }
 
+// 1 / |s| for a direction s in {-1, 0, 1}^3 with nz non-zero components.
+__device__ __forceinline__ float invDirNorm(int nz) { return nz == 3 ? 0.57735027f : (nz == 2 ? 0.70710678f : 1.0f); }
+
+template <bool kInside>
 __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
-                                                                 float theta2, bool checkInside, uint32_t numGroups,
+                                                                 float theta2, uint32_t numGroups,
                                                                  uint32_t* groupCounter) {
-    __shared__ GravWarpSmem smem[kGravWarps];
+    __shared__ GravWarpSmem<kInside> smem[kGravWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GravWarpSmem& S = smem[warp];
+    GravWarpSmem<kInside>& S = smem[warp];
     unsigned long long nInter = 0, nTests = 0, nUndecided = 0;
     bool overflowed = false;
 
@@ -160,7 +178,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         g = __shfl_sync(0xffffffffu, g, 0);
         if (g >= numGroups) break;
         const uint32_t i = g * 32u + static_cast<uint32_t>(lane);
-        const bool active = i < n;
+        const bool active = i < n;                  // active members are lanes 0 .. act-1
         const int act = static_cast<int>(min(32u, n - g * 32u));
         float4 me = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         float epsI = 0.8e-6f;
@@ -173,19 +191,26 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         const float gminx = warpMinF(active ? xi : 3.0e38f), gmaxx = warpMaxF(active ? xi : -3.0e38f);
         const float gminy = warpMinF(active ? yi : 3.0e38f), gmaxy = warpMaxF(active ? yi : -3.0e38f);
         const float gminz = warpMinF(active ? zi : 3.0e38f), gmaxz = warpMaxF(active ? zi : -3.0e38f);
-        // representative member: the one nearest the group-box centre
         const float cxg = 0.5f * (gminx + gmaxx), cyg = 0.5f * (gminy + gmaxy), czg = 0.5f * (gminz + gmaxz);
-        float dc = active ? (xi - cxg) * (xi - cxg) + (yi - cyg) * (yi - cyg) + (zi - czg) * (zi - czg) : 3.0e38f;
-        int best = lane;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float od = __shfl_xor_sync(0xffffffffu, dc, o);
-            const int ob = __shfl_xor_sync(0xffffffffu, best, o);
-            if (od < dc || (od == dc && ob < best)) { dc = od; best = ob; }
+        const float gExt = (gmaxx - gminx) + (gmaxy - gminy) + (gmaxz - gminz);
+
+        // Per-direction extreme members (dirPos); member positions staged in und[].
+        S.und[lane] = make_float4(xi, yi, zi, 0.0f);
+        __syncwarp();
+        if (lane < 27) {
+            const float sx = static_cast<float>(lane / 9 - 1), sy = static_cast<float>((lane / 3) % 3 - 1),
+                        sz = static_cast<float>(lane % 3 - 1);
+            const float inv = invDirNorm(static_cast<int>(fabsf(sx) + fabsf(sy) + fabsf(sz)));
+            float best = -3.0e38f;
+            int bi = 0;
+            for (int m = 0; m < act; ++m) {
+                const float4 q = S.und[m];
+                const float pr = (sx * (q.x - cxg) + sy * (q.y - cyg) + sz * (q.z - czg)) * inv;
+                if (pr > best) { best = pr; bi = m; }
+            }
+            const float4 q = S.und[bi];
+            S.dirPos[lane] = make_float4(q.x, q.y, q.z, best);
         }
-        const float repx = __shfl_sync(0xffffffffu, xi, best);
-        const float repy = __shfl_sync(0xffffffffu, yi, best);
-        const float repz = __shfl_sync(0xffffffffu, zi, best);
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, mCount = 0, pCount = 0;
         uint32_t rounds = 0;
@@ -223,46 +248,62 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 cr = __float_as_int(r1.z);
                 dd = __fmul_rn(r1.x, r1.x);
                 bool disjoint = true;
-                if (checkInside) {
+                if (kInside) {
                     bmin = __ldg(&rec[2]);
                     bmax = __ldg(&rec[3]);
                     disjoint = bmax.x < gminx || bmin.x > gmaxx || bmax.y < gminy || bmin.y > gmaxy ||
                                bmax.z < gminz || bmin.z > gmaxz;
                 }
-                // (1) Sound group test: every member lies in the group box, so
-                // its distance to the COM is at least the box distance D; the
-                // 1e-5 margin covers the rounding of both computations.
+                // (1) Sound lower bound on every member's distance to the COM:
+                // the group-box distance, or the distance to the supporting
+                // plane of the group in the direction s of the COM (all
+                // members lie behind it).  Rounding: the box terms are single
+                // subtractions (relative error 2^-24), the plane term carries
+                // an absolute margin of 1e-6 (|u|_1 + group extent), several
+                // times its error bound; 0.99999 covers the final products.
                 const float bx = fmaxf(0.0f, fmaxf(gminx - r0.x, r0.x - gmaxx));
                 const float by = fmaxf(0.0f, fmaxf(gminy - r0.y, r0.y - gmaxy));
                 const float bz = fmaxf(0.0f, fmaxf(gminz - r0.z, r0.z - gmaxz));
                 const float D2 = bx * bx + by * by + bz * bz;
-                if (disjoint && D2 > 2.0e-20f && dd < theta2 * D2 * 0.99999f) {
+                const float ux = r0.x - cxg, uy = r0.y - cyg, uz = r0.z - czg;
+                const float ax = fabsf(ux), ay = fabsf(uy), az = fabsf(uz);
+                const float t = 0.41421356f * fmaxf(ax, fmaxf(ay, az));
+                const int sx = (ux >= t) - (ux <= -t), sy = (uy >= t) - (uy <= -t), sz = (uz >= t) - (uz <= -t);
+                const float4 dp = S.dirPos[13 + 9 * sx + 3 * sy + sz];
+                const float inv = invDirNorm(abs(sx) + abs(sy) + abs(sz));
+                const float L = (static_cast<float>(sx) * ux + static_cast<float>(sy) * uy +
+                                 static_cast<float>(sz) * uz) * inv - dp.w - 1.0e-6f * (ax + ay + az + gExt);
+                const float Lb2 = fmaxf(D2, L > 0.0f ? L * L : 0.0f);
+                if (disjoint && Lb2 > 2.0e-20f && dd < theta2 * Lb2 * 0.99999f) {
                     accept = true;
-                } else if (!acceptsMember(repx, repy, repz, r0, dd, theta2, checkInside, bmin, bmax)) {
-                    accept = false;   // (2) one member (the representative) already opens it
+                } else if (!acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax)) {
+                    accept = false;   // (2) the member furthest towards the node opens it
                 } else {
                     undecided = true; // (3) decided below by the whole group
                 }
             }
             // (3) exact test of each undecided node by all members at once
-            unsigned und = __ballot_sync(0xffffffffu, undecided);
-            nUndecided += __popc(und);
-            while (und) {
-                const int k = __ffs(und) - 1;
-                und &= und - 1;
-                float4 q = make_float4(__shfl_sync(0xffffffffu, r0.x, k), __shfl_sync(0xffffffffu, r0.y, k),
-                                       __shfl_sync(0xffffffffu, r0.z, k), 0.0f);
-                const float ddk = __shfl_sync(0xffffffffu, dd, k);
-                float4 mn = bmin, mx = bmax;
-                if (checkInside) {
-                    mn = make_float4(__shfl_sync(0xffffffffu, bmin.x, k), __shfl_sync(0xffffffffu, bmin.y, k),
-                                     __shfl_sync(0xffffffffu, bmin.z, k), 0.0f);
-                    mx = make_float4(__shfl_sync(0xffffffffu, bmax.x, k), __shfl_sync(0xffffffffu, bmax.y, k),
-                                     __shfl_sync(0xffffffffu, bmax.z, k), 0.0f);
+            const unsigned und = __ballot_sync(0xffffffffu, undecided);
+            if (und) {
+                const int nu = __popc(und);
+                nUndecided += nu;
+                const int slot = __popc(und & laneMaskLt());
+                if (undecided) {
+                    S.und[slot] = make_float4(r0.x, r0.y, r0.z, dd);
+                    if (kInside) { S.undMin[slot] = bmin; S.undMax[slot] = bmax; }
                 }
-                const bool ok = !active || acceptsMember(xi, yi, zi, q, ddk, theta2, checkInside, mn, mx);
-                const bool all = __all_sync(0xffffffffu, ok);
-                if (lane == k) accept = all;
+                __syncwarp();
+                unsigned bits = 0u;
+#pragma unroll 2
+                for (int k = 0; k < nu; ++k) {
+                    const float4 q = S.und[k];
+                    float4 mn = q, mx = q;
+                    if (kInside) { mn = S.undMin[k]; mx = S.undMax[k]; }
+                    const bool ok = !active || acceptsMember(xi, yi, zi, q, q.w, theta2, kInside, mn, mx);
+                    bits |= (__all_sync(0xffffffffu, ok) ? 1u : 0u) << k;
+                }
+                if (undecided) accept = (bits >> slot) & 1u;
+                __syncwarp();
             }
             bool open = isNode && !accept;
             unsigned openMask = __ballot_sync(0xffffffffu, open);
@@ -371,12 +412,13 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
     uint32_t* counter = w.words + kWGroupCounter;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
+    auto kernel = checkInside ? gravityKernel<true> : gravityKernel<false>;
     int perSm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, gravityKernel, kGravWarps * 32, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kGravWarps * 32, 0);
     if (e != cudaSuccess) return e;
     const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(std::max(1, perSm) * sms),
                                                (groups + kGravWarps - 1) / kGravWarps);
-    gravityKernel<<<blocks, kGravWarps * 32, 0, st>>>(p, w, n, theta2, checkInside, groups, counter);
+    kernel<<<blocks, kGravWarps * 32, 0, st>>>(p, w, n, theta2, groups, counter);
     return cudaGetLastError();
 }
 
