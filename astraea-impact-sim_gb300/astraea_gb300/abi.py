@@ -72,8 +72,8 @@ DEVFLAG_LOOKBACK_TIMEOUT = 0x1
 DEVFLAG_NEIGHBOR_OVERFLOW = 0x2
 DEVFLAG_STACK_OVERFLOW = 0x4
 
-COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "pass2_pairs",
-            "pass1_pairs", "fallback_walks", "neighbor_candidates", "gravity_undecided"]
+COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "gravity_rounds",
+            "gravity_stack_peak", "fallback_walks", "neighbor_candidates", "gravity_undecided"]
 
 # (symbol, argtypes) of every exported entry point, in header order.
 _P = ctypes.POINTER(Particles)

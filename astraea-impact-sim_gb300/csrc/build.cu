@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, 
         const float dNode = fmaxf(out.mxx - out.mnx, fmaxf(out.mxy - out.mny, out.mxz - out.mnz));
         float4* rec = w.node + 4 * static_cast<size_t>(pNode);
         __stcg(&rec[0], make_float4(out.cx, out.cy, out.cz, mSum));
-        __stcg(&rec[1], make_float4(dNode, __int_as_float(lc), __int_as_float(rc), out.maxHs));
+        __stcg(&rec[1], make_float4(__fmul_rn(dNode, dNode), __int_as_float(lc), __int_as_float(rc), out.maxHs));
         __stcg(&rec[2], make_float4(out.mnx, out.mny, out.mnz, out.maxH));
         __stcg(&rec[3], make_float4(out.mxx, out.mxy, out.mxz, 0.0f));
         double2* mp = reinterpret_cast<double2*>(w.nodeMom + pNode);

@@ -10,7 +10,7 @@
 //   rec2    [5N]  float4 x5 per particle          pass-2 neighbour record
 //   node    [4(N-1)] float4 x4 per internal node:
 //        r0 {comX, comY, comZ, mass}
-//        r1 {dNode, left (int bits), right (int bits), maxHs}
+//        r1 {dNode^2 (dNode = largest box side), left (int bits), right (int bits), maxHs}
 //        r2 {minX, minY, minZ, maxH}             maxH = max 2h (engine field)
 //        r3 {maxX, maxY, maxZ, 0}
 //   nodeMom [N-1] NodeMom {sum m x, sum m y, sum m z, sum m}  FP64 refit
@@ -44,8 +44,8 @@ enum Counter : int {
     kCntGravityInteractions = 0,   // particle-node + particle-particle evaluations
     kCntGravityNodeTests = 1,      // internal nodes tested by the group walk
     kCntNeighborEntries = 2,       // neighbour-list entries written
-    kCntPass2Pairs = 3,            // in-range pairs of SPH pass 2
-    kCntPass1Pairs = 4,            // in-range pairs of SPH pass 1
+    kCntGravityRounds = 3,         // gravity walk rounds (up to 32 pending entries each)
+    kCntGravityStackPeak = 4,      // deepest gravity walk stack (maximum, not a sum)
     kCntFallbackWalks = 5,         // particles served by the per-thread walk
     kCntNeighborCandidates = 6,    // leaves tested by the neighbour build (after the group-box filter)
     kCntGravityUndecided = 7,      // nodes the whole group had to test in the gravity walk

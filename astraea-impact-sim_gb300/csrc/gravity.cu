@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
     __shared__ GravWarpSmem<kInside> smem[kGravWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GravWarpSmem<kInside>& S = smem[warp];
-    unsigned long long nInter = 0, nTests = 0, nUndecided = 0;
+    unsigned long long nInter = 0, nTests = 0, nUndecided = 0, nRounds = 0;
+    int spPeak = 0;
     bool overflowed = false;
 
     if (n == 1u) {                                   // sph_gravity.cu:824-832
@@ -226,6 +227,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 overflowed = true;
                 break;
             }
+            spPeak = max(spPeak, sp);
             const int take = min(sp, 32);
             const int c = (lane < take) ? S.stack[sp - take + lane] : 0;
             sp -= take;
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 const float4 r1 = __ldg(&rec[1]);
                 cl = __float_as_int(r1.y);
                 cr = __float_as_int(r1.z);
-                dd = __fmul_rn(r1.x, r1.x);
+                dd = r1.x;                       // dNode^2, rounded once by the refit
                 bool disjoint = true;
                 if (kInside) {
                     bmin = __ldg(&rec[2]);
@@ -387,6 +389,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             p.accZ[i] = c0 + c1;
             p.phiGrav[i] = phi;
         }
+        nRounds += rounds;
         nInter += static_cast<unsigned long long>(act) * static_cast<unsigned>(mCount + pCount);
         if (lane == 0) nInter -= static_cast<unsigned long long>(__popc(selfSeen));
         __syncwarp();
@@ -396,6 +399,8 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         atomicAdd(&st->counters[kCntGravityInteractions], nInter);
         atomicAdd(&st->counters[kCntGravityNodeTests], nTests);
         atomicAdd(&st->counters[kCntGravityUndecided], nUndecided);
+        atomicAdd(&st->counters[kCntGravityRounds], nRounds);
+        atomicMax(&st->counters[kCntGravityStackPeak], static_cast<unsigned long long>(spPeak));
         if (overflowed) atomicOr(&st->flags, kFlagStackOverflow);
     }
 }

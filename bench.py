@@ -227,7 +227,9 @@ def run_gpu(args):
                      "interactions_per_launch": inter, "launch_ms": grav_ms},
         "step_hbm": step_hbm_roofline(n, ms_max / args.steps),
         "force_error_rms_vs_fp64": err_rms,
-        "step_counters_per_particle": {k: v / (args.steps * n) for k, v in counters.items()},
+        "step_counters_per_particle": {k: v / (args.steps * n) for k, v in counters.items()
+                                       if k != "gravity_stack_peak"},
+        "gravity_stack_peak": counters.get("gravity_stack_peak"),
         "device_flags": flags,
         "e2e": e2e,
     }
