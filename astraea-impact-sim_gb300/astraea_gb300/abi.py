@@ -76,6 +76,14 @@ COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "g
             "gravity_stack_peak", "fallback_walks", "neighbor_candidates", "gravity_undecided"]
 
 # (symbol, argtypes) of every exported entry point, in header order.
+class PclsFrameInfo(ctypes.Structure):
+    """AstraeaPclsFrameInfo of include/astraea_gb300.h."""
+    _fields_ = [("simTimeSec", ctypes.c_double), ("frameSeq", ctypes.c_uint64), ("dtSec", ctypes.c_float),
+                ("tracerCount", ctypes.c_uint32), ("tracerGridRes", ctypes.c_uint32),
+                ("livingBodyPresent", ctypes.c_int32), ("withSpeed", ctypes.c_int32),
+                ("livingCom", ctypes.c_float * 3), ("sysCom", ctypes.c_float * 3)]
+
+
 _P = ctypes.POINTER(Particles)
 _B = ctypes.POINTER(RadixBvh)
 _U32 = ctypes.c_uint32
@@ -98,6 +106,11 @@ SIGNATURES = [
     ("astraea_gb300_leapfrog_kick_half", [_P, _F, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_leapfrog_drift", [_P, _F, _B], ctypes.c_int),
     ("astraea_gb300_reduce_dt_psu", [_P, _F, _F, ctypes.POINTER(_F)], ctypes.c_int),
+    ("astraea_gb300_pack_render_records", [_P, _VP, _VP, _F, _F, _F], ctypes.c_int),
+    ("astraea_gb300_extract_tracers", [_P, _VP, _U32, _U32, _F, _F, _F, _F, _F, _F], ctypes.c_int),
+    ("astraea_gb300_pcls_frame_bytes", [_U32, _U32, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    ("astraea_gb300_pack_pcls_frame", [_P, ctypes.POINTER(PclsFrameInfo), _VP, ctypes.c_size_t,
+                                       ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

@@ -213,6 +213,39 @@ def step(p, alt, bvh, prev_dt, max_dt, theta=0.5, out_dt_ptr=None):
     _rebind_after_swap(p, alt, sp, salt)
 
 
+def pack_render_records(p, records, speed=None, sys_com=(0.0, 0.0, 0.0)):
+    """launchPackRenderRecords: 20-byte records (uint8 tensor of 20 N) and,
+    when `speed` is given, one speed byte per particle."""
+    s = p.struct()
+    abi.check(lib().astraea_gb300_pack_render_records(ctypes.byref(s), records.data_ptr(),
+                                                      speed.data_ptr() if speed is not None else None,
+                                                      *map(float, sys_com)))
+
+
+def extract_tracers(p, records, tracer_count, grid_res=0, living_com=(0.0, 0.0, 0.0), sys_com=(0.0, 0.0, 0.0)):
+    """launchExtractTracers: 40-byte tracer records (uint8 tensor of 40 T)."""
+    s = p.struct()
+    abi.check(lib().astraea_gb300_extract_tracers(ctypes.byref(s), records.data_ptr(), int(tracer_count),
+                                                  int(grid_res), *map(float, living_com), *map(float, sys_com)))
+
+
+def pcls_frame_bytes(n, tracer_count, with_speed=True):
+    out = ctypes.c_size_t(0)
+    abi.check(lib().astraea_gb300_pcls_frame_bytes(int(n), int(tracer_count), int(bool(with_speed)),
+                                                   ctypes.byref(out)))
+    return out.value
+
+
+def pack_pcls_frame(p, info, frame):
+    """One uncompressed PCLS frame into `frame` (uint8 device tensor);
+    `info` is an abi.PclsFrameInfo.  Returns the frame size in bytes."""
+    s = p.struct()
+    size = ctypes.c_size_t(0)
+    abi.check(lib().astraea_gb300_pack_pcls_frame(ctypes.byref(s), ctypes.byref(info), frame.data_ptr(),
+                                                  frame.numel(), ctypes.byref(size)))
+    return size.value
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 

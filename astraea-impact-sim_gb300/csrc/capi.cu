@@ -567,6 +567,70 @@ AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevD
     return ASTRAEA_OK;
 }
 
+AstraeaStatus astraea_gb300_pack_render_records(const AstraeaParticles* p, uint8_t* records20, uint8_t* speedBytes,
+                                                float sysComX, float sysComY, float sysComZ) {
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    if (p->count == 0u || records20 == nullptr) return ASTRAEA_OK;            // sph_gravity.cu:2195-2197
+    AG_LAUNCH(launchPackRender(*p, p->count, records20, speedBytes, sysComX, sysComY, sysComZ, stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_extract_tracers(const AstraeaParticles* p, uint8_t* records40, uint32_t tracerCount,
+                                            uint32_t tracerGridRes, float livingComX, float livingComY,
+                                            float livingComZ, float sysComX, float sysComY, float sysComZ) {
+    (void)tracerGridRes;                                                     // unused, as in the engine
+    if (p == nullptr) return fail(ASTRAEA_ERR_INVALID, "null particle descriptor");
+    AG_LAUNCH(launchExtractTracers(*p, p->count, records40, tracerCount, livingComX, livingComY, livingComZ, sysComX,
+                                   sysComY, sysComZ, stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_pcls_frame_bytes(uint32_t particleCount, uint32_t tracerCount, int withSpeed,
+                                              size_t* outBytes) {
+    if (outBytes == nullptr) return fail(ASTRAEA_ERR_INVALID, "null output");
+    const size_t n = particleCount, t = tracerCount;
+    *outBytes = 40u + 20u * n + 40u * t + ((withSpeed && n > 0u) ? n : 0u);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_pack_pcls_frame(const AstraeaParticles* p, const AstraeaPclsFrameInfo* info,
+                                            uint8_t* frame, size_t frameCapacity, size_t* outFrameBytes) {
+    if (p == nullptr || info == nullptr || frame == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const uint32_t n = p->count, t = info->tracerCount;
+    const bool hasSpeed = info->withSpeed != 0 && n > 0u;                    // binary_protocol.cpp:163
+    const size_t payload = 20u * static_cast<size_t>(n) + 40u * static_cast<size_t>(t) + (hasSpeed ? n : 0u);
+    if (payload > 0xffffffffull) return fail(ASTRAEA_ERR_CAPACITY, "PCLS payload exceeds 4 GiB");
+    if (frameCapacity < 40u + payload) return fail(ASTRAEA_ERR_CAPACITY, "frame buffer too small");
+    PclsHeaderWords h{};                                                     // binary_protocol.cpp:76-87, 168-187
+    uint32_t flags = 0u;
+    if (t > 0u) flags |= 2u;                       // kFlagHasTracers
+    if (info->livingBodyPresent) flags |= 4u;      // kFlagHasLivingCom
+    if (hasSpeed) flags |= 8u;                     // kFlagHasSpeedArray (never kFlagZlib: no device deflate)
+    uint64_t simBits;
+    std::memcpy(&simBits, &info->simTimeSec, 8);
+    uint32_t dtBits;
+    std::memcpy(&dtBits, &info->dtSec, 4);
+    h.w[0] = 0x50434C53u;                          // "PCLS"
+    h.w[1] = 1u | (flags << 16);                   // version 1
+    h.w[2] = static_cast<uint32_t>(simBits);
+    h.w[3] = static_cast<uint32_t>(simBits >> 32);
+    h.w[4] = static_cast<uint32_t>(info->frameSeq & 0xffffffffull);
+    h.w[5] = dtBits;
+    h.w[6] = n;
+    h.w[7] = t;
+    h.w[8] = t > 0u ? info->tracerGridRes : 0u;
+    h.w[9] = static_cast<uint32_t>(payload);
+    AG_LAUNCH(launchWriteHeader(frame, h, stream()));
+    uint8_t* particles = frame + 40;
+    uint8_t* tracers = particles + 20u * static_cast<size_t>(n);
+    uint8_t* speed = hasSpeed ? tracers + 40u * static_cast<size_t>(t) : nullptr;
+    AG_LAUNCH(launchPackRender(*p, n, particles, speed, info->sysCom[0], info->sysCom[1], info->sysCom[2], stream()));
+    AG_LAUNCH(launchExtractTracers(*p, n, tracers, t, info->livingCom[0], info->livingCom[1], info->livingCom[2],
+                                   info->sysCom[0], info->sysCom[1], info->sysCom[2], stream()));
+    if (outFrameBytes != nullptr) *outFrameBytes = 40u + payload;
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult) {
     DeviceState* ds = nullptr;
     AstraeaStatus s = deviceState(&ds);

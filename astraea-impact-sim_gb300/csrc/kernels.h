@@ -56,6 +56,17 @@ cudaError_t launchRefreshLeaves(const AstraeaParticles& p, const Work& w, uint32
                                 cudaStream_t st);
 cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, cudaStream_t st);
 
+// ----------------------------------------------------------- render.cu ---
+// PCLS frame header as ten little-endian words (server/binary_protocol.cpp:76-87).
+struct PclsHeaderWords {
+    uint32_t w[10];
+};
+cudaError_t launchPackRender(const AstraeaParticles& p, uint32_t n, uint8_t* records, uint8_t* speed, float sx, float sy,
+                             float sz, cudaStream_t st);
+cudaError_t launchExtractTracers(const AstraeaParticles& p, uint32_t n, uint8_t* records, uint32_t tracerCount,
+                                 float lx, float ly, float lz, float sx, float sy, float sz, cudaStream_t st);
+cudaError_t launchWriteHeader(uint8_t* frame, const PclsHeaderWords& h, cudaStream_t st);
+
 // ---------------------------------------------------------- gravity.cu ---
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, int sms,
                           cudaStream_t st);

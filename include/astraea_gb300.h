@@ -169,6 +169,50 @@ AstraeaStatus astraea_gb300_leapfrog_drift(AstraeaParticles* p, float dtPsu,
 AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevDtPsu,
                                           float maxDtPsu, float* outDtPsu);
 
+/* ---- render frame packing (engine/sph_gravity.cu:1554-1743, 2163-2201) -- */
+
+/* Replaces launchPackRenderRecords (engine/sph_gravity.cu:2189-2201): one
+ * 20-byte ParticleRecordPacked per particle (position in km relative to the
+ * system COM, log-quantised temperature, pressure and radius, material,
+ * phase|body, damage) into records20 (device, any alignment), and one
+ * log-quantised speed byte per particle into speedBytes when it is not NULL.
+ * count == 0 or records20 == NULL is a no-op. */
+AstraeaStatus astraea_gb300_pack_render_records(const AstraeaParticles* p, uint8_t* records20, uint8_t* speedBytes,
+                                                float sysComX, float sysComY, float sysComZ);
+/* Replaces launchExtractTracers (engine/sph_gravity.cu:2163-2187): zeroes
+ * tracerCount 40-byte CrustTracerRecordPacked records, then writes one for
+ * every particle whose tracerIndex is in [0, tracerCount).  tracerGridRes is
+ * unused, as in the engine.  tracerCount == 0 or records40 == NULL is a no-op. */
+AstraeaStatus astraea_gb300_extract_tracers(const AstraeaParticles* p, uint8_t* records40, uint32_t tracerCount,
+                                            uint32_t tracerGridRes, float livingComX, float livingComY,
+                                            float livingComZ, float sysComX, float sysComY, float sysComZ);
+
+/* Uncompressed PCLS frame (server/binary_protocol.hpp:11-59): the fields of
+ * the 40-byte header that come from the telemetry snapshot, and the COMs the
+ * two packing kernels take.  No engine counterpart as one call: the engine
+ * packs on the device, copies three arrays to the host and assembles the
+ * frame there (engine/simulation.cpp:1810-1860, binary_protocol.cpp:155-217). */
+typedef struct AstraeaPclsFrameInfo {
+    double   simTimeSec;
+    uint64_t frameSeq;          /* low 32 bits go into the header */
+    float    dtSec;
+    uint32_t tracerCount;
+    uint32_t tracerGridRes;
+    int32_t  livingBodyPresent;
+    int32_t  withSpeed;         /* append the speed-byte array */
+    float    livingCom[3];
+    float    sysCom[3];
+} AstraeaPclsFrameInfo;
+/* Bytes of the uncompressed frame: 40 + 20 N + 40 T (+ N with speed). */
+AstraeaStatus astraea_gb300_pcls_frame_bytes(uint32_t particleCount, uint32_t tracerCount, int withSpeed,
+                                             size_t* outBytes);
+/* Writes header, particle records, tracer records and speed bytes of one
+ * frame into `frame` (device, frameCapacity bytes); *outFrameBytes (host, may
+ * be NULL) receives its size.  Byte-identical to buildBinaryFrame with
+ * compressZlib = false on the same records; zlib stays a host step. */
+AstraeaStatus astraea_gb300_pack_pcls_frame(const AstraeaParticles* p, const AstraeaPclsFrameInfo* info,
+                                            uint8_t* frame, size_t frameCapacity, size_t* outFrameBytes);
+
 /* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
 
 /* One Simulation::step() kernel sequence (engine/simulation.cpp:1711-1753):

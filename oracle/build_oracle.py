@@ -4,6 +4,8 @@
   compiled with OpenMP and with multiply-add contraction off
   (-ffp-contract=off) so its float arithmetic rounds like the reference
   expressions it restates, on x86_64 and aarch64 alike.
+* oracle/_ref/libref_pcls.so -- the reference's server/binary_protocol.cpp
+  (PCLS frame builder) behind oracle/ref_pcls_capi.cpp, same conditions.
 * oracle/_ref/libref_eos.so -- the reference's own engine/eos.cu compiled as
   host C++ from the reference checkout where it lies (only when that checkout
   exists; it is absent on GPU machines, which use the committed golden
@@ -79,7 +81,27 @@ def build_reference_cubin(force=False):
     return out
 
 
+def build_reference_pcls(force=False):
+    """The reference's PCLS frame builder (server/binary_protocol.cpp, host
+    C++ with zlib) behind a C entry point; None where the checkout or zlib is
+    absent."""
+    server = os.path.join(os.path.dirname(REFERENCE_ENGINE), "server")
+    src = os.path.join(server, "binary_protocol.cpp")
+    if not os.path.exists(src) or not os.path.exists("/usr/include/zlib.h"):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libref_pcls.so")
+    shim = os.path.join(HERE, "ref_pcls_capi.cpp")
+    if force or _stale(out, [src, shim]):
+        tmp = out + ".tmp%d" % os.getpid()
+        _run(["g++"] + CXXFLAGS + ["-I", REFERENCE_ENGINE, "-I", server, src, shim, "-lz", "-o", tmp])
+        os.replace(tmp, out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_reference_eos(force="--force" in sys.argv))
     print(build_reference_cubin(force="--force" in sys.argv))
+    print(build_reference_pcls(force="--force" in sys.argv))

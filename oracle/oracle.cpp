@@ -1077,6 +1077,133 @@ float oracle_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* b
     return dt;
 }
 
+// ---------------------------------------------------------- render ----
+// engine/sph_gravity.cu:1583-1585
+static inline float finite0(float v) { return std::isfinite(v) ? v : 0.0f; }
+static inline void putU32(uint8_t* d, uint32_t v) { for (int k = 0; k < 4; ++k) d[k] = static_cast<uint8_t>(v >> (8 * k)); }
+static inline void putF32(uint8_t* d, float f) { uint32_t v; std::memcpy(&v, &f, 4); putU32(d, v); }
+static inline void putU16(uint8_t* d, uint16_t v) { d[0] = static_cast<uint8_t>(v); d[1] = static_cast<uint8_t>(v >> 8); }
+
+// packRenderRecordsKernel, engine/sph_gravity.cu:1670-1743 (20-byte records,
+// little-endian, layout of ParticleRecordPacked :1570-1581).
+void oracle_pack_render_records(const AstraeaParticles* p, uint8_t* rec20, uint8_t* speed, float sx, float sy,
+                                float sz) {
+    const float kInvLog20000 = 1.0f / 9.9034875525361280f;
+    const float kInvLog1e7 = 1.0f / 16.118095650958320f;
+    const float kInvLog2000 = 1.0f / 7.6009024595420823f;
+    for (uint32_t i = 0; i < p->count; ++i) {
+        uint8_t* d = rec20 + 20u * static_cast<size_t>(i);
+        putF32(d + 0, finite0((p->posX[i] - sx) * 1000.0f));
+        putF32(d + 4, finite0((p->posY[i] - sy) * 1000.0f));
+        putF32(d + 8, finite0((p->posZ[i] - sz) * 1000.0f));
+        const float T = std::fmax(10.0f, finite0(p->tempK[i]));
+        const float tNorm = std::fmin(1.0f, std::fmax(0.0f, std::log(T * 0.1f) * kInvLog20000));
+        putU16(d + 12, static_cast<uint16_t>(std::lrint(65535.0f * tNorm)));
+        const float pGPa = finite0(p->pressure[i]) * 1000.0f;
+        uint16_t pu = 0;
+        if (pGPa > 1.0e-3f) {
+            const float pNorm = std::fmin(1.0f, std::fmax(0.0f, std::log(pGPa * 1000.0f) * kInvLog1e7));
+            pu = static_cast<uint16_t>(std::lrint(1.0f + 65534.0f * pNorm));
+        }
+        putU16(d + 14, pu);
+        d[16] = p->materialId[i];
+        d[17] = static_cast<uint8_t>(((p->bodyId[i] & 0x0Fu) << 4) | (p->phaseId[i] & 0x0Fu));
+        const float dam = std::fmin(1.0f, std::fmax(0.0f, finite0(p->damage[i])));
+        d[18] = static_cast<uint8_t>(std::lrint(dam * 255.0f));
+        const float vol = std::fmax(p->mass[i], 0.0f) / std::fmax(p->rho[i], 1.0e-9f);
+        const float rKm = std::cbrt((3.0f * vol) / (4.0f * kPiF)) * 1000.0f;
+        const float rNorm = std::fmin(1.0f, std::fmax(0.0f, std::log(std::fmax(rKm, 1.0f)) * kInvLog2000));
+        d[19] = static_cast<uint8_t>(std::lrint(255.0f * rNorm));
+        if (speed != nullptr) {
+            const float vx = p->velX[i], vy = p->velY[i], vz = p->velZ[i];
+            const float sp = finite0(std::sqrt(vx * vx + vy * vy + vz * vz));
+            const float vNorm = std::fmin(1.0f, std::fmax(0.0f, std::log(std::fmax(sp, 0.05f) * 20.0f) * kInvLog2000));
+            speed[i] = static_cast<uint8_t>(std::lrint(255.0f * vNorm));
+        }
+    }
+}
+
+// extractTracersKernel + launchExtractTracers, engine/sph_gravity.cu:1586-1668,
+// 2163-2187 (40-byte records, layout of CrustTracerRecordPacked :1554-1567).
+void oracle_extract_tracers(const AstraeaParticles* p, uint8_t* rec40, uint32_t tracerCount, float lx, float ly,
+                            float lz, float sx, float sy, float sz) {
+    if (tracerCount == 0 || rec40 == nullptr) return;
+    std::memset(rec40, 0, 40u * static_cast<size_t>(tracerCount));
+    for (uint32_t i = 0; i < p->count; ++i) {
+        const int32_t t = p->tracerIndex[i];
+        if (t < 0 || static_cast<uint32_t>(t) >= tracerCount) continue;
+        const float px = p->posX[i], py = p->posY[i], pz = p->posZ[i];
+        const float dx = px - lx, dy = py - ly, dz = pz - lz;
+        const float r = std::sqrt(dx * dx + dy * dy + dz * dz);
+        const float rRest = p->tracerRestRadiusPsu[i];
+        const float dispKm = (r - rRest) * 1000.0f;
+        float normalDelta = 0.0f;
+        if (r > 1.0e-9f) {
+            const float invR = 1.0f / r;
+            const float nx = dx * invR, ny = dy * invR, nz = dz * invR;
+            const float dot = std::fmin(1.0f, std::fmax(-1.0f, nx * p->tracerRestNormalX[i] +
+                                                                   ny * p->tracerRestNormalY[i] +
+                                                                   nz * p->tracerRestNormalZ[i]));
+            normalDelta = std::acos(dot);
+        }
+        const float dam = std::fmin(1.0f, std::fmax(0.0f, finite0(p->damage[i])));
+        const float tempK = std::fmax(3.0f, finite0(p->tempK[i]));
+        const uint8_t phase = p->phaseId[i];
+        const bool ocean = p->tracerIsOcean[i] != 0;
+        const bool disrupted = dam >= 0.85f || phase == 2 || phase == 3 ||
+                               std::fabs(r - rRest) > 0.5f * std::fmax(rRest, 1.0e-3f);
+        const float dv = std::fmax(0.0f, -finite0(p->divV[i])) * std::fmax(p->h[i], 0.0f) * 1000.0f;
+        const float over = std::fmax(0.0f, 1.225f * 340.0f * dv * 1.0e-3f);
+        const float tsunami = ocean ? std::fmax(0.0f, finite0(dispKm) * 1000.0f) : 0.0f;
+        uint8_t* d = rec40 + 40u * static_cast<size_t>(t);
+        putU16(d + 0, static_cast<uint16_t>(t));
+        putU16(d + 2, static_cast<uint16_t>((ocean ? 1u : 0u) | (disrupted ? 2u : 0u)));
+        putF32(d + 4, finite0((px - sx) * 1000.0f));
+        putF32(d + 8, finite0((py - sy) * 1000.0f));
+        putF32(d + 12, finite0((pz - sz) * 1000.0f));
+        putF32(d + 16, finite0(dispKm));
+        putF32(d + 20, finite0(normalDelta));
+        putF32(d + 24, tempK);
+        putF32(d + 28, dam);
+        putF32(d + 32, finite0(over));
+        putF32(d + 36, finite0(tsunami));
+    }
+}
+
+// Uncompressed PCLS frame: encodeHeader40 + buildBinaryFrame with
+// compressZlib = false (server/binary_protocol.cpp:76-87, 155-217), records
+// from the two functions above.  Returns the frame size (0 if cap too small).
+size_t oracle_pcls_frame(const AstraeaParticles* p, const AstraeaPclsFrameInfo* info, uint8_t* out, size_t cap) {
+    const size_t n = p->count, t = info->tracerCount;
+    const bool hasSpeed = info->withSpeed != 0 && n > 0;
+    const size_t payload = 20 * n + 40 * t + (hasSpeed ? n : 0);
+    if (cap < 40 + payload) return 0;
+    uint16_t flags = 0;
+    if (t > 0) flags |= 2u;
+    if (info->livingBodyPresent) flags |= 4u;
+    if (hasSpeed) flags |= 8u;
+    putU32(out + 0, 0x50434C53u);
+    putU16(out + 4, 1u);
+    putU16(out + 6, flags);
+    uint64_t sb;
+    std::memcpy(&sb, &info->simTimeSec, 8);
+    putU32(out + 8, static_cast<uint32_t>(sb));
+    putU32(out + 12, static_cast<uint32_t>(sb >> 32));
+    putU32(out + 16, static_cast<uint32_t>(info->frameSeq & 0xffffffffull));
+    putF32(out + 20, info->dtSec);
+    putU32(out + 24, static_cast<uint32_t>(n));
+    putU32(out + 28, static_cast<uint32_t>(t));
+    putU32(out + 32, t > 0 ? info->tracerGridRes : 0u);
+    putU32(out + 36, static_cast<uint32_t>(payload));
+    uint8_t* recs = out + 40;
+    uint8_t* trc = recs + 20 * n;
+    uint8_t* spd = hasSpeed ? trc + 40 * t : nullptr;
+    oracle_pack_render_records(p, recs, spd, info->sysCom[0], info->sysCom[1], info->sysCom[2]);
+    oracle_extract_tracers(p, trc, static_cast<uint32_t>(t), info->livingCom[0], info->livingCom[1],
+                           info->livingCom[2], info->sysCom[0], info->sysCom[1], info->sysCom[2]);
+    return 40 + payload;
+}
+
 int oracle_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
 void oracle_set_group_stride(int k) { g_groupStride = k < 1 ? 1 : k; }
 

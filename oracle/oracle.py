@@ -54,11 +54,15 @@ def load(build=True):
             "oracle_drift": [P, f, B, ctypes.c_int],
             "oracle_reduce_dt": [P, f, f, vp],
             "oracle_step": [P, P, B, f, f, f],
+            "oracle_pack_render_records": [P, vp, vp, f, f, f],
+            "oracle_extract_tracers": [P, vp, u32, f, f, f, f, f, f],
+            "oracle_pcls_frame": [P, ctypes.POINTER(abi.PclsFrameInfo), vp, ctypes.c_size_t],
         }
         for name, args in sig.items():
             getattr(_lib, name).argtypes = args
         _lib.oracle_reduce_dt.restype = f
         _lib.oracle_step.restype = f
+        _lib.oracle_pcls_frame.restype = ctypes.c_size_t
         _lib.oracle_set_group_stride.argtypes = [ctypes.c_int]
         _lib.oracle_cold_energy.restype = ctypes.c_double
         _lib.oracle_cold_energy.argtypes = [ctypes.c_int, ctypes.c_double]
@@ -85,6 +89,109 @@ def load_reference_eos():
         _ref.ref_cold_energy.argtypes = [ctypes.c_int, ctypes.c_double]
         _ref.ref_cold_energy.restype = ctypes.c_double
     return _ref
+
+
+def load_reference_pcls():
+    """The reference's PCLS frame builder (server/binary_protocol.cpp) as a
+    host library (None where the checkout or zlib is absent)."""
+    sys.path.insert(0, HERE)
+    import build_oracle
+    path = build_oracle.build_reference_pcls()
+    if path is None or not os.path.exists(path):
+        return None
+    lib = ctypes.CDLL(path)
+    vp, sz = ctypes.c_void_p, ctypes.c_size_t
+    lib.ref_build_frame.argtypes = [vp, sz, vp, sz, vp, sz, ctypes.c_double, ctypes.c_uint64, ctypes.c_float,
+                                    ctypes.c_int, ctypes.c_uint32, ctypes.c_int, vp, sz]
+    lib.ref_build_frame.restype = sz
+    return lib
+
+
+def random_render_state(n, tracer_count, seed=7):
+    """Seeded particle state for the packing kernels, with the edge cases
+    their clamps handle: non-finite and negative temperatures, pressures below
+    the 1 kPa cut, damage outside [0, 1], zero density, tracer indices that are
+    negative or >= tracer_count, particles sitting on the living COM."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    st = {k: (rng.normal(0.0, 2.0, n)).astype(f32) for k in ("posX", "posY", "posZ")}
+    for k in ("velX", "velY", "velZ"):
+        st[k] = (rng.normal(0.0, 1.0, n) * 10.0 ** rng.uniform(-3, 1, n)).astype(f32)
+    st["tempK"] = (10.0 ** rng.uniform(0.0, 6.0, n)).astype(f32)
+    st["pressure"] = (np.sign(rng.normal(size=n)) * 10.0 ** rng.uniform(-10, 2, n)).astype(f32)
+    st["damage"] = rng.uniform(-0.3, 1.3, n).astype(f32)
+    st["mass"] = (10.0 ** rng.uniform(-12, -3, n)).astype(f32)
+    st["rho"] = (10.0 ** rng.uniform(-4, 1.5, n)).astype(f32)
+    st["divV"] = rng.normal(0.0, 5.0, n).astype(f32)
+    st["h"] = (10.0 ** rng.uniform(-4, -1, n)).astype(f32)
+    st["materialId"] = rng.integers(0, 5, n).astype(np.uint8)
+    st["phaseId"] = rng.integers(0, 6, n).astype(np.uint8)
+    st["bodyId"] = rng.integers(0, 20, n).astype(np.uint8)
+    bad = rng.choice(n, max(n // 64, 8), replace=False)
+    st["tempK"][bad[0::4]] = np.nan
+    st["tempK"][bad[1::4]] = -5.0
+    st["pressure"][bad[2::4]] = np.inf
+    st["damage"][bad[3::4]] = np.nan
+    st["rho"][bad[:4]] = 0.0
+    tr = np.full(n, -1, np.int32)
+    owners = rng.choice(n, min(n, tracer_count + 16), replace=False)
+    slots = rng.permutation(tracer_count + 16).astype(np.int32)
+    tr[owners] = slots[: len(owners)]                 # some slots >= tracer_count: skipped
+    st["tracerIndex"] = tr
+    r = np.sqrt(st["posX"].astype(np.float64) ** 2 + st["posY"] ** 2 + st["posZ"] ** 2)
+    st["tracerRestRadiusPsu"] = (r * rng.uniform(0.8, 1.2, n)).astype(f32)
+    nrm = rng.normal(size=(3, n))
+    nrm /= np.linalg.norm(nrm, axis=0)
+    st["tracerRestNormalX"], st["tracerRestNormalY"], st["tracerRestNormalZ"] = nrm.astype(f32)
+    st["tracerIsOcean"] = (rng.uniform(size=n) < 0.3).astype(np.uint8)
+    st["posX"][owners[0]] = st["posY"][owners[0]] = st["posZ"][owners[0]] = 0.0   # r = 0 at the living COM
+    return st
+
+
+def frame_info(sim_time=0.0, frame_seq=0, dt_sec=0.0, tracer_count=0, grid_res=0, living=False, speed=True,
+               living_com=(0.0, 0.0, 0.0), sys_com=(0.0, 0.0, 0.0)):
+    fi = abi.PclsFrameInfo()
+    fi.simTimeSec, fi.frameSeq, fi.dtSec = sim_time, frame_seq, dt_sec
+    fi.tracerCount, fi.tracerGridRes = tracer_count, grid_res
+    fi.livingBodyPresent, fi.withSpeed = int(bool(living)), int(bool(speed))
+    fi.livingCom[:] = list(living_com)
+    fi.sysCom[:] = list(sys_com)
+    return fi
+
+
+def pack_render_records(state, sys_com, speed=True):
+    """engine/sph_gravity.cu:1670-1743 on a host state: (records u8[20N], speed u8[N] or None)."""
+    lib = load()
+    hp = HostParticles(state)
+    n = hp.count
+    rec = np.zeros(20 * n, np.uint8)
+    spd = np.zeros(n, np.uint8) if speed else None
+    s = hp.struct()
+    lib.oracle_pack_render_records(ctypes.byref(s), _ptr(rec), _ptr(spd) if speed else None, *map(float, sys_com))
+    return rec, spd
+
+
+def extract_tracers(state, tracer_count, living_com, sys_com):
+    """engine/sph_gravity.cu:1586-1668 + 2163-2187 on a host state: u8[40 T]."""
+    lib = load()
+    hp = HostParticles(state)
+    out = np.zeros(40 * tracer_count, np.uint8)
+    s = hp.struct()
+    lib.oracle_extract_tracers(ctypes.byref(s), _ptr(out), tracer_count, *map(float, living_com),
+                               *map(float, sys_com))
+    return out
+
+
+def pcls_frame(state, info):
+    """Uncompressed PCLS frame (server/binary_protocol.cpp:76-87, 155-217)."""
+    lib = load()
+    hp = HostParticles(state)
+    n, t = hp.count, info.tracerCount
+    cap = 40 + 20 * n + 40 * t + n
+    out = np.zeros(cap, np.uint8)
+    s = hp.struct()
+    size = lib.oracle_pcls_frame(ctypes.byref(s), ctypes.byref(info), _ptr(out), cap)
+    return out[:size]
 
 
 def _ptr(a):

@@ -12,6 +12,9 @@ used at engine/sph_gravity.cu:2042).
 Uses:
   python oracle/ref_gpu.py golden OUT.npz   -- stage-by-stage outputs of the
       reference on the small two-sphere scene (tests/golden/ref_stages.npz)
+  python oracle/ref_gpu.py golden_render OUT.npz   -- the reference's render
+      and tracer packing kernels on a seeded edge-case state
+      (tests/golden/render_records.npz)
   python oracle/ref_gpu.py bench N STEPS WARMUP  -- the reference's GPU step
       time (gpuStepMs span, engine/simulation.cpp:1719-1739) on the
       differentiated-impact workload, one JSON line
@@ -35,7 +38,7 @@ KERNELS = {
     "karras": "initLeavesAndBuildKarrasKernel", "refit": "bottomUpBvhMomentsKernel", "clear": "clearStatsKernel",
     "pass1": "sphPass1KernelILb1E", "eos": "evaluateEosKernel", "gravity": "gravityBarnesHutKernelILb1E",
     "pass2": "sphPass2KernelILb1E", "kick": "leapfrogKickHalfKernel", "drift": "leapfrogDriftKernelILb1E",
-    "dt": "reduceDtMinKernel",
+    "dt": "reduceDtMinKernel", "render": "packRenderRecordsKernel", "tracers": "extractTracersKernel",
 }
 
 
@@ -199,6 +202,49 @@ STAGE_FIELDS = {
 }
 
 
+def ref_pack_render(K, p, records, speed, sys_com):         # sph_gravity.cu:2189-2201
+    """Reference render packing into device buffers (torch uint8 tensors)."""
+    n = p.count
+    if n == 0:
+        return
+    K.launch("render", grid(n, 256), 256, p.struct(), ctypes.c_uint32(n), ctypes.c_void_p(records.data_ptr()),
+             ctypes.c_void_p(speed.data_ptr() if speed is not None else None), *[ctypes.c_float(c) for c in sys_com])
+
+
+def ref_extract_tracers(K, p, records, tracer_count, living_com, sys_com):   # sph_gravity.cu:2163-2187
+    records.zero_()
+    n = p.count
+    if n == 0 or tracer_count == 0:
+        return
+    K.launch("tracers", grid(n, 256), 256, p.struct(), ctypes.c_uint32(n), ctypes.c_void_p(records.data_ptr()),
+             ctypes.c_uint32(tracer_count), *[ctypes.c_float(c) for c in living_com],
+             *[ctypes.c_float(c) for c in sys_com])
+
+
+RENDER_CASE = dict(n=2048, tracers=384, seed=11, sys_com=(0.125, -0.25, 0.0625), living_com=(0.5, 0.25, -0.125))
+
+
+def golden_render(out_path):
+    """Reference packing kernels on a seeded edge-case state (tests/golden/render_records.npz)."""
+    import torch
+    sys.path.insert(0, HERE)
+    import oracle
+    from astraea_gb300 import engine
+    c = RENDER_CASE
+    st = oracle.random_render_state(c["n"], c["tracers"], c["seed"])
+    K = RefKernels()
+    p = engine.DeviceParticles(c["n"])
+    p.upload(st)
+    rec = torch.zeros(20 * c["n"], dtype=torch.uint8, device="cuda")
+    spd = torch.zeros(c["n"], dtype=torch.uint8, device="cuda")
+    trc = torch.zeros(40 * c["tracers"], dtype=torch.uint8, device="cuda")
+    ref_pack_render(K, p, rec, spd, c["sys_com"])
+    ref_extract_tracers(K, p, trc, c["tracers"], c["living_com"], c["sys_com"])
+    torch.cuda.synchronize()
+    np.savez_compressed(out_path, records=rec.cpu().numpy(), speed=spd.cpu().numpy(), tracers=trc.cpu().numpy())
+    print("wrote", out_path)
+
+
 def golden(out_path):
     """Reference outputs of every stage on the two-sphere scene (3,072 + 1,024)."""
     import torch
@@ -304,5 +350,7 @@ def bench(n, steps, warmup, theta=0.5):
 if __name__ == "__main__":
     if sys.argv[1] == "golden":
         golden(sys.argv[2])
+    elif sys.argv[1] == "golden_render":
+        golden_render(sys.argv[2])
     elif sys.argv[1] == "bench":
         bench(int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))
