@@ -84,6 +84,39 @@ class PclsFrameInfo(ctypes.Structure):
                 ("livingCom", ctypes.c_float * 3), ("sysCom", ctypes.c_float * 3)]
 
 
+class TelemetryParams(ctypes.Structure):
+    """AstraeaTelemetryParams of include/astraea_gb300.h."""
+    _fields_ = [("targetRadiusPsu", ctypes.c_double), ("livingBodyPresent", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+_D3 = ctypes.c_double * 3
+
+
+class Telemetry(ctypes.Structure):
+    """AstraeaTelemetry of include/astraea_gb300.h (392 bytes)."""
+    _fields_ = [("totalMassPsu", ctypes.c_double), ("sysComPsu", _D3),
+                ("massBody0Psu", ctypes.c_double), ("comBody0Psu", _D3), ("velBody0Psu", _D3),
+                ("massOtherPsu", ctypes.c_double), ("comOtherPsu", _D3), ("velOtherPsu", _D3),
+                ("livingComPsu", _D3),
+                ("kineticPsu", ctypes.c_double), ("potentialPsu", ctypes.c_double), ("internalPsu", ctypes.c_double),
+                ("momentumPsu", _D3), ("angularMomentumPsu", _D3),
+                ("maxTempK", ctypes.c_double), ("maxPressureGPa", ctypes.c_double), ("maxDamage", ctypes.c_double),
+                ("radiatedPowerW", ctypes.c_double), ("spinLPsu", ctypes.c_double), ("spinIPsu", ctypes.c_double),
+                ("remnantPsu", _D3), ("remnantVelPsu", _D3), ("remnantMassPsu", ctypes.c_double),
+                ("remnantRadiusPsu", ctypes.c_double),
+                ("boundPlanetMassPsu", ctypes.c_double), ("diskMassPsu", ctypes.c_double),
+                ("ejectaMassPsu", ctypes.c_double), ("impactorBoundMassPsu", ctypes.c_double),
+                ("remnantSeedIndex", ctypes.c_uint32), ("remnantIterations", ctypes.c_int32)]
+
+    def as_dict(self):
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if isinstance(v, ctypes.Array) else v
+        return out
+
+
 _P = ctypes.POINTER(Particles)
 _B = ctypes.POINTER(RadixBvh)
 _U32 = ctypes.c_uint32
@@ -111,6 +144,8 @@ SIGNATURES = [
     ("astraea_gb300_pcls_frame_bytes", [_U32, _U32, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     ("astraea_gb300_pack_pcls_frame", [_P, ctypes.POINTER(PclsFrameInfo), _VP, ctypes.c_size_t,
                                        ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    ("astraea_gb300_reduce_telemetry", [_P, ctypes.POINTER(TelemetryParams), ctypes.POINTER(Telemetry)],
+     ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

@@ -246,6 +246,16 @@ def pack_pcls_frame(p, info, frame):
     return size.value
 
 
+def reduce_telemetry(p, target_radius_psu, living_body_present=True):
+    """The O(N) telemetry loops on the device; returns a dict of
+    AstraeaTelemetry fields (PSU, FP64)."""
+    s = p.struct()
+    prm = abi.TelemetryParams(float(target_radius_psu), int(bool(living_body_present)), 0)
+    out = abi.Telemetry()
+    abi.check(lib().astraea_gb300_reduce_telemetry(ctypes.byref(s), ctypes.byref(prm), ctypes.byref(out)))
+    return out.as_dict()
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 

@@ -631,6 +631,18 @@ AstraeaStatus astraea_gb300_pack_pcls_frame(const AstraeaParticles* p, const Ast
     return ASTRAEA_OK;
 }
 
+static_assert(sizeof(AstraeaTelemetry) == 392, "AstraeaTelemetry layout");
+
+AstraeaStatus astraea_gb300_reduce_telemetry(const AstraeaParticles* p, const AstraeaTelemetryParams* params,
+                                             AstraeaTelemetry* out) {
+    if (p == nullptr || params == nullptr || out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    if (p->count == 0u) return ASTRAEA_OK;                                   // simulation.cpp:962-965
+    AG_LAUNCH(launchTelemetry(*p, p->count, params->targetRadiusPsu, params->livingBodyPresent, smCount(), out,
+                              stream()));
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult) {
     DeviceState* ds = nullptr;
     AstraeaStatus s = deviceState(&ds);

@@ -67,6 +67,10 @@ cudaError_t launchExtractTracers(const AstraeaParticles& p, uint32_t n, uint8_t*
                                  float lx, float ly, float lz, float sx, float sy, float sz, cudaStream_t st);
 cudaError_t launchWriteHeader(uint8_t* frame, const PclsHeaderWords& h, cudaStream_t st);
 
+// -------------------------------------------------------- telemetry.cu ---
+cudaError_t launchTelemetry(const AstraeaParticles& p, uint32_t n, double targetRadiusPsu, int livingBodyPresent,
+                            int sms, AstraeaTelemetry* hostOut, cudaStream_t st);
+
 // ---------------------------------------------------------- gravity.cu ---
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, int sms,
                           cudaStream_t st);

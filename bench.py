@@ -206,6 +206,8 @@ def run_gpu(args):
     # ---- force error of the plain path vs an FP64 direct sum (sampled targets)
     err_rms = force_error_fp64(sim, engine, torch, np, samples=1024)
 
+    frame = frame_stages(sim, engine, torch, np, n)
+
     # ---- e2e through the C-ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -231,6 +233,7 @@ def run_gpu(args):
                                        if k != "gravity_stack_peak"},
         "gravity_stack_peak": counters.get("gravity_stack_peak"),
         "device_flags": flags,
+        "frame_stages": frame,
         "e2e": e2e,
     }
     out["config"]["max_dt_psu"] = max_dt
@@ -240,6 +243,34 @@ def run_gpu(args):
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def frame_stages(sim, engine, torch, np, n, reps=5):
+    """Per-frame work outside the step: the telemetry reduction (FP64 device
+    passes; about 219 B per particle over its seven passes) and one PCLS
+    frame (about 47 B read + 21 B written per particle), median of `reps`."""
+    from astraea_gb300 import abi
+    tele = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        engine.reduce_telemetry(sim.p, 1.0, True)          # blocks until the result is on the host
+        tele.append((time.perf_counter() - t0) * 1e3)
+    size = engine.pcls_frame_bytes(n, 0, True)
+    buf = torch.empty(size, dtype=torch.uint8, device="cuda")
+    info = abi.PclsFrameInfo()
+    info.withSpeed = 1
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    pk = []
+    for _ in range(reps):
+        ev[0].record()
+        engine.pack_pcls_frame(sim.p, info, buf)
+        ev[1].record()
+        torch.cuda.synchronize()
+        pk.append(ev[0].elapsed_time(ev[1]))
+    tm, pm = float(np.median(tele)), float(np.median(pk))
+    return {"telemetry_ms": tm, "telemetry_gbs": 219.0 * n / (tm * 1e-3) / 1e9,
+            "pcls_frame_ms": pm, "pcls_frame_bytes": size, "pcls_frame_gbs": 68.0 * n / (pm * 1e-3) / 1e9}
 
 
 def step_hbm_roofline(n, ms):

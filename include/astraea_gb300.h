@@ -213,6 +213,44 @@ AstraeaStatus astraea_gb300_pcls_frame_bytes(uint32_t particleCount, uint32_t tr
 AstraeaStatus astraea_gb300_pack_pcls_frame(const AstraeaParticles* p, const AstraeaPclsFrameInfo* info,
                                             uint8_t* frame, size_t frameCapacity, size_t* outFrameBytes);
 
+/* ---- per-frame telemetry on the device (engine/simulation.cpp:567-582, 948-1285) */
+
+/* Engine state the telemetry loops read besides the particles. */
+typedef struct AstraeaTelemetryParams {
+    double  targetRadiusPsu;      /* Simulation::Impl::targetRadiusPsu */
+    int32_t livingBodyPresent;    /* compute the living-body spin sums */
+    int32_t reserved;
+} AstraeaTelemetryParams;
+
+/* Results of the O(N) loops of computeTelemetryFromDevice and
+ * sumDeviceRadPowerW, in PSU (FP64).  The engine's remaining scalar code
+ * (unit conversion, energy drift, spin = spinL / spinI / T_UNIT_S, mass
+ * fractions, the collision-outcome rules) runs on the host from these. */
+typedef struct AstraeaTelemetry {
+    double   totalMassPsu;
+    double   sysComPsu[3];
+    double   massBody0Psu, comBody0Psu[3], velBody0Psu[3];   /* bodyId == 0 (COM / mean velocity if mass > 0) */
+    double   massOtherPsu, comOtherPsu[3], velOtherPsu[3];   /* bodyId != 0 */
+    double   livingComPsu[3];                              /* body-0 COM, else the system COM */
+    double   kineticPsu, potentialPsu, internalPsu;         /* sum 1/2 m v^2, 1/2 m phi, m u */
+    double   momentumPsu[3], angularMomentumPsu[3];
+    double   maxTempK, maxPressureGPa, maxDamage;
+    double   radiatedPowerW;                                /* sum of finite positive radPowerW */
+    double   spinLPsu, spinIPsu;                            /* lSpinY, I_yy of the living body */
+    double   remnantPsu[3], remnantVelPsu[3], remnantMassPsu, remnantRadiusPsu;
+    double   boundPlanetMassPsu, diskMassPsu, ejectaMassPsu, impactorBoundMassPsu;
+    uint32_t remnantSeedIndex;                              /* particle of lowest finite phiGrav (first) */
+    int32_t  remnantIterations;                             /* remnant updates made (0..5) */
+} AstraeaTelemetry;
+
+/* Replaces the host loops of computeTelemetryFromDevice and
+ * sumDeviceRadPowerW: seven FP64 reduction passes on the device, one 392-byte
+ * copy to *out (host).  Blocks until the result is on the host.  Allocates
+ * nothing (its scratch is fixed device memory); calls must not overlap on
+ * the GPU.  count == 0 zeroes *out. */
+AstraeaStatus astraea_gb300_reduce_telemetry(const AstraeaParticles* p, const AstraeaTelemetryParams* params,
+                                             AstraeaTelemetry* out);
+
 /* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
 
 /* One Simulation::step() kernel sequence (engine/simulation.cpp:1711-1753):

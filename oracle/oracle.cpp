@@ -1204,6 +1204,136 @@ size_t oracle_pcls_frame(const AstraeaParticles* p, const AstraeaPclsFrameInfo* 
     return 40 + payload;
 }
 
+// ------------------------------------------------------- telemetry ----
+// The O(N) loops of Simulation::Impl::computeTelemetryFromDevice
+// (engine/simulation.cpp:948-1285) and sumDeviceRadPowerW (:567-582), serial
+// and in FP64 like the engine's host code, on host copies of the fields.
+// Parity unpinned by reference outputs: these loops run inside the engine's
+// Simulation object, which needs the whole CUDA engine to construct.
+void oracle_telemetry(const AstraeaParticles* p, const AstraeaTelemetryParams* prm, AstraeaTelemetry* o) {
+    std::memset(o, 0, sizeof(*o));
+    const uint32_t n = p->count;
+    if (n == 0) return;
+    const double G = kGPsuD;
+    const double targetR = prm->targetRadiusPsu;
+    double M = 0, sx = 0, sy = 0, sz = 0;
+    double m0 = 0, x0 = 0, y0 = 0, z0 = 0, vx0 = 0, vy0 = 0, vz0 = 0;
+    double m1 = 0, x1 = 0, y1 = 0, z1 = 0, vx1 = 0, vy1 = 0, vz1 = 0;
+    double ke = 0, pe = 0, ie = 0, px = 0, py = 0, pz = 0, lx = 0, ly = 0, lz = 0, maxT = 0, maxP = 0, rad = 0;
+    uint32_t seed = 0;
+    double minPhi = HUGE_VAL;
+    for (uint32_t i = 0; i < n; ++i) {                              // :982-1047
+        const double m = p->mass[i], x = p->posX[i], y = p->posY[i], z = p->posZ[i];
+        const double vx = p->velX[i], vy = p->velY[i], vz = p->velZ[i];
+        const double phi = p->phiGrav[i], uv = p->u[i], T = p->tempK[i];
+        const double PG = static_cast<double>(p->pressure[i]) * 1000.0;
+        M += m; sx += m * x; sy += m * y; sz += m * z;
+        if (p->bodyId[i] == 0) {
+            m0 += m; x0 += m * x; y0 += m * y; z0 += m * z; vx0 += m * vx; vy0 += m * vy; vz0 += m * vz;
+        } else {
+            m1 += m; x1 += m * x; y1 += m * y; z1 += m * z; vx1 += m * vx; vy1 += m * vy; vz1 += m * vz;
+        }
+        ke += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        pe += 0.5 * m * phi;
+        ie += m * uv;
+        px += m * vx; py += m * vy; pz += m * vz;
+        lx += m * (y * vz - z * vy); ly += m * (z * vx - x * vz); lz += m * (x * vy - y * vx);
+        if (std::isfinite(T)) maxT = std::max(maxT, T);
+        if (std::isfinite(PG)) maxP = std::max(maxP, PG);
+        if (std::isfinite(phi) && phi < minPhi) { minPhi = phi; seed = i; }
+        const double w = p->radPowerW[i];                             // :572-579
+        if (std::isfinite(w) && w > 0.0) rad += w;
+    }
+    o->totalMassPsu = M;
+    if (M > 0) { o->sysComPsu[0] = sx / M; o->sysComPsu[1] = sy / M; o->sysComPsu[2] = sz / M; }
+    if (m0 > 0) { x0 /= m0; y0 /= m0; z0 /= m0; vx0 /= m0; vy0 /= m0; vz0 /= m0; }
+    if (m1 > 0) { x1 /= m1; y1 /= m1; z1 /= m1; vx1 /= m1; vy1 /= m1; vz1 /= m1; }
+    o->massBody0Psu = m0; o->massOtherPsu = m1;
+    const double c0[6] = {x0, y0, z0, vx0, vy0, vz0}, c1[6] = {x1, y1, z1, vx1, vy1, vz1};
+    for (int k = 0; k < 3; ++k) {
+        o->comBody0Psu[k] = c0[k]; o->velBody0Psu[k] = c0[3 + k];
+        o->comOtherPsu[k] = c1[k]; o->velOtherPsu[k] = c1[3 + k];
+        o->livingComPsu[k] = m0 > 0 ? c0[k] : o->sysComPsu[k];
+    }
+    o->kineticPsu = ke; o->potentialPsu = pe; o->internalPsu = ie;
+    o->momentumPsu[0] = px; o->momentumPsu[1] = py; o->momentumPsu[2] = pz;
+    o->angularMomentumPsu[0] = lx; o->angularMomentumPsu[1] = ly; o->angularMomentumPsu[2] = lz;
+    o->maxTempK = maxT; o->maxPressureGPa = maxP; o->radiatedPowerW = rad;
+    o->remnantSeedIndex = seed;
+    if (prm->livingBodyPresent) {                                   // :1092-1111
+        double L = 0, I = 0;
+        const double rLim2 = (1.5 * targetR) * (1.5 * targetR);
+        for (uint32_t i = 0; i < n; ++i) {
+            if (p->bodyId[i] != 0) continue;
+            const double dx = static_cast<double>(p->posX[i]) - x0, dy = static_cast<double>(p->posY[i]) - y0,
+                         dz = static_cast<double>(p->posZ[i]) - z0;
+            if (dx * dx + dy * dy + dz * dz <= rLim2) {
+                const double m = p->mass[i];
+                const double dvx = static_cast<double>(p->velX[i]) - vx0, dvz = static_cast<double>(p->velZ[i]) - vz0;
+                L += m * (dz * dvx - dx * dvz);
+                I += m * (dx * dx + dz * dz);
+            }
+        }
+        o->spinLPsu = L; o->spinIPsu = I;
+    }
+    double rX = p->posX[seed], rY = p->posY[seed], rZ = p->posZ[seed];   // :1121-1128
+    double rVx = p->velX[seed], rVy = p->velY[seed], rVz = p->velZ[seed];
+    double rM = std::max(m0, M * 0.5), rR = std::max(targetR, 0.25);
+    int iters = 0;
+    for (int it = 0; it < 5; ++it) {                                  // :1131-1174
+        double nm = 0, nx = 0, ny = 0, nz = 0, nvx = 0, nvy = 0, nvz = 0, mr2 = 0;
+        const double rSoft = std::max(0.5 * rR, 0.1);
+        for (uint32_t i = 0; i < n; ++i) {
+            const double dx = static_cast<double>(p->posX[i]) - rX, dy = static_cast<double>(p->posY[i]) - rY,
+                         dz = static_cast<double>(p->posZ[i]) - rZ;
+            const double r2 = dx * dx + dy * dy + dz * dz, r = std::sqrt(r2);
+            const double dvx = static_cast<double>(p->velX[i]) - rVx, dvy = static_cast<double>(p->velY[i]) - rVy,
+                         dvz = static_cast<double>(p->velZ[i]) - rVz;
+            const double v2 = dvx * dvx + dvy * dvy + dvz * dvz;
+            const double e = 0.5 * v2 + (-G * rM / std::max(r, rSoft));
+            if (e < 0.0) {
+                const double m = p->mass[i];
+                nm += m; nx += m * p->posX[i]; ny += m * p->posY[i]; nz += m * p->posZ[i];
+                nvx += m * p->velX[i]; nvy += m * p->velY[i]; nvz += m * p->velZ[i];
+                mr2 += m * r2;
+            }
+        }
+        if (!(nm > 0.0)) break;
+        rM = nm; rX = nx / nm; rY = ny / nm; rZ = nz / nm; rVx = nvx / nm; rVy = nvy / nm; rVz = nvz / nm;
+        rR = std::max(0.5 * targetR, std::sqrt(5.0 / 3.0) * std::sqrt(mr2 / nm));
+        ++iters;
+    }
+    double bound = 0, disk = 0, ej = 0, impB = 0, maxD = 0;
+    const double rSoftF = std::max(0.5 * rR, 0.1), mu = G * rM;
+    for (uint32_t i = 0; i < n; ++i) {                                // :1183-1224
+        const double m = p->mass[i];
+        maxD = std::max(maxD, static_cast<double>(p->damage[i]));
+        const double dx = static_cast<double>(p->posX[i]) - rX, dy = static_cast<double>(p->posY[i]) - rY,
+                     dz = static_cast<double>(p->posZ[i]) - rZ;
+        const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+        const double dvx = static_cast<double>(p->velX[i]) - rVx, dvy = static_cast<double>(p->velY[i]) - rVy,
+                     dvz = static_cast<double>(p->velZ[i]) - rVz;
+        const double v2 = dvx * dvx + dvy * dvy + dvz * dvz;
+        const double e = 0.5 * v2 + (-mu / std::max(r, rSoftF));
+        if (e >= 0.0) { ej += m; continue; }
+        if (p->bodyId[i] != 0) impB += m;
+        bool isDisk = false;
+        if (r > rR && mu > 0.0) {
+            const double jx = dy * dvz - dz * dvy, jy = dz * dvx - dx * dvz, jz = dx * dvy - dy * dvx;
+            const double j2 = jx * jx + jy * jy + jz * jz;
+            const double ecc = std::sqrt(std::max(0.0, 1.0 + (2.0 * e * j2) / (mu * mu)));
+            isDisk = j2 / (mu * (1.0 + ecc)) > rR;
+        }
+        (isDisk ? disk : bound) += m;
+    }
+    o->maxDamage = maxD;
+    o->boundPlanetMassPsu = bound; o->diskMassPsu = disk; o->ejectaMassPsu = ej; o->impactorBoundMassPsu = impB;
+    o->remnantPsu[0] = rX; o->remnantPsu[1] = rY; o->remnantPsu[2] = rZ;
+    o->remnantVelPsu[0] = rVx; o->remnantVelPsu[1] = rVy; o->remnantVelPsu[2] = rVz;
+    o->remnantMassPsu = rM; o->remnantRadiusPsu = rR;
+    o->remnantIterations = iters;
+}
+
 int oracle_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
 void oracle_set_group_stride(int k) { g_groupStride = k < 1 ? 1 : k; }
 

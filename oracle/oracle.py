@@ -57,6 +57,7 @@ def load(build=True):
             "oracle_pack_render_records": [P, vp, vp, f, f, f],
             "oracle_extract_tracers": [P, vp, u32, f, f, f, f, f, f],
             "oracle_pcls_frame": [P, ctypes.POINTER(abi.PclsFrameInfo), vp, ctypes.c_size_t],
+            "oracle_telemetry": [P, ctypes.POINTER(abi.TelemetryParams), ctypes.POINTER(abi.Telemetry)],
         }
         for name, args in sig.items():
             getattr(_lib, name).argtypes = args
@@ -180,6 +181,17 @@ def extract_tracers(state, tracer_count, living_com, sys_com):
     lib.oracle_extract_tracers(ctypes.byref(s), _ptr(out), tracer_count, *map(float, living_com),
                                *map(float, sys_com))
     return out
+
+
+def telemetry(state, target_radius_psu, living_body_present=True):
+    """engine/simulation.cpp:567-582, 948-1285 loops on a host state (dict)."""
+    lib = load()
+    hp = HostParticles(state)
+    s = hp.struct()
+    prm = abi.TelemetryParams(float(target_radius_psu), int(bool(living_body_present)), 0)
+    out = abi.Telemetry()
+    lib.oracle_telemetry(ctypes.byref(s), ctypes.byref(prm), ctypes.byref(out))
+    return out.as_dict()
 
 
 def pcls_frame(state, info):
