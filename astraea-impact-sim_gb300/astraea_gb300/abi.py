@@ -156,6 +156,7 @@ SIGNATURES = [
     ("astraea_gb300_reset_device_status", [], ctypes.c_int),
     ("astraea_gb300_measure_fp32_tflops", [ctypes.POINTER(_F)], ctypes.c_int),
     ("astraea_gb300_set_lookback_spin_limit", [_U32], ctypes.c_int),
+    ("astraea_gb300_set_far_field", [ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_debug_lookback_probe", [_U32, ctypes.POINTER(_U32)], ctypes.c_int),
 ]
 EXPORTED_SYMBOLS = [name for name, _, _ in SIGNATURES]

@@ -291,6 +291,11 @@ def reset_device_status():
     abi.check(lib().astraea_gb300_reset_device_status())
 
 
+def set_far_field(mode):
+    """0: monopole (the engine's kernel); 1: monopole + quadrupole."""
+    abi.check(lib().astraea_gb300_set_far_field(int(mode)))
+
+
 def set_lookback_spin_limit(limit):
     abi.check(lib().astraea_gb300_set_lookback_spin_limit(int(limit)))
 

@@ -167,10 +167,14 @@ struct ChildData {
     float mnx, mny, mnz, mxx, mxy, mxz, maxH, maxHs;
     NodeMom mom;
     float cx, cy, cz;
+    float s[6];            // central second moments xx yy zz xy xz yz (moments refit only)
 };
 
+template <bool kMoments>
 __device__ __forceinline__ ChildData loadChild(const Work& w, int c, int n) {
     ChildData d;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) d.s[k] = 0.0f;
     if (c < 0) {
         const int leaf = ~c;
         const float4 pm = __ldg(&w.leafPM[leaf]);
@@ -196,18 +200,28 @@ __device__ __forceinline__ ChildData loadChild(const Work& w, int c, int n) {
         const double2 a = __ldcg(&mp[0]);
         const double2 b = __ldcg(&mp[1]);
         d.mom = NodeMom{a.x, a.y, b.x, b.y};
+        if (kMoments) {
+            const float4 q0 = __ldcg(&w.nodeQuad[2 * static_cast<size_t>(c)]);
+            const float4 q1 = __ldcg(&w.nodeQuad[2 * static_cast<size_t>(c) + 1]);
+            d.s[0] = q0.x; d.s[1] = q0.y; d.s[2] = q0.z; d.s[3] = q0.w; d.s[4] = q1.x; d.s[5] = q1.y;
+        }
     }
     (void)n;
     return d;
 }
 
+// kMoments: also the central second moments S = sum m (x - c)(x - c)^T of
+// every node, combined with the parallel-axis rule
+//   S = S_L + S_R + m_L d_L d_L^T + m_R d_R d_R^T,   d = c_child - c,
+// in FP32 (no cancellation: every term is non-negative or a small offset).
+template <bool kMoments>
 __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, uint32_t n) {
     const uint32_t leafIdx = blockIdx.x * blockDim.x + threadIdx.x;
     if (leafIdx >= n || n < 2u) return;
     // The data of the node this thread just finished stays in registers; at
     // each level only the sibling is loaded (the engine reloads both children).
     int curr = ~static_cast<int>(leafIdx);          // child reference of the leaf
-    ChildData mine = loadChild(w, curr, static_cast<int>(n));
+    ChildData mine = loadChild<kMoments>(w, curr, static_cast<int>(n));
     int pNode = __ldcg(&bvh.parent[(n - 1u) + leafIdx]);
     // A radix tree over 63-bit keys + 32-bit index ties is at most 96 deep;
     // the bound only matters for a tree built from a failed sort.
@@ -224,7 +238,7 @@ __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, 
         if (atomicAdd(&bvh.atomicVisited[pNode], 1u) == 0u) return;   // first arrival stops
         __threadfence();
         const bool fromLeft = (lc == curr);
-        const ChildData other = loadChild(w, fromLeft ? rc : lc, static_cast<int>(n));
+        const ChildData other = loadChild<kMoments>(w, fromLeft ? rc : lc, static_cast<int>(n));
         const ChildData& L = fromLeft ? mine : other;
         const ChildData& R = fromLeft ? other : mine;
         ChildData out;
@@ -242,6 +256,19 @@ __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, 
             out.cx = 0.5f * (L.cx + R.cx);
             out.cy = 0.5f * (L.cy + R.cy);
             out.cz = 0.5f * (L.cz + R.cz);
+        }
+        if (kMoments) {
+            const float mL = static_cast<float>(L.mom.m), mR = static_cast<float>(R.mom.m);
+            const float lx = L.cx - out.cx, ly = L.cy - out.cy, lz = L.cz - out.cz;
+            const float rx = R.cx - out.cx, ry = R.cy - out.cy, rz = R.cz - out.cz;
+            out.s[0] = L.s[0] + R.s[0] + mL * lx * lx + mR * rx * rx;
+            out.s[1] = L.s[1] + R.s[1] + mL * ly * ly + mR * ry * ry;
+            out.s[2] = L.s[2] + R.s[2] + mL * lz * lz + mR * rz * rz;
+            out.s[3] = L.s[3] + R.s[3] + mL * lx * ly + mR * rx * ry;
+            out.s[4] = L.s[4] + R.s[4] + mL * lx * lz + mR * rx * rz;
+            out.s[5] = L.s[5] + R.s[5] + mL * ly * lz + mR * ry * rz;
+            __stcg(&w.nodeQuad[2 * static_cast<size_t>(pNode)], make_float4(out.s[0], out.s[1], out.s[2], out.s[3]));
+            __stcg(&w.nodeQuad[2 * static_cast<size_t>(pNode) + 1], make_float4(out.s[4], out.s[5], 0.0f, 0.0f));
         }
         const float mSum = static_cast<float>(out.mom.m);
         const float dNode = fmaxf(out.mxx - out.mnx, fmaxf(out.mxy - out.mny, out.mxz - out.mnz));
@@ -301,9 +328,12 @@ cudaError_t launchRefreshLeaves(const AstraeaParticles& p, const Work& w, uint32
     return cudaGetLastError();
 }
 
-cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, cudaStream_t st) {
+cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, bool moments, cudaStream_t st) {
     if (n < 2u) return cudaSuccess;
-    refitKernel<<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n);
+    if (moments)
+        refitKernel<true><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n);
+    else
+        refitKernel<false><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n);
     return cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@ namespace {
 thread_local std::string g_lastError;
 std::atomic<cudaStream_t> g_stream{nullptr};
 std::atomic<uint32_t> g_spinLimit{1u << 22};
+std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: monopole + quadrupole
 std::mutex g_mutex;
 
 AstraeaStatus fail(AstraeaStatus s, const std::string& msg) {
@@ -95,6 +96,7 @@ struct Workspace {
     uint32_t* rawMin = nullptr;    // 2 words (inside block)
     bool treeBuilt = false;        // node records hold a tree built here
     uint32_t builtN = 0;           // particle count of that tree
+    bool momentsBuilt = false;     // ... with second moments (far-field mode 1)
     bool stepCacheValid = false;   // neighbour lists + device dt valid for the next fused step
     const void* stepToken = nullptr;
     uint32_t stepCount = 0;
@@ -126,7 +128,7 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     size_t off = 0;
     auto take = [&](size_t bytes) { const size_t o = off; off += alignUp(bytes); return o; };
     const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 80);
-    const size_t oNode = take(C * 64), oMom = take(C * 32), oDrift = take(C * 16);
+    const size_t oNode = take(C * 64), oMom = take(C * 32), oQuad = take(C * 32), oDrift = take(C * 16);
     const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
     const size_t oSort = take(sortWords * 4), oDt = take(64);
     void* block = nullptr;
@@ -145,6 +147,7 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     w.rec2 = reinterpret_cast<float4*>(b + oRec);
     w.node = reinterpret_cast<float4*>(b + oNode);
     w.nodeMom = reinterpret_cast<NodeMom*>(b + oMom);
+    w.nodeQuad = reinterpret_cast<float4*>(b + oQuad);
     w.driftPos = reinterpret_cast<float4*>(b + oDrift);
     w.nbrCount = reinterpret_cast<uint32_t*>(b + oCnt);
     w.nbrList = reinterpret_cast<uint32_t*>(b + oList);
@@ -267,9 +270,11 @@ AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadix
     AG_LAUNCH(launchPermuteLeavesKarras(*p, *alt, *bvh, driftPos, w, n, living, allFields, st));
     swapParticlePointers(*p, *alt);
     alt->count = p->count;
-    AG_LAUNCH(launchRefit(*bvh, w, n, st));
+    const bool moments = g_farField.load() == 1;
+    AG_LAUNCH(launchRefit(*bvh, w, n, moments, st));
     ws->treeBuilt = true;
     ws->builtN = n;
+    ws->momentsBuilt = moments;
     return ASTRAEA_OK;
 }
 
@@ -307,6 +312,12 @@ int astraea_gb300_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
 
 AstraeaStatus astraea_gb300_set_stream(void* s) {
     g_stream.store(static_cast<cudaStream_t>(s));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_set_far_field(int mode) {
+    if (mode != 0 && mode != 1) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0 or 1");
+    g_farField.store(mode);
     return ASTRAEA_OK;
 }
 
@@ -487,7 +498,9 @@ AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const Astrae
     AstraeaStatus s = builtWorkspace(bvh, n, &ws);
     if (s != ASTRAEA_OK) return s;
     AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
-    AG_LAUNCH(launchGravity(*p, ws->w, n, theta, smCount(), stream()));
+    const bool quad = g_farField.load() == 1;
+    if (quad && !ws->momentsBuilt) return fail(ASTRAEA_ERR_INVALID, "far-field mode 1 needs a tree built in that mode");
+    AG_LAUNCH(launchGravity(*p, ws->w, n, theta, quad, smCount(), stream()));
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
 }
@@ -701,7 +714,7 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
     AG_LAUNCH(launchPass1(*p, w, n, st));
     AG_LAUNCH(launchEos(*p, &w, n, st));
-    AG_LAUNCH(launchGravity(*p, w, n, theta, sms, st));
+    AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt, sms, st));
     AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));
     // 5. closing half kick + EOS + next dt minimum
     KickArgs k2{};

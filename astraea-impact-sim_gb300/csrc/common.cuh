@@ -359,6 +359,8 @@ struct Work {
     float4* rec2;
     float4* node;          // 4 x float4 per internal node
     NodeMom* nodeMom;
+    float4* nodeQuad;      // 2 x float4 per internal node: central second moments
+                           // {Sxx, Syy, Szz, Sxy}, {Sxz, Syz, 0, 0} (far-field mode 1)
     float4* driftPos;      // {x, y, z, 0} after the drift
     uint32_t* nbrCount;
     uint32_t* nbrList;     // particle-major, maxNbr per particle

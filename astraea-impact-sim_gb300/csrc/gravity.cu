@@ -36,16 +36,19 @@ constexpr int kGravList = 64;
 // Interaction lists are stored pair-interleaved so that one 16-byte shared
 // load yields packed (entry 2k, entry 2k+1) operands for the f32x2 pipes:
 // mlist[8k..8k+7] = {xA, xB, yA, yB, zA, zB, -GmA, -GmB}; plist likewise,
-// with peps[2k..2k+1] = {eps_jA / 2, eps_jB / 2}.
+// with peps[2k..2k+1] = {eps_jA / 2, eps_jB / 2}.  With the quadrupole
+// (far-field mode 1) an mlist pair block is 20 floats: the 8 above, then
+// G Q_xx, G Q_yy, G Q_zz, G Q_xy, G Q_xz, G Q_yz of both entries, where
+// Q = 3 S - tr(S) I is the node's traceless quadrupole.
 // dirPos[k] (k = 9 (sx + 1) + 3 (sy + 1) + (sz + 1), s in {-1, 0, 1}): the
 // member with the largest projection on the unit direction s / |s| (first
 // member on ties) and, in .w, that projection measured from the group-box
 // centre.  und[] holds the compacted undecided nodes of one walk round; the
 // same storage holds the member positions while dirPos is computed.
-template <bool kInside>
+template <bool kInside, bool kQuad>
 struct __align__(16) GravWarpSmem {
     int stack[kGravStack];
-    float mlist[8 * (kGravList / 2)];
+    float mlist[(kQuad ? 20 : 8) * (kGravList / 2)];
     float plist[8 * (kGravList / 2)];
     float peps[kGravList];
     float4 dirPos[27];
@@ -105,20 +108,44 @@ struct Accum2 {
 // two entries per instruction.  `pairs` pairs starting at list pair `first`.
 // E2 = packed eps_i^2 + 1e-20 (eps >= 8e-7, so 1e-20 is below half an ulp of
 // eps^2 and the order of the two additions does not matter).
+// kQuad adds the quadrupole field of the node, r = x_i - COM, with the same
+// softened 1/r:  a += G [Q r / r^5 - 5/2 (r.Q.r) r / r^7],
+//                phi -= G (r.Q.r) / (2 r^5).
+template <bool kQuad>
 __device__ __forceinline__ void evalMonopoles2(const float* list, int first, int pairs, f2 X, f2 Y, f2 Z, f2 E2,
                                                Accum2& a) {
+    constexpr int kW = kQuad ? 20 : 8;
+    const f2 kHalfNeg = pack2(-0.5f, -0.5f), kFiveHalvesNeg = pack2(-2.5f, -2.5f);
 #pragma unroll 2
     for (int k = first; k < first + pairs; ++k) {
-        const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(list + 8 * k);       // (x), (y)
-        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(list + 8 * k + 4);   // (z), (-Gm)
+        const float* b = list + kW * k;
+        const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(b);       // (x), (y)
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(b + 4);   // (z), (-Gm)
         const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
         const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
         const f2 inv = rsqrt2(add2(r2, E2));
-        const f2 f = mul2(v.y, mul2(inv, mul2(inv, inv)));
+        const f2 inv2 = mul2(inv, inv);
+        const f2 inv3 = mul2(inv2, inv);
+        const f2 f = mul2(v.y, inv3);
         a.ax = fma2(f, dx, a.ax);
         a.ay = fma2(f, dy, a.ay);
         a.az = fma2(f, dz, a.az);
         a.phi = fma2(v.y, inv, a.phi);
+        if constexpr (kQuad) {
+            const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(b + 8);    // Qxx, Qyy
+            const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(b + 12);   // Qzz, Qxy
+            const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(b + 16);   // Qxz, Qyz
+            const f2 qr0 = fma2(q2.x, dz, fma2(q1.y, dy, mul2(q0.x, dx)));
+            const f2 qr1 = fma2(q2.y, dz, fma2(q0.y, dy, mul2(q1.y, dx)));
+            const f2 qr2 = fma2(q1.x, dz, fma2(q2.y, dy, mul2(q2.x, dx)));
+            const f2 rqr = fma2(dz, qr2, fma2(dy, qr1, mul2(dx, qr0)));
+            const f2 i5 = mul2(inv3, inv2);
+            const f2 t = mul2(mul2(rqr, mul2(i5, inv2)), kFiveHalvesNeg);
+            a.ax = fma2(t, dx, fma2(qr0, i5, a.ax));
+            a.ay = fma2(t, dy, fma2(qr1, i5, a.ay));
+            a.az = fma2(t, dz, fma2(qr2, i5, a.az));
+            a.phi = fma2(mul2(rqr, i5), kHalfNeg, a.phi);
+        }
     }
 }
 
@@ -150,16 +177,30 @@ __device__ __forceinline__ void putEntry(float* list, int slot, float x, float y
     b[0] = x; b[2] = y; b[4] = z; b[6] = w;
 }
 
+// Monopole entry of the mlist; with kQuad also its six quadrupole terms.
+template <bool kQuad>
+__device__ __forceinline__ void putMono(float* list, int slot, const float (&e)[10]) {
+    float* b = list + (kQuad ? 20 : 8) * (slot >> 1) + (slot & 1);
+#pragma unroll
+    for (int k = 0; k < (kQuad ? 10 : 4); ++k) b[2 * k] = e[k];
+}
+template <bool kQuad>
+__device__ __forceinline__ void getMono(const float* list, int slot, float (&e)[10]) {
+    const float* b = list + (kQuad ? 20 : 8) * (slot >> 1) + (slot & 1);
+#pragma unroll
+    for (int k = 0; k < (kQuad ? 10 : 4); ++k) e[k] = b[2 * k];
+}
+
 // 1 / |s| for a direction s in {-1, 0, 1}^3 with nz non-zero components.
 __device__ __forceinline__ float invDirNorm(int nz) { return nz == 3 ? 0.57735027f : (nz == 2 ? 0.70710678f : 1.0f); }
 
-template <bool kInside>
+template <bool kInside, bool kQuad>
 __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
                                                                  float theta2, uint32_t numGroups,
                                                                  uint32_t* groupCounter) {
-    __shared__ GravWarpSmem<kInside> smem[kGravWarps];
+    __shared__ GravWarpSmem<kInside, kQuad> smem[kGravWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GravWarpSmem<kInside>& S = smem[warp];
+    GravWarpSmem<kInside, kQuad>& S = smem[warp];
     unsigned long long nInter = 0, nTests = 0, nUndecided = 0, nRounds = 0;
     int spPeak = 0;
     bool overflowed = false;
@@ -323,7 +364,21 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             }
             sp += 2 * __popc(openMask);
             const unsigned accMask = __ballot_sync(0xffffffffu, accept);
-            if (accept) putEntry(S.mlist, mCount + __popc(accMask & laneMaskLt()), r0.x, r0.y, r0.z, -kGPsuF * r0.w);
+            if (accept) {
+                float e[10] = {r0.x, r0.y, r0.z, -kGPsuF * r0.w, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if (kQuad) {
+                    const float4 s0 = __ldg(&w.nodeQuad[2 * static_cast<size_t>(c)]);      // Sxx Syy Szz Sxy
+                    const float4 s1 = __ldg(&w.nodeQuad[2 * static_cast<size_t>(c) + 1]);  // Sxz Syz
+                    const float tr = s0.x + s0.y + s0.z;
+                    e[4] = kGPsuF * (3.0f * s0.x - tr);
+                    e[5] = kGPsuF * (3.0f * s0.y - tr);
+                    e[6] = kGPsuF * (3.0f * s0.z - tr);
+                    e[7] = kGPsuF * 3.0f * s0.w;
+                    e[8] = kGPsuF * 3.0f * s1.x;
+                    e[9] = kGPsuF * 3.0f * s1.y;
+                }
+                putMono<kQuad>(S.mlist, mCount + __popc(accMask & laneMaskLt()), e);
+            }
             mCount += __popc(accMask);
             const unsigned leafMask = __ballot_sync(0xffffffffu, isLeaf);
             unsigned selfBit = 0u;
@@ -342,13 +397,14 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             nTests += __popc(__ballot_sync(0xffffffffu, isNode));
             __syncwarp();
             if (mCount >= 32) {                 // evaluate entries 0..31, move the rest down
-                if (active) evalMonopoles2(S.mlist, 0, 16, X, Y, Z, E2, acc);
+                if (active) evalMonopoles2<kQuad>(S.mlist, 0, 16, X, Y, Z, E2, acc);
                 nInter += static_cast<unsigned long long>(act) * 32u;
                 __syncwarp();
                 mCount -= 32;
                 if (lane < mCount) {
-                    const float* src = S.mlist + 8 * (16 + (lane >> 1)) + (lane & 1);
-                    putEntry(S.mlist, lane, src[0], src[2], src[4], src[6]);
+                    float e[10];
+                    getMono<kQuad>(S.mlist, 32 + lane, e);
+                    putMono<kQuad>(S.mlist, lane, e);
                 }
                 __syncwarp();
             }
@@ -367,12 +423,15 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         }
         // odd tails: pad with a massless entry (adds exactly zero)
         if (lane == 0) {
-            if (mCount & 1) putEntry(S.mlist, mCount, 0.0f, 0.0f, 0.0f, 0.0f);
+            if (mCount & 1) {
+                const float zero[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                putMono<kQuad>(S.mlist, mCount, zero);
+            }
             if (pCount & 1) { putEntry(S.plist, pCount, 0.0f, 0.0f, 0.0f, 0.0f); S.peps[pCount] = 0.0f; }
         }
         __syncwarp();
         if (active) {
-            evalMonopoles2(S.mlist, 0, (mCount + 1) >> 1, X, Y, Z, E2, acc);
+            evalMonopoles2<kQuad>(S.mlist, 0, (mCount + 1) >> 1, X, Y, Z, E2, acc);
             evalParticles2(S.plist, S.peps, 0, (pCount + 1) >> 1, X, Y, Z, HE, acc);
             float a0, a1, b0, b1, c0, c1, d0, d1;
             unpack2(acc.ax, a0, a1);
@@ -407,7 +466,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
 
 }  // namespace
 
-cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, int sms,
+cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
                           cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     const float th = fmaxf(0.0f, theta);
@@ -417,7 +476,8 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
     uint32_t* counter = w.words + kWGroupCounter;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    auto kernel = checkInside ? gravityKernel<true> : gravityKernel<false>;
+    auto kernel = checkInside ? (quadrupole ? gravityKernel<true, true> : gravityKernel<true, false>)
+                              : (quadrupole ? gravityKernel<false, true> : gravityKernel<false, false>);
     int perSm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kGravWarps * 32, 0);
     if (e != cudaSuccess) return e;

@@ -54,7 +54,7 @@ cudaError_t launchPermuteLeavesKarras(const AstraeaParticles& p, const AstraeaPa
                                       uint32_t* livingFlags, bool allFields, cudaStream_t st);
 cudaError_t launchRefreshLeaves(const AstraeaParticles& p, const Work& w, uint32_t n, bool withVelRho,
                                 cudaStream_t st);
-cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, cudaStream_t st);
+cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, bool moments, cudaStream_t st);
 
 // ----------------------------------------------------------- render.cu ---
 // PCLS frame header as ten little-endian words (server/binary_protocol.cpp:76-87).
@@ -72,7 +72,7 @@ cudaError_t launchTelemetry(const AstraeaParticles& p, uint32_t n, double target
                             int sms, AstraeaTelemetry* hostOut, cudaStream_t st);
 
 // ---------------------------------------------------------- gravity.cu ---
-cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, int sms,
+cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
                           cudaStream_t st);
 
 // -------------------------------------------------------------- sph.cu ---

@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--max-dt-sec", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-far-field", action="store_true", help="skip the quadrupole far-field comparison")
     ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
     return ap.parse_args()
 
@@ -204,9 +205,11 @@ def run_gpu(args):
             traffic = None
 
     # ---- force error of the plain path vs an FP64 direct sum (sampled targets)
-    err_rms = force_error_fp64(sim, engine, torch, np, samples=1024)
+    truth = fp64_truth(sim, torch, samples=1024)
+    err_rms = force_error_fp64(sim, engine, torch, np, truth=truth)
 
     frame = frame_stages(sim, engine, torch, np, n)
+    far = None if args.no_far_field else far_field_scan(sim, engine, torch, np, args, max_dt, truth)
 
     # ---- e2e through the C-ABI with pinned host buffers
     e2e = None
@@ -234,6 +237,7 @@ def run_gpu(args):
         "gravity_stack_peak": counters.get("gravity_stack_peak"),
         "device_flags": flags,
         "frame_stages": frame,
+        "far_field": far,
         "e2e": e2e,
     }
     out["config"]["max_dt_psu"] = max_dt
@@ -286,11 +290,26 @@ def step_hbm_roofline(n, ms):
             "bytes_per_particle_step": 1580.0}
 
 
-def force_error_fp64(sim, engine, torch, np, samples=1024):
-    """RMS of |a - a_FP64| / |a_FP64| over sampled targets; the FP64 direct sum
-    (eps_ij softening, G_PSU) runs on the GPU in torch float64."""
+def force_error_fp64(sim, engine, torch, np, samples=1024, truth=None):
+    """RMS of |a - a_FP64| / |a_FP64| over sampled targets of the plain
+    theta = 0.5 gravity; the FP64 direct sum runs on the GPU in float64."""
     engine.gravity_barnes_hut(sim.p, sim.bvh, 0.5)
     torch.cuda.synchronize()
+    return rms_vs_truth(sim, torch, truth or fp64_truth(sim, torch, samples))
+
+
+def rms_vs_truth(sim, torch, truth):
+    tgt, acc = truth
+    n = sim.p.count
+    A = sim.p.arrays
+    bh = torch.stack([A["accX"][:n][tgt], A["accY"][:n][tgt], A["accZ"][:n][tgt]], 1).double()
+    rel = (bh - acc).norm(dim=1) / acc.norm(dim=1)
+    return float(torch.sqrt((rel * rel).mean()))
+
+
+def fp64_truth(sim, torch, samples=1024):
+    """Sampled targets and their FP64 direct-sum accelerations (eps_ij
+    softening, G_PSU), on the GPU in torch float64."""
     n = sim.p.count
     A = sim.p.arrays
     g = torch.Generator(device="cpu").manual_seed(1234)
@@ -310,9 +329,64 @@ def force_error_fp64(sim, engine, torch, np, samples=1024):
         idx = torch.arange(s0, s1, device="cuda")
         w = torch.where(tgt[:, None] == idx[None, :], torch.zeros_like(w), w)
         acc -= G * (w[:, :, None] * d).sum(1)
-    bh = torch.stack([A["accX"][:n][tgt], A["accY"][:n][tgt], A["accZ"][:n][tgt]], 1).double()
-    rel = (bh - acc).norm(dim=1) / acc.norm(dim=1)
-    return float(torch.sqrt((rel * rel).mean()))
+    return tgt, acc
+
+
+def far_field_scan(sim, engine, torch, np, args, max_dt, truth,
+                   configs=((0.5, 0), (0.6, 1), (0.7, 1), (0.8, 1))):
+    """Plain monopole at theta 0.5 (the engine's kernel) against the
+    quadrupole far field (mode 1) at larger opening angles: gravity time,
+    interactions and RMS force error vs the FP64 direct sum on the same
+    tree, then the whole fused step at each setting."""
+    out = []
+    for theta, mode in configs:
+        engine.set_far_field(mode)
+        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)   # the order is already sorted: identity permutation
+        engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+        torch.cuda.synchronize()
+        engine.reset_device_status()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(5):
+            engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+        ev[1].record()
+        torch.cuda.synchronize()
+        _, gc = engine.read_device_status()
+        out.append({"theta": theta, "far_field": "monopole" if mode == 0 else "monopole+quadrupole",
+                    "gravity_ms": ev[0].elapsed_time(ev[1]) / 5,
+                    "interactions_per_particle": gc["gravity_interactions"] / 5 / sim.p.count,
+                    "force_rms_vs_fp64": rms_vs_truth(sim, torch, truth)})
+    # whole steps (the state advances; e2e re-uploads its own inputs afterwards)
+    dt_host = torch.zeros(1, dtype=torch.float32).pin_memory()
+    for rec, (theta, mode) in zip(out, configs):
+        engine.set_far_field(mode)
+        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+        engine.invalidate_step_cache(sim.bvh)
+        for _ in range(2):
+            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, theta, dt_host.data_ptr())
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        k = max(3, args.steps // 2)
+        ev[0].record()
+        for _ in range(k):
+            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, theta, dt_host.data_ptr())
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / k
+        rec["step_ms"] = ms
+        rec["particle_steps_per_s"] = sim.p.count / (ms * 1e-3)
+    engine.set_far_field(0)
+    engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+    engine.invalidate_step_cache(sim.bvh)
+    base = out[0]
+    ok = [r for r in out[1:] if r["force_rms_vs_fp64"] <= base["force_rms_vs_fp64"]]
+    best = max(ok, key=lambda r: r["particle_steps_per_s"]) if ok else None
+    return {"runs": out,
+            "equal_error_choice": best and {"theta": best["theta"], "far_field": best["far_field"],
+                                            "speedup_vs_plain_theta05": best["particle_steps_per_s"] /
+                                            base["particle_steps_per_s"]},
+            "note": "quadrupole far field (analytic, from refitted second moments); "
+                    "a learned correction is not built"}
 
 
 def run_e2e(sim, engine, torch, args, max_dt, world, dist):

@@ -169,6 +169,18 @@ AstraeaStatus astraea_gb300_leapfrog_drift(AstraeaParticles* p, float dtPsu,
 AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevDtPsu,
                                           float maxDtPsu, float* outDtPsu);
 
+/* ---- far-field correction (no counterpart in the engine) ---------------- */
+
+/* Far-field model of every later tree build and gravity evaluation (stage
+ * calls and the fused step): 0 = monopole, the engine's
+ * gravityBarnesHutKernel (engine/sph_gravity.cu:810-961), the default;
+ * 1 = monopole + quadrupole: the build also refits every node's central
+ * second moments and each accepted node adds its quadrupole acceleration
+ * and potential, so a larger opening angle (0.7 instead of 0.5) gives the
+ * same force error with about half the interactions.  Process-wide; gravity
+ * in mode 1 on a tree built in mode 0 returns ASTRAEA_ERR_INVALID. */
+AstraeaStatus astraea_gb300_set_far_field(int mode);
+
 /* ---- render frame packing (engine/sph_gravity.cu:1554-1743, 2163-2201) -- */
 
 /* Replaces launchPackRenderRecords (engine/sph_gravity.cu:2189-2201): one

@@ -619,7 +619,13 @@ void oracle_evaluate_eos(AstraeaParticles* p) {
 
 // --------------------------------------------------------- Barnes-Hut ----
 // engine/sph_gravity.cu:810-961 (float), per group of 32.
-void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, uint64_t* interactionsOut) {
+// S6 == nullptr: the reference kernel.  Otherwise (the library's far-field
+// mode 1) each accepted node also adds its quadrupole field, with S6 the
+// node's central second moments {xx, yy, zz, xy, xz, yz} from
+// oracle_node_moments: Q = 3 S - tr(S) I, r = x_i - COM, the softened 1/r of
+// the monopole, a += G [Q r / r^5 - 5/2 (r.Q.r) r / r^7], phi -= G (r.Q.r) / (2 r^5).
+void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, const float* S6,
+                       uint64_t* interactionsOut) {
     const uint32_t n = p->count;
     if (n == 0) return;
     if (n == 1) { p->accX[0] = p->accY[0] = p->accZ[0] = p->phiGrav[0] = 0.0f; return; }
@@ -687,6 +693,24 @@ void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, 
                             const float f = -kGPsuF * nb.m * iR3;
                             ax[l] += f * dxs[l]; ay[l] += f * dys[l]; az[l] += f * dzs[l];
                             ph[l] -= kGPsuF * nb.m * iR;
+                            if (S6 != nullptr) {
+                                const float* sc = S6 + 6 * static_cast<size_t>(c);
+                                const float tr = sc[0] + sc[1] + sc[2];
+                                const float qxx = kGPsuF * (3.0f * sc[0] - tr), qyy = kGPsuF * (3.0f * sc[1] - tr);
+                                const float qzz = kGPsuF * (3.0f * sc[2] - tr), qxy = kGPsuF * 3.0f * sc[3];
+                                const float qxz = kGPsuF * 3.0f * sc[4], qyz = kGPsuF * 3.0f * sc[5];
+                                const float dx = dxs[l], dy = dys[l], dz = dzs[l];
+                                const float qr0 = qxx * dx + qxy * dy + qxz * dz;
+                                const float qr1 = qxy * dx + qyy * dy + qyz * dz;
+                                const float qr2 = qxz * dx + qyz * dy + qzz * dz;
+                                const float rqr = dx * qr0 + dy * qr1 + dz * qr2;
+                                const float i2 = iR * iR, i5 = iR * i2 * i2, i7 = i5 * i2;
+                                const float t = -2.5f * rqr * i7;
+                                ax[l] += qr0 * i5 + t * dx;
+                                ay[l] += qr1 * i5 + t * dy;
+                                az[l] += qr2 * i5 + t * dz;
+                                ph[l] += -0.5f * rqr * i5;
+                            }
                             ++total;
                         }
                     } else {
@@ -701,6 +725,55 @@ void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, 
         }
     }
     if (interactionsOut) *interactionsOut = total;
+}
+
+void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, uint64_t* interactionsOut) {
+    oracle_gravity_ff(p, b, theta, nullptr, interactionsOut);
+}
+
+// Central second moments of every internal node, S = sum m (x - c)(x - c)^T,
+// combined bottom-up with the parallel-axis rule in FP32 exactly as the
+// library's moments refit does (children first, then
+// S = S_L + S_R + m_L d_L d_L^T + m_R d_R d_R^T with d = c_child - c and the
+// node COMs of b).  Leaves have S = 0.
+void oracle_node_moments(const AstraeaParticles* p, const AstraeaRadixBvh* b, float* S6) {
+    const uint32_t n = p->count;
+    if (n < 2) return;
+    std::vector<int> order;
+    order.reserve(n - 1);
+    std::vector<int> stack{0};
+    while (!stack.empty()) {
+        const int c = stack.back();
+        stack.pop_back();
+        order.push_back(c);
+        for (int ch : {b->leftChild[c], b->rightChild[c]})
+            if (ch >= 0) stack.push_back(ch);
+    }
+    auto child = [&](int ch, float& m, float& cx, float& cy, float& cz, const float*& s) {
+        static const float zero[6] = {0, 0, 0, 0, 0, 0};
+        if (ch < 0) {
+            const int j = ~ch;
+            m = p->mass[j]; cx = p->posX[j]; cy = p->posY[j]; cz = p->posZ[j]; s = zero;
+        } else {
+            m = b->nodeMass[ch]; cx = b->comX[ch]; cy = b->comY[ch]; cz = b->comZ[ch]; s = S6 + 6 * static_cast<size_t>(ch);
+        }
+    };
+    for (auto it = order.rbegin(); it != order.rend(); ++it) {
+        const int c = *it;
+        float mL, lx, ly, lz, mR, rx, ry, rz;
+        const float *sL, *sR;
+        child(b->leftChild[c], mL, lx, ly, lz, sL);
+        child(b->rightChild[c], mR, rx, ry, rz, sR);
+        lx -= b->comX[c]; ly -= b->comY[c]; lz -= b->comZ[c];
+        rx -= b->comX[c]; ry -= b->comY[c]; rz -= b->comZ[c];
+        float* o = S6 + 6 * static_cast<size_t>(c);
+        o[0] = sL[0] + sR[0] + mL * lx * lx + mR * rx * rx;
+        o[1] = sL[1] + sR[1] + mL * ly * ly + mR * ry * ry;
+        o[2] = sL[2] + sR[2] + mL * lz * lz + mR * rz * rz;
+        o[3] = sL[3] + sR[3] + mL * lx * ly + mR * rx * ry;
+        o[4] = sL[4] + sR[4] + mL * lx * lz + mR * rx * rz;
+        o[5] = sL[5] + sR[5] + mL * ly * lz + mR * ry * rz;
+    }
 }
 
 // FP64 direct sum with eps_ij = (eps_i + eps_j)/2, eps = 0.8 h0, for the

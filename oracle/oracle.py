@@ -47,6 +47,8 @@ def load(build=True):
             "oracle_sph_pass1_f64": [P, B],
             "oracle_evaluate_eos": [P],
             "oracle_gravity": [P, B, f, vp],
+            "oracle_gravity_ff": [P, B, f, vp, vp],
+            "oracle_node_moments": [P, B, vp],
             "oracle_direct_gravity_f64": [u32, vp, vp, vp, vp, vp, u32, vp, vp, vp],
             "oracle_sph_pass2": [P, B],
             "oracle_sph_pass2_f64": [P, B],
@@ -299,11 +301,23 @@ class Oracle:
         s = self.p.struct()
         self.lib.oracle_evaluate_eos(ctypes.byref(s))
 
-    def gravity(self, theta=0.5):
+    def gravity(self, theta=0.5, far_field=0):
+        """far_field 0: the reference kernel; 1: + quadrupole of accepted nodes."""
         s = self.p.struct()
         cnt = np.zeros(1, np.uint64)
-        self.lib.oracle_gravity(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(cnt))
+        if far_field == 0:
+            self.lib.oracle_gravity(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(cnt))
+        else:
+            S6 = self.node_moments()
+            self.lib.oracle_gravity_ff(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(S6), _ptr(cnt))
         return int(cnt[0])
+
+    def node_moments(self):
+        """Central second moments of the internal nodes, float32 (n-1, 6)."""
+        s = self.p.struct()
+        S6 = np.zeros((max(self.p.count - 1, 1), 6), np.float32)
+        self.lib.oracle_node_moments(ctypes.byref(s), ctypes.byref(self.bvh.s), _ptr(S6))
+        return S6
 
     def pass2(self, f64=False):
         s = self.p.struct()

@@ -1,0 +1,147 @@
+"""Far-field mode 1: monopole + quadrupole of every accepted node.
+
+No counterpart in the reference (its kernel is monopole only and stays the
+library's default, mode 0).  Checks:
+  * CPU: the oracle's FP32 parallel-axis moments refit against central
+    second moments computed independently from FP64 prefix sums over each
+    node's sorted-particle range (Karras nodes cover contiguous ranges);
+  * CPU: against the FP64 direct sum, the quadrupole lowers the RMS force
+    error at a fixed opening angle, and at theta = 0.7 stays within the
+    plain theta = 0.5 error with far fewer interactions;
+  * GPU: the library's mode-1 gravity against the oracle's (same group-union
+    acceptance, FP32), to 1e-5 norm-relative RMS; a mode-1 evaluation on a
+    tree built in mode 0 is refused.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from astraea_gb300 import scenarios
+from conftest import rel_rms
+
+
+def impact_state(n=65536, seed=42):
+    st, _ = scenarios.differentiated_impact(n_total=n, seed=seed)
+    return st
+
+
+def node_ranges(left, right, n):
+    lo = np.zeros(n - 1, np.int64)
+    hi = np.zeros(n - 1, np.int64)
+    order, stack = [], [0]
+    while stack:
+        c = stack.pop()
+        order.append(c)
+        for ch in (left[c], right[c]):
+            if ch >= 0:
+                stack.append(ch)
+    for c in reversed(order):
+        l, r = left[c], right[c]
+        lo[c] = ~l if l < 0 else lo[l]
+        hi[c] = ~r if r < 0 else hi[r]
+    return lo, hi
+
+
+def test_moments_refit_matches_prefix_sums():
+    o = oracle.Oracle(impact_state(16384))
+    o.sort_and_build()
+    s = o.p.state()
+    n = len(s["posX"])
+    S = o.node_moments().astype(np.float64)
+    lo, hi = node_ranges(o.bvh.a["leftChild"], o.bvh.a["rightChild"], n)
+    m = s["mass"].astype(np.float64)
+    X = np.stack([s["posX"], s["posY"], s["posZ"]], 1).astype(np.float64)
+
+    def pref(a):
+        return np.concatenate([np.zeros((1,) + a.shape[1:]), np.cumsum(a, 0)])
+    Pm, Px = pref(m), pref(m[:, None] * X)
+    pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+    Pxx = pref(np.stack([m * X[:, a] * X[:, b] for a, b in pairs], 1))
+    M = Pm[hi + 1] - Pm[lo]
+    C = (Px[hi + 1] - Px[lo]) / M[:, None]
+    ref = np.stack([(Pxx[hi + 1] - Pxx[lo])[:, k] - M * C[:, a] * C[:, b] for k, (a, b) in enumerate(pairs)], 1)
+    # node scale: trace of S; FP32 parallel-axis sums vs FP64 (prefix-sum
+    # cancellation limits the FP64 side to ~1e-9 of |x|^2 M)
+    scale = ref[:, :3].sum(1)[:, None] + 1e-9 * M[:, None] * np.max(np.abs(X)) ** 2
+    assert np.max(np.abs(S - ref) / scale) < 2e-4
+
+
+@pytest.fixture(scope="module")
+def impact_truth():
+    st = impact_state()
+    o = oracle.Oracle(st)
+    o.sort_and_build()
+    s = o.p.state()
+    n = len(s["posX"])
+    sel = np.random.default_rng(1).choice(n, 1024, replace=False)
+    ref, _ = oracle.direct_gravity_f64(s, sel)
+    return o, sel, ref
+
+
+def rms_error(o, sel, ref):
+    n = o.p.count
+    a = np.stack([o.p.arrays[k][:n] for k in ("accX", "accY", "accZ")], 1)[sel].astype(np.float64)
+    e = np.linalg.norm(a - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    return float(np.sqrt(np.mean(e * e)))
+
+
+def test_quadrupole_lowers_force_error(impact_truth):
+    o, sel, ref = impact_truth
+    n = o.p.count
+    c50 = o.gravity(0.5, 0)
+    e50 = rms_error(o, sel, ref)
+    for th in (0.5, 0.7):
+        o.gravity(th, 0)
+        plain = rms_error(o, sel, ref)
+        cq = o.gravity(th, 1)
+        quad = rms_error(o, sel, ref)
+        print("theta %.1f plain %.2e quad %.2e interactions %.0f" % (th, plain, quad, cq / n))
+        assert quad < 0.75 * plain
+    # theta 0.7 with the quadrupole: close to plain theta 0.5, half the interactions
+    assert quad < 1.3 * e50
+    assert cq < 0.6 * c50
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_gpu_quadrupole_gravity_matches_oracle(theta):
+    from astraea_gb300 import engine
+    st = impact_state(32768, seed=5)
+    n = len(st["posX"])
+    o = oracle.Oracle(st)
+    o.sort_and_build()
+    o.gravity(theta, 1)
+    ref = o.p.state()
+    try:
+        engine.set_far_field(1)
+        p, alt = engine.DeviceParticles(n), engine.DeviceParticles(n)
+        bvh = engine.DeviceBvh(n)
+        p.upload(st)
+        alt.count = n
+        engine.sort_and_build_bvh(p, alt, bvh)
+        engine.gravity_barnes_hut(p, bvh, theta)
+        got = p.download()
+    finally:
+        engine.set_far_field(0)
+    for f in ("accX", "accY", "accZ", "phiGrav"):
+        assert rel_rms(got[f], ref[f]) < 1e-5, f
+
+
+@pytest.mark.gpu
+def test_gpu_quadrupole_needs_moments_tree():
+    from astraea_gb300 import abi, engine
+    st = impact_state(8192, seed=6)
+    n = len(st["posX"])
+    p, alt = engine.DeviceParticles(n), engine.DeviceParticles(n)
+    bvh = engine.DeviceBvh(n)
+    p.upload(st)
+    alt.count = n
+    engine.sort_and_build_bvh(p, alt, bvh)            # mode 0 tree
+    try:
+        engine.set_far_field(1)
+        with pytest.raises(abi.AstraeaError):
+            engine.gravity_barnes_hut(p, bvh, 0.7)
+    finally:
+        engine.set_far_field(0)
+    with pytest.raises(abi.AstraeaError):
+        engine.set_far_field(2)
