@@ -66,17 +66,20 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-far-field", action="store_true", help="skip the quadrupole far-field comparison")
+    ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
+                    help="far-field model of the timed steps: 0 monopole (the engine's), 1 + quadrupole")
     ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
     return ap.parse_args()
 
 
-def workload_config(n, theta):
+def workload_config(n, theta, far_field=0):
     return {
         "workload": "differentiated Earth-Theia-like impact, N=%d (target %d + impactor %d), Iron core 30%% "
                     "+ Granite mantle, hydrostatic radial density, mass ratio 0.1, 1.1 v_esc at 45 deg, strength "
                     "+ damage on" % (n, n - int(round(0.2 * n)), int(round(0.2 * n))),
         "n_particles": n,
-        "traversal": "plain Barnes-Hut theta=%.2f (learned far-field correction not built)" % theta,
+        "traversal": ("plain Barnes-Hut theta=%.2f (monopole, the engine's kernel)" % theta if far_field == 0 else
+                      "Barnes-Hut theta=%.2f, monopole + quadrupole far field" % theta),
         "max_dt_psu": None,
         "l2": "inputs larger than L2: particle SoA %.0f MB + tree/neighbour scratch ~%.0f MB (L2 129 MB)"
               % (2 * n * 212 / 1e6, n * 1.15e3 / 1e6),
@@ -126,6 +129,19 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- GPU arm
+def replica_rate(local_units, local_ms, dist=None, device="cpu"):
+    """Whole-job throughput of independent replicas: the particle-steps of all
+    ranks over the slowest rank's time (max over ranks).  Returns
+    (units per second, slowest ms)."""
+    import torch
+    units = torch.tensor([float(local_units)], dtype=torch.float64, device=device)
+    ms = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(units, op=dist.ReduceOp.SUM)
+        dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+    return float(units.item()) / (float(ms.item()) / 1.0e3), float(ms.item())
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -142,6 +158,7 @@ def run_gpu(args):
 
     n = args.n
     max_dt = max(1.0e-5, args.max_dt_sec) / 1.0e3
+    engine.set_far_field(args.far_field)
     st, info = scenarios.differentiated_impact(n_total=n, seed=42 + rank)
     sim = engine.Simulation(n)
     sim.load_state(st)
@@ -172,11 +189,7 @@ def run_gpu(args):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     flags, counters = engine.read_device_status()
-    t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * n * args.steps / (ms_max / 1.0e3)
+    value, ms_max = replica_rate(n * args.steps, ms, dist, "cuda")
     sim.prev_dt = float(dt_host[0])
 
     # ---- dominant kernel: gravity, timed standalone on the current tree
@@ -206,7 +219,7 @@ def run_gpu(args):
 
     # ---- force error of the plain path vs an FP64 direct sum (sampled targets)
     truth = fp64_truth(sim, torch, samples=1024)
-    err_rms = force_error_fp64(sim, engine, torch, np, truth=truth)
+    err_rms = force_error_fp64(sim, engine, torch, np, truth=truth, theta=args.theta)
 
     frame = frame_stages(sim, engine, torch, np, n)
     far = None if args.no_far_field else far_field_scan(sim, engine, torch, np, args, max_dt, truth)
@@ -221,7 +234,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 in drift, refit moments)",
         "data": "synthetic (seeded hydrostatic bodies)",
-        "config": workload_config(n, args.theta),
+        "config": workload_config(n, args.theta, args.far_field),
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "clocks": clk,
         "roofline": {"kernel": "gravity (Barnes-Hut group walk + pair evaluation)", "bound": "fp32",
@@ -290,10 +303,10 @@ def step_hbm_roofline(n, ms):
             "bytes_per_particle_step": 1580.0}
 
 
-def force_error_fp64(sim, engine, torch, np, samples=1024, truth=None):
-    """RMS of |a - a_FP64| / |a_FP64| over sampled targets of the plain
-    theta = 0.5 gravity; the FP64 direct sum runs on the GPU in float64."""
-    engine.gravity_barnes_hut(sim.p, sim.bvh, 0.5)
+def force_error_fp64(sim, engine, torch, np, samples=1024, truth=None, theta=0.5):
+    """RMS of |a - a_FP64| / |a_FP64| over sampled targets of the gravity of
+    the timed configuration; the FP64 direct sum runs on the GPU in float64."""
+    engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
     torch.cuda.synchronize()
     return rms_vs_truth(sim, torch, truth or fp64_truth(sim, torch, samples))
 
@@ -413,10 +426,8 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return {"value": world * n * args.steps / (float(t.item()) / 1e3), "unit": UNIT,
+    rate, _ = replica_rate(n * args.steps, ms, dist, "cuda")
+    return {"value": rate, "unit": UNIT,
             "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
             "note": "every step: H2D of the step's input fields from pinned memory, fused step (step cache "
                     "invalidated: neighbour lists and dt recomputed from the uploaded state), D2H of the "
