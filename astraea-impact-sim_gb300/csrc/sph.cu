@@ -25,10 +25,18 @@ constexpr int kNbWarps = 4;
 constexpr int kNbStack = 1024;
 constexpr int kNbList = 64;
 
+// dirMem[k] (k = 9 (sx + 1) + 3 (sy + 1) + (sz + 1), s in {-1, 0, 1}): the
+// member {x, y, z, Hs} with the largest projection on direction s (first
+// member on ties); undMin/undMax: the undecided nodes of one walk round
+// {box min, node maxHs} / {box max}; the member positions are staged in
+// undMin while dirMem is computed.
 struct NbWarpSmem {
     int stack[kNbStack];
     float4 cand[kNbList];    // {x, y, z, Hs}
     int candIdx[kNbList];
+    float4 dirMem[27];
+    float4 undMin[32];
+    float4 undMax[32];
 };
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
@@ -72,19 +80,23 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
         const float gminy = warpMinF(active ? me.y : 3.0e38f), gmaxy = warpMaxF(active ? me.y : -3.0e38f);
         const float gminz = warpMinF(active ? me.z : 3.0e38f), gmaxz = warpMaxF(active ? me.z : -3.0e38f);
         const float gHs = warpMaxF(Hs);
-        // representative member: the one nearest the group-box centre
+        // per-direction extreme members (dirMem); member data staged in undMin
         const float cxg = 0.5f * (gminx + gmaxx), cyg = 0.5f * (gminy + gmaxy), czg = 0.5f * (gminz + gmaxz);
-        float dc = active ? (me.x - cxg) * (me.x - cxg) + (me.y - cyg) * (me.y - cyg) + (me.z - czg) * (me.z - czg)
-                          : 3.0e38f;
-        int best = lane;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float od = __shfl_xor_sync(0xffffffffu, dc, o);
-            const int ob = __shfl_xor_sync(0xffffffffu, best, o);
-            if (od < dc || (od == dc && ob < best)) { dc = od; best = ob; }
+        S.undMin[lane] = make_float4(me.x, me.y, me.z, Hs);
+        __syncwarp();
+        if (lane < 27) {
+            const float sx = static_cast<float>(lane / 9 - 1), sy = static_cast<float>((lane / 3) % 3 - 1),
+                        sz = static_cast<float>(lane % 3 - 1);
+            float best = -3.0e38f;
+            int bi = 0;
+            for (int m = 0; m < act; ++m) {
+                const float4 q = S.undMin[m];
+                const float pr = sx * (q.x - cxg) + sy * (q.y - cyg) + sz * (q.z - czg);
+                if (pr > best) { best = pr; bi = m; }
+            }
+            S.dirMem[lane] = S.undMin[bi];
         }
-        const float repx = __shfl_sync(0xffffffffu, me.x, best), repy = __shfl_sync(0xffffffffu, me.y, best);
-        const float repz = __shfl_sync(0xffffffffu, me.z, best), repHs = __shfl_sync(0xffffffffu, Hs, best);
+        __syncwarp();
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, cCount = 0;
         uint32_t cnt = 0, rounds = 0;
@@ -140,27 +152,40 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
                 const float dz = fmaxf(0.0f, fmaxf(bmin.z - gmaxz, gminz - bmax.z));
                 const float Rg = fmaxf(gHs, nodeHs);
                 if (dx * dx + dy * dy + dz * dz <= Rg * Rg * 1.00001f) {
-                    // (2) one member in range opens it; (3) otherwise the group decides
-                    const float R = fmaxf(repHs, nodeHs);
-                    if (pointBoxDist2(repx, repy, repz, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <=
+                    // (2) the member furthest towards the node opens it when in range;
+                    // (3) otherwise the whole group decides
+                    const float ux = 0.5f * (bmin.x + bmax.x) - cxg, uy = 0.5f * (bmin.y + bmax.y) - cyg,
+                                uz = 0.5f * (bmin.z + bmax.z) - czg;
+                    const float t = 0.41421356f * fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
+                    const int sx = (ux >= t) - (ux <= -t), sy = (uy >= t) - (uy <= -t), sz = (uz >= t) - (uz <= -t);
+                    const float4 dm = S.dirMem[13 + 9 * sx + 3 * sy + sz];
+                    const float R = fmaxf(dm.w, nodeHs);
+                    if (pointBoxDist2(dm.x, dm.y, dm.z, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <=
                         R * R * 1.00001f)
                         open = true;
                     else
                         undecided = true;
                 }
             }
-            unsigned und = __ballot_sync(0xffffffffu, undecided);
-            while (und) {
-                const int k = __ffs(und) - 1;
-                und &= und - 1;
-                const float mnx = __shfl_sync(0xffffffffu, bmin.x, k), mny = __shfl_sync(0xffffffffu, bmin.y, k);
-                const float mnz = __shfl_sync(0xffffffffu, bmin.z, k), mxx = __shfl_sync(0xffffffffu, bmax.x, k);
-                const float mxy = __shfl_sync(0xffffffffu, bmax.y, k), mxz = __shfl_sync(0xffffffffu, bmax.z, k);
-                const float hk = __shfl_sync(0xffffffffu, nodeHs, k);
-                const float R = fmaxf(Hs, hk);
-                const bool near = active && pointBoxDist2(me.x, me.y, me.z, mnx, mny, mnz, mxx, mxy, mxz) <= R * R * 1.00001f;
-                const bool any = __any_sync(0xffffffffu, near);
-                if (lane == k) open = any;
+            const unsigned und = __ballot_sync(0xffffffffu, undecided);
+            if (und) {
+                const int nu = __popc(und);
+                const int slot = __popc(und & laneMaskLt());
+                if (undecided) {
+                    S.undMin[slot] = make_float4(bmin.x, bmin.y, bmin.z, nodeHs);
+                    S.undMax[slot] = make_float4(bmax.x, bmax.y, bmax.z, 0.0f);
+                }
+                __syncwarp();
+                unsigned bits = 0u;
+                for (int k = 0; k < nu; ++k) {
+                    const float4 mn = S.undMin[k], mx = S.undMax[k];
+                    const float R = fmaxf(Hs, mn.w);
+                    const bool near = active && pointBoxDist2(me.x, me.y, me.z, mn.x, mn.y, mn.z, mx.x, mx.y, mx.z) <=
+                                                    R * R * 1.00001f;
+                    bits |= (__any_sync(0xffffffffu, near) ? 1u : 0u) << k;
+                }
+                if (undecided) open = (bits >> slot) & 1u;
+                __syncwarp();
             }
             unsigned openMask = __ballot_sync(0xffffffffu, open);
             if (sp + 2 * __popc(openMask) > kNbStack) {
