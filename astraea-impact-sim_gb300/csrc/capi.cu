@@ -127,7 +127,7 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     const size_t sortWords = sortScratchWords(static_cast<uint32_t>(C), &maxTiles);
     size_t off = 0;
     auto take = [&](size_t bytes) { const size_t o = off; off += alignUp(bytes); return o; };
-    const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 80);
+    const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 16 * kRec2Width);
     const size_t oNode = take(C * 64), oMom = take(C * 32), oQuad = take(C * 32), oDrift = take(C * 16);
     const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
     const size_t oSort = take(sortWords * 4), oDt = take(64);

@@ -7,7 +7,7 @@
 //   leafPM  [N]   float4 {x, y, z, m}            sorted positions + mass
 //   leafAux [N]   float4 {Hs, eps, 2h, 0}        Hs = search radius (below)
 //   velRho  [N]   float4 {vx, vy, vz, rho}       neighbour velocity + density
-//   rec2    [5N]  float4 x5 per particle          pass-2 neighbour record
+//   rec2    [6N]  float4 x6 per particle          pass-2 neighbour record
 //   node    [4(N-1)] float4 x4 per internal node:
 //        r0 {comX, comY, comZ, mass}
 //        r1 {dNode^2 (dNode = largest box side), left (int bits), right (int bits), maxHs}
@@ -102,6 +102,8 @@ __device__ __forceinline__ float wendlandC2(float r, float H) {
     return norm * omq2 * omq2 * (1.0f + 4.0f * q);
 }
 // g with grad_i W(r_i - r_j, H) = g (r_i - r_j) (sph_gravity.cu:211-220).
+// wendlandC2GradN takes norm = 210 / (pi H^5), computed once per particle
+// with the same expression.
 __device__ __forceinline__ float wendlandC2Grad(float r, float H) {
     if (r >= H || H <= 0.0f) return 0.0f;
     const float q = r / H;
@@ -109,6 +111,11 @@ __device__ __forceinline__ float wendlandC2Grad(float r, float H) {
     const float H2 = H * H;
     const float H5 = H2 * H2 * H;
     return -(210.0f / (kPiF * H5)) * omq * omq * omq;
+}
+__device__ __forceinline__ float wendlandC2GradN(float r, float H, float norm) {
+    if (r >= H || H <= 0.0f) return 0.0f;
+    const float omq = 1.0f - r / H;
+    return -norm * omq * omq * omq;
 }
 // Balsara switch (sph_gravity.cu:222-228).
 __device__ __forceinline__ float balsaraSwitch(float divV, float cx, float cy, float cz, float cs, float h) {
@@ -343,6 +350,8 @@ __device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, fl
     return o;
 }
 
+constexpr int kRec2Width = 6;   // float4 per pass-2 record
+
 // FP64 mass moments of one internal node (32 bytes, 16-byte aligned).
 struct __align__(16) NodeMom {
     double sx, sy, sz, m;
@@ -356,7 +365,7 @@ struct Work {
     float4* leafPM;
     float4* leafAux;
     float4* velRho;
-    float4* rec2;
+    float4* rec2;          // kRec2Width float4 per particle: the pass-2 record
     float4* node;          // 4 x float4 per internal node
     NodeMom* nodeMom;
     float4* nodeQuad;      // 2 x float4 per internal node: central second moments

@@ -59,6 +59,34 @@ __device__ __forceinline__ float resolveDt(uint32_t rawBits, float prevDt, float
     return fminf(upper, fmaxf(floorDt, raw));
 }
 
+// Pass-2 record of particle i (6 float4, read by pass 2 for i and for every
+// neighbour j):
+//   q0 {x, y, z, h}  q1 {vx, vy, vz, m}  q2 {rho, P_eff / rho^2, cs, f_Balsara}
+//   q3 {sXX, sYY, sZZ, sXY} / rho^2   q4 {sXZ / rho^2, sYZ / rho^2, material, R_tensile}
+//   q5 {m / rho, 210 / (pi H^5), 1 / rho^2, 0}    (H = 2h)
+// with h, rho and cs clamped as the engine clamps them on load.  Every
+// derived value is the IEEE operation the engine's pair loop performs on
+// the same inputs (sph_gravity.cu:1076-1142), done once per particle.
+__device__ __forceinline__ void writePass2Record(float4* R, float x, float y, float z, float hRaw, float vx, float vy,
+                                                 float vz, float m, float rhoRaw, float pEff, float csRaw, float fBalIn,
+                                                 float sxx, float syy, float szz, float sxy, float sxz, float syz,
+                                                 int mat) {
+    const float h = fmaxf(hRaw, 1.0e-6f);
+    const float rho = fmaxf(rhoRaw, 1.0e-9f);
+    const float invRho2 = 1.0f / (rho * rho);
+    const float H = 2.0f * h;
+    const float H2 = H * H;
+    const float H5 = H2 * H2 * H;
+    const float gradNorm = 210.0f / (kPiF * H5);
+    const float rTens = (pEff < 0.0f) ? (0.3f * (-pEff) * invRho2) : 0.0f;
+    R[0] = make_float4(x, y, z, h);
+    R[1] = make_float4(vx, vy, vz, m);
+    R[2] = make_float4(rho, pEff * invRho2, csRaw, fBalIn);
+    R[3] = make_float4(sxx * invRho2, syy * invRho2, szz * invRho2, sxy * invRho2);
+    R[4] = make_float4(sxz * invRho2, syz * invRho2, __int_as_float(mat), rTens);
+    R[5] = make_float4(m / rho, gradNorm, invRho2, 0.0f);
+}
+
 __global__ void __launch_bounds__(256) eosKernel(AstraeaParticles p, Work w, bool withRecords, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -74,12 +102,11 @@ __global__ void __launch_bounds__(256) eosKernel(AstraeaParticles p, Work w, boo
         const float cs = fmaxf(e.cs, 0.05f);
         const float fBal = balsaraSwitch(__ldg(&p.divV[i]), __ldg(&p.curlVX[i]), __ldg(&p.curlVY[i]),
                                          __ldg(&p.curlVZ[i]), cs, h);
-        float4* R = w.rec2 + 5 * static_cast<size_t>(i);
-        R[0] = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), h);
-        R[1] = make_float4(__ldg(&p.velX[i]), __ldg(&p.velY[i]), __ldg(&p.velZ[i]), __ldg(&p.mass[i]));
-        R[2] = make_float4(fmaxf(rho, 1.0e-9f), effectivePressure(e.P, e.phase), cs, fBal);
-        R[3] = make_float4(__ldg(&p.sXX[i]), __ldg(&p.sYY[i]), __ldg(&p.sZZ[i]), __ldg(&p.sXY[i]));
-        R[4] = make_float4(__ldg(&p.sXZ[i]), __ldg(&p.sYZ[i]), __int_as_float(static_cast<int>(mat)), 0.0f);
+        writePass2Record(w.rec2 + kRec2Width * static_cast<size_t>(i), __ldg(&p.posX[i]), __ldg(&p.posY[i]),
+                         __ldg(&p.posZ[i]), h, __ldg(&p.velX[i]), __ldg(&p.velY[i]), __ldg(&p.velZ[i]),
+                         __ldg(&p.mass[i]), rho, effectivePressure(e.P, e.phase), cs, fBal, __ldg(&p.sXX[i]),
+                         __ldg(&p.sYY[i]), __ldg(&p.sZZ[i]), __ldg(&p.sXY[i]), __ldg(&p.sXZ[i]), __ldg(&p.sYZ[i]),
+                         static_cast<int>(mat));
     }
 }
 
@@ -178,14 +205,12 @@ __global__ void __launch_bounds__(256) packPass2Kernel(AstraeaParticles p, Work 
     const float cs = fmaxf(__ldg(&p.soundSpeed[i]), 0.05f);
     const float fBal = balsaraSwitch(__ldg(&p.divV[i]), __ldg(&p.curlVX[i]), __ldg(&p.curlVY[i]),
                                      __ldg(&p.curlVZ[i]), cs, h);
-    float4* R = w.rec2 + 5 * static_cast<size_t>(i);
-    R[0] = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), h);
-    R[1] = make_float4(__ldg(&p.velX[i]), __ldg(&p.velY[i]), __ldg(&p.velZ[i]), __ldg(&p.mass[i]));
-    R[2] = make_float4(fmaxf(__ldg(&p.rho[i]), 1.0e-9f), effectivePressure(__ldg(&p.pressure[i]), __ldg(&p.phaseId[i])),
-                       cs, fBal);
-    R[3] = make_float4(__ldg(&p.sXX[i]), __ldg(&p.sYY[i]), __ldg(&p.sZZ[i]), __ldg(&p.sXY[i]));
-    R[4] = make_float4(__ldg(&p.sXZ[i]), __ldg(&p.sYZ[i]), __int_as_float(static_cast<int>(__ldg(&p.materialId[i]))),
-                       0.0f);
+    writePass2Record(w.rec2 + kRec2Width * static_cast<size_t>(i), __ldg(&p.posX[i]), __ldg(&p.posY[i]),
+                     __ldg(&p.posZ[i]), h, __ldg(&p.velX[i]), __ldg(&p.velY[i]), __ldg(&p.velZ[i]),
+                     __ldg(&p.mass[i]), __ldg(&p.rho[i]),
+                     effectivePressure(__ldg(&p.pressure[i]), __ldg(&p.phaseId[i])), cs, fBal, __ldg(&p.sXX[i]),
+                     __ldg(&p.sYY[i]), __ldg(&p.sZZ[i]), __ldg(&p.sXY[i]), __ldg(&p.sXZ[i]), __ldg(&p.sYZ[i]),
+                     static_cast<int>(__ldg(&p.materialId[i])));
 }
 
 __global__ void __launch_bounds__(256) driftPlainKernel(AstraeaParticles p, uint32_t n, float dt) {

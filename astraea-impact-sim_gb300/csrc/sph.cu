@@ -300,19 +300,33 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
     }
 }
 
+// List words are read once per pass and the lists (308 B per particle) do
+// not fit in L1: read them without allocating in L1, which keeps L1 for the
+// neighbour records.
+__device__ __forceinline__ uint4 ldListNoL1(const uint32_t* p) {
+    uint4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
 // Same candidate set as forEachCandidate, with each candidate's first record
 // loaded by `load(j)` for four list entries before any `body(j, rec)` runs,
-// so four independent gathers are in flight per thread.
+// so four independent gathers are in flight per thread, and the next four
+// list entries loaded before those four bodies run.
 template <class L, class B>
 __device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32_t i, L&& load, B&& body) {
     const uint32_t c = __ldg(&w.nbrCount[i]);
     if (c <= w.maxNbr) {
         const uint32_t* list = w.nbrList + static_cast<size_t>(i) * w.maxNbr;
         uint32_t k = 0;
+        uint4 q = c >= 4 ? ldListNoL1(list) : make_uint4(0u, 0u, 0u, 0u);
         for (; k + 4 <= c; k += 4) {
-            const uint4 q = __ldg(reinterpret_cast<const uint4*>(list + k));
+            const uint4 next = (k + 8 <= c) ? ldListNoL1(list + k + 4) : q;
             const float4 r0 = load(q.x), r1 = load(q.y), r2 = load(q.z), r3 = load(q.w);
             body(q.x, r0); body(q.y, r1); body(q.z, r2); body(q.w, r3);
+            q = next;
         }
         for (; k < c; ++k) {
             const uint32_t j = __ldg(&list[k]);
@@ -377,57 +391,57 @@ __global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, u
 }
 
 // ---------------------------------------------------------------- pass 2 ---
-// Pass-2 record (written by the EOS kernel), 5 float4 per particle:
-//   q0 {x, y, z, h}   q1 {vx, vy, vz, m}   q2 {rho, P_eff, cs, f_Balsara}
-//   q3 {sXX, sYY, sZZ, sXY}   q4 {sXZ, sYZ, material, 0}
-// with h, rho, cs already clamped as the engine clamps them on load.
+// Reads the pass-2 records written by the EOS kernel (layout and derived
+// values: integrate.cu, writePass2Record): one 16-byte load per group of
+// fields, and no per-pair division for quantities of the neighbour alone.
 __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
                                                    const uint32_t* livingFlags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* R = w.rec2;
-    const float4 a0 = __ldg(&R[5 * i + 0]);
-    const float4 a1 = __ldg(&R[5 * i + 1]);
-    const float4 a2 = __ldg(&R[5 * i + 2]);
-    const float4 a3 = __ldg(&R[5 * i + 3]);
-    const float4 a4 = __ldg(&R[5 * i + 4]);
+    const float4 a0 = __ldg(&R[kRec2Width * i + 0]);
+    const float4 a1 = __ldg(&R[kRec2Width * i + 1]);
+    const float4 a2 = __ldg(&R[kRec2Width * i + 2]);
+    const float4 a4 = __ldg(&R[kRec2Width * i + 4]);
+    const float4 a5 = __ldg(&R[kRec2Width * i + 5]);
     const float xi = a0.x, yi = a0.y, zi = a0.z, hi = a0.w, Hi = 2.0f * hi;
     const float vxi = a1.x, vyi = a1.y, vzi = a1.z, mi = a1.w;
-    const float rhoI = a2.x, pI = a2.y, csI = a2.z, fBalI = a2.w;
-    const float sXXi = a3.x, sYYi = a3.y, sZZi = a3.z, sXYi = a3.w, sXZi = a4.x, sYZi = a4.y;
+    const float rhoI = a2.x, pOverRho2I = a2.y, csI = a2.z, fBalI = a2.w;
+    const float sXXi = __ldg(&p.sXX[i]), sYYi = __ldg(&p.sYY[i]), sZZi = __ldg(&p.sZZ[i]);
+    const float sXYi = __ldg(&p.sXY[i]), sXZi = __ldg(&p.sXZ[i]), sYZi = __ldg(&p.sYZ[i]);
     const int matI = __float_as_int(a4.z);
-    const float invRhoI2 = 1.0f / (rhoI * rhoI);
-    const float Ri = (pI < 0.0f) ? (0.3f * (-pI) * invRhoI2) : 0.0f;
-    const float pOverRho2I = pI * invRhoI2;
+    const float Ri = a4.w;
+    const float gradNormI = a5.y, invRhoI2 = a5.z;
+    const float pI = effectivePressure(__ldg(&p.pressure[i]), __ldg(&p.phaseId[i]));   // the record's P_eff
+    const float sXXr = sXXi * invRhoI2, sYYr = sYYi * invRhoI2, sZZr = sZZi * invRhoI2;
+    const float sXYr = sXYi * invRhoI2, sXZr = sXZi * invRhoI2, sYZr = sYZi * invRhoI2;
     const float tempI = __ldg(&p.tempK[i]);
     const float damI = __ldg(&p.damage[i]);
     const float fSurf = __ldg(&p.surfFactor[i]);
 
     float axS = 0.f, ayS = 0.f, azS = 0.f, drC = 0.f, drD = 0.f, duP = 0.f, duAv = 0.f, duT = 0.f, duS = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
-    unsigned pairs = 0;
     if (n >= 2u) {
-        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&R[5 * j + 0]); }, [&](uint32_t j, float4 b0) {
+        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&R[kRec2Width * j + 0]); }, [&](uint32_t j, float4 b0) {
             const float dx = __fsub_rn(xi, b0.x), dy = __fsub_rn(yi, b0.y), dz = __fsub_rn(zi, b0.z);
             const float r2 = len2Exact(dx, dy, dz);
             const float hj = b0.w, Hj = 2.0f * hj;
             const float Hm = fmaxf(Hi, Hj);
             if (!(r2 < __fmul_rn(Hm, Hm))) return;          // sph_gravity.cu:1071
-            ++pairs;
-            const float4 b1 = __ldg(&R[5 * j + 1]);
-            const float4 b2 = __ldg(&R[5 * j + 2]);
-            const float4 b3 = __ldg(&R[5 * j + 3]);
-            const float4 b4 = __ldg(&R[5 * j + 4]);
-            const float mj = b1.w, rhoJ = b2.x, pJ = b2.y, csJ = b2.z, fBalJ = b2.w;
+            const float4 b1 = __ldg(&R[kRec2Width * j + 1]);
+            const float4 b2 = __ldg(&R[kRec2Width * j + 2]);
+            const float4 b3 = __ldg(&R[kRec2Width * j + 3]);
+            const float4 b4 = __ldg(&R[kRec2Width * j + 4]);
+            const float4 b5 = __ldg(&R[kRec2Width * j + 5]);
+            const float mj = b1.w, rhoJ = b2.x, pOverRho2J = b2.y, csJ = b2.z, fBalJ = b2.w;
+            const float volJ = b5.x, invRhoJ2 = b5.z;
             const float dvx = vxi - b1.x, dvy = vyi - b1.y, dvz = vzi - b1.z;
             const float vDotR = dvx * dx + dvy * dy + dvz * dz;
             const float r = sqrtf(r2);
-            const float gI = wendlandC2Grad(r, Hi), gJ = wendlandC2Grad(r, Hj);
+            const float gI = wendlandC2GradN(r, Hi, gradNormI), gJ = wendlandC2GradN(r, Hj, b5.y);
             const float gb = 0.5f * (gI + gJ);
             const float gx = gb * dx, gy = gb * dy, gz = gb * dz;
-            const float invRhoJ2 = 1.0f / (rhoJ * rhoJ);
             const float vDotG = dvx * gx + dvy * gy + dvz * gz;
-            const float volJ = mj / rhoJ;
             drC += volJ * vDotG;                               // continuity (:1114)
             if (__float_as_int(b4.z) == matI) {                // delta-SPH diffusion (:1115-1119)
                 const float rDotG = -(dx * gx + dy * gy + dz * gz);
@@ -441,7 +455,7 @@ __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w
                 piIJ = ((-1.0f * cB * muIJ + 2.0f * muIJ * muIJ) / rB) * (0.5f * (fBalI + fBalJ));
             }
             float tens = 0.0f;                                 // tensile correction (:1130-1142)
-            const float Rj = (pJ < 0.0f) ? (0.3f * (-pJ) * invRhoJ2) : 0.0f;
+            const float Rj = b4.w;
             if (Ri + Rj > 0.0f) {
                 const float Hb = 0.5f * (Hi + Hj);
                 if (r < Hb) {
@@ -451,14 +465,13 @@ __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w
                     tens = (Ri + Rj) * (fr2 * fr2);
                 }
             }
-            const float iso = -mj * ((pOverRho2I + pJ * invRhoJ2) + piIJ + tens);
+            const float iso = -mj * ((pOverRho2I + pOverRho2J) + piIJ + tens);
             axS += iso * gx; ayS += iso * gy; azS += iso * gz;
             duP += mj * vDotG;
             duAv += 0.5f * mj * piIJ * vDotG;
             duT += 0.5f * mj * tens * vDotG;
-            const float tXX = sXXi * invRhoI2 + b3.x * invRhoJ2, tYY = sYYi * invRhoI2 + b3.y * invRhoJ2;
-            const float tZZ = sZZi * invRhoI2 + b3.z * invRhoJ2, tXY = sXYi * invRhoI2 + b3.w * invRhoJ2;
-            const float tXZ = sXZi * invRhoI2 + b4.x * invRhoJ2, tYZ = sYZi * invRhoI2 + b4.y * invRhoJ2;
+            const float tXX = sXXr + b3.x, tYY = sYYr + b3.y, tZZ = sZZr + b3.z, tXY = sXYr + b3.w;
+            const float tXZ = sXZr + b4.x, tYZ = sYZr + b4.y;
             axS += mj * (tXX * gx + tXY * gy + tXZ * gz);      // deviatoric stress (:1161-1163)
             ayS += mj * (tXY * gx + tYY * gy + tYZ * gz);
             azS += mj * (tXZ * gx + tYZ * gy + tZZ * gz);
@@ -525,7 +538,6 @@ __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w
     } else {
         p.dDamageCbrtDt[i] = 0.0f;
     }
-    (void)pairs;
 }
 
 // ----------------------------------------------------------------- drift ---
