@@ -158,6 +158,9 @@ __global__ void __launch_bounds__(256) refreshLeavesKernel(AstraeaParticles p, W
     const float h0I = fmaxf(__ldg(&p.h0[i]), 1.0e-6f);
     w.leafPM[i] = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), __ldg(&p.mass[i]));
     w.leafAux[i] = make_float4(2.0f * fmaxf(1.09f * hI, 0.351f * h0I), 0.8f * h0I, 2.0f * __ldg(&p.h[i]), 0.0f);
+    const float H = 2.0f * hI;                                      // the drift's 2 max(h, 1e-6)
+    w.driftRec[i] = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), H);
+    w.driftAux[i] = make_float2(__ldg(&p.mass[i]), wendlandNorm(H));
     if (withVelRho)
         w.velRho[i] = make_float4(__ldg(&p.velX[i]), __ldg(&p.velY[i]), __ldg(&p.velZ[i]), __ldg(&p.rho[i]));
 }

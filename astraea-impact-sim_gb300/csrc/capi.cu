@@ -129,6 +129,7 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     auto take = [&](size_t bytes) { const size_t o = off; off += alignUp(bytes); return o; };
     const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 16 * kRec2Width);
     const size_t oNode = take(C * 64), oMom = take(C * 32), oQuad = take(C * 32), oDrift = take(C * 16);
+    const size_t oDRec = take(C * 16), oDAux = take(C * 8);
     const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
     const size_t oSort = take(sortWords * 4), oDt = take(64);
     void* block = nullptr;
@@ -149,6 +150,8 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     w.nodeMom = reinterpret_cast<NodeMom*>(b + oMom);
     w.nodeQuad = reinterpret_cast<float4*>(b + oQuad);
     w.driftPos = reinterpret_cast<float4*>(b + oDrift);
+    w.driftRec = reinterpret_cast<float4*>(b + oDRec);
+    w.driftAux = reinterpret_cast<float2*>(b + oDAux);
     w.nbrCount = reinterpret_cast<uint32_t*>(b + oCnt);
     w.nbrList = reinterpret_cast<uint32_t*>(b + oList);
     w.words = reinterpret_cast<uint32_t*>(b + oWords);
@@ -267,11 +270,19 @@ AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadix
     if (bvh->sceneBoundsOrdered != nullptr)
         AG_CUDA(cudaMemcpyAsync(bvh->sceneBoundsOrdered, w.words + kWBounds, 6 * sizeof(uint32_t),
                                 cudaMemcpyDeviceToDevice, st));
-    AG_LAUNCH(launchPermuteLeavesKarras(*p, *alt, *bvh, driftPos, w, n, living, allFields, st));
+    // The fused step (allFields == false) keeps its tree in the library's node
+    // records only; the descriptor's node arrays (SoA and packed) are written
+    // by the stage call, whose callers may read them.
+    AstraeaRadixBvh kb = *bvh;
+    if (!allFields) {
+        kb.aabbMinX = nullptr;
+        kb.nodeComMass = nullptr;
+    }
+    AG_LAUNCH(launchPermuteLeavesKarras(*p, *alt, kb, driftPos, w, n, living, allFields, st));
     swapParticlePointers(*p, *alt);
     alt->count = p->count;
     const bool moments = g_farField.load() == 1;
-    AG_LAUNCH(launchRefit(*bvh, w, n, moments, st));
+    AG_LAUNCH(launchRefit(kb, w, n, moments, st));
     ws->treeBuilt = true;
     ws->builtN = n;
     ws->momentsBuilt = moments;

@@ -112,6 +112,14 @@ __device__ __forceinline__ float wendlandC2Grad(float r, float H) {
     const float H5 = H2 * H2 * H;
     return -(210.0f / (kPiF * H5)) * omq * omq * omq;
 }
+__device__ __forceinline__ float wendlandC2N(float r, float H, float norm) {   // norm = 21 / (2 pi H^3)
+    if (r >= H || H <= 0.0f) return 0.0f;
+    const float q = r / H;
+    const float omq = 1.0f - q;
+    const float omq2 = omq * omq;
+    return norm * omq2 * omq2 * (1.0f + 4.0f * q);
+}
+__device__ __forceinline__ float wendlandNorm(float H) { return 21.0f / (2.0f * kPiF * H * H * H); }
 __device__ __forceinline__ float wendlandC2GradN(float r, float H, float norm) {
     if (r >= H || H <= 0.0f) return 0.0f;
     const float omq = 1.0f - r / H;
@@ -371,6 +379,8 @@ struct Work {
     float4* nodeQuad;      // 2 x float4 per internal node: central second moments
                            // {Sxx, Syy, Szz, Sxy}, {Sxz, Syz, 0, 0} (far-field mode 1)
     float4* driftPos;      // {x, y, z, 0} after the drift
+    float4* driftRec;      // {x, y, z, H = 2 max(h, 1e-6)} for the next drift (pass 1 / leaf refresh)
+    float2* driftAux;      // {m, 21 / (2 pi H^3)} (the Wendland norm of H)
     uint32_t* nbrCount;
     uint32_t* nbrList;     // particle-major, maxNbr per particle
     uint32_t* words;       // small words, see WordIndex

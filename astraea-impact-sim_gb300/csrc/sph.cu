@@ -387,7 +387,12 @@ __global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, u
     p.curlVZ[i] = gYX - gXY;
     const float ratio = 56.0f / static_cast<float>(ngb);
     const float factor = fminf(1.08f, fmaxf(0.92f, cbrtf(ratio)));
-    p.h[i] = fminf(6.0f * h0i, fmaxf(0.35f * h0i, hi * factor));
+    const float hNew = fminf(6.0f * h0i, fmaxf(0.35f * h0i, hi * factor));
+    p.h[i] = hNew;
+    // records of the next drift (positions and h do not change before it)
+    const float Hd = 2.0f * fmaxf(hNew, 1.0e-6f);
+    w.driftRec[i] = make_float4(me.x, me.y, me.z, Hd);
+    w.driftAux[i] = make_float2(mi, wendlandNorm(Hd));
 }
 
 // ---------------------------------------------------------------- pass 2 ---
@@ -551,24 +556,25 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
     float mn[3] = {1.0e30f, 1.0e30f, 1.0e30f}, mx[3] = {-1.0e30f, -1.0e30f, -1.0e30f};
     if (i < n) {
         const float dt = (dtDev != nullptr) ? *dtDev : dtHost;
-        const float4 me = __ldg(&w.leafPM[i]);
+        const float4 me = __ldg(&w.driftRec[i]);            // {x, y, z, H}
         const float4 vr = __ldg(&w.velRho[i]);
-        const float hi = fmaxf(__ldg(&p.h[i]), 1.0e-6f);
-        const float Hi = 2.0f * hi;
+        const float Hi = me.w;
+        const float normI = __ldg(&w.driftAux[i]).y;
         const float rhoI = fmaxf(vr.w, 1.0e-9f);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         if (useList && n >= 2u) {
-            forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&w.leafPM[j]); }, [&](uint32_t j, float4 q) {
+            forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&w.driftRec[j]); }, [&](uint32_t j, float4 q) {
                 const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
                 const float r2 = len2Exact(dx, dy, dz);
-                const float Hj = 2.0f * fmaxf(__ldg(&p.h[j]), 1.0e-6f);
+                const float Hj = q.w;
                 const float Hm = fmaxf(Hi, Hj);
                 if (!(r2 < __fmul_rn(Hm, Hm))) return;
                 const float4 vj = __ldg(&w.velRho[j]);
+                const float2 aj = __ldg(&w.driftAux[j]);          // {m, Wendland norm of H_j}
                 const float r = sqrtf(r2);
-                const float wb = 0.5f * (wendlandC2(r, Hi) + wendlandC2(r, Hj));
+                const float wb = 0.5f * (wendlandC2N(r, Hi, normI) + wendlandC2N(r, Hj, aj.y));
                 const float rb = 0.5f * (rhoI + fmaxf(vj.w, 1.0e-9f));
-                const float co = (q.w / rb) * wb;
+                const float co = (aj.x / rb) * wb;
                 sx += co * (vj.x - vr.x);
                 sy += co * (vj.y - vr.y);
                 sz += co * (vj.z - vr.z);

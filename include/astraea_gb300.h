@@ -278,8 +278,11 @@ AstraeaStatus astraea_gb300_reduce_telemetry(const AstraeaParticles* p, const As
  * Needs one astraea_gb300_sort_and_build_bvh on this BVH beforehand (the
  * engine's evaluateInitialForcesOnDevice does that).  Fields the engine's
  * permutation moves but the step recomputes before reading (forces, rates,
- * EOS outputs, pass-1 outputs) are not moved.  After writing positions or h
- * from outside the library between steps, call
+ * EOS outputs, pass-1 outputs) are not moved, and the step's tree is kept in
+ * the library's own node records: the BVH descriptor's node arrays (aabb*,
+ * nodeMass, com*, nodeMaxH and the packed float4 arrays) keep the tree of the
+ * last astraea_gb300_sort_and_build_bvh.  After writing positions or h from
+ * outside the library between steps, call
  * astraea_gb300_invalidate_step_cache. */
 AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh,
                                  float prevDtPsu, float maxDtPsu, float theta, float* outDtPsu);
