@@ -146,6 +146,8 @@ SIGNATURES = [
                                        ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     ("astraea_gb300_reduce_telemetry", [_P, ctypes.POINTER(TelemetryParams), ctypes.POINTER(Telemetry)],
      ctypes.c_int),
+    ("astraea_gb300_relax_single_body", [_P, _P, _B, _VP, _U32, ctypes.c_double, _U32,
+                                         ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

@@ -256,6 +256,23 @@ def reduce_telemetry(p, target_radius_psu, living_body_present=True):
     return out.as_dict()
 
 
+def relax_single_body(p, alt, bvh, anchor_temp=None, nominal_radius=1.0, steps=20):
+    """Simulation::Impl::relaxLoadedSingleBody on the device; `anchor_temp`
+    is a float64 CUDA tensor indexed by originalId (None: 288 K).  Returns
+    v_rms / v_esc after the 4 diagnostic steps."""
+    sp, salt = p.struct(), alt.struct()
+    out = ctypes.c_double(0.0)
+    ptr = anchor_temp.data_ptr() if anchor_temp is not None else None
+    cnt = anchor_temp.numel() if anchor_temp is not None else 0
+    try:
+        abi.check(lib().astraea_gb300_relax_single_body(ctypes.byref(sp), ctypes.byref(salt), ctypes.byref(bvh.s),
+                                                        ptr, int(cnt), float(nominal_radius), int(steps),
+                                                        ctypes.byref(out)))
+    finally:
+        _rebind_after_swap(p, alt, sp, salt)
+    return out.value
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 

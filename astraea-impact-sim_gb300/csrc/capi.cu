@@ -667,6 +667,65 @@ AstraeaStatus astraea_gb300_reduce_telemetry(const AstraeaParticles* p, const As
     return ASTRAEA_OK;
 }
 
+// Simulation::Impl::relaxLoadedSingleBody (engine/simulation.cpp:585-781)
+// with the per-iteration host round trip replaced by device passes.
+AstraeaStatus astraea_gb300_relax_single_body(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh,
+                                              const double* anchorTempByOrigId, uint32_t anchorCount,
+                                              double nominalRadiusPsu, uint32_t steps, double* outFinalVrmsOverVesc) {
+    if (p == nullptr || alt == nullptr || bvh == nullptr || outFinalVrmsOverVesc == nullptr)
+        return fail(ASTRAEA_ERR_INVALID, "null argument");
+    *outFinalVrmsOverVesc = 0.0;
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;                                          // :590-593
+    AstraeaStatus s;
+#define AG_STAGE(call) do { s = (call); if (s != ASTRAEA_OK) return s; } while (0)
+    auto forces = [&]() -> AstraeaStatus {                                   // :616 / :709-711
+        AstraeaStatus r = astraea_gb300_evaluate_eos(p);
+        if (r == ASTRAEA_OK) r = astraea_gb300_gravity_barnes_hut(p, bvh, 0.5f);
+        if (r == ASTRAEA_OK) r = astraea_gb300_sph_pass2_forces(p, bvh);
+        return r;
+    };
+    auto build = [&]() -> AstraeaStatus {
+        AstraeaStatus r = astraea_gb300_sort_and_build_bvh(p, alt, bvh);
+        if (r == ASTRAEA_OK) r = astraea_gb300_sph_pass1_neighbors(p, bvh);
+        return r;
+    };
+    float prevDt = 0.0f;
+    auto step = [&]() -> AstraeaStatus {                                     // :604-616
+        float dt = 0.0f;
+        AstraeaStatus r = astraea_gb300_reduce_dt_psu(p, prevDt, 0.02f, &dt);
+        if (r != ASTRAEA_OK) return r;
+        prevDt = dt;
+        if ((r = astraea_gb300_leapfrog_kick_half(p, 0.5f * dt, 1, 1)) != ASTRAEA_OK) return r;
+        if ((r = astraea_gb300_leapfrog_drift(p, dt, bvh)) != ASTRAEA_OK) return r;
+        if ((r = build()) != ASTRAEA_OK) return r;
+        if ((r = forces()) != ASTRAEA_OK) return r;
+        return astraea_gb300_leapfrog_kick_half(p, 0.5f * dt, 0, 1);
+    };
+    AG_STAGE(astraea_gb300_clear_stats(p));                                  // evaluateInitialForcesOnDevice
+    AG_STAGE(build());
+    AG_STAGE(forces());
+    for (uint32_t it = 0; it < steps; ++it) {
+        AG_STAGE(step());
+        AG_LAUNCH(launchRelaxRecentre(*p, p->count, anchorTempByOrigId, anchorCount, smCount(), stream()));
+        if (it + 1u < steps) AG_STAGE(forces());                             // :708-712
+    }
+    if (steps > 0u) {                                                        // :715-737
+        AG_STAGE(build());
+        AG_STAGE(forces());
+        for (int c = 0; c < 4; ++c) AG_STAGE(step());
+        AG_STAGE(astraea_gb300_evaluate_eos(p));
+    }
+    AG_LAUNCH(launchRelaxDiagnostic(*p, p->count, nominalRadiusPsu, smCount(), outFinalVrmsOverVesc, stream()));
+    if (steps > 0u) {                                                        // :769-780
+        AG_LAUNCH(launchRelaxAnchor(*p, p->count, anchorTempByOrigId, anchorCount, stream()));
+        AG_STAGE(astraea_gb300_evaluate_eos(p));
+        AG_CUDA(cudaStreamSynchronize(stream()));
+    }
+#undef AG_STAGE
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult) {
     DeviceState* ds = nullptr;
     AstraeaStatus s = deviceState(&ds);

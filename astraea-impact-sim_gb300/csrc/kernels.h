@@ -71,6 +71,14 @@ cudaError_t launchWriteHeader(uint8_t* frame, const PclsHeaderWords& h, cudaStre
 cudaError_t launchTelemetry(const AstraeaParticles& p, uint32_t n, double targetRadiusPsu, int livingBodyPresent,
                             int sms, AstraeaTelemetry* hostOut, cudaStream_t st);
 
+// ------------------------------------------------------------ relax.cu ---
+cudaError_t launchRelaxRecentre(const AstraeaParticles& p, uint32_t n, const double* anchorT, uint32_t anchorCount,
+                                int sms, cudaStream_t st);
+cudaError_t launchRelaxDiagnostic(const AstraeaParticles& p, uint32_t n, double nominalRadius, int sms,
+                                  double* hostOut, cudaStream_t st);
+cudaError_t launchRelaxAnchor(const AstraeaParticles& p, uint32_t n, const double* anchorT, uint32_t anchorCount,
+                              cudaStream_t st);
+
 // ---------------------------------------------------------- gravity.cu ---
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
                           cudaStream_t st);

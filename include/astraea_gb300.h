@@ -263,6 +263,22 @@ typedef struct AstraeaTelemetry {
 AstraeaStatus astraea_gb300_reduce_telemetry(const AstraeaParticles* p, const AstraeaTelemetryParams* params,
                                              AstraeaTelemetry* out);
 
+/* ---- body relaxation (engine/simulation.cpp:585-781) -------------------- */
+
+/* Replaces Simulation::Impl::relaxLoadedSingleBody: the initial forces, then
+ * `steps` damped steps (dt bound 0.02 PSU, thermal clamp on) each followed by
+ * COM/bulk-velocity removal, 0.85 velocity damping, u re-anchored to
+ * u_cold(rho) + c_v T_anchor(originalId) and stresses/damage cleared, then 4
+ * undamped diagnostic steps; *outFinalVrmsOverVesc (host) receives
+ * v_rms / v_esc of the result, and u / strength are re-anchored once more.
+ * anchorTempByOrigId: device array of anchorCount temperatures [K] indexed by
+ * originalId (NULL: 288 K for all, the engine's fallback).  The engine copies
+ * ten arrays to the host and back every iteration; here the recentring runs
+ * on the device.  Blocks until done. */
+AstraeaStatus astraea_gb300_relax_single_body(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh,
+                                              const double* anchorTempByOrigId, uint32_t anchorCount,
+                                              double nominalRadiusPsu, uint32_t steps, double* outFinalVrmsOverVesc);
+
 /* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
 
 /* One Simulation::step() kernel sequence (engine/simulation.cpp:1711-1753):
