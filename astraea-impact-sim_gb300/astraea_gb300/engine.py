@@ -308,6 +308,12 @@ def reset_device_status():
     abi.check(lib().astraea_gb300_reset_device_status())
 
 
+def set_stream(stream):
+    """Launch stream of every later library call (a torch.cuda.Stream, or
+    None for the legacy default stream)."""
+    abi.check(lib().astraea_gb300_set_stream(stream.cuda_stream if stream is not None else None))
+
+
 def set_far_field(mode):
     """0: monopole (the engine's kernel); 1: monopole + quadrupole."""
     abi.check(lib().astraea_gb300_set_far_field(int(mode)))
