@@ -237,9 +237,16 @@ __global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, 
         const int lc = __ldcg(&bvh.leftChild[pNode]);
         const int rc = __ldcg(&bvh.rightChild[pNode]);
         const int grand = __ldcg(&bvh.parent[pNode]);
-        __threadfence();
-        if (atomicAdd(&bvh.atomicVisited[pNode], 1u) == 0u) return;   // first arrival stops
-        __threadfence();
+        // Arrival counter with release (this thread's node records, written
+        // with st.cg, become visible to the second arrival) and acquire (the
+        // sibling's records are read after it) in one atomic, instead of two
+        // full fences.
+        uint32_t before;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
+                     : "=r"(before)
+                     : "l"(&bvh.atomicVisited[pNode])
+                     : "memory");
+        if (before == 0u) return;   // first arrival stops
         const bool fromLeft = (lc == curr);
         const ChildData other = loadChild<kMoments>(w, fromLeft ? rc : lc, static_cast<int>(n));
         const ChildData& L = fromLeft ? mine : other;
