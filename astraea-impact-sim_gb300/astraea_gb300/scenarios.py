@@ -289,6 +289,31 @@ def differentiated_impact(n_total=1_000_000, impactor_frac=0.2, mass_target=M_EA
     return _merge_on_orbit(t, i, r_t, r_i, v_ratio, math.sin(math.radians(angle_deg)), sep_radii)
 
 
+def ensemble_impact(n_total, material=1, v_ratio=1.1, angle_deg=45.0, r_target=1.0, r_impactor=0.6, temp=300.0,
+                    seed=42):
+    """Two uniform single-material spheres (radii 1.0 and 0.6, equal density,
+    particles split by volume) on the impact orbit of _merge_on_orbit."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vol_i = r_impactor ** 3 / (r_target ** 3 + r_impactor ** 3)
+    n_i = max(64, int(round(n_total * vol_i)))
+    t = _uniform_body(n_total - n_i, r_target, material, temp, 0, rng)
+    i = _uniform_body(n_i, r_impactor, material, temp, 1, rng)
+    return _merge_on_orbit(t, i, r_target, r_impactor, v_ratio, math.sin(math.radians(angle_deg)), 1.05)
+
+
+def ensemble_configs(count=64, n_min=8192, n_max=131072, seed=7):
+    """Instances of the batched-ensemble workload: N log-uniform in
+    [n_min, n_max], impact angle uniform in 0..75 deg, velocity uniform in
+    1..3 v_esc, material drawn from Iron, Granite, WaterIce, Regolith."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(count):
+        out.append(dict(n_total=int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))),
+                        material=int(rng.choice([0, 1, 2, 4])), v_ratio=float(rng.uniform(1.0, 3.0)),
+                        angle_deg=float(rng.uniform(0.0, 75.0)), seed=int(seed * 1000 + k)))
+    return out
+
+
 def plummer_sphere(n, a=1.0, softening=1.0e-3, seed=42):
     rng = np.random.Generator(np.random.PCG64(seed))
     x = rng.uniform(1e-10, 1.0 - 1e-10, size=n)

@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-far-field", action="store_true", help="skip the quadrupole far-field comparison")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
                     help="far-field model of the timed steps: 0 monopole (the engine's), 1 + quadrupole")
     ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
@@ -223,6 +224,7 @@ def run_gpu(args):
 
     frame = frame_stages(sim, engine, torch, np, n)
     far = None if args.no_far_field else far_field_scan(sim, engine, torch, np, args, max_dt, truth)
+    ens = None if (args.no_ensemble or world > 1) else ensemble_run(engine, scenarios, torch, max_dt, args.theta)
 
     # ---- e2e through the C-ABI with pinned host buffers
     e2e = None
@@ -251,6 +253,7 @@ def run_gpu(args):
         "device_flags": flags,
         "frame_stages": frame,
         "far_field": far,
+        "ensemble": ens,
         "e2e": e2e,
     }
     out["config"]["max_dt_psu"] = max_dt
@@ -260,6 +263,41 @@ def run_gpu(args):
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def ensemble_run(engine, scenarios, torch, max_dt, theta, replays=4):
+    """The batched-ensemble workload: 64 independent impacts, N log-uniform
+    in [8k, 128k] (2.76M particles in all), angle 0..75 deg, 1..3 v_esc,
+    materials Iron / Granite / WaterIce / Regolith.  Eager fused steps
+    instance after instance vs one CUDA graph holding two steps of every
+    instance on its own stream."""
+    states = [scenarios.ensemble_impact(**c)[0] for c in scenarios.ensemble_configs()]
+    ens = engine.Ensemble(states, max_dt, theta)
+    ens.step_sequential(2)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record()
+    ens.step_sequential(2 * replays)
+    ev[1].record()
+    ens.capture()
+    torch.cuda.synchronize()
+    ens.replay(1)
+    torch.cuda.synchronize()
+    ev[2].record()
+    ens.replay(replays)
+    ev[3].record()
+    torch.cuda.synchronize()
+    steps = 2 * replays
+    eager_ms = ev[0].elapsed_time(ev[1]) / steps
+    graph_ms = ev[2].elapsed_time(ev[3]) / steps
+    total = ens.particles
+    del ens
+    torch.cuda.empty_cache()
+    return {"instances": len(states), "particles": total, "steps": steps,
+            "eager_ms_per_step": eager_ms, "graph_ms_per_step": graph_ms,
+            "eager_particle_steps_per_s": total / (eager_ms * 1e-3),
+            "graph_particle_steps_per_s": total / (graph_ms * 1e-3),
+            "graph_speedup": eager_ms / graph_ms}
 
 
 def frame_stages(sim, engine, torch, np, n, reps=5):
