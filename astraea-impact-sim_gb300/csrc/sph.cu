@@ -25,16 +25,16 @@ constexpr int kNbWarps = 4;
 constexpr int kNbStack = 1024;
 constexpr int kNbList = 64;
 
-// dirMem[k] (k = 9 (sx + 1) + 3 (sy + 1) + (sz + 1), s in {-1, 0, 1}): the
-// member {x, y, z, Hs} with the largest projection on direction s (first
-// member on ties); undMin/undMax: the undecided nodes of one walk round
+// dirMem[k] (k = 4 [sx > 0] + 2 [sy > 0] + [sz > 0], s in {-1, 1}^3, the
+// octant diagonals): the member {x, y, z, Hs} with the largest projection
+// on direction s (first member on ties); undMin/undMax: the undecided nodes of one walk round
 // {box min, node maxHs} / {box max}; the member positions are staged in
 // undMin while dirMem is computed.
 struct NbWarpSmem {
     int stack[kNbStack];
     float4 cand[kNbList];    // {x, y, z, Hs}
     int candIdx[kNbList];
-    float4 dirMem[27];
+    float4 dirMem[8];
     float4 undMin[32];
     float4 undMax[32];
 };
@@ -84,9 +84,8 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
         const float cxg = 0.5f * (gminx + gmaxx), cyg = 0.5f * (gminy + gmaxy), czg = 0.5f * (gminz + gmaxz);
         S.undMin[lane] = make_float4(me.x, me.y, me.z, Hs);
         __syncwarp();
-        if (lane < 27) {
-            const float sx = static_cast<float>(lane / 9 - 1), sy = static_cast<float>((lane / 3) % 3 - 1),
-                        sz = static_cast<float>(lane % 3 - 1);
+        if (lane < 8) {
+            const float sx = (lane & 4) ? 1.0f : -1.0f, sy = (lane & 2) ? 1.0f : -1.0f, sz = (lane & 1) ? 1.0f : -1.0f;
             float best = -3.0e38f;
             int bi = 0;
             for (int m = 0; m < act; ++m) {
@@ -156,9 +155,7 @@ __global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, ui
                     // (3) otherwise the whole group decides
                     const float ux = 0.5f * (bmin.x + bmax.x) - cxg, uy = 0.5f * (bmin.y + bmax.y) - cyg,
                                 uz = 0.5f * (bmin.z + bmax.z) - czg;
-                    const float t = 0.41421356f * fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
-                    const int sx = (ux >= t) - (ux <= -t), sy = (uy >= t) - (uy <= -t), sz = (uz >= t) - (uz <= -t);
-                    const float4 dm = S.dirMem[13 + 9 * sx + 3 * sy + sz];
+                    const float4 dm = S.dirMem[(ux >= 0.0f ? 4 : 0) | (uy >= 0.0f ? 2 : 0) | (uz >= 0.0f ? 1 : 0)];
                     const float R = fmaxf(dm.w, nodeHs);
                     if (pointBoxDist2(dm.x, dm.y, dm.z, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z) <=
                         R * R * 1.00001f)
