@@ -119,7 +119,8 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.fh.close()
-        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        with open(self.path) as fh:
+            rows = [r.split(",") for r in fh.read().strip().splitlines() if r.count(",") >= 8]
         os.unlink(self.path)
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
@@ -213,7 +214,8 @@ def run_gpu(args):
     tpath = os.path.join(ROOT, "profiles", "gravity_traffic.json")
     if os.path.exists(tpath):
         try:
-            tr = json.load(open(tpath))
+            with open(tpath) as fh:
+                tr = json.load(fh)
             traffic = tr.get("bytes_per_particle") and tr["bytes_per_particle"] * n
         except ValueError:
             traffic = None
@@ -333,7 +335,8 @@ def step_hbm_roofline(n, ms):
     per-stage sum of the engine's reads/writes) against measured HBM."""
     peak = None
     try:
-        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peak = json.load(fh)["hbm_gbs"]
     except (OSError, ValueError, KeyError):
         peak = 6800.0
     achieved = 1580.0 * n / (ms * 1e-3) / 1e9

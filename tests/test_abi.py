@@ -12,7 +12,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_functions():
-    text = open(os.path.join(ROOT, "include", "astraea_gb300.h")).read()
+    with open(os.path.join(ROOT, "include", "astraea_gb300.h")) as fh:
+        text = fh.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(astraea_gb300_[a-z0-9_]+)\s*\(", text)))
 
