@@ -156,6 +156,7 @@ SIGNATURES = [
     ("astraea_gb300_radix_sort_pairs_noalloc", [_VP, _VP, _VP, _VP, _U32, ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_read_device_status", [ctypes.POINTER(_U32), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     ("astraea_gb300_reset_device_status", [], ctypes.c_int),
+    ("astraea_gb300_direct_gravity_f64", [_P, _VP, _U32, _VP, _VP], ctypes.c_int),
     ("astraea_gb300_measure_fp32_tflops", [ctypes.POINTER(_F)], ctypes.c_int),
     ("astraea_gb300_set_lookback_spin_limit", [_U32], ctypes.c_int),
     ("astraea_gb300_set_far_field", [ctypes.c_int], ctypes.c_int),

@@ -273,6 +273,18 @@ def relax_single_body(p, alt, bvh, anchor_temp=None, nominal_radius=1.0, steps=2
     return out.value
 
 
+def direct_gravity_f64(p, targets):
+    """FP64 direct-sum accelerations (N, 3) and potentials at the listed
+    target indices (an int CUDA tensor), as float64 CUDA tensors."""
+    t = targets.to(device="cuda", dtype=torch.int32).contiguous()
+    acc = torch.empty((t.numel(), 3), dtype=torch.float64, device="cuda")
+    phi = torch.empty(t.numel(), dtype=torch.float64, device="cuda")
+    s = p.struct()
+    abi.check(lib().astraea_gb300_direct_gravity_f64(ctypes.byref(s), t.data_ptr(), t.numel(), acc.data_ptr(),
+                                                     phi.data_ptr()))
+    return acc, phi
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 

@@ -289,6 +289,60 @@ def differentiated_impact(n_total=1_000_000, impactor_frac=0.2, mass_target=M_EA
     return _merge_on_orbit(t, i, r_t, r_i, v_ratio, math.sin(math.radians(angle_deg)), sep_radii)
 
 
+def _polytrope_envelope(n, mass_psu, r_in, r_out, temp, body_id, rng):
+    """HydrogenHelium (material 3) shell r_in..r_out with the n = 1 polytrope
+    profile rho ~ sin(pi r / r_out) / (pi r / r_out), equal-mass particles."""
+    rs = np.linspace(r_in, r_out, 4000)
+    x = np.pi * rs / r_out
+    shape = np.sin(x) / x
+    dm = 4.0 * np.pi * rs * rs * shape
+    ms = np.concatenate([[0.0], np.cumsum(0.5 * (dm[1:] + dm[:-1]) * np.diff(rs))])
+    rho_c = mass_psu / ms[-1]
+    pts, _ = _lattice_ball(n, rng)
+    r0 = np.linalg.norm(pts, axis=1)
+    frac = np.clip(r0, 0.0, 1.0) ** 3
+    r = np.interp(frac * ms[-1], ms, rs)
+    scale = np.where(r0 > 0, r / np.maximum(r0, 1e-30), 0.0)
+    pts = pts * scale[:, None]
+    rho = np.maximum(rho_c * np.interp(r, rs, shape), 1.0e-9)
+    m = mass_psu / n
+    st = empty_state(n)
+    st["posX"][:], st["posY"][:], st["posZ"][:] = pts[:, 0], pts[:, 1], pts[:, 2]
+    st["mass"][:] = m
+    h0 = 1.2 * (m / rho) ** (1.0 / 3.0)
+    st["h"][:] = h0
+    st["h0"][:] = h0
+    st["rho"][:] = rho
+    st["u"][:] = (8260.0 * temp) / 1.0e6          # HydrogenHelium c_v, thermal part
+    st["tempK"][:] = temp
+    st["epsFail"][:] = 1.0
+    st["materialId"][:] = 3
+    st["bodyId"][:] = body_id
+    return st
+
+
+def gas_giant_impact(n_total=16_000_000, n_impactor=2_000_000, mass_target=10.0 * M_EARTH_PSU, core_mass_frac=0.1,
+                     envelope_radius_factor=4.0, mass_ratio=0.1, v_ratio=2.0, angle_deg=30.0, temp=2000.0, seed=42):
+    """Gas-giant core impact: a HydrogenHelium n = 1 polytrope envelope over an
+    Iron + Granite core holding core_mass_frac of the target mass, hit by a
+    uniform Regolith impactor.  Particle counts split by mass between core and
+    envelope (equal particle mass within each)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n_t = n_total - n_impactor
+    n_core = max(1024, int(round(n_t * core_mass_frac)))
+    core, r_core = _layered_body(n_core, mass_target * core_mass_frac, 0.33, temp, 0, rng)
+    env = _polytrope_envelope(n_t - n_core, mass_target * (1.0 - core_mass_frac), r_core,
+                              envelope_radius_factor * r_core, temp, 0, rng)
+    target = {k: np.concatenate([core[k], env[k]]) for k in core}
+    m_i = mass_target * mass_ratio
+    rho_i = 2000.0 / 1.0e6
+    r_i = (3.0 * m_i / (4.0 * math.pi * rho_i)) ** (1.0 / 3.0)
+    imp = _uniform_body(n_impactor, r_i, 4, temp, 1, rng)
+    imp["mass"][:] = m_i / n_impactor
+    return _merge_on_orbit(target, imp, envelope_radius_factor * r_core, r_i, v_ratio,
+                           math.sin(math.radians(angle_deg)), 1.05)
+
+
 def ensemble_impact(n_total, material=1, v_ratio=1.1, angle_deg=45.0, r_target=1.0, r_impactor=0.6, temp=300.0,
                     seed=42):
     """Two uniform single-material spheres (radii 1.0 and 0.6, equal density,

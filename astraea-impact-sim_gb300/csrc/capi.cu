@@ -726,6 +726,14 @@ AstraeaStatus astraea_gb300_relax_single_body(AstraeaParticles* p, AstraeaPartic
     return ASTRAEA_OK;
 }
 
+AstraeaStatus astraea_gb300_direct_gravity_f64(const AstraeaParticles* p, const uint32_t* targets, uint32_t count,
+                                              double* acc3, double* phi) {
+    if (p == nullptr || (count > 0u && (targets == nullptr || acc3 == nullptr || phi == nullptr)))
+        return fail(ASTRAEA_ERR_INVALID, "null argument");
+    AG_LAUNCH(launchDirectGravityF64(*p, p->count, targets, count, acc3, phi, stream()));
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult) {
     DeviceState* ds = nullptr;
     AstraeaStatus s = deviceState(&ds);

@@ -48,3 +48,71 @@ cudaError_t measureFp32Tflops(int sms, float* tflops, cudaStream_t st) {
 }
 
 }  // namespace astraea_gb300
+
+// ---------------------------------------------------------------------------
+// FP64 direct-sum gravity at listed targets: the truth the Barnes-Hut and
+// far-field accuracies are measured against (the N^2 check of the engine's
+// tests/cpp/test_gravity_sph.cpp:366-378, eps_ij = (eps_i + eps_j) / 2 with
+// eps = 0.8 max(h0, 1e-6), G_PSU).  One thread per target; sources staged
+// through shared memory in tiles; every operation in FP64.
+namespace astraea_gb300 {
+namespace {
+constexpr int kDirectThreads = 128;
+constexpr double kGPsuDirect = 6.67430e-11 * 1.0e24 * 1.0e3 * 1.0e3 / (1.0e6 * 1.0e6 * 1.0e6);
+
+__global__ void __launch_bounds__(kDirectThreads) directGravityF64Kernel(AstraeaParticles p, uint32_t n,
+                                                                        const uint32_t* targets, uint32_t nt,
+                                                                        double* acc3, double* phiOut) {
+    __shared__ double4 src[kDirectThreads];   // x, y, z, m
+    __shared__ double srcEps[kDirectThreads];
+    const uint32_t t = blockIdx.x * kDirectThreads + threadIdx.x;
+    const bool live = t < nt;
+    const uint32_t i = live ? targets[t] : 0u;
+    const bool valid = live && i < n;
+    double xi = 0.0, yi = 0.0, zi = 0.0, ei = 0.0;
+    if (valid) {
+        xi = p.posX[i]; yi = p.posY[i]; zi = p.posZ[i];
+        ei = 0.8 * static_cast<double>(fmaxf(p.h0[i], 1.0e-6f));
+    }
+    double ax = 0.0, ay = 0.0, az = 0.0, phi = 0.0;
+    for (uint32_t base = 0; base < n; base += kDirectThreads) {
+        const uint32_t j = base + threadIdx.x;
+        __syncthreads();
+        if (j < n) {
+            src[threadIdx.x] = make_double4(p.posX[j], p.posY[j], p.posZ[j], p.mass[j]);
+            srcEps[threadIdx.x] = 0.8 * static_cast<double>(fmaxf(p.h0[j], 1.0e-6f));
+        } else {
+            src[threadIdx.x] = make_double4(0.0, 0.0, 0.0, 0.0);
+            srcEps[threadIdx.x] = 1.0;
+        }
+        __syncthreads();
+        const int cnt = static_cast<int>(min(static_cast<uint32_t>(kDirectThreads), n - base));
+        for (int k = 0; k < cnt; ++k) {
+            if (base + static_cast<uint32_t>(k) == i) continue;
+            const double4 s = src[k];
+            const double dx = xi - s.x, dy = yi - s.y, dz = zi - s.z;
+            const double e = 0.5 * (ei + srcEps[k]);
+            const double r2 = dx * dx + dy * dy + dz * dz + e * e;
+            const double inv = 1.0 / sqrt(r2);
+            const double f = -kGPsuDirect * s.w * inv * inv * inv;
+            ax += f * dx; ay += f * dy; az += f * dz;
+            phi -= kGPsuDirect * s.w * inv;
+        }
+    }
+    if (live) {
+        acc3[3 * t] = valid ? ax : 0.0;
+        acc3[3 * t + 1] = valid ? ay : 0.0;
+        acc3[3 * t + 2] = valid ? az : 0.0;
+        phiOut[t] = valid ? phi : 0.0;
+    }
+}
+}  // namespace
+
+cudaError_t launchDirectGravityF64(const AstraeaParticles& p, uint32_t n, const uint32_t* targets, uint32_t nt,
+                                   double* acc3, double* phi, cudaStream_t st) {
+    if (nt == 0) return cudaSuccess;
+    directGravityF64Kernel<<<(nt + kDirectThreads - 1) / kDirectThreads, kDirectThreads, 0, st>>>(p, n, targets, nt,
+                                                                                                  acc3, phi);
+    return cudaGetLastError();
+}
+}  // namespace astraea_gb300

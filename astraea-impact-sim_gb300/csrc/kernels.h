@@ -79,6 +79,10 @@ cudaError_t launchRelaxDiagnostic(const AstraeaParticles& p, uint32_t n, double 
 cudaError_t launchRelaxAnchor(const AstraeaParticles& p, uint32_t n, const double* anchorT, uint32_t anchorCount,
                               cudaStream_t st);
 
+// ------------------------------------------------------------- diag.cu ---
+cudaError_t launchDirectGravityF64(const AstraeaParticles& p, uint32_t n, const uint32_t* targets, uint32_t nt,
+                                   double* acc3, double* phi, cudaStream_t st);
+
 // ---------------------------------------------------------- gravity.cu ---
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
                           cudaStream_t st);

@@ -60,7 +60,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--n", type=int, default=None,
+                    help="particles (default: 1M for c2, 4M for c3, 16M for c5)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+                    help="c2: the 1M differentiated impact (the headline line); c3: 4M Plummer sphere, "
+                         "gravity only, plain vs quadrupole far field; c5: 16M gas-giant core impact")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--max-dt-sec", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -73,11 +77,17 @@ def parse():
     return ap.parse_args()
 
 
-def workload_config(n, theta, far_field=0):
+def workload_config(n, theta, far_field=0, workload="c2"):
+    if workload == "c5":
+        name = ("gas-giant core impact, N=%d: HydrogenHelium n=1 polytrope envelope over an Iron+Granite core "
+                "(10%% of the target mass, 10 Earth masses), Regolith impactor of %d particles (mass ratio 0.1) "
+                "at 2.0 v_esc and 30 deg" % (n, n // 8))
+    else:
+        name = ("differentiated Earth-Theia-like impact, N=%d (target %d + impactor %d), Iron core 30%% "
+                "+ Granite mantle, hydrostatic radial density, mass ratio 0.1, 1.1 v_esc at 45 deg, strength "
+                "+ damage on" % (n, n - int(round(0.2 * n)), int(round(0.2 * n))))
     return {
-        "workload": "differentiated Earth-Theia-like impact, N=%d (target %d + impactor %d), Iron core 30%% "
-                    "+ Granite mantle, hydrostatic radial density, mass ratio 0.1, 1.1 v_esc at 45 deg, strength "
-                    "+ damage on" % (n, n - int(round(0.2 * n)), int(round(0.2 * n))),
+        "workload": name,
         "n_particles": n,
         "traversal": ("plain Barnes-Hut theta=%.2f (monopole, the engine's kernel)" % theta if far_field == 0 else
                       "Barnes-Hut theta=%.2f, monopole + quadrupole far field" % theta),
@@ -161,7 +171,10 @@ def run_gpu(args):
     n = args.n
     max_dt = max(1.0e-5, args.max_dt_sec) / 1.0e3
     engine.set_far_field(args.far_field)
-    st, info = scenarios.differentiated_impact(n_total=n, seed=42 + rank)
+    if args.workload == "c5":
+        st, info = scenarios.gas_giant_impact(n_total=n, n_impactor=n // 8, seed=42 + rank)
+    else:
+        st, info = scenarios.differentiated_impact(n_total=n, seed=42 + rank)
     sim = engine.Simulation(n)
     sim.load_state(st)
     engine.reserve(sim.bvh, n)
@@ -238,7 +251,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 in drift, refit moments)",
         "data": "synthetic (seeded hydrostatic bodies)",
-        "config": workload_config(n, args.theta, args.far_field),
+        "config": workload_config(n, args.theta, args.far_field, args.workload),
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "clocks": clk,
         "roofline": {"kernel": "gravity (Barnes-Hut group walk + pair evaluation)", "bound": "fp32",
@@ -519,6 +532,65 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
                     "neighbouring steps' kernels"}
 
 
+def run_c3(args):
+    """Gravity-only traversal on a seeded Plummer sphere (a = 1, G = 1,
+    softening 1e-3): plain monopole theta = 0.5 and the quadrupole far field
+    at larger opening angles, RMS force error against the FP64 direct sum on
+    65,536 sampled targets (the library's FP64 kernel)."""
+    import numpy as np
+    import torch
+    from astraea_gb300 import engine, scenarios
+    n = args.n
+    st = scenarios.plummer_sphere(n)
+    sim = engine.Simulation(n)
+    sim.load_state(st)
+    engine.reserve(sim.bvh, n)
+    engine.set_far_field(0)
+    engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+    g = torch.Generator(device="cpu").manual_seed(4321)
+    tgt = torch.randperm(n, generator=g)[: min(65536, n)].cuda()
+    t0 = time.perf_counter()
+    acc64, _ = engine.direct_gravity_f64(sim.p, tgt)
+    torch.cuda.synchronize()
+    truth_s = time.perf_counter() - t0
+    runs = []
+    for theta, mode in ((0.5, 0), (0.6, 0), (0.7, 0), (0.8, 0), (0.6, 1), (0.7, 1), (0.8, 1), (0.9, 1)):
+        engine.set_far_field(mode)
+        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+        engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+        torch.cuda.synchronize()
+        engine.reset_device_status()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(max(args.steps // 2, 3)):
+            engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+        ev[1].record()
+        torch.cuda.synchronize()
+        reps = max(args.steps // 2, 3)
+        ms = ev[0].elapsed_time(ev[1]) / reps
+        _, c = engine.read_device_status()
+        A = sim.p.arrays
+        bh = torch.stack([A["accX"][:n][tgt], A["accY"][:n][tgt], A["accZ"][:n][tgt]], 1).double()
+        rel = (bh - acc64).norm(dim=1) / acc64.norm(dim=1)
+        runs.append({"theta": theta, "far_field": "monopole" if mode == 0 else "monopole+quadrupole",
+                     "gravity_ms": ms, "particles_per_s": n / (ms * 1e-3),
+                     "interactions_per_particle": c["gravity_interactions"] / reps / n,
+                     "force_rms_vs_fp64": float(torch.sqrt((rel * rel).mean())),
+                     "force_p99_vs_fp64": float(torch.quantile(rel.float(), 0.99))})
+    engine.set_far_field(0)
+    base = runs[0]
+    ok = [r for r in runs[1:] if r["force_rms_vs_fp64"] <= base["force_rms_vs_fp64"]]
+    best = max(ok, key=lambda r: r["particles_per_s"]) if ok else None
+    print(json.dumps({
+        "workload": "c3", "metric": "gravity traversals: particles/s at equal force error", "unit": "particles/s",
+        "config": {"workload": "Plummer sphere N=%d (a=1, G=1 via m/G_PSU, softening 1e-3 => h0=1.25e-3), "
+                               "gravity only" % n, "targets_fp64": int(tgt.numel()), "truth_seconds": truth_s},
+        "runs": runs,
+        "equal_error_choice": best and {"theta": best["theta"], "far_field": best["far_field"],
+                                        "speedup_vs_plain_theta05": best["particles_per_s"] /
+                                        base["particles_per_s"]}}))
+
+
 # ------------------------------------------------------------- CPU arm
 def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -597,7 +669,13 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
+    if a.n is None:
+        a.n = {"c2": 1_000_000, "c3": 4_000_000, "c5": 16_000_000}[a.workload]
+    if a.workload != "c2":
+        a.no_cpu_baseline = a.no_ensemble = a.no_far_field = True
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "c3":
+        run_c3(a)
     else:
         run_gpu(a)

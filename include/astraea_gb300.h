@@ -347,6 +347,15 @@ AstraeaStatus astraea_gb300_read_device_status(uint32_t* outFlags, uint64_t* out
  * counterpart. */
 AstraeaStatus astraea_gb300_measure_fp32_tflops(float* outTflops);
 AstraeaStatus astraea_gb300_reset_device_status(void);
+/* FP64 direct-sum gravity at `count` listed targets (device indices; device
+ * outputs: acc3[3 count] as x, y, z, and phi[count]), over all p->count
+ * particles with eps_ij = (eps_i + eps_j)/2, eps = 0.8 max(h0, 1e-6): the
+ * accuracy reference of the Barnes-Hut and far-field modes (the N^2 check of
+ * tests/cpp/test_gravity_sph.cpp:366-378).  A target index >= count of
+ * particles gives zeros.  Asynchronous; no engine counterpart. */
+AstraeaStatus astraea_gb300_direct_gravity_f64(const AstraeaParticles* p, const uint32_t* targets, uint32_t count,
+                                              double* acc3, double* phi);
+
 /* Test hook: lower the onesweep look-back spin limit (0 restores default). */
 AstraeaStatus astraea_gb300_set_lookback_spin_limit(uint32_t limit);
 /* Failure-detection probe: runs the onesweep look-back wait on a status word

@@ -145,3 +145,18 @@ def test_gpu_quadrupole_needs_moments_tree():
         engine.set_far_field(0)
     with pytest.raises(abi.AstraeaError):
         engine.set_far_field(2)
+
+
+@pytest.mark.gpu
+def test_gpu_direct_sum_f64_matches_oracle():
+    import torch
+    from astraea_gb300 import engine
+    st = impact_state(4096, seed=8)
+    n = len(st["posX"])
+    p = engine.DeviceParticles(n)
+    p.upload(st)
+    tgt = np.random.default_rng(2).choice(n, 300, replace=False).astype(np.uint32)
+    acc, phi = engine.direct_gravity_f64(p, torch.from_numpy(tgt.astype(np.int64)))
+    ref_acc, ref_phi = oracle.direct_gravity_f64(st, tgt)
+    assert np.max(np.abs(acc.cpu().numpy() - ref_acc)) <= 1e-12 * np.max(np.abs(ref_acc))
+    assert np.max(np.abs(phi.cpu().numpy() - ref_phi)) <= 1e-12 * np.max(np.abs(ref_phi))
