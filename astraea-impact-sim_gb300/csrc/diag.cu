@@ -100,9 +100,9 @@ __global__ void __launch_bounds__(kDirectThreads) directGravityF64Kernel(Astraea
         }
     }
     if (live) {
-        acc3[3 * t] = valid ? ax : 0.0;
-        acc3[3 * t + 1] = valid ? ay : 0.0;
-        acc3[3 * t + 2] = valid ? az : 0.0;
+        acc3[3 * static_cast<size_t>(t)] = valid ? ax : 0.0;
+        acc3[3 * static_cast<size_t>(t) + 1] = valid ? ay : 0.0;
+        acc3[3 * static_cast<size_t>(t) + 2] = valid ? az : 0.0;
         phiOut[t] = valid ? phi : 0.0;
     }
 }

@@ -401,11 +401,11 @@ __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4* R = w.rec2;
-    const float4 a0 = __ldg(&R[kRec2Width * i + 0]);
-    const float4 a1 = __ldg(&R[kRec2Width * i + 1]);
-    const float4 a2 = __ldg(&R[kRec2Width * i + 2]);
-    const float4 a4 = __ldg(&R[kRec2Width * i + 4]);
-    const float4 a5 = __ldg(&R[kRec2Width * i + 5]);
+    const float4 a0 = __ldg(&R[kRec2Width * static_cast<size_t>(i) + 0]);
+    const float4 a1 = __ldg(&R[kRec2Width * static_cast<size_t>(i) + 1]);
+    const float4 a2 = __ldg(&R[kRec2Width * static_cast<size_t>(i) + 2]);
+    const float4 a4 = __ldg(&R[kRec2Width * static_cast<size_t>(i) + 4]);
+    const float4 a5 = __ldg(&R[kRec2Width * static_cast<size_t>(i) + 5]);
     const float xi = a0.x, yi = a0.y, zi = a0.z, hi = a0.w, Hi = 2.0f * hi;
     const float vxi = a1.x, vyi = a1.y, vzi = a1.z, mi = a1.w;
     const float rhoI = a2.x, pOverRho2I = a2.y, csI = a2.z, fBalI = a2.w;
@@ -424,17 +424,17 @@ __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w
     float axS = 0.f, ayS = 0.f, azS = 0.f, drC = 0.f, drD = 0.f, duP = 0.f, duAv = 0.f, duT = 0.f, duS = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
     if (n >= 2u) {
-        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&R[kRec2Width * j + 0]); }, [&](uint32_t j, float4 b0) {
+        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&R[kRec2Width * static_cast<size_t>(j) + 0]); }, [&](uint32_t j, float4 b0) {
             const float dx = __fsub_rn(xi, b0.x), dy = __fsub_rn(yi, b0.y), dz = __fsub_rn(zi, b0.z);
             const float r2 = len2Exact(dx, dy, dz);
             const float hj = b0.w, Hj = 2.0f * hj;
             const float Hm = fmaxf(Hi, Hj);
             if (!(r2 < __fmul_rn(Hm, Hm))) return;          // sph_gravity.cu:1071
-            const float4 b1 = __ldg(&R[kRec2Width * j + 1]);
-            const float4 b2 = __ldg(&R[kRec2Width * j + 2]);
-            const float4 b3 = __ldg(&R[kRec2Width * j + 3]);
-            const float4 b4 = __ldg(&R[kRec2Width * j + 4]);
-            const float4 b5 = __ldg(&R[kRec2Width * j + 5]);
+            const float4 b1 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 1]);
+            const float4 b2 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 2]);
+            const float4 b3 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 3]);
+            const float4 b4 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 4]);
+            const float4 b5 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 5]);
             const float mj = b1.w, rhoJ = b2.x, pOverRho2J = b2.y, csJ = b2.z, fBalJ = b2.w;
             const float volJ = b5.x, invRhoJ2 = b5.z;
             const float dvx = vxi - b1.x, dvy = vyi - b1.y, dvz = vzi - b1.z;
