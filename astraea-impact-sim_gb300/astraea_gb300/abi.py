@@ -67,6 +67,8 @@ assert ctypes.sizeof(Particles) == 8 + 56 * 8
 assert ctypes.sizeof(RadixBvh) == 8 + 19 * 8 + 8 + 8 + 6 * 8
 
 STATUS_NAMES = {0: "OK", 1: "CUDA", 2: "CAPACITY", 3: "INVALID", 4: "DEVICE_TIMEOUT", 5: "DEVICE_STATE"}
+ASTRAEA_ERR_CAPACITY = 2
+ASTRAEA_ERR_INVALID = 3
 
 DEVFLAG_LOOKBACK_TIMEOUT = 0x1
 DEVFLAG_NEIGHBOR_OVERFLOW = 0x2
@@ -122,6 +124,26 @@ _B = ctypes.POINTER(RadixBvh)
 _U32 = ctypes.c_uint32
 _F = ctypes.c_float
 _VP = ctypes.c_void_p
+class BodySpec(ctypes.Structure):
+    """AstraeaBodySpec = BodyInitSpec (engine/types.hpp:60-67)."""
+    _fields_ = [("archetype", _U32), ("relaxSteps", _U32), ("massKg", ctypes.c_double),
+                ("surfaceTempK", ctypes.c_double), ("coreTempK", ctypes.c_double),
+                ("spinOmegaRadS", ctypes.c_double)]
+
+
+class RadialSample(ctypes.Structure):
+    """AstraeaRadialSample = RadialProfileSample (engine/planet_builder.hpp:10-17)."""
+    _fields_ = [("rM", ctypes.c_double), ("rhoKgM3", ctypes.c_double), ("pressurePa", ctypes.c_double),
+                ("enclosedMassKg", ctypes.c_double), ("tempK", ctypes.c_double), ("material", _U32),
+                ("reserved", _U32)]
+
+
+class PlanetInfo(ctypes.Structure):
+    _fields_ = [("equatorialRadiusM", ctypes.c_double), ("actualMassKg", ctypes.c_double),
+                ("centralPressurePa", ctypes.c_double), ("tracerCount", _U32), ("profileSamples", _U32),
+                ("shells", _U32), ("reserved", _U32)]
+
+
 SIGNATURES = [
     ("astraea_gb300_last_error", [], ctypes.c_char_p),
     ("astraea_gb300_abi_version", [], ctypes.c_int),
@@ -148,6 +170,11 @@ SIGNATURES = [
      ctypes.c_int),
     ("astraea_gb300_relax_single_body", [_P, _P, _B, _VP, _U32, ctypes.c_double, _U32,
                                          ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    ("astraea_gb300_solve_hydrostatic", [ctypes.POINTER(BodySpec), ctypes.POINTER(RadialSample), _U32,
+                                         ctypes.POINTER(_U32), ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    ("astraea_gb300_build_planet", [ctypes.POINTER(BodySpec), _U32, _U32, _U32, ctypes.c_uint64, _P, _U32,
+                                    ctypes.POINTER(PlanetInfo)], ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

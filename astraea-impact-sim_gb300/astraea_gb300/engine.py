@@ -285,6 +285,60 @@ def direct_gravity_f64(p, targets):
     return acc, phi
 
 
+# makeDefaultBodySpec (engine/presets.cpp:9-88): mass [kg], surface and core
+# temperature [K], spin [rad/s] of each archetype.
+ARCHETYPES = ("LivingTerra", "IronCore", "OceanIce", "LavaIo", "GasGiant", "ProtoTheia")
+ARCHETYPE_DEFAULTS = {
+    0: (5.97219e24, 288.0, 5500.0, 7.292115e-5),
+    1: (3.3011e23, 440.0, 3200.0, 1.24e-6),
+    2: (4.0e24, 275.0, 3800.0, 5.0e-5),
+    3: (2.0e24, 1550.0, 4200.0, 4.11e-5),
+    4: (1.2e26, 165.0, 18000.0, 1.76e-4),
+    5: (6.417e23, 240.0, 2200.0, 7.09e-5),
+}
+
+
+def body_spec(archetype, mass_kg=None, surface_temp_k=None, core_temp_k=None, spin=None, relax_steps=80):
+    """AstraeaBodySpec with the archetype's defaults for every field not given."""
+    a = ARCHETYPES.index(archetype) if isinstance(archetype, str) else int(archetype)
+    m, ts, tc, w = ARCHETYPE_DEFAULTS.get(a, (1.0, 0.0, 0.0, 0.0))
+    return abi.BodySpec(a, int(relax_steps), m if mass_kg is None else mass_kg,
+                        ts if surface_temp_k is None else surface_temp_k,
+                        tc if core_temp_k is None else core_temp_k, w if spin is None else spin)
+
+
+def solve_hydrostatic(spec):
+    """PlanetBuilder::solveHydrostatic1D on the host: (profile dict of numpy
+    columns r, rho, P, M, T, material; radius [m]; central pressure [Pa])."""
+    n, r, pc = ctypes.c_uint32(0), ctypes.c_double(0.0), ctypes.c_double(0.0)
+    cap = 16384                                    # the shooting makes at most ~12,000 steps
+    buf = (abi.RadialSample * cap)()
+    st = lib().astraea_gb300_solve_hydrostatic(ctypes.byref(spec), buf, cap, ctypes.byref(n), ctypes.byref(r),
+                                               ctypes.byref(pc))
+    if st == abi.ASTRAEA_ERR_CAPACITY and n.value > cap:
+        buf = (abi.RadialSample * n.value)()
+        st = lib().astraea_gb300_solve_hydrostatic(ctypes.byref(spec), buf, n.value, ctypes.byref(n),
+                                                   ctypes.byref(r), ctypes.byref(pc))
+    abi.check(st)
+    a = np.frombuffer(buf, dtype=np.dtype([("r", "f8"), ("rho", "f8"), ("P", "f8"), ("M", "f8"), ("T", "f8"),
+                                           ("material", "u4"), ("reserved", "u4")]), count=n.value)
+    prof = {k: np.array(a[k]) for k in ("r", "rho", "P", "M", "T", "material")}
+    return prof, r.value, pc.value
+
+
+def build_planet(spec, particle_count, p, offset=0, body_id=0, tracer_grid_res=0, seed=42):
+    """PlanetBuilder::buildPlanet written straight into particles
+    [offset, offset + particle_count) of p (DeviceParticles); p.count is
+    raised to cover the body.  Returns the AstraeaPlanetInfo as a dict."""
+    info = abi.PlanetInfo()
+    s = p.struct()
+    abi.check(lib().astraea_gb300_build_planet(ctypes.byref(spec), int(particle_count), int(body_id),
+                                               int(tracer_grid_res), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                               ctypes.byref(s), int(offset), ctypes.byref(info)))
+    p.count = max(p.count, int(offset) + int(particle_count))
+    return {f: getattr(info, f) for f, _ in abi.PlanetInfo._fields_ if f != "reserved"}
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 

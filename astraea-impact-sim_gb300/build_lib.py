@@ -15,8 +15,11 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libastraea_gb300.so")
-SOURCES = ["sort.cu", "build.cu", "gravity.cu", "sph.cu", "integrate.cu", "diag.cu", "render.cu", "telemetry.cu", "relax.cu", "noalloc.cu", "capi.cu"]
+SOURCES = ["sort.cu", "build.cu", "gravity.cu", "sph.cu", "integrate.cu", "diag.cu", "render.cu", "telemetry.cu", "relax.cu", "planet.cu", "noalloc.cu", "capi.cu"]
 HEADERS = ["common.cuh", "internal.h", "kernels.h"]
+# planet.cu reproduces the engine's host and device arithmetic operation for
+# operation: no multiply-add contraction on either side.
+EXTRA_FLAGS = {"planet.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 NVCC = os.environ.get("NVCC", "nvcc")
 NVCC_FLAGS = [
@@ -52,7 +55,7 @@ def build(force=False, verbose_ptxas=False):
         o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
         objs.append(o)
         if force or not os.path.exists(o) or os.path.getmtime(o) < max(dep_time, os.path.getmtime(s)):
-            flags = list(NVCC_FLAGS)
+            flags = list(NVCC_FLAGS) + EXTRA_FLAGS.get(src, [])
             if verbose_ptxas:
                 flags += ["-Xptxas", "-v"]
             jobs.append([NVCC] + flags + ["-c", s, "-o", o])

@@ -734,6 +734,60 @@ AstraeaStatus astraea_gb300_direct_gravity_f64(const AstraeaParticles* p, const 
     return ASTRAEA_OK;
 }
 
+// ------------------------------------------------------ planet building
+static planet::BodySpec toBodySpec(const AstraeaBodySpec& s) {
+    return planet::BodySpec{static_cast<int>(s.archetype > 5u ? 99u : s.archetype), s.massKg, s.surfaceTempK,
+                            s.coreTempK, s.spinOmegaRadS};
+}
+
+AstraeaStatus astraea_gb300_solve_hydrostatic(const AstraeaBodySpec* spec, AstraeaRadialSample* profile,
+                                              uint32_t capacity, uint32_t* outCount, double* outRadiusM,
+                                              double* outCentralPressurePa) {
+    if (spec == nullptr || outCount == nullptr || outRadiusM == nullptr || outCentralPressurePa == nullptr)
+        return fail(ASTRAEA_ERR_INVALID, "null argument");
+    std::vector<planet::Sample> prof;
+    double radius = 0.0, pc = 0.0;
+    std::string err;
+    if (!planet::solveHydrostatic(toBodySpec(*spec), prof, radius, pc, &err))
+        return fail(ASTRAEA_ERR_INVALID, "solve_hydrostatic: " + err);
+    *outCount = static_cast<uint32_t>(prof.size());
+    *outRadiusM = radius;
+    *outCentralPressurePa = pc;
+    if (profile == nullptr || capacity < prof.size())
+        return fail(ASTRAEA_ERR_CAPACITY, "solve_hydrostatic: profile capacity below the sample count");
+    for (size_t i = 0; i < prof.size(); ++i) {
+        const planet::Sample& s = prof[i];
+        profile[i] = AstraeaRadialSample{s.r, s.rho, s.P, s.M, s.T, static_cast<uint32_t>(s.mat), 0u};
+    }
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_build_planet(const AstraeaBodySpec* spec, uint32_t particleCount, uint32_t bodyId,
+                                         uint32_t tracerGridRes, uint64_t seed, AstraeaParticles* p, uint32_t offset,
+                                         AstraeaPlanetInfo* info) {
+    if (spec == nullptr || p == nullptr || info == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    if (particleCount == 0u) return fail(ASTRAEA_ERR_INVALID, "build_planet: particleCount must be > 0");
+    if (bodyId > 255u) return fail(ASTRAEA_ERR_INVALID, "build_planet: bodyId must fit in 8 bits");
+    if (tracerGridRes > 1024u) return fail(ASTRAEA_ERR_INVALID, "build_planet: tracerGridRes above 1024");
+    if (static_cast<uint64_t>(offset) + particleCount > p->capacity)
+        return fail(ASTRAEA_ERR_CAPACITY, "build_planet: offset + particleCount exceeds the buffer capacity");
+#define AG_NONNULL(f) if (p->f == nullptr) return fail(ASTRAEA_ERR_INVALID, "build_planet: null array " #f);
+    AG_ALL_PARTICLE_ARRAYS(AG_NONNULL)
+#undef AG_NONNULL
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    planet::BuildResult r{};
+    std::string err;
+    const cudaError_t e = planet::buildOnDevice(toBodySpec(*spec), particleCount, static_cast<uint8_t>(bodyId),
+                                                tracerGridRes, seed, *p, offset, ds->status, g_spinLimit.load(),
+                                                stream(), &r, &err);
+    if (!err.empty()) return fail(ASTRAEA_ERR_INVALID, "build_planet: " + err);
+    AG_CUDA(e);
+    *info = AstraeaPlanetInfo{r.radiusM, r.massKg, r.pcPa, r.tracerCount, r.profileCount, r.shellCount, 0u};
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_debug_lookback_probe(uint32_t spinLimit, uint32_t* outResult) {
     DeviceState* ds = nullptr;
     AstraeaStatus s = deviceState(&ds);

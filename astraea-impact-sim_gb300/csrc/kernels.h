@@ -2,6 +2,9 @@
 // small device helpers more than one translation unit inlines.
 #pragma once
 
+#include <string>
+#include <vector>
+
 #include "internal.h"
 
 namespace astraea_gb300 {
@@ -132,5 +135,30 @@ cudaError_t launchDriftPlain(const AstraeaParticles& p, uint32_t n, float dt, cu
 
 // -------------------------------------------------------------- diag.cu ---
 cudaError_t measureFp32Tflops(int sms, float* tflops, cudaStream_t st);
+
+// ------------------------------------------------------------ planet.cu ---
+namespace planet {
+struct BodySpec {
+    int archetype;            // PlanetArchetype, 0..5
+    double massKg, surfaceTempK, coreTempK, spinOmegaRadS;
+};
+struct Sample {               // RadialProfileSample (engine/planet_builder.hpp:10-17)
+    double r, rho, P, M, T;
+    int mat;
+};
+struct BuildResult {
+    double radiusM, massKg, pcPa;
+    uint32_t tracerCount, profileCount, shellCount;
+};
+bool validSpec(const BodySpec& spec, std::string* err);
+// Host only: PlanetBuilder::solveHydrostatic1D.
+bool solveHydrostatic(const BodySpec& spec, std::vector<Sample>& profile, double& radiusM, double& pcPa,
+                      std::string* err);
+// PlanetBuilder::buildPlanet into particles [offset, offset + n) of p;
+// blocks until the body is on the device.
+cudaError_t buildOnDevice(const BodySpec& spec, uint32_t n, uint8_t bodyId, uint32_t gridRes, uint64_t seed,
+                          const AstraeaParticles& p, uint32_t offset, DevStatus* status, uint32_t spinLimit,
+                          cudaStream_t st, BuildResult* out, std::string* err);
+}  // namespace planet
 
 }  // namespace astraea_gb300

@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-far-field", action="store_true", help="skip the quadrupole far-field comparison")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-planet", action="store_true", help="skip the planet-construction measurement")
     ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
                     help="far-field model of the timed steps: 0 monopole (the engine's), 1 + quadrupole")
     ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
@@ -240,6 +241,7 @@ def run_gpu(args):
     frame = frame_stages(sim, engine, torch, np, n)
     far = None if args.no_far_field else far_field_scan(sim, engine, torch, np, args, max_dt, truth)
     ens = None if (args.no_ensemble or world > 1) else ensemble_run(engine, scenarios, torch, max_dt, args.theta)
+    planet = None if (args.no_planet or world > 1) else planet_stage(engine, torch, np)
 
     # ---- e2e through the C-ABI with pinned host buffers
     e2e = None
@@ -269,6 +271,7 @@ def run_gpu(args):
         "frame_stages": frame,
         "far_field": far,
         "ensemble": ens,
+        "planet_builder": planet,
         "e2e": e2e,
     }
     out["config"]["max_dt_psu"] = max_dt
@@ -313,6 +316,47 @@ def ensemble_run(engine, scenarios, torch, max_dt, theta, replays=4):
             "eager_particle_steps_per_s": total / (eager_ms * 1e-3),
             "graph_particle_steps_per_s": total / (graph_ms * 1e-3),
             "graph_speedup": eager_ms / graph_ms}
+
+
+def planet_stage(engine, torch, np, reps=3):
+    """Scenario construction (PlanetBuilder::buildPlanet + the body upload)
+    for the two-body setups of the 1M and 16M workloads: target and
+    impactor written straight into one particle buffer by
+    astraea_gb300_build_planet (wall time, median of `reps`), against the
+    oracle's serial restatement of the reference builder on this host (one
+    run; bit-identical to the reference library where that was built)."""
+    orc = _oracle()
+    cases = {
+        "1M: LivingTerra 800k (6x16x16 tracers) + ProtoTheia 200k": [(0, 800_000, 0, 16, 42, None),
+                                                                    (5, 200_000, 1, 0, 43, 0.025 * 5.97219e24)],
+        "16M: GasGiant 14M + ProtoTheia 2M": [(4, 14_000_000, 0, 0, 42, None), (5, 2_000_000, 1, 0, 43, None)],
+    }
+    out = {}
+    for name, bodies in cases.items():
+        total = sum(b[1] for b in bodies)
+        p = engine.DeviceParticles(total)
+        times = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            off = 0
+            for a, n, body, grid, seed, mass in bodies:
+                engine.build_planet(engine.body_spec(a, mass_kg=mass), n, p, offset=off, body_id=body,
+                                    tracer_grid_res=grid, seed=seed)
+                off += n
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        del p
+        torch.cuda.empty_cache()
+        t0 = time.perf_counter()
+        for a, n, body, grid, seed, mass in bodies:
+            orc.build_planet(engine.body_spec(a, mass_kg=mass), n, body, grid, seed)
+        cpu_s = time.perf_counter() - t0
+        dev_s = float(np.median(times))
+        out[name] = {"particles": total, "device_s": dev_s, "oracle_cpu_s": cpu_s,
+                     "device_particles_per_s": total / dev_s, "cpu_particles_per_s": total / cpu_s,
+                     "speedup": cpu_s / dev_s}
+    return out
 
 
 def frame_stages(sim, engine, torch, np, n, reps=5):

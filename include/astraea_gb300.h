@@ -279,6 +279,68 @@ AstraeaStatus astraea_gb300_relax_single_body(AstraeaParticles* p, AstraeaPartic
                                               const double* anchorTempByOrigId, uint32_t anchorCount,
                                               double nominalRadiusPsu, uint32_t steps, double* outFinalVrmsOverVesc);
 
+/* ---- planet construction (engine/planet_builder.cpp:398-905) ------------ */
+
+/* BodyInitSpec (engine/types.hpp:60-67). */
+typedef struct AstraeaBodySpec {
+    uint32_t archetype;      /* PlanetArchetype: 0 LivingTerra, 1 IronCore, 2 OceanIce,
+                                3 LavaIo, 4 GasGiant, 5 ProtoTheia */
+    uint32_t relaxSteps;     /* carried for the caller; the builder ignores it */
+    double massKg;
+    double surfaceTempK;
+    double coreTempK;
+    double spinOmegaRadS;
+} AstraeaBodySpec;
+
+/* RadialProfileSample (engine/planet_builder.hpp:10-17). */
+typedef struct AstraeaRadialSample {
+    double rM;
+    double rhoKgM3;
+    double pressurePa;
+    double enclosedMassKg;
+    double tempK;
+    uint32_t material;       /* MaterialId */
+    uint32_t reserved;
+} AstraeaRadialSample;
+
+/* The scalar members of BuiltPlanetHost (engine/planet_builder.hpp:19-34). */
+typedef struct AstraeaPlanetInfo {
+    double equatorialRadiusM;
+    double actualMassKg;     /* enclosed mass of the last profile sample */
+    double centralPressurePa;
+    uint32_t tracerCount;
+    uint32_t profileSamples;
+    uint32_t shells;         /* particle shells placed */
+    uint32_t reserved;
+} AstraeaPlanetInfo;
+
+/* PlanetBuilder::solveHydrostatic1D: RK4 shooting outward from the centre
+ * with bisection on log P_c, on the host, no GPU work; thread-safe.  The
+ * profile is bit-identical to the engine's.  *outCount receives the sample
+ * count; a NULL profile or too small capacity returns ASTRAEA_ERR_CAPACITY
+ * with nothing written to profile.  massKg <= 0 or archetype > 5:
+ * ASTRAEA_ERR_INVALID (the engine throws std::invalid_argument). */
+AstraeaStatus astraea_gb300_solve_hydrostatic(const AstraeaBodySpec* spec, AstraeaRadialSample* profile,
+                                              uint32_t capacity, uint32_t* outCount, double* outRadiusM,
+                                              double* outCentralPressurePa);
+
+/* PlanetBuilder::buildPlanet followed by the engine's upload of that body
+ * (engine/simulation.cpp:468-523, 852-880), as one call that writes the
+ * body straight into particles [offset, offset + particleCount) of p: the
+ * hydrostatic profile and shell plan on the host (bit-identical to the
+ * engine's), the engine's mt19937_64 stream drawn on the host and shipped
+ * in pinned chunks, particle placement and the LivingTerra surface-tracer
+ * selection (tracerGridRes > 0, 6 G^2 bins) on the device.  Written: pos,
+ * vel and velHalf (= vel), mass, h = h0, h0, rho, u, tempK, epsFail,
+ * materialId, bodyId, originalId = offset + i, the tracer fields; zeroed:
+ * stresses, damage, damageCbrt, pressure, soundSpeed, phaseId.  p->count is
+ * not changed.  particleCount == 0 or massKg <= 0: ASTRAEA_ERR_INVALID (the
+ * engine throws); offset + particleCount > p->capacity: ASTRAEA_ERR_CAPACITY.
+ * Blocks until the body is on the device. */
+AstraeaStatus astraea_gb300_build_planet(const AstraeaBodySpec* spec, uint32_t particleCount, uint32_t bodyId,
+                                         uint32_t tracerGridRes, uint64_t seed, AstraeaParticles* p, uint32_t offset,
+                                         AstraeaPlanetInfo* info);
+
 /* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
 
 /* One Simulation::step() kernel sequence (engine/simulation.cpp:1711-1753):

@@ -100,8 +100,28 @@ def build_reference_pcls(force=False):
     return out
 
 
+def build_reference_planet(force=False):
+    """The reference's PlanetBuilder (engine/planet_builder.cpp with
+    engine/presets.cpp and engine/eos.cu as host C++) behind the C entry
+    points of oracle/ref_planet_capi.cpp; None where the checkout is absent."""
+    srcs = [os.path.join(REFERENCE_ENGINE, f) for f in ("planet_builder.cpp", "presets.cpp", "eos.cu")]
+    if not all(os.path.exists(x) for x in srcs):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libref_planet.so")
+    shim = os.path.join(HERE, "ref_planet_capi.cpp")
+    if force or _stale(out, srcs + [shim]):
+        tmp = out + ".tmp%d" % os.getpid()
+        _run(["g++"] + CXXFLAGS + ["-I", REFERENCE_ENGINE, srcs[0], srcs[1], "-x", "c++", srcs[2], "-x", "none",
+                                   shim, "-o", tmp])
+        os.replace(tmp, out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_reference_eos(force="--force" in sys.argv))
     print(build_reference_cubin(force="--force" in sys.argv))
     print(build_reference_pcls(force="--force" in sys.argv))
+    print(build_reference_planet(force="--force" in sys.argv))

@@ -20,7 +20,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <numeric>
+#include <random>
 #include <vector>
 
 #include "astraea_gb300.h"
@@ -1409,5 +1411,649 @@ void oracle_telemetry(const AstraeaParticles* p, const AstraeaTelemetryParams* p
 
 int oracle_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
 void oracle_set_group_stride(int k) { g_groupStride = k < 1 ? 1 : k; }
+
+}  // extern "C"
+
+// ======================================================== planet builder ===
+// Restates engine/planet_builder.cpp (PlanetBuilder::solveHydrostatic1D and
+// ::buildPlanet) with the archetype table of engine/presets.cpp:9-88 and the
+// host EOS helpers of engine/eos.cu:390-535, in the reference's own order of
+// operations.  Writes the body into HOST particle arrays the way the engine's
+// upload writes it (engine/simulation.cpp:468-523, 852-880).
+namespace {
+
+constexpr double kLUnitD = 1.0e6, kMUnitD = 1.0e24, kTUnitD = 1.0e3;
+constexpr double kRhoUnitD = kMUnitD / (kLUnitD * kLUnitD * kLUnitD);
+constexpr double kPUnitD = kMUnitD / (kLUnitD * kTUnitD * kTUnitD);
+constexpr double kUUnitD = (kLUnitD * kLUnitD) / (kTUnitD * kTUnitD);
+constexpr double kGSiD = 6.67430e-11;
+
+struct Layers { uint32_t count; int mat[3]; double frac[3]; };
+const Layers kArchLayers[6] = {
+    {3, {0, 1, 2}, {0.320, 0.675, 0.005}}, {2, {0, 1, 1}, {0.680, 0.320, 0.0}},
+    {3, {0, 1, 2}, {0.150, 0.450, 0.400}}, {2, {0, 1, 1}, {0.250, 0.750, 0.0}},
+    {3, {0, 1, 3}, {0.050, 0.100, 0.850}}, {3, {0, 1, 4}, {0.220, 0.580, 0.200}},
+};
+const Layers& archLayers(uint32_t a) { return kArchLayers[a > 5 ? 0 : a]; }   // presets.cpp:92-98
+
+inline double mxD(double a, double b) { return a > b ? a : b; }
+inline double clD(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// engine/eos.cu:390-442
+void fromRhoTempSI(int mat, double rhoKgM3, double tempK, double& uSi, double& pSi) {
+    const MatParams& p = kMat[matIndex(mat)];
+    const double rho = mxD(rhoKgM3, 1.0e-12);
+    const double tc = mxD(tempK, 0.0);
+    if (mat == kHH) {
+        const double uColdSi = p.kH2 * rho;
+        const double uThSi = p.cv * tc;
+        uSi = uColdSi + uThSi;
+        pSi = p.kH2 * rho * rho + (p.gamma - 1.0) * rho * uThSi;
+        return;
+    }
+    const double rhoPsu = rho / kRhoUnitD;
+    const double uColdPsu = coldEnergy(mat, rhoPsu);
+    const double uColdSi = uColdPsu * kUUnitD;
+    uSi = uColdSi + p.cv * tc;
+    const double uThExcess = mxD(0.0, uSi - uColdSi - p.cv * p.tRef);
+    const double uEosPsu = uColdPsu + uThExcess / kUUnitD;
+    const double rho0Psu = p.rho0 / kRhoUnitD;
+    const double eta = rhoPsu / rho0Psu;
+    const double mu = eta - 1.0;
+    const double Eiv = p.Eiv / kUUnitD, Ecv = p.Ecv / kUUnitD;
+    double pr;
+    if (eta >= 1.0 || uEosPsu < Eiv) {
+        pr = tillotsonCompressed(p, rhoPsu, rho0Psu, eta, mu, uEosPsu, 0.0).p;
+    } else if (uEosPsu >= Ecv) {
+        pr = tillotsonExpanded(p, rhoPsu, rho0Psu, eta, mu, uEosPsu).p;
+    } else {
+        const double pc = tillotsonCompressed(p, rhoPsu, rho0Psu, eta, mu, uEosPsu, 0.0).p;
+        const double pe = tillotsonExpanded(p, rhoPsu, rho0Psu, eta, mu, uEosPsu).p;
+        const double f = clD((uEosPsu - Eiv) / mxD(1.0e-30, Ecv - Eiv), 0.0, 1.0);
+        pr = (1.0 - f) * pc + f * pe;
+    }
+    pSi = pr * kPUnitD;
+}
+
+// engine/eos.cu:444-535
+double invertDensity(int mat, double targetPSi, double tempK, double rhoGuess) {
+    const MatParams& p = kMat[matIndex(mat)];
+    if (mat == kHH) {
+        if (targetPSi <= 0.0) return 1.0e-6;
+        const double bLin = (p.gamma - 1.0) * p.cv * mxD(tempK, 0.0);
+        const double disc = std::sqrt(bLin * bLin + 4.0 * p.kH2 * targetPSi);
+        return (2.0 * targetPSi) / mxD(1.0e-30, bLin + disc);
+    }
+    auto evalP = [&](double rho) {
+        double u = 0.0, pp = 0.0;
+        fromRhoTempSI(mat, rho, tempK, u, pp);
+        return pp;
+    };
+    double rhoStart = (rhoGuess > 0.0) ? rhoGuess : p.rho0;
+    rhoStart = clD(rhoStart, 0.05 * p.rho0, 50.0 * p.rho0);
+    double rhoLow = rhoStart, rhoHigh = rhoStart;
+    const double pStart = evalP(rhoStart);
+    if (pStart > targetPSi) {
+        for (int i = 0; i < 64; ++i) {
+            rhoLow *= (i < 12) ? 0.85 : 0.5;
+            if (rhoLow < 1.0e-6) rhoLow = 1.0e-6;
+            if (evalP(rhoLow) <= targetPSi || rhoLow <= 1.0e-6) break;
+        }
+    } else if (pStart < targetPSi) {
+        for (int i = 0; i < 64; ++i) {
+            rhoHigh *= (i < 12) ? 1.25 : 2.0;
+            if (evalP(rhoHigh) >= targetPSi || rhoHigh > 1.0e8) break;
+        }
+    } else {
+        return rhoStart;
+    }
+    double fLow = evalP(rhoLow) - targetPSi;
+    double fHigh = evalP(rhoHigh) - targetPSi;
+    if (fLow >= 0.0) return rhoLow;
+    if (fHigh <= 0.0) return rhoHigh;
+    double rho = 0.5 * (rhoLow + rhoHigh);
+    for (int iter = 0; iter < 64; ++iter) {
+        const double fMid = evalP(rho) - targetPSi;
+        if (std::abs(fMid) <= 1.0e-9 * mxD(1.0, std::abs(targetPSi))) return rho;
+        if (fMid < 0.0) { rhoLow = rho; fLow = fMid; } else { rhoHigh = rho; fHigh = fMid; }
+        if (rhoHigh - rhoLow <= 1.0e-12 * mxD(1.0, rho)) return 0.5 * (rhoLow + rhoHigh);
+        double nextRho = 0.5 * (rhoLow + rhoHigh);
+        const double denom = fHigh - fLow;
+        if (std::abs(denom) > 1.0e-30) {
+            const double secant = rhoLow - fLow * (rhoHigh - rhoLow) / denom;
+            if (secant > rhoLow && secant < rhoHigh) nextRho = secant;
+        }
+        rho = nextRho;
+    }
+    return 0.5 * (rhoLow + rhoHigh);
+}
+
+struct PSample { double r, rho, P, M, T; int mat; };
+
+// planet_builder.cpp:21-46
+double densityOnGeotherm(const AstraeaBodySpec& s, int mat, double P, double pc, double pSurf, double guess,
+                         double& outT) {
+    const double denom = std::max(pc - pSurf, 1.0);
+    const double pFrac = std::clamp((P - pSurf) / denom, 0.0, 1.0);
+    outT = s.surfaceTempK + (s.coreTempK - s.surfaceTempK) * pFrac;
+    double rho = invertDensity(mat, std::max(P, 0.0), outT, guess);
+    if (mat == kHH) rho = std::max(rho, 1.0e-3);
+    return rho;
+}
+
+struct ShootRes { double radius = 0.0, mass = 0.0; bool cap = false; std::vector<PSample> prof; };
+
+// planet_builder.cpp:55-264
+ShootRes shootOutward(const AstraeaBodySpec& s, double pc, double pSurf, double drM, bool rec) {
+    ShootRes res;
+    const Layers& comp = archLayers(s.archetype);
+    const double target = s.massKg;
+    const double bail = 20.0 * target;
+    double layerEnd[3] = {};
+    double cum = 0.0;
+    for (uint32_t i = 0; i < comp.count; ++i) {
+        cum += comp.frac[i];
+        layerEnd[i] = (i + 1 == comp.count) ? std::numeric_limits<double>::infinity() : (cum * target);
+    }
+    uint32_t li = 0;
+    double r = 0.0, P = pc, M = 0.0;
+    const int mat0 = comp.mat[0];
+    double t0 = s.coreTempK;
+    double guess = kMat[matIndex(mat0)].rho0;
+    double rho = densityOnGeotherm(s, mat0, P, pc, pSurf, guess, t0);
+    guess = rho;
+    if (rec) res.prof.push_back({0.0, rho, P, 0.0, t0, mat0});
+    auto deriv = [&](int mat, double rv, double pv, double mv, double hint, double& dP, double& dM) {
+        double tk = t0;
+        const double rl = densityOnGeotherm(s, mat, pv, pc, pSurf, hint, tk);
+        dM = 4.0 * kPiD * rv * rv * rl;
+        if (rv <= 1.0e-9) dP = -(4.0 / 3.0) * kPiD * kGSiD * rl * rl * rv;
+        else dP = -kGSiD * mv * rl / (rv * rv);
+        return rl;
+    };
+    auto rk4 = [&](int mat, double r0, double p0, double m0, double h, double hint, double& oP, double& oM) {
+        double k1P = 0, k1M = 0, k2P = 0, k2M = 0, k3P = 0, k3M = 0, k4P = 0, k4M = 0;
+        const double r1 = deriv(mat, r0, p0, m0, hint, k1P, k1M);
+        const double r2 = deriv(mat, r0 + 0.5 * h, std::max(pSurf, p0 + 0.5 * h * k1P), m0 + 0.5 * h * k1M, r1, k2P, k2M);
+        const double r3 = deriv(mat, r0 + 0.5 * h, std::max(pSurf, p0 + 0.5 * h * k2P), m0 + 0.5 * h * k2M, r2, k3P, k3M);
+        deriv(mat, r0 + h, std::max(pSurf, p0 + h * k3P), m0 + h * k3M, r3, k4P, k4M);
+        oP = p0 + (h / 6.0) * (k1P + 2.0 * k2P + 2.0 * k3P + k4P);
+        oM = m0 + (h / 6.0) * (k1M + 2.0 * k2M + 2.0 * k3M + k4M);
+    };
+    for (int step = 0; step < 12000; ++step) {
+        const int mat = comp.mat[li];
+        const double h = (s.archetype == 4 && li + 1 < comp.count) ? (0.25 * drM) : drM;
+        double nP = P, nM = M;
+        if (r == 0.0) {
+            nP = P - (2.0 / 3.0) * kPiD * kGSiD * rho * rho * h * h;
+            nM = (4.0 / 3.0) * kPiD * rho * h * h * h;
+        } else {
+            rk4(mat, r, P, M, h, guess, nP, nM);
+        }
+        const bool cS = nP <= pSurf;
+        const bool cL = (li + 1 < comp.count) && (nM >= layerEnd[li]);
+        const double fP = cS ? ((P - nP > 1.0e-30) ? std::clamp((P - pSurf) / (P - nP), 0.0, 1.0) : 1.0) : 2.0;
+        const double fM = cL ? ((nM - M > 1.0e-30) ? std::clamp((layerEnd[li] - M) / (nM - M), 0.0, 1.0) : 1.0) : 2.0;
+        if (cS && (!cL || fP <= fM)) {
+            double rS = r + fP * h, mS = M;
+            if (r == 0.0) {
+                const double dp = std::max(0.0, P - pSurf);
+                const double rA = std::sqrt(dp / ((2.0 / 3.0) * kPiD * kGSiD * rho * rho));
+                rS = std::min(h, rA);
+                mS = (4.0 / 3.0) * kPiD * rho * rS * rS * rS;
+            } else {
+                double d = 0.0;
+                rk4(mat, r, P, M, fP * h, guess, d, mS);
+            }
+            if (rec) {
+                double tS = s.surfaceTempK;
+                const double rhoS = densityOnGeotherm(s, mat, pSurf, pc, pSurf, guess, tS);
+                res.prof.push_back({rS, rhoS, pSurf, mS, tS, mat});
+            }
+            res.radius = rS; res.mass = mS;
+            return res;
+        }
+        if (cL) {
+            const double mB = layerEnd[li];
+            double sub = 0.0;
+            if (r == 0.0) {
+                sub = std::cbrt((3.0 * mB) / (4.0 * kPiD * rho));
+                sub = std::clamp(sub, 0.0, h);
+                nP = P - (2.0 / 3.0) * kPiD * kGSiD * rho * rho * sub * sub;
+                nM = mB;
+            } else {
+                double lo = 0.0, hi = h;
+                sub = fM * h;
+                for (int it = 0; it < 4; ++it) {
+                    rk4(mat, r, P, M, sub, guess, nP, nM);
+                    if (std::abs(nM - mB) <= 1.0e-10 * target) break;
+                    if (nM < mB) lo = sub; else hi = sub;
+                    sub = 0.5 * (lo + hi);
+                }
+                rk4(mat, r, P, M, sub, guess, nP, nM);
+            }
+            if (nP <= pSurf) {
+                const double den = P - nP;
+                const double sf = (den > 1.0e-30) ? std::clamp((P - pSurf) / den, 0.0, 1.0) : 1.0;
+                const double rS = r + sf * sub;
+                double d = 0.0, mS = M;
+                rk4(mat, r, P, M, sf * sub, guess, d, mS);
+                if (rec) {
+                    double tS = s.surfaceTempK;
+                    const double rhoS = densityOnGeotherm(s, mat, pSurf, pc, pSurf, guess, tS);
+                    res.prof.push_back({rS, rhoS, pSurf, mS, tS, mat});
+                }
+                res.radius = rS; res.mass = mS;
+                return res;
+            }
+            r += sub; P = nP; M = mB;
+            if (rec) {
+                double tE = 0.0;
+                const double rhoE = densityOnGeotherm(s, mat, P, pc, pSurf, guess, tE);
+                res.prof.push_back({r, rhoE, P, M, tE, mat});
+            }
+            ++li;
+            const int nm = comp.mat[li];
+            double tN = 0.0;
+            guess = kMat[matIndex(nm)].rho0;
+            rho = densityOnGeotherm(s, nm, P, pc, pSurf, guess, tN);
+            guess = rho;
+            if (rec) res.prof.push_back({r, rho, P, M, tN, nm});
+            continue;
+        }
+        r += h; P = nP; M = nM;
+        double tC = s.coreTempK;
+        rho = densityOnGeotherm(s, mat, P, pc, pSurf, guess, tC);
+        guess = rho;
+        if (rec) res.prof.push_back({r, rho, P, M, tC, mat});
+        if (M > bail) { res.radius = r; res.mass = M; res.cap = true; return res; }
+    }
+    res.radius = r; res.mass = M;
+    return res;
+}
+
+// planet_builder.cpp:398-473
+bool solveHydrostatic(const AstraeaBodySpec& s, std::vector<PSample>& prof, double& radius, double& pcOut) {
+    if (!(s.massKg > 0.0) || s.archetype > 5) return false;
+    const Layers& comp = archLayers(s.archetype);
+    const double pSurf = (s.archetype == 4) ? 1.0e5 : 0.0;
+    double invRho = 0.0;
+    for (uint32_t i = 0; i < comp.count; ++i) {
+        double rho0 = kMat[matIndex(comp.mat[i])].rho0;
+        if (comp.mat[i] == kHH) rho0 = 600.0;
+        invRho += comp.frac[i] / std::max(rho0, 1.0);
+    }
+    const double rhoEst = 1.0 / std::max(invRho, 1.0e-6);
+    double rEst = std::cbrt((3.0 * s.massKg) / (4.0 * kPiD * rhoEst));
+    if (s.archetype == 4) rEst = std::max(rEst, 6.5e7);
+    const double drM = std::max(rEst / 800.0, 1.0e2);
+    const double pEst = (3.0 * kGSiD * s.massKg * s.massKg) / (8.0 * kPiD * rEst * rEst * rEst * rEst);
+    double lo = std::log(std::max(pSurf + 1.0e4, 1.0e-3 * pEst));
+    double hi = std::log(std::max(pSurf + 1.0e6, 1.0e3 * pEst));
+    for (int i = 0; i < 20; ++i) {
+        const ShootRes r = shootOutward(s, std::exp(lo), pSurf, drM, false);
+        if (!r.cap && r.mass <= s.massKg) break;
+        lo -= 2.0;
+    }
+    for (int i = 0; i < 20; ++i) {
+        const ShootRes r = shootOutward(s, std::exp(hi), pSurf, drM, false);
+        if (r.cap || r.mass >= s.massKg) break;
+        hi += 2.0;
+    }
+    double mid = 0.5 * (lo + hi);
+    for (int it = 0; it < 60; ++it) {
+        mid = 0.5 * (lo + hi);
+        const ShootRes r = shootOutward(s, std::exp(mid), pSurf, drM, false);
+        const double rel = (r.mass - s.massKg) / s.massKg;
+        if (!r.cap && std::abs(rel) <= 1.0e-6) break;
+        if (r.cap || r.mass > s.massKg) hi = mid; else lo = mid;
+        if (hi - lo < 1.0e-12) break;
+    }
+    pcOut = std::exp(mid);
+    ShootRes fin = shootOutward(s, pcOut, pSurf, drM, true);
+    radius = fin.radius;
+    prof = std::move(fin.prof);
+    return !prof.empty();
+}
+
+// planet_builder.cpp:267-300
+PSample atMass(const std::vector<PSample>& prof, double m) {
+    if (prof.empty()) return PSample{0, 0, 0, 0, 0, 1};
+    if (m <= prof.front().M) return prof.front();
+    if (m >= prof.back().M) return prof.back();
+    auto it = std::lower_bound(prof.begin(), prof.end(), m, [](const PSample& a, double v) { return a.M < v; });
+    if (it == prof.begin()) return *it;
+    const PSample& h = *it;
+    const PSample& l = *(it - 1);
+    const double dm = h.M - l.M;
+    const double t = (dm > 1.0e-30) ? std::clamp((m - l.M) / dm, 0.0, 1.0) : 0.0;
+    PSample o;
+    o.r = l.r + t * (h.r - l.r);
+    o.rho = l.rho + t * (h.rho - l.rho);
+    o.P = l.P + t * (h.P - l.P);
+    o.M = m;
+    o.T = l.T + t * (h.T - l.T);
+    o.mat = (t < 0.5) ? l.mat : h.mat;
+    return o;
+}
+
+// planet_builder.cpp:329-396
+void faceUvToNormal(uint32_t face, float u, float v, float& nx, float& ny, float& nz) {
+    const float sx = 2.0f * u - 1.0f, sy = 2.0f * v - 1.0f;
+    float vx = 0.0f, vy = 0.0f, vz = 0.0f;
+    switch (face % 6u) {
+        case 0: vx = 1.0f; vy = sy; vz = -sx; break;
+        case 1: vx = -1.0f; vy = sy; vz = sx; break;
+        case 2: vx = sx; vy = 1.0f; vz = -sy; break;
+        case 3: vx = sx; vy = -1.0f; vz = sy; break;
+        case 4: vx = sx; vy = sy; vz = 1.0f; break;
+        case 5: vx = -sx; vy = sy; vz = -1.0f; break;
+    }
+    const float inv = 1.0f / std::sqrt(vx * vx + vy * vy + vz * vz);
+    nx = vx * inv; ny = vy * inv; nz = vz * inv;
+}
+
+void normalToFaceUv(float nx, float ny, float nz, uint32_t& face, float& u, float& v) {
+    const float ax = std::abs(nx), ay = std::abs(ny), az = std::abs(nz);
+    float sx = 0.0f, sy = 0.0f;
+    if (ax >= ay && ax >= az) {
+        const float d = std::max(ax, 1.0e-12f);
+        if (nx >= 0.0f) { face = 0; sx = -nz / d; sy = ny / d; } else { face = 1; sx = nz / d; sy = ny / d; }
+    } else if (ay >= ax && ay >= az) {
+        const float d = std::max(ay, 1.0e-12f);
+        if (ny >= 0.0f) { face = 2; sx = nx / d; sy = -nz / d; } else { face = 3; sx = nx / d; sy = nz / d; }
+    } else {
+        const float d = std::max(az, 1.0e-12f);
+        if (nz >= 0.0f) { face = 4; sx = nx / d; sy = ny / d; } else { face = 5; sx = -nx / d; sy = ny / d; }
+    }
+    u = std::clamp(0.5f * (sx + 1.0f), 0.0f, 1.0f);
+    v = std::clamp(0.5f * (sy + 1.0f), 0.0f, 1.0f);
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_solve_hydrostatic(const AstraeaBodySpec* s, AstraeaRadialSample* out, uint32_t cap, uint32_t* count,
+                             double* radius, double* pc) {
+    std::vector<PSample> prof;
+    if (!solveHydrostatic(*s, prof, *radius, *pc)) return ASTRAEA_ERR_INVALID;
+    *count = static_cast<uint32_t>(prof.size());
+    if (out == nullptr || cap < prof.size()) return ASTRAEA_ERR_CAPACITY;
+    for (size_t i = 0; i < prof.size(); ++i)
+        out[i] = AstraeaRadialSample{prof[i].r, prof[i].rho, prof[i].P, prof[i].M, prof[i].T,
+                                     static_cast<uint32_t>(prof[i].mat), 0u};
+    return ASTRAEA_OK;
+}
+
+// planet_builder.cpp:475-905 into HOST arrays [offset, offset + n) of p.
+// stableTies = 0 orders tracer candidates with std::sort as the engine does;
+// 1 keeps particle order among equal radii (std::stable_sort).
+int oracle_build_planet(const AstraeaBodySpec* spec, uint32_t n, uint32_t bodyId, uint32_t grid, uint64_t seed,
+                        int stableTies, AstraeaParticles* p, uint32_t offset, AstraeaPlanetInfo* info) {
+    if (n == 0) return ASTRAEA_ERR_INVALID;
+    std::vector<PSample> prof;
+    double radius = 0.0, pcPa = 0.0;
+    if (!solveHydrostatic(*spec, prof, radius, pcPa)) return ASTRAEA_ERR_INVALID;
+    const double actualMass = prof.back().M;
+    const Layers& comp = archLayers(spec->archetype);
+    const uint32_t L = comp.count;
+    uint32_t layerN[3] = {};
+    double cumEnd[3] = {};
+    double cumFrac = 0.0;
+    uint32_t given = 0;
+    for (uint32_t k = 0; k < L; ++k) {
+        cumFrac += comp.frac[k];
+        cumEnd[k] = (k + 1 == L) ? actualMass : (cumFrac * actualMass);
+        if (k + 1 == L) {
+            layerN[k] = n - given;
+        } else {
+            uint32_t c = static_cast<uint32_t>(std::llround(comp.frac[k] * n));
+            if (n >= L && c == 0) c = 1;
+            const uint32_t maxAvail = n - given - ((n >= L) ? (L - 1 - k) : 0u);
+            c = std::min(c, maxAvail);
+            layerN[k] = c;
+            given += c;
+        }
+    }
+    std::mt19937_64 rng(seed ^ (static_cast<uint64_t>(static_cast<uint8_t>(bodyId)) * 0x9e3779b97f4a7c15ULL));
+    std::uniform_real_distribution<double> u01(1.0e-6, 1.0 - 1.0e-6);
+    const double nominalMass = actualMass / static_cast<double>(n);
+    const double golden = kPiD * (3.0 - std::sqrt(5.0));
+    uint32_t g = 0, shellsPlaced = 0;
+    double mStart = 0.0;
+    for (uint32_t k = 0; k < L; ++k) {
+        const uint32_t nk = layerN[k];
+        const double mEnd = cumEnd[k];
+        if (nk == 0) { mStart = mEnd; continue; }
+        const double layerTotal = std::max(mEnd - mStart, 0.0);
+        const double pMassKg = layerTotal / static_cast<double>(nk);
+        const double pMassPsu = pMassKg / kMUnitD;
+        const int mat = comp.mat[k];
+        const MatParams& ep = kMat[matIndex(mat)];
+        const PSample sIn = atMass(prof, mStart);
+        const PSample sOut = atMass(prof, mEnd);
+        std::vector<double> bounds{mStart};
+        double curM = mStart, curR = sIn.r;
+        if (k == 0 && nk >= 2 && sOut.r > 0.0) {
+            const double cM = std::min(mStart + pMassKg, mEnd);
+            const double cR = std::cbrt((3.0 * cM) / (4.0 * kPiD * std::max(sIn.rho, 1.0e-3)));
+            if (cM < mEnd && cR < sOut.r) { bounds.push_back(cM); curM = cM; curR = cR; }
+        }
+        auto massAtR = [&](double rT) {
+            auto it = std::lower_bound(prof.begin(), prof.end(), rT, [](const PSample& a, double v) { return a.r < v; });
+            double mv = mEnd;
+            if (it != prof.end() && it != prof.begin()) {
+                const PSample& h = *it;
+                const PSample& l = *(it - 1);
+                const double dr = h.r - l.r;
+                const double t = (dr > 1.0e-30) ? std::clamp((rT - l.r) / dr, 0.0, 1.0) : 0.0;
+                mv = l.M + t * (h.M - l.M);
+            }
+            return std::clamp(mv, curM + 1.0e-9 * layerTotal, mEnd);
+        };
+        while (curM < mEnd) {
+            const PSample sc = atMass(prof, curM);
+            const double spacing = std::cbrt(nominalMass / std::max(sc.rho, 1.0e-3));
+            const double stepR = (k == 0 && nk >= 64 && curR < 3.5 * spacing) ? (0.62 * spacing) : spacing;
+            const double nextR = curR + stepR;
+            if (nextR >= sOut.r - 0.35 * stepR) { bounds.push_back(mEnd); break; }
+            const double nextM = massAtR(nextR);
+            bounds.push_back(nextM);
+            if (nextM >= mEnd) break;
+            curM = nextM; curR = nextR;
+        }
+        if (bounds.size() < 2) bounds.push_back(mEnd);
+        if (bounds.size() == 2 && nk >= 128 && sOut.r > sIn.r) {
+            const double avgRho = std::max(0.5 * (sIn.rho + sOut.rho), 1.0e-3);
+            const double lsp = std::cbrt(nominalMass / avgRho);
+            if ((sOut.r - sIn.r) > 0.25 * lsp) {
+                bounds.clear();
+                bounds.push_back(mStart);
+                curM = mStart;
+                for (size_t sub = 1; sub < 3; ++sub) {
+                    const double fr = static_cast<double>(sub) / static_cast<double>(3);
+                    const double nextM = massAtR(sIn.r + fr * (sOut.r - sIn.r));
+                    if (nextM > curM && nextM < mEnd) { bounds.push_back(nextM); curM = nextM; }
+                }
+                bounds.push_back(mEnd);
+            }
+        }
+        const size_t S = bounds.size() - 1;
+        std::vector<uint32_t> cnt(S, 0);
+        std::vector<double> rem(S, 0.0);
+        uint32_t sum = 0;
+        for (size_t s = 0; s < S; ++s) {
+            const double dm = bounds[s + 1] - bounds[s];
+            const double ex = (layerTotal > 0.0) ? (static_cast<double>(nk) * (dm / layerTotal)) : 0.0;
+            const uint32_t fl = static_cast<uint32_t>(std::floor(ex));
+            cnt[s] = fl; rem[s] = ex - static_cast<double>(fl); sum += fl;
+        }
+        if (sum < nk) {
+            std::vector<size_t> idx(S);
+            std::iota(idx.begin(), idx.end(), 0);
+            std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return rem[a] > rem[b]; });
+            for (uint32_t r = 0; r < nk - sum; ++r) cnt[idx[r % S]] += 1;
+        }
+        for (size_t s = 0; s < S; ++s) {
+            const uint32_t ns = cnt[s];
+            if (ns == 0) continue;
+            ++shellsPlaced;
+            const double mMid = 0.5 * (bounds[s] + bounds[s + 1]);
+            const PSample smp = atMass(prof, mMid);
+            const double rShell = (s == 0 && k == 0 && ns == 1) ? 0.0 : smp.r;
+            const double rho = std::max(smp.rho, 1.0e-3);
+            const double tK = smp.T;
+            double uSi = 0.0, pSi = 0.0;
+            fromRhoTempSI(mat, rho, tK, uSi, pSi);
+            const double rPsu = rShell / kLUnitD;
+            const double rhoPsu = rho / kRhoUnitD;
+            const double uPsu = uSi / kUUnitD;
+            const double h0Psu = 1.2 * std::cbrt(pMassPsu / rhoPsu);
+            // Shoemake rotation, planet_builder.cpp:303-326
+            std::uniform_real_distribution<double> r01(0.0, 1.0);
+            const double q1 = r01(rng);
+            const double q2 = 2.0 * kPiD * r01(rng);
+            const double q3 = 2.0 * kPiD * r01(rng);
+            const double s1 = std::sqrt(std::max(0.0, 1.0 - q1)), s2 = std::sqrt(std::max(0.0, q1));
+            const double qx = s1 * std::sin(q2), qy = s1 * std::cos(q2), qz = s2 * std::sin(q3), qw = s2 * std::cos(q3);
+            const double xx = qx * qx, yy = qy * qy, zz = qz * qz, xy = qx * qy, xz = qx * qz, yz = qy * qz;
+            const double wx = qw * qx, wy = qw * qy, wz = qw * qz;
+            const double rot[9] = {1.0 - 2.0 * (yy + zz), 2.0 * (xy - wz), 2.0 * (xz + wy),
+                                   2.0 * (xy + wz), 1.0 - 2.0 * (xx + zz), 2.0 * (yz - wx),
+                                   2.0 * (xz - wy), 2.0 * (yz + wx), 1.0 - 2.0 * (xx + yy)};
+            for (uint32_t q = 0; q < ns; ++q) {
+                double px = 0.0, py = 0.0, pz = 0.0;
+                if (rPsu > 0.0) {
+                    const double zl = (ns == 1) ? 1.0 : (1.0 - 2.0 * (static_cast<double>(q) + 0.5) / static_cast<double>(ns));
+                    const double rxy = std::sqrt(std::max(0.0, 1.0 - zl * zl));
+                    const double th = golden * static_cast<double>(q);
+                    const double ux = rxy * std::cos(th), uy = rxy * std::sin(th), uz = zl;
+                    px = rPsu * (rot[0] * ux + rot[1] * uy + rot[2] * uz);
+                    py = rPsu * (rot[3] * ux + rot[4] * uy + rot[5] * uz);
+                    pz = rPsu * (rot[6] * ux + rot[7] * uy + rot[8] * uz);
+                }
+                const double vx = spec->spinOmegaRadS * kTUnitD * pz;
+                const double vz = -spec->spinOmegaRadS * kTUnitD * px;
+                const double wDraw = -std::log(u01(rng));
+                const double ws = std::clamp(std::pow(std::max(wDraw, 1.0e-6), 1.0 / 9.0), 1.0, 3.0);
+                const uint32_t o = offset + g++;
+                p->posX[o] = static_cast<float>(px); p->posY[o] = static_cast<float>(py); p->posZ[o] = static_cast<float>(pz);
+                p->velX[o] = static_cast<float>(vx); p->velY[o] = 0.0f; p->velZ[o] = static_cast<float>(vz);
+                p->velHalfX[o] = p->velX[o]; p->velHalfY[o] = 0.0f; p->velHalfZ[o] = p->velZ[o];
+                p->mass[o] = static_cast<float>(pMassPsu);
+                p->h0[o] = static_cast<float>(h0Psu); p->h[o] = p->h0[o];
+                p->rho[o] = static_cast<float>(rhoPsu);
+                p->u[o] = static_cast<float>(uPsu);
+                p->tempK[o] = static_cast<float>(tK);
+                p->epsFail[o] = static_cast<float>(ep.epsFailMin * ws);
+                p->sXX[o] = p->sYY[o] = p->sZZ[o] = p->sXY[o] = p->sXZ[o] = p->sYZ[o] = 0.0f;
+                p->damage[o] = 0.0f; p->damageCbrt[o] = 0.0f;
+                p->pressure[o] = 0.0f; p->soundSpeed[o] = 0.0f; p->phaseId[o] = 0;
+                p->materialId[o] = static_cast<uint8_t>(mat);
+                p->bodyId[o] = static_cast<uint8_t>(bodyId);
+                p->originalId[o] = o;
+                p->tracerIndex[o] = -1;
+                p->tracerRestRadiusPsu[o] = 0.0f;
+                p->tracerRestNormalX[o] = p->tracerRestNormalY[o] = p->tracerRestNormalZ[o] = 0.0f;
+                p->tracerIsOcean[o] = 0;
+            }
+        }
+        mStart = mEnd;
+    }
+    if (g != n) return ASTRAEA_ERR_INVALID;
+
+    // surface tracers, planet_builder.cpp:735-902
+    uint32_t tracerCount = 0;
+    const uint32_t T = 6u * grid * grid;
+    if (spec->archetype == 0 && grid > 0 && n >= T) {
+        std::vector<uint32_t> cand;
+        std::vector<float> radii(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            const float x = p->posX[offset + i], y = p->posY[offset + i], z = p->posZ[offset + i];
+            radii[i] = std::sqrt(x * x + y * y + z * z);
+            if (radii[i] > 1.0e-6f) cand.push_back(i);
+        }
+        auto byRadius = [&](uint32_t a, uint32_t b) { return radii[a] > radii[b]; };
+        if (stableTies) std::stable_sort(cand.begin(), cand.end(), byRadius);
+        else std::sort(cand.begin(), cand.end(), byRadius);
+        if (cand.size() < T)
+            for (uint32_t i = 0; i < n && cand.size() < T; ++i)
+                if (radii[i] <= 1.0e-6f) cand.push_back(i);
+        if (!cand.empty()) {
+            const float rMax = radii[cand.front()];
+            const float drSurf = p->h0[offset + cand.front()];
+            size_t pool = 0;
+            const size_t minPool = std::min(cand.size(), static_cast<size_t>(T) * 3u);
+            for (; pool < cand.size(); ++pool) {
+                const uint32_t pid = cand[pool];
+                const bool inShell = (radii[pid] >= rMax - 1.8f * drSurf) || (p->materialId[offset + pid] == 2);
+                if (!inShell && pool >= minPool) break;
+            }
+            if (pool < T) pool = std::min(cand.size(), static_cast<size_t>(T));
+            cand.resize(pool);
+            std::vector<float> cx(pool), cy(pool), cz(pool), tx(T), ty(T), tz(T);
+            std::vector<uint8_t> used(pool, 0), filled(T, 0);
+            std::vector<std::vector<uint32_t>> bins(T);
+            for (size_t c = 0; c < pool; ++c) {
+                const uint32_t pid = cand[c];
+                if (radii[pid] > 1.0e-6f) {
+                    const float inv = 1.0f / radii[pid];
+                    cx[c] = p->posX[offset + pid] * inv; cy[c] = p->posY[offset + pid] * inv; cz[c] = p->posZ[offset + pid] * inv;
+                } else {
+                    cx[c] = 0.0f; cy[c] = 0.0f; cz[c] = 1.0f;
+                }
+                uint32_t face = 0;
+                float u = 0.0f, v = 0.0f;
+                normalToFaceUv(cx[c], cy[c], cz[c], face, u, v);
+                const uint32_t gx = std::min(grid - 1u, static_cast<uint32_t>(u * static_cast<float>(grid)));
+                const uint32_t gy = std::min(grid - 1u, static_cast<uint32_t>(v * static_cast<float>(grid)));
+                bins[face * grid * grid + gy * grid + gx].push_back(static_cast<uint32_t>(c));
+            }
+            auto assign = [&](uint32_t b, size_t c) {
+                const uint32_t o = offset + cand[c];
+                used[c] = 1; filled[b] = 1; ++tracerCount;
+                p->tracerIndex[o] = static_cast<int32_t>(b);
+                p->tracerRestRadiusPsu[o] = radii[cand[c]];
+                p->tracerRestNormalX[o] = cx[c]; p->tracerRestNormalY[o] = cy[c]; p->tracerRestNormalZ[o] = cz[c];
+                p->tracerIsOcean[o] = (p->materialId[o] == 2) ? 1 : 0;
+            };
+            for (uint32_t face = 0; face < 6; ++face)
+                for (uint32_t gy = 0; gy < grid; ++gy)
+                    for (uint32_t gx = 0; gx < grid; ++gx) {
+                        const uint32_t b = face * grid * grid + gy * grid + gx;
+                        faceUvToNormal(face, (static_cast<float>(gx) + 0.5f) / static_cast<float>(grid),
+                                       (static_cast<float>(gy) + 0.5f) / static_cast<float>(grid), tx[b], ty[b], tz[b]);
+                        float best = -2.0f;
+                        size_t bc = SIZE_MAX;
+                        for (uint32_t c : bins[b]) {
+                            if (used[c]) continue;
+                            const float d = cx[c] * tx[b] + cy[c] * ty[b] + cz[c] * tz[b];
+                            if (d > best) { best = d; bc = c; }
+                        }
+                        if (bc != SIZE_MAX) assign(b, bc);
+                    }
+            for (uint32_t b = 0; b < T; ++b) {
+                if (filled[b]) continue;
+                float best = -2.0f;
+                size_t bc = SIZE_MAX;
+                for (size_t c = 0; c < pool; ++c) {
+                    if (used[c]) continue;
+                    const float d = cx[c] * tx[b] + cy[c] * ty[b] + cz[c] * tz[b];
+                    if (d > best) { best = d; bc = c; }
+                }
+                if (bc != SIZE_MAX) assign(b, bc);
+            }
+            if (tracerCount < T) {
+                int32_t next = 0;
+                for (uint32_t i = 0; i < n; ++i)
+                    if (p->tracerIndex[offset + i] >= 0) p->tracerIndex[offset + i] = next++;
+            }
+        }
+    }
+    *info = AstraeaPlanetInfo{radius, actualMass, pcPa, tracerCount, static_cast<uint32_t>(prof.size()),
+                              shellsPlaced, 0u};
+    return ASTRAEA_OK;
+}
 
 }  // extern "C"

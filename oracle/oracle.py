@@ -60,6 +60,11 @@ def load(build=True):
             "oracle_extract_tracers": [P, vp, u32, f, f, f, f, f, f],
             "oracle_pcls_frame": [P, ctypes.POINTER(abi.PclsFrameInfo), vp, ctypes.c_size_t],
             "oracle_telemetry": [P, ctypes.POINTER(abi.TelemetryParams), ctypes.POINTER(abi.Telemetry)],
+            "oracle_solve_hydrostatic": [ctypes.POINTER(abi.BodySpec), ctypes.POINTER(abi.RadialSample), u32,
+                                         ctypes.POINTER(u32), ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double)],
+            "oracle_build_planet": [ctypes.POINTER(abi.BodySpec), u32, u32, u32, ctypes.c_uint64, ctypes.c_int, P,
+                                    u32, ctypes.POINTER(abi.PlanetInfo)],
         }
         for name, args in sig.items():
             getattr(_lib, name).argtypes = args
@@ -108,6 +113,100 @@ def load_reference_pcls():
                                     ctypes.c_int, ctypes.c_uint32, ctypes.c_int, vp, sz]
     lib.ref_build_frame.restype = sz
     return lib
+
+
+PROFILE_COLUMNS = ("r", "rho", "P", "M", "T", "material")
+_SAMPLE_DTYPE = np.dtype([("r", "f8"), ("rho", "f8"), ("P", "f8"), ("M", "f8"), ("T", "f8"), ("material", "u4"),
+                          ("reserved", "u4")])
+
+
+def solve_hydrostatic(spec):
+    """The oracle's PlanetBuilder::solveHydrostatic1D: (profile columns,
+    radius [m], central pressure [Pa])."""
+    lib = load()
+    cap = 16384
+    buf = (abi.RadialSample * cap)()
+    n, r, pc = ctypes.c_uint32(0), ctypes.c_double(0.0), ctypes.c_double(0.0)
+    st = lib.oracle_solve_hydrostatic(ctypes.byref(spec), buf, cap, ctypes.byref(n), ctypes.byref(r), ctypes.byref(pc))
+    if st != 0:
+        raise RuntimeError("oracle_solve_hydrostatic status %d" % st)
+    a = np.frombuffer(buf, dtype=_SAMPLE_DTYPE, count=n.value)
+    return {k: np.array(a[k]) for k in PROFILE_COLUMNS}, r.value, pc.value
+
+
+PLANET_FIELDS = ("posX", "posY", "posZ", "velX", "velY", "velZ", "velHalfX", "velHalfY", "velHalfZ", "mass", "h",
+                 "h0", "rho", "u", "tempK", "epsFail", "materialId", "bodyId", "originalId", "tracerIndex",
+                 "tracerRestRadiusPsu", "tracerRestNormalX", "tracerRestNormalY", "tracerRestNormalZ",
+                 "tracerIsOcean")
+
+
+def build_planet(spec, n, body_id=0, grid=0, seed=42, stable_ties=False):
+    """The oracle's PlanetBuilder::buildPlanet + body upload: (state dict of
+    the fields the builder writes, info dict)."""
+    lib = load()
+    hp = HostParticles({"posX": np.zeros(n, np.float32)}, capacity=n)
+    s = hp.struct()
+    info = abi.PlanetInfo()
+    st = lib.oracle_build_planet(ctypes.byref(spec), n, body_id, grid, seed & 0xFFFFFFFFFFFFFFFF,
+                                 int(bool(stable_ties)), ctypes.byref(s), 0, ctypes.byref(info))
+    if st != 0:
+        raise RuntimeError("oracle_build_planet status %d" % st)
+    out = {k: hp.arrays[k][:n].copy() for k in PLANET_FIELDS}
+    return out, {f: getattr(info, f) for f, _ in abi.PlanetInfo._fields_ if f != "reserved"}
+
+
+def load_reference_planet():
+    """The reference's PlanetBuilder (engine/planet_builder.cpp) as a host
+    library behind oracle/ref_planet_capi.cpp (None where absent)."""
+    sys.path.insert(0, HERE)
+    import build_oracle
+    path = build_oracle.build_reference_planet()
+    if path is None or not os.path.exists(path):
+        return None
+    return ctypes.CDLL(path)
+
+
+def reference_solve_hydrostatic(lib, spec, cap=20000):
+    D = ctypes.c_double
+    cols = [np.zeros(cap) for _ in range(5)]
+    mat = np.zeros(cap, np.uint8)
+    R, Pc, sec = D(), D(), D()
+    n = lib.ref_solve_hydrostatic(int(spec.archetype), D(spec.massKg), D(spec.surfaceTempK), D(spec.coreTempK),
+                                  D(spec.spinOmegaRadS), ctypes.c_uint32(cap), *[_ptr(c) for c in cols], _ptr(mat),
+                                  ctypes.byref(R), ctypes.byref(Pc), ctypes.byref(sec))
+    prof = {k: c[:n].copy() for k, c in zip(PROFILE_COLUMNS[:5], cols)}
+    prof["material"] = mat[:n].astype(np.uint32)
+    return prof, R.value, Pc.value, sec.value
+
+
+def reference_build_planet(lib, spec, n, body_id=0, grid=0, seed=42):
+    """Runs the reference's PlanetBuilder::buildPlanet; returns (fields,
+    info) in the layout of build_planet (velHalf = vel, h = h0 and the
+    zeroed fields added as the engine's upload writes them), and the
+    reference's own wall time in info['seconds']."""
+    D = ctypes.c_double
+    names = ("posX", "posY", "posZ", "velX", "velY", "velZ", "mass", "h0", "rho", "u", "tempK", "epsFail")
+    f = {k: np.zeros(n, np.float32) for k in names}
+    t4n = ("tracerRestRadiusPsu", "tracerRestNormalX", "tracerRestNormalY", "tracerRestNormalZ")
+    t4 = {k: np.zeros(n, np.float32) for k in t4n}
+    mat, body, oce = np.zeros(n, np.uint8), np.zeros(n, np.uint8), np.zeros(n, np.uint8)
+    tidx = np.zeros(n, np.int32)
+    info = np.zeros(5)
+    fp = (ctypes.c_void_p * 12)(*[f[k].ctypes.data for k in names])
+    tp = (ctypes.c_void_p * 4)(*[t4[k].ctypes.data for k in t4n])
+    rc = lib.ref_build_planet(int(spec.archetype), D(spec.massKg), D(spec.surfaceTempK), D(spec.coreTempK),
+                              D(spec.spinOmegaRadS), ctypes.c_uint32(n), ctypes.c_uint32(body_id),
+                              ctypes.c_uint32(grid), ctypes.c_uint64(seed), fp, _ptr(mat), _ptr(body), _ptr(tidx), tp,
+                              _ptr(oce), _ptr(info))
+    if rc != 0:
+        raise RuntimeError("ref_build_planet failed")
+    out = dict(f)
+    out.update(t4)
+    out.update({"velHalfX": f["velX"].copy(), "velHalfY": f["velY"].copy(), "velHalfZ": f["velZ"].copy(),
+                "h": f["h0"].copy(), "materialId": mat, "bodyId": body, "tracerIndex": tidx, "tracerIsOcean": oce,
+                "originalId": np.arange(n, dtype=np.uint32)})
+    return out, {"equatorialRadiusM": info[0], "actualMassKg": info[1], "centralPressurePa": info[2],
+                 "tracerCount": int(info[3]), "seconds": info[4]}
 
 
 def random_render_state(n, tracer_count, seed=7):

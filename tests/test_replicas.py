@@ -39,7 +39,7 @@ def _rank_main(rank, world, port, out):
 
 def test_replica_rate_two_gloo_ranks():
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
