@@ -144,6 +144,19 @@ class PlanetInfo(ctypes.Structure):
                 ("shells", _U32), ("reserved", _U32)]
 
 
+class FarFieldConfig(ctypes.Structure):
+    _fields_ = [("thetaFar", ctypes.c_float), ("gamma", ctypes.c_float), ("gateTolerance", ctypes.c_float),
+                ("gateTargets", _U32), ("pairsPerGroup", _U32), ("reserved", _U32)]
+
+
+class FarFieldStats(ctypes.Structure):
+    _fields_ = [("calls", ctypes.c_uint64), ("fallbacks", ctypes.c_uint64), ("lastPairs", _U32), ("reserved", _U32),
+                ("lastGateRms", ctypes.c_float), ("lastLoss", ctypes.c_float)]
+
+
+FF_PARAMS = 6288
+
+
 SIGNATURES = [
     ("astraea_gb300_last_error", [], ctypes.c_char_p),
     ("astraea_gb300_abi_version", [], ctypes.c_int),
@@ -175,6 +188,16 @@ SIGNATURES = [
                                          ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     ("astraea_gb300_build_planet", [ctypes.POINTER(BodySpec), _U32, _U32, _U32, ctypes.c_uint64, _P, _U32,
                                     ctypes.POINTER(PlanetInfo)], ctypes.c_int),
+    ("astraea_gb300_ff_configure", [ctypes.POINTER(FarFieldConfig)], ctypes.c_int),
+    ("astraea_gb300_ff_collect", [_P, _B, _F, _U32, _VP, _VP, _U32, ctypes.POINTER(_U32)], ctypes.c_int),
+    ("astraea_gb300_ff_init", [ctypes.c_uint64], ctypes.c_int),
+    ("astraea_gb300_ff_fit_output_scale", [_VP, _U32], ctypes.c_int),
+    ("astraea_gb300_ff_gradients", [_VP, _VP, _U32, _VP, ctypes.POINTER(_F)], ctypes.c_int),
+    ("astraea_gb300_ff_train_step", [_VP, _VP, _U32, _F, ctypes.POINTER(_F)], ctypes.c_int),
+    ("astraea_gb300_ff_predict", [_VP, _U32, _VP], ctypes.c_int),
+    ("astraea_gb300_ff_get_params", [_VP, _U32, _VP], ctypes.c_int),
+    ("astraea_gb300_ff_set_params", [_VP, _U32, _VP], ctypes.c_int),
+    ("astraea_gb300_ff_stats", [ctypes.POINTER(FarFieldStats)], ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

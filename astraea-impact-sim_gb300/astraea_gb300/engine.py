@@ -339,6 +339,114 @@ def build_planet(spec, particle_count, p, offset=0, body_id=0, tracer_grid_res=0
     return {f: getattr(info, f) for f, _ in abi.PlanetInfo._fields_ if f != "reserved"}
 
 
+# ------------------------------------------------- learned far field (mode 2)
+def ff_configure(theta_far=0.8, gamma=0.3, gate_tolerance=0.0, gate_targets=64, pairs_per_group=64):
+    cfg = abi.FarFieldConfig(float(theta_far), float(gamma), float(gate_tolerance), int(gate_targets),
+                             int(pairs_per_group), 0)
+    abi.check(lib().astraea_gb300_ff_configure(ctypes.byref(cfg)))
+
+
+def ff_collect(p, bvh, theta=0.5, group_stride=1, capacity=1 << 20):
+    """Training rows (features, labels) as float32 CUDA tensors (rows x 16)
+    from the current tree (built in far-field mode 2)."""
+    feat = torch.empty((capacity, 16), dtype=torch.float32, device="cuda")
+    lab = torch.empty((capacity, 16), dtype=torch.float32, device="cuda")
+    cnt = ctypes.c_uint32(0)
+    s = p.struct()
+    abi.check(lib().astraea_gb300_ff_collect(ctypes.byref(s), ctypes.byref(bvh.s), float(theta), int(group_stride),
+                                             feat.data_ptr(), lab.data_ptr(), capacity, ctypes.byref(cnt)))
+    return feat[:cnt.value], lab[:cnt.value]
+
+
+def ff_init(seed=1):
+    abi.check(lib().astraea_gb300_ff_init(int(seed)))
+
+
+def ff_fit_output_scale(labels):
+    labels = labels.contiguous()
+    abi.check(lib().astraea_gb300_ff_fit_output_scale(labels.data_ptr(), labels.shape[0]))
+
+
+def ff_gradients(features, labels):
+    """(gradient of the 6,288 parameters as float32 numpy, loss)."""
+    g = np.zeros(abi.FF_PARAMS, np.float32)
+    loss = ctypes.c_float(0.0)
+    features, labels = features.contiguous(), labels.contiguous()
+    abi.check(lib().astraea_gb300_ff_gradients(features.data_ptr(), labels.data_ptr(), features.shape[0],
+                                               g.ctypes.data, ctypes.byref(loss)))
+    return g, loss.value
+
+
+def ff_train_step(features, labels, lr, want_loss=True):
+    loss = ctypes.c_float(0.0)
+    abi.check(lib().astraea_gb300_ff_train_step(features.data_ptr(), labels.data_ptr(), features.shape[0],
+                                                float(lr), ctypes.byref(loss) if want_loss else None))
+    return loss.value if want_loss else None
+
+
+def ff_predict(features):
+    features = features.contiguous()
+    out = torch.empty((features.shape[0], 16), dtype=torch.float32, device="cuda")
+    abi.check(lib().astraea_gb300_ff_predict(features.data_ptr(), features.shape[0], out.data_ptr()))
+    return out
+
+
+def ff_get_params():
+    p = np.zeros(abi.FF_PARAMS, np.float32)
+    sc = np.zeros(16, np.float32)
+    abi.check(lib().astraea_gb300_ff_get_params(p.ctypes.data, abi.FF_PARAMS, sc.ctypes.data))
+    return p, sc
+
+
+def ff_set_params(params, scale=None):
+    p = np.ascontiguousarray(params, np.float32)
+    sc = None if scale is None else np.ascontiguousarray(scale, np.float32)
+    abi.check(lib().astraea_gb300_ff_set_params(p.ctypes.data, p.size, None if sc is None else sc.ctypes.data))
+
+
+def ff_stats():
+    st = abi.FarFieldStats()
+    abi.check(lib().astraea_gb300_ff_stats(ctypes.byref(st)))
+    return {f: getattr(st, f) for f, _ in abi.FarFieldStats._fields_ if f != "reserved"}
+
+
+def train_far_field(states, theta=0.5, group_stride=1, steps=600, batch=8192, lr=2e-3, seed=1, capacity=1 << 20):
+    """Trains the mode-2 network on the GPU from the solver's own trees:
+    every state is uploaded, built in mode 2, and its recorded pairs are
+    labelled by FP64 direct sums; then `steps` Adam steps on random batches
+    (the library's forward / backward kernels).  Leaves the far-field mode
+    as it was.  Returns (rows, loss history)."""
+    feats, labs = [], []
+    for st in states:
+        n = len(st["posX"])
+        p, alt, bvh = DeviceParticles(n), DeviceParticles(n), DeviceBvh(n)
+        p.upload(st)
+        alt.count = n
+        set_far_field(2)
+        try:
+            sort_and_build_bvh(p, alt, bvh)
+            f, l = ff_collect(p, bvh, theta, group_stride, capacity)
+        finally:
+            set_far_field(0)
+        feats.append(f.clone())
+        labs.append(l.clone())
+        del p, alt, bvh
+    X = torch.cat(feats)
+    T = torch.cat(labs)
+    ff_init(seed)
+    ff_fit_output_scale(T)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    hist = []
+    for k in range(steps):
+        idx = torch.randint(0, X.shape[0], (min(batch, X.shape[0]),), device="cuda", generator=gen)
+        want = (k % 50 == 0) or k == steps - 1
+        loss = ff_train_step(X[idx].contiguous(), T[idx].contiguous(), lr, want_loss=want)
+        if want:
+            hist.append((k, loss))
+    return X.shape[0], hist
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 
@@ -381,7 +489,7 @@ def set_stream(stream):
 
 
 def set_far_field(mode):
-    """0: monopole (the engine's kernel); 1: monopole + quadrupole."""
+    """0: monopole (the engine's kernel), 1: + quadrupole, 2: + learned correction."""
     abi.check(lib().astraea_gb300_set_far_field(int(mode)))
 
 

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libastraea_gb300.so")
-SOURCES = ["sort.cu", "build.cu", "gravity.cu", "sph.cu", "integrate.cu", "diag.cu", "render.cu", "telemetry.cu", "relax.cu", "planet.cu", "noalloc.cu", "capi.cu"]
+SOURCES = ["sort.cu", "build.cu", "gravity.cu", "sph.cu", "integrate.cu", "diag.cu", "render.cu", "telemetry.cu", "relax.cu", "planet.cu", "ff.cu", "noalloc.cu", "capi.cu"]
 HEADERS = ["common.cuh", "internal.h", "kernels.h"]
 # planet.cu reproduces the engine's host and device arithmetic operation for
 # operation: no multiply-add contraction on either side.

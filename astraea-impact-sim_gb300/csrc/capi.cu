@@ -28,7 +28,7 @@ namespace {
 thread_local std::string g_lastError;
 std::atomic<cudaStream_t> g_stream{nullptr};
 std::atomic<uint32_t> g_spinLimit{1u << 22};
-std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: monopole + quadrupole
+std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: + quadrupole, 2: + learned correction
 std::mutex g_mutex;
 
 AstraeaStatus fail(AstraeaStatus s, const std::string& msg) {
@@ -96,7 +96,7 @@ struct Workspace {
     uint32_t* rawMin = nullptr;    // 2 words (inside block)
     bool treeBuilt = false;        // node records hold a tree built here
     uint32_t builtN = 0;           // particle count of that tree
-    bool momentsBuilt = false;     // ... with second moments (far-field mode 1)
+    bool momentsBuilt = false;     // ... with second moments (far-field modes 1 and 2)
     bool stepCacheValid = false;   // neighbour lists + device dt valid for the next fused step
     const void* stepToken = nullptr;
     uint32_t stepCount = 0;
@@ -237,6 +237,121 @@ AstraeaStatus checkLaunch(cudaError_t e, const char* what) {
         if (agS != ASTRAEA_OK) return agS;                           \
     } while (0)
 
+// ------------------------------------------- far-field mode 2 (learned)
+struct FfState {
+    ff::Net net{};
+    bool ready = false;            // parameters initialised or loaded
+    int adamStep = 0;
+    AstraeaFarFieldConfig cfg{0.8f, 0.3f, 0.0f, 64u, 64u, 0u};
+    uint2* pairs = nullptr;
+    uint32_t pairCap = 0;
+    float4* groups = nullptr;
+    float* groupCorr = nullptr;
+    uint32_t groupCap = 0;
+    uint32_t* word = nullptr;      // [0]: pair count
+    float* gateSum = nullptr;
+    float* pinned = nullptr;       // 4 floats / words for read-backs
+    AstraeaFarFieldStats stats{0ull, 0ull, 0u, 0u, -1.0f, 0.0f};
+};
+std::map<int, FfState> g_ff;
+
+AstraeaStatus ffState(FfState** out) {
+    FfState& f = g_ff[currentDevice()];
+    if (f.net.params == nullptr) {
+        AG_CUDA(cudaMalloc(&f.net.params, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.net.grads, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.net.adamM, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.net.adamV, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.net.outScale, ff::kOut * sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.net.loss, sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.word, 4 * sizeof(uint32_t)));
+        AG_CUDA(cudaMalloc(&f.gateSum, sizeof(float)));
+        AG_CUDA(cudaMallocHost(&f.pinned, 4 * sizeof(float)));
+        AG_CUDA(cudaMemset(f.net.params, 0, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMemset(f.net.grads, 0, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMemset(f.net.adamM, 0, ff::kParams * sizeof(float)));
+        AG_CUDA(cudaMemset(f.net.adamV, 0, ff::kParams * sizeof(float)));
+        const float ones[ff::kOut] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+        AG_CUDA(cudaMemcpy(f.net.outScale, ones, sizeof(ones), cudaMemcpyHostToDevice));
+        AG_CUDA(ff::prepareKernels());
+    }
+    *out = &f;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus ffCapacity(FfState* f, uint32_t groups) {
+    const uint64_t want = static_cast<uint64_t>(groups) * std::max<uint32_t>(1u, f->cfg.pairsPerGroup);
+    if (want > 0xFFFFFFFFull) return fail(ASTRAEA_ERR_CAPACITY, "far-field pair buffer above 2^32 entries");
+    if (f->pairCap < want) {
+        if (f->pairs) cudaFree(f->pairs);
+        f->pairs = nullptr;
+        f->pairCap = 0;
+        AG_CUDA(cudaMalloc(&f->pairs, want * sizeof(uint2)));
+        f->pairCap = static_cast<uint32_t>(want);
+    }
+    if (f->groupCap < groups) {
+        if (f->groups) cudaFree(f->groups);
+        if (f->groupCorr) cudaFree(f->groupCorr);
+        f->groups = nullptr;
+        f->groupCorr = nullptr;
+        f->groupCap = 0;
+        AG_CUDA(cudaMalloc(&f->groups, groups * sizeof(float4)));
+        AG_CUDA(cudaMalloc(&f->groupCorr, 12ull * groups * sizeof(float)));
+        f->groupCap = groups;
+    }
+    return ASTRAEA_OK;
+}
+
+// The mode-2 walk: the theta walk plus the far test; records pairs.
+AstraeaStatus ffWalk(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta, FfState* f, uint32_t stride) {
+    const uint32_t groups = (n + 31u) / 32u;
+    AstraeaStatus s = ffCapacity(f, groups);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    AG_CUDA(cudaMemsetAsync(f->word, 0, sizeof(uint32_t), st));
+    FarCapture cap{f->pairs, f->pairCap, f->word, f->groups, f->cfg.thetaFar * f->cfg.thetaFar,
+                   f->cfg.gamma * f->cfg.gamma, std::max<uint32_t>(1u, stride)};
+    AG_LAUNCH(launchGravity(*p, ws->w, n, theta, false, smCount(), st, &cap));
+    return ASTRAEA_OK;
+}
+
+// Gravity of far-field mode 2: walk, network on the recorded pairs,
+// per-member correction, and (gateTolerance > 0) the direct-sum gate with
+// fallback to the plain walk at theta.  Blocks when the gate runs.
+AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta, bool gate) {
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    if (!f->ready) return fail(ASTRAEA_ERR_INVALID, "far-field mode 2 needs network parameters (ff_init / ff_set_params)");
+    s = ffWalk(p, ws, n, theta, f, 1u);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    const uint32_t groups = (n + 31u) / 32u;
+    AG_CUDA(cudaMemsetAsync(f->groupCorr, 0, 12ull * groups * sizeof(float), st));
+    AG_LAUNCH(ff::launchApply(f->net, ws->w, f->pairs, f->word, f->pairCap, f->groups, f->groupCorr, smCount(), st));
+    AG_LAUNCH(ff::launchCorrect(*p, f->groups, f->groupCorr, n, st));
+    f->stats.calls++;
+    f->stats.lastGateRms = -1.0f;
+    if (gate && f->cfg.gateTolerance > 0.0f && n >= 2u) {
+        const uint32_t K = std::max<uint32_t>(1u, std::min(f->cfg.gateTargets, n));
+        AG_CUDA(cudaMemsetAsync(f->gateSum, 0, sizeof(float), st));
+        AG_LAUNCH(ff::launchGate(*p, ws->w, n, K, f->gateSum, st));
+        AG_CUDA(cudaMemcpyAsync(f->pinned, f->gateSum, sizeof(float), cudaMemcpyDeviceToHost, st));
+        AG_CUDA(cudaMemcpyAsync(f->pinned + 1, f->word, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        AG_CUDA(cudaStreamSynchronize(st));
+        const float rms = std::sqrt(f->pinned[0] / static_cast<float>(K));
+        uint32_t pairs = 0;
+        std::memcpy(&pairs, f->pinned + 1, sizeof(uint32_t));
+        f->stats.lastPairs = std::min(pairs, f->pairCap);
+        f->stats.lastGateRms = rms;
+        if (!(rms <= f->cfg.gateTolerance)) {      // the gate failed: plain walk at theta
+            AG_LAUNCH(launchGravity(*p, ws->w, n, theta, false, smCount(), st));
+            f->stats.fallbacks++;
+        }
+    }
+    return ASTRAEA_OK;
+}
+
 uint32_t* livingPtr(const AstraeaRadixBvh* bvh, Workspace* ws) {
     return (bvh->livingFlags != nullptr) ? bvh->livingFlags : ws->w.words + kWLiving;
 }
@@ -281,7 +396,7 @@ AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadix
     AG_LAUNCH(launchPermuteLeavesKarras(*p, *alt, kb, driftPos, w, n, living, allFields, st));
     swapParticlePointers(*p, *alt);
     alt->count = p->count;
-    const bool moments = g_farField.load() == 1;
+    const bool moments = g_farField.load() != 0;
     AG_LAUNCH(launchRefit(kb, w, n, moments, st));
     ws->treeBuilt = true;
     ws->builtN = n;
@@ -327,7 +442,7 @@ AstraeaStatus astraea_gb300_set_stream(void* s) {
 }
 
 AstraeaStatus astraea_gb300_set_far_field(int mode) {
-    if (mode != 0 && mode != 1) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0 or 1");
+    if (mode < 0 || mode > 2) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0, 1 or 2");
     g_farField.store(mode);
     return ASTRAEA_OK;
 }
@@ -509,9 +624,15 @@ AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const Astrae
     AstraeaStatus s = builtWorkspace(bvh, n, &ws);
     if (s != ASTRAEA_OK) return s;
     AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
-    const bool quad = g_farField.load() == 1;
-    if (quad && !ws->momentsBuilt) return fail(ASTRAEA_ERR_INVALID, "far-field mode 1 needs a tree built in that mode");
-    AG_LAUNCH(launchGravity(*p, ws->w, n, theta, quad, smCount(), stream()));
+    const int mode = g_farField.load();
+    if (mode != 0 && !ws->momentsBuilt)
+        return fail(ASTRAEA_ERR_INVALID, "far-field modes 1 and 2 need a tree built in that mode");
+    if (mode == 2) {
+        s = learnedGravity(p, ws, n, theta, true);
+        if (s != ASTRAEA_OK) return s;
+    } else {
+        AG_LAUNCH(launchGravity(*p, ws->w, n, theta, mode == 1, smCount(), stream()));
+    }
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
 }
@@ -734,6 +855,181 @@ AstraeaStatus astraea_gb300_direct_gravity_f64(const AstraeaParticles* p, const 
     return ASTRAEA_OK;
 }
 
+// ------------------------------------------- learned far field (mode 2)
+AstraeaStatus astraea_gb300_ff_configure(const AstraeaFarFieldConfig* cfg) {
+    if (cfg == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    if (!(cfg->thetaFar > 0.0f) || !(cfg->gamma > 0.0f) || !(cfg->gateTolerance >= 0.0f) || cfg->pairsPerGroup == 0u)
+        return fail(ASTRAEA_ERR_INVALID, "ff_configure: thetaFar, gamma, pairsPerGroup must be > 0");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    f->cfg = *cfg;
+    if (f->cfg.gateTargets == 0u) f->cfg.gateTargets = 64u;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_collect(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                       uint32_t groupStride, float* features, float* labels, uint32_t capacity,
+                                       uint32_t* outCount) {
+    if (p == nullptr || bvh == nullptr || outCount == nullptr || (capacity > 0u && (features == nullptr || labels == nullptr)))
+        return fail(ASTRAEA_ERR_INVALID, "null argument");
+    *outCount = 0;
+    const uint32_t n = p->count;
+    if (n < 2u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (!ws->momentsBuilt) return fail(ASTRAEA_ERR_INVALID, "ff_collect needs a tree built in far-field mode 2");
+    FfState* f = nullptr;
+    s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, st));
+    s = ffWalk(p, ws, n, theta, f, groupStride);
+    if (s != ASTRAEA_OK) return s;
+    uint32_t recorded = 0;
+    AG_CUDA(cudaMemcpyAsync(f->pinned, f->word, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AG_CUDA(cudaStreamSynchronize(st));
+    std::memcpy(&recorded, f->pinned, sizeof(uint32_t));
+    const uint32_t rows = std::min(std::min(recorded, f->pairCap), capacity);
+    AG_LAUNCH(ff::launchLabels(ws->w, n, f->pairs, rows, f->groups, features, labels, st));
+    AG_CUDA(cudaStreamSynchronize(st));
+    ws->stepCacheValid = false;
+    *outCount = rows;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_init(uint64_t seed) {
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    std::vector<float> h(ff::kParams, 0.0f);
+    uint64_t x = seed ^ 0x2545F4914F6CDD1Dull;
+    auto uni = [&]() {                             // xorshift64*, uniform in [-1, 1)
+        x ^= x >> 12; x ^= x << 25; x ^= x >> 27;
+        return static_cast<float>(static_cast<double>((x * 0x2545F4914F6CDD1Dull) >> 11) * 0x1.0p-52 - 1.0);
+    };
+    auto fill = [&](int off, int fanIn, int fanOut) {
+        const float a = std::sqrt(6.0f / static_cast<float>(fanIn + fanOut));
+        for (int k = 0; k < fanIn * fanOut; ++k) h[off + k] = a * uni();
+    };
+    fill(ff::kW1, ff::kIn, ff::kHid);
+    fill(ff::kW2, ff::kHid, ff::kHid);
+    fill(ff::kW3, ff::kHid, ff::kOut);
+    AG_CUDA(cudaMemcpy(f->net.params, h.data(), ff::kParams * sizeof(float), cudaMemcpyHostToDevice));
+    AG_CUDA(cudaMemset(f->net.grads, 0, ff::kParams * sizeof(float)));
+    AG_CUDA(cudaMemset(f->net.adamM, 0, ff::kParams * sizeof(float)));
+    AG_CUDA(cudaMemset(f->net.adamV, 0, ff::kParams * sizeof(float)));
+    f->adamStep = 0;
+    f->ready = true;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_fit_output_scale(const float* labels, uint32_t count) {
+    if (labels == nullptr || count == 0u) return fail(ASTRAEA_ERR_INVALID, "ff_fit_output_scale: no labels");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    std::vector<float> h(static_cast<size_t>(count) * ff::kOut);
+    AG_CUDA(cudaMemcpy(h.data(), labels, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    float scale[ff::kOut];
+    for (int o = 0; o < ff::kOut; ++o) {
+        double acc = 0.0;
+        for (uint32_t r = 0; r < count; ++r) acc += static_cast<double>(h[static_cast<size_t>(r) * ff::kOut + o]) *
+                                                   h[static_cast<size_t>(r) * ff::kOut + o];
+        const double rms = std::sqrt(acc / count);
+        scale[o] = (o < ff::kUsedOut && rms > 1.0e-12) ? static_cast<float>(rms) : 1.0f;
+    }
+    AG_CUDA(cudaMemcpy(f->net.outScale, scale, sizeof(scale), cudaMemcpyHostToDevice));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_gradients(const float* features, const float* labels, uint32_t count,
+                                         float* outGrads, float* outLoss) {
+    if (features == nullptr || labels == nullptr || count == 0u) return fail(ASTRAEA_ERR_INVALID, "ff_gradients: no rows");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    AG_CUDA(cudaMemsetAsync(f->net.grads, 0, ff::kParams * sizeof(float), st));
+    AG_CUDA(cudaMemsetAsync(f->net.loss, 0, sizeof(float), st));
+    AG_LAUNCH(ff::launchTrain(f->net, features, labels, count, smCount(), st));
+    if (outGrads) AG_CUDA(cudaMemcpyAsync(outGrads, f->net.grads, ff::kParams * sizeof(float), cudaMemcpyDeviceToHost, st));
+    AG_CUDA(cudaMemcpyAsync(f->pinned, f->net.loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+    AG_CUDA(cudaMemsetAsync(f->net.grads, 0, ff::kParams * sizeof(float), st));
+    AG_CUDA(cudaStreamSynchronize(st));
+    f->stats.lastLoss = f->pinned[0];
+    if (outLoss) *outLoss = f->pinned[0];
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_train_step(const float* features, const float* labels, uint32_t count,
+                                          float learningRate, float* outLoss) {
+    if (features == nullptr || labels == nullptr || count == 0u) return fail(ASTRAEA_ERR_INVALID, "ff_train_step: no rows");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    if (!f->ready) return fail(ASTRAEA_ERR_INVALID, "ff_train_step: call ff_init or ff_set_params first");
+    cudaStream_t st = stream();
+    AG_CUDA(cudaMemsetAsync(f->net.loss, 0, sizeof(float), st));
+    AG_LAUNCH(ff::launchTrain(f->net, features, labels, count, smCount(), st));
+    AG_LAUNCH(ff::launchAdam(f->net, learningRate, ++f->adamStep, st));
+    if (outLoss) {
+        AG_CUDA(cudaMemcpyAsync(f->pinned, f->net.loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+        AG_CUDA(cudaStreamSynchronize(st));
+        f->stats.lastLoss = f->pinned[0];
+        *outLoss = f->pinned[0];
+    }
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_predict(const float* features, uint32_t count, float* out) {
+    if (count == 0u) return ASTRAEA_OK;
+    if (features == nullptr || out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    AG_LAUNCH(ff::launchPredict(f->net, features, count, out, smCount(), stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_get_params(float* params, uint32_t capacity, float* outScale16) {
+    if (params == nullptr || capacity < static_cast<uint32_t>(ff::kParams))
+        return fail(ASTRAEA_ERR_CAPACITY, "ff_get_params: needs 6288 floats");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    AG_CUDA(cudaStreamSynchronize(stream()));
+    AG_CUDA(cudaMemcpy(params, f->net.params, ff::kParams * sizeof(float), cudaMemcpyDeviceToHost));
+    if (outScale16) AG_CUDA(cudaMemcpy(outScale16, f->net.outScale, ff::kOut * sizeof(float), cudaMemcpyDeviceToHost));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_set_params(const float* params, uint32_t count, const float* outScale16) {
+    if (params == nullptr || count != static_cast<uint32_t>(ff::kParams))
+        return fail(ASTRAEA_ERR_INVALID, "ff_set_params: needs exactly 6288 floats");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    AG_CUDA(cudaStreamSynchronize(stream()));
+    AG_CUDA(cudaMemcpy(f->net.params, params, ff::kParams * sizeof(float), cudaMemcpyHostToDevice));
+    if (outScale16) AG_CUDA(cudaMemcpy(f->net.outScale, outScale16, ff::kOut * sizeof(float), cudaMemcpyHostToDevice));
+    AG_CUDA(cudaMemset(f->net.adamM, 0, ff::kParams * sizeof(float)));
+    AG_CUDA(cudaMemset(f->net.adamV, 0, ff::kParams * sizeof(float)));
+    f->adamStep = 0;
+    f->ready = true;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out) {
+    if (out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    FfState* f = nullptr;
+    AstraeaStatus s = ffState(&f);
+    if (s != ASTRAEA_OK) return s;
+    *out = f->stats;
+    return ASTRAEA_OK;
+}
+
 // ------------------------------------------------------ planet building
 static planet::BodySpec toBodySpec(const AstraeaBodySpec& s) {
     return planet::BodySpec{static_cast<int>(s.archetype > 5u ? 99u : s.archetype), s.massKg, s.surfaceTempK,
@@ -846,7 +1142,12 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
     AG_LAUNCH(launchPass1(*p, w, n, st));
     AG_LAUNCH(launchEos(*p, &w, n, st));
-    AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt, sms, st));
+    if (ws->momentsBuilt && g_farField.load() == 2) {
+        s = learnedGravity(p, ws, n, theta, true);
+        if (s != ASTRAEA_OK) return s;
+    } else {
+        AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt && g_farField.load() == 1, sms, st));
+    }
     AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));
     // 5. closing half kick + EOS + next dt minimum
     KickArgs k2{};

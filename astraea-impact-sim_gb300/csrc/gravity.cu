@@ -194,10 +194,10 @@ __device__ __forceinline__ void getMono(const float* list, int slot, float (&e)[
 // 1 / |s| for a direction s in {-1, 0, 1}^3 with nz non-zero components.
 __device__ __forceinline__ float invDirNorm(int nz) { return nz == 3 ? 0.57735027f : (nz == 2 ? 0.70710678f : 1.0f); }
 
-template <bool kInside, bool kQuad>
+template <bool kInside, bool kQuad, bool kLearned>
 __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
                                                                  float theta2, uint32_t numGroups,
-                                                                 uint32_t* groupCounter) {
+                                                                 uint32_t* groupCounter, FarCapture ff) {
     __shared__ GravWarpSmem<kInside, kQuad> smem[kGravWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GravWarpSmem<kInside, kQuad>& S = smem[warp];
@@ -235,6 +235,8 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
         const float gminz = warpMinF(active ? zi : 3.0e38f), gmaxz = warpMaxF(active ? zi : -3.0e38f);
         const float cxg = 0.5f * (gminx + gmaxx), cyg = 0.5f * (gminy + gmaxy), czg = 0.5f * (gminz + gmaxz);
         const float gExt = (gmaxx - gminx) + (gmaxy - gminy) + (gmaxz - gminz);
+        const bool emitFar = kLearned && (g % ff.groupStride) == 0u;
+        if (kLearned && lane == 0) ff.groups[g] = make_float4(cxg, cyg, czg, gExt);
 
         // Per-direction extreme members (dirPos); member positions staged in und[].
         S.und[lane] = make_float4(xi, yi, zi, 0.0f);
@@ -281,6 +283,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
             float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             int cl = 0, cr = 0;
             bool undecided = false;
+            bool farOk = false;
             float dd = 0.0f;
             float4 bmin = make_float4(0.f, 0.f, 0.f, 0.f), bmax = bmin;
             if (isNode) {
@@ -290,12 +293,14 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 cl = __float_as_int(r1.y);
                 cr = __float_as_int(r1.z);
                 dd = r1.x;                       // dNode^2, rounded once by the refit
-                bool disjoint = true;
-                if (kInside) {
+                bool disjoint = true;   // the inside-box rule of the theta test (kInside)
+                bool boxApart = true;   // the same rule for the far test (theta_far^2 > 1/3)
+                if (kInside || kLearned) {
                     bmin = __ldg(&rec[2]);
                     bmax = __ldg(&rec[3]);
-                    disjoint = bmax.x < gminx || bmin.x > gmaxx || bmax.y < gminy || bmin.y > gmaxy ||
+                    boxApart = bmax.x < gminx || bmin.x > gmaxx || bmax.y < gminy || bmin.y > gmaxy ||
                                bmax.z < gminz || bmin.z > gmaxz;
+                    if (kInside) disjoint = boxApart;
                 }
                 // (1) Sound lower bound on every member's distance to the COM:
                 // the group-box distance, or the distance to the supporting
@@ -317,6 +322,11 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 const float L = (static_cast<float>(sx) * ux + static_cast<float>(sy) * uy +
                                  static_cast<float>(sz) * uz) * inv - dp.w - 1.0e-6f * (ax + ay + az + gExt);
                 const float Lb2 = fmaxf(D2, L > 0.0f ? L * L : 0.0f);
+                // far test of mode 2: every member passes theta_far (by the
+                // sound bound) and the node is far against the group's size
+                if (kLearned)
+                    farOk = emitFar && boxApart && Lb2 > 2.0e-20f && dd < ff.thetaFar2 * Lb2 * 0.99999f &&
+                            gExt * gExt <= ff.gamma2 * (ux * ux + uy * uy + uz * uz);
                 if (disjoint && Lb2 > 2.0e-20f && dd < theta2 * Lb2 * 0.99999f) {
                     accept = true;
                 } else if (!acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax)) {
@@ -347,6 +357,24 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
                 }
                 if (undecided) accept = (bits >> slot) & 1u;
                 __syncwarp();
+            }
+            if (kLearned) {
+                // a node the theta test opens but the far test takes: a
+                // monopole plus the learned correction of this (group, node)
+                bool far = isNode && !accept && farOk;
+                const unsigned farMask = __ballot_sync(0xffffffffu, far);
+                if (farMask) {
+                    uint32_t fb = 0;
+                    if (lane == 0) fb = atomicAdd(ff.count, static_cast<uint32_t>(__popc(farMask)));
+                    fb = __shfl_sync(0xffffffffu, fb, 0);
+                    if (far) {
+                        const uint32_t slot = fb + static_cast<uint32_t>(__popc(farMask & laneMaskLt()));
+                        if (slot < ff.cap) {                     // full buffer: the node is opened
+                            ff.pairs[slot] = make_uint2(g, static_cast<uint32_t>(c));
+                            accept = true;
+                        }
+                    }
+                }
             }
             bool open = isNode && !accept;
             unsigned openMask = __ballot_sync(0xffffffffu, open);
@@ -467,7 +495,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
 }  // namespace
 
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
-                          cudaStream_t st) {
+                          cudaStream_t st, const FarCapture* far) {
     if (n == 0) return cudaSuccess;
     const float th = fmaxf(0.0f, theta);
     const float theta2 = th * th;
@@ -476,14 +504,20 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
     uint32_t* counter = w.words + kWGroupCounter;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    auto kernel = checkInside ? (quadrupole ? gravityKernel<true, true> : gravityKernel<true, false>)
-                              : (quadrupole ? gravityKernel<false, true> : gravityKernel<false, false>);
+    FarCapture ff{};
+    auto kernel = checkInside ? (quadrupole ? gravityKernel<true, true, false> : gravityKernel<true, false, false>)
+                              : (quadrupole ? gravityKernel<false, true, false> : gravityKernel<false, false, false>);
+    if (far != nullptr) {
+        ff = *far;
+        if (ff.groupStride == 0u) ff.groupStride = 1u;
+        kernel = checkInside ? gravityKernel<true, false, true> : gravityKernel<false, false, true>;
+    }
     int perSm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kGravWarps * 32, 0);
     if (e != cudaSuccess) return e;
     const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(std::max(1, perSm) * sms),
                                                (groups + kGravWarps - 1) / kGravWarps);
-    kernel<<<blocks, kGravWarps * 32, 0, st>>>(p, w, n, theta2, groups, counter);
+    kernel<<<blocks, kGravWarps * 32, 0, st>>>(p, w, n, theta2, groups, counter, ff);
     return cudaGetLastError();
 }
 

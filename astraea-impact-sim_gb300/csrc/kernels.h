@@ -87,8 +87,47 @@ cudaError_t launchDirectGravityF64(const AstraeaParticles& p, uint32_t n, const 
                                    double* acc3, double* phi, cudaStream_t st);
 
 // ---------------------------------------------------------- gravity.cu ---
+// Far-field mode 2: the walk also takes a node the theta test opens when
+// every member passes theta_far (sound bound) and L1 group extent <=
+// gamma r; it records the (group, node) pair and each group's centre.
+struct FarCapture {
+    uint2* pairs;          // {group, node}
+    uint32_t cap;
+    uint32_t* count;       // device word, zeroed by the caller
+    float4* groups;        // per group {centre x, y, z, L1 extent}
+    float thetaFar2;
+    float gamma2;
+    uint32_t groupStride;  // only groups g % stride == 0 apply the far test
+};
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
+                          cudaStream_t st, const FarCapture* far = nullptr);
+
+// ---------------------------------------------------------------- ff.cu ---
+namespace ff {
+constexpr int kIn = 16, kHid = 64, kOut = 16, kUsedOut = 12;
+constexpr int kW1 = 0, kB1 = kW1 + kIn * kHid, kW2 = kB1 + kHid, kB2 = kW2 + kHid * kHid, kW3 = kB2 + kHid;
+constexpr int kB3 = kW3 + kHid * kOut, kParams = kB3 + kOut;   // 6,288 FP32 parameters
+struct Net {
+    float* params;     // FP32 master weights (W row-major in x out, then bias), layout above
+    float* grads;
+    float* adamM;
+    float* adamV;
+    float* outScale;   // kOut
+    float* loss;       // one word
+};
+cudaError_t prepareKernels();
+cudaError_t launchLabels(const Work& w, uint32_t n, const uint2* pairs, uint32_t count, const float4* groups,
+                         float* feat, float* label, cudaStream_t st);
+cudaError_t launchTrain(const Net& net, const float* feat, const float* label, uint32_t count, int sms,
+                        cudaStream_t st);
+cudaError_t launchAdam(const Net& net, float lr, int step, cudaStream_t st);
+cudaError_t launchPredict(const Net& net, const float* feat, uint32_t count, float* out, int sms, cudaStream_t st);
+cudaError_t launchApply(const Net& net, const Work& w, const uint2* pairs, const uint32_t* countWord, uint32_t cap,
+                        const float4* groups, float* groupCorr, int sms, cudaStream_t st);
+cudaError_t launchCorrect(const AstraeaParticles& p, const float4* groups, const float* groupCorr, uint32_t n,
                           cudaStream_t st);
+cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float* out, cudaStream_t st);
+}  // namespace ff
 
 // -------------------------------------------------------------- sph.cu ---
 cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st);

@@ -177,8 +177,10 @@ AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevD
  * 1 = monopole + quadrupole: the build also refits every node's central
  * second moments and each accepted node adds its quadrupole acceleration
  * and potential, so a larger opening angle (0.7 instead of 0.5) gives the
- * same force error with about half the interactions.  Process-wide; gravity
- * in mode 1 on a tree built in mode 0 returns ASTRAEA_ERR_INVALID. */
+ * same force error with about half the interactions; 2 = monopole + the
+ * learned far-field correction (astraea_gb300_ff_*, below).  Process-wide;
+ * gravity in mode 1 or 2 on a tree built in mode 0 returns
+ * ASTRAEA_ERR_INVALID. */
 AstraeaStatus astraea_gb300_set_far_field(int mode);
 
 /* ---- render frame packing (engine/sph_gravity.cu:1554-1743, 2163-2201) -- */
@@ -340,6 +342,72 @@ AstraeaStatus astraea_gb300_solve_hydrostatic(const AstraeaBodySpec* spec, Astra
 AstraeaStatus astraea_gb300_build_planet(const AstraeaBodySpec* spec, uint32_t particleCount, uint32_t bodyId,
                                          uint32_t tracerGridRes, uint64_t seed, AstraeaParticles* p, uint32_t offset,
                                          AstraeaPlanetInfo* info);
+
+/* ---- far-field mode 2: learned correction (no engine counterpart) ------- */
+
+/* In mode 2 (astraea_gb300_set_far_field(2); trees built in that mode carry
+ * second moments) the gravity walk keeps the engine's theta test and also
+ * takes a node the theta test opens when every member of the group of 32
+ * passes theta_far and the node is far against the group (L1 group extent
+ * <= gamma r).  For each such (group, node) pair an MLP (16 -> 64 -> 64 ->
+ * 12, SiLU, BF16 tensor-core arithmetic with FP32 accumulation) predicts the
+ * residual between the node's exact field and its monopole at the group
+ * centre c, and the residual's Jacobian; member i adds the sum over its
+ * group's pairs of R + J (x_i - c).  Features: (COM - c)/r, dNode/r,
+ * S/(M dNode^2) (central second moments), group extent/r.  With
+ * gateTolerance > 0 every mode-2 gravity call checks the RMS relative error
+ * of gateTargets sampled particles against an FP32 direct sum and, above the
+ * tolerance, recomputes plain theta gravity (the call then blocks). */
+typedef struct AstraeaFarFieldConfig {
+    float thetaFar;          /* opening angle of the far test (default 0.8) */
+    float gamma;             /* far test: L1 group extent <= gamma r (default 0.3) */
+    float gateTolerance;     /* RMS relative force error at the gate; 0: no gate (default) */
+    uint32_t gateTargets;    /* sampled particles of the gate (default 64) */
+    uint32_t pairsPerGroup;  /* pair buffer per group of 32 (default 64); a full buffer opens the node */
+    uint32_t reserved;
+} AstraeaFarFieldConfig;
+
+typedef struct AstraeaFarFieldStats {
+    uint64_t calls;          /* mode-2 gravity evaluations */
+    uint64_t fallbacks;      /* ... that the gate sent back to the plain walk */
+    uint32_t lastPairs;      /* (group, node) pairs corrected by the last gated call */
+    uint32_t reserved;
+    float lastGateRms;       /* RMS relative error of the last gate; -1 when no gate ran */
+    float lastLoss;          /* loss of the last train step or gradient evaluation */
+} AstraeaFarFieldStats;
+
+AstraeaStatus astraea_gb300_ff_configure(const AstraeaFarFieldConfig* cfg);
+/* Training rows from the current tree (built in mode 2): runs the mode-2
+ * walk at theta (p's accelerations are overwritten with its monopole-only
+ * result), with the far test on every groupStride-th group, and writes for
+ * up to `capacity` recorded pairs 16 features and 16 labels (12 used: the
+ * residual and Jacobian, normalised by G M / r^2 and G M / r^3, from an FP64
+ * direct sum over the node's particles) to device arrays.  *outCount
+ * receives the rows written. */
+AstraeaStatus astraea_gb300_ff_collect(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                       uint32_t groupStride, float* features, float* labels, uint32_t capacity,
+                                       uint32_t* outCount);
+/* Network parameters: Xavier-uniform weights from `seed`, zero biases,
+ * fresh Adam state.  6,288 FP32 parameters: W1 (16x64, in-major), b1, W2
+ * (64x64), b2, W3 (64x16), b3. */
+AstraeaStatus astraea_gb300_ff_init(uint64_t seed);
+/* Per-output scale = RMS of the labels (device, count x 16). */
+AstraeaStatus astraea_gb300_ff_fit_output_scale(const float* labels, uint32_t count);
+/* Loss (mean squared error of the 12 used outputs in scaled units) and its
+ * gradient over `count` rows (device arrays) by the tensor-core forward and
+ * backward kernels; outGrads (host, 6,288 floats) may be NULL.  Blocks. */
+AstraeaStatus astraea_gb300_ff_gradients(const float* features, const float* labels, uint32_t count,
+                                         float* outGrads, float* outLoss);
+/* One Adam step (beta 0.9 / 0.999) on the gradient of `count` rows;
+ * *outLoss (host, may be NULL: no sync) receives the batch loss. */
+AstraeaStatus astraea_gb300_ff_train_step(const float* features, const float* labels, uint32_t count,
+                                          float learningRate, float* outLoss);
+/* Network outputs (scaled units, count x 16, device) of `count` feature rows. */
+AstraeaStatus astraea_gb300_ff_predict(const float* features, uint32_t count, float* out);
+/* Host copies of the 6,288 parameters and the 16 output scales. */
+AstraeaStatus astraea_gb300_ff_get_params(float* params, uint32_t capacity, float* outScale16);
+AstraeaStatus astraea_gb300_ff_set_params(const float* params, uint32_t count, const float* outScale16);
+AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out);
 
 /* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
 

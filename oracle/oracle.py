@@ -527,3 +527,75 @@ def karras(codes_sorted):
     parent = np.zeros(2 * n - 1, np.int32)
     lib.oracle_karras(n, _ptr(c), _ptr(left), _ptr(right), _ptr(parent))
     return left, right, parent
+
+
+# ------------------------------------------------ learned far field (mode 2)
+# The network of astraea_gb300_ff_* restated in numpy FP64: 16 -> 64 -> 64 ->
+# 16, SiLU, loss = mean over rows and the first 12 outputs of
+# (y - label / scale)^2.  With bf16=True the operands are rounded to bfloat16
+# (round to nearest even) where the GPU kernels round them: inputs, weights,
+# the hidden activations, and the backward signals dY, dZ2, dZ1 before they
+# enter a product; sums stay FP64 here (FP32 on the GPU).
+FF_IN, FF_HID, FF_OUT, FF_USED = 16, 64, 16, 12
+FF_SHAPES = [("W1", (FF_IN, FF_HID)), ("b1", (FF_HID,)), ("W2", (FF_HID, FF_HID)), ("b2", (FF_HID,)),
+             ("W3", (FF_HID, FF_OUT)), ("b3", (FF_OUT,))]
+
+
+def bf16_round(a):
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def ff_unpack(params):
+    out, off = {}, 0
+    for name, shp in FF_SHAPES:
+        k = int(np.prod(shp))
+        out[name] = np.asarray(params[off:off + k], np.float64).reshape(shp)
+        off += k
+    return out
+
+
+def ff_pack(d):
+    return np.concatenate([np.asarray(d[name], np.float64).ravel() for name, _ in FF_SHAPES])
+
+
+def _silu(z):
+    s = 1.0 / (1.0 + np.exp(-z))
+    return z * s, s * (1.0 + z * (1.0 - s))
+
+
+def ff_forward(params, X, bf16=False):
+    P = ff_unpack(params)
+    r = bf16_round if bf16 else (lambda a: np.asarray(a, np.float64))
+    x = r(X)
+    z1 = x @ r(P["W1"]) + P["b1"]
+    h1 = r(_silu(z1)[0])
+    z2 = h1 @ r(P["W2"]) + P["b2"]
+    h2 = r(_silu(z2)[0])
+    y = h2 @ r(P["W3"]) + P["b3"]
+    return y, (x, z1, h1, z2, h2)
+
+
+def ff_loss_grad(params, scale, X, T, bf16=False):
+    """(loss, gradient over the packed parameters) of one batch."""
+    P = ff_unpack(params)
+    r = bf16_round if bf16 else (lambda a: np.asarray(a, np.float64))
+    y, (x, z1, h1, z2, h2) = ff_forward(params, X, bf16)
+    n = X.shape[0]
+    t = np.asarray(T, np.float64)[:, :FF_USED] / np.asarray(scale, np.float64)[:FF_USED]
+    d = np.zeros_like(y)
+    d[:, :FF_USED] = y[:, :FF_USED] - t
+    loss = float(np.sum(d * d) / (n * FF_USED))
+    dy = 2.0 * d / (n * FF_USED)
+    dyr = r(dy)
+    g = {"b3": dy.sum(0), "W3": h2.T @ dyr}
+    dz2 = (dyr @ r(P["W3"]).T) * _silu(z2)[1]
+    dz2r = r(dz2)
+    g["b2"] = dz2.sum(0)
+    g["W2"] = h1.T @ dz2r
+    dz1 = (dz2r @ r(P["W2"]).T) * _silu(z1)[1]
+    dz1r = r(dz1)
+    g["b1"] = dz1.sum(0)
+    g["W1"] = x.T @ dz1r
+    return loss, ff_pack(g)
