@@ -64,12 +64,12 @@ def parse():
                     help="particles (default: 1M for c2, 4M for c3, 16M for c5)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
                     help="c2: the 1M differentiated impact (the headline line); c3: 4M Plummer sphere, "
-                         "gravity only, plain vs quadrupole far field; c5: 16M gas-giant core impact")
+                         "gravity only, plain vs quadrupole and learned far field; c5: 16M gas-giant core impact")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--max-dt-sec", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-far-field", action="store_true", help="skip the quadrupole far-field comparison")
+    ap.add_argument("--no-far-field", action="store_true", help="skip the far-field comparison (quadrupole and learned)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-planet", action="store_true", help="skip the planet-construction measurement")
     ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
@@ -239,7 +239,11 @@ def run_gpu(args):
     err_rms = force_error_fp64(sim, engine, torch, np, truth=truth, theta=args.theta)
 
     frame = frame_stages(sim, engine, torch, np, n)
-    far = None if args.no_far_field else far_field_scan(sim, engine, torch, np, args, max_dt, truth)
+    far = None
+    if not args.no_far_field:
+        learned = train_learned(engine, torch, [scenarios.differentiated_impact(n_total=262_144, seed=s)[0]
+                                                for s in (901, 902)])
+        far = far_field_scan(sim, engine, torch, np, args, max_dt, truth, learned=learned)
     ens = None if (args.no_ensemble or world > 1) else ensemble_run(engine, scenarios, torch, max_dt, args.theta)
     planet = None if (args.no_planet or world > 1) else planet_stage(engine, torch, np)
 
@@ -443,14 +447,43 @@ def fp64_truth(sim, torch, samples=1024):
     return tgt, acc
 
 
-def far_field_scan(sim, engine, torch, np, args, max_dt, truth,
-                   configs=((0.5, 0), (0.6, 1), (0.7, 1), (0.8, 1))):
+def train_learned(engine, torch, states, steps=1500):
+    """Trains the far-field network of mode 2 on the GPU on other snapshots
+    of the same kind of workload (never the measured one)."""
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rows, hist = engine.train_far_field(states, steps=steps, batch=8192, lr=2e-3, seed=1)
+    torch.cuda.synchronize()
+    return {"training_rows": rows, "training_steps": steps, "loss_first": hist[0][1], "loss_last": hist[-1][1],
+            "training_s": time.perf_counter() - t0, "snapshots": len(states)}
+
+
+FAR_CONFIGS = (
+    {"theta": 0.5, "mode": 0},
+    {"theta": 0.6, "mode": 1}, {"theta": 0.7, "mode": 1}, {"theta": 0.8, "mode": 1},
+    {"theta": 0.5, "mode": 2, "theta_far": 0.9, "gamma": 0.3},
+    {"theta": 0.5, "mode": 2, "theta_far": 1.2, "gamma": 0.3},
+    {"theta": 0.5, "mode": 2, "theta_far": 0.9, "gamma": 0.5},
+)
+FAR_NAMES = {0: "monopole", 1: "monopole+quadrupole", 2: "monopole+learned correction"}
+
+
+def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONFIGS, learned=None):
     """Plain monopole at theta 0.5 (the engine's kernel) against the
-    quadrupole far field (mode 1) at larger opening angles: gravity time,
-    interactions and RMS force error vs the FP64 direct sum on the same
-    tree, then the whole fused step at each setting."""
+    quadrupole far field (mode 1) at larger opening angles and the learned
+    correction (mode 2: far nodes taken at theta_far with the network's
+    residual and Jacobian): gravity time, interactions and RMS force error
+    vs the FP64 direct sum on the same tree (mode 2 also without the
+    correction, the network zeroed), then the whole fused step."""
     out = []
-    for theta, mode in configs:
+    if learned is not None:
+        params, scale = engine.ff_get_params()
+    for cfg in configs:
+        theta, mode = cfg["theta"], cfg["mode"]
+        if mode == 2 and learned is None:
+            continue
+        if mode == 2:
+            engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=0.0)
         engine.set_far_field(mode)
         engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)   # the order is already sorted: identity permutation
         engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
@@ -463,24 +496,34 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth,
         ev[1].record()
         torch.cuda.synchronize()
         _, gc = engine.read_device_status()
-        out.append({"theta": theta, "far_field": "monopole" if mode == 0 else "monopole+quadrupole",
-                    "gravity_ms": ev[0].elapsed_time(ev[1]) / 5,
-                    "interactions_per_particle": gc["gravity_interactions"] / 5 / sim.p.count,
-                    "force_rms_vs_fp64": rms_vs_truth(sim, torch, truth)})
+        rec = {"theta": theta, "far_field": FAR_NAMES[mode], "gravity_ms": ev[0].elapsed_time(ev[1]) / 5,
+               "interactions_per_particle": gc["gravity_interactions"] / 5 / sim.p.count,
+               "force_rms_vs_fp64": rms_vs_truth(sim, torch, truth)}
+        if mode == 2:
+            rec.update({"theta_far": cfg["theta_far"], "gamma": cfg["gamma"]})
+            engine.ff_set_params(np.zeros_like(params), scale)
+            engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+            rec["force_rms_without_correction"] = rms_vs_truth(sim, torch, truth)
+            engine.ff_set_params(params, scale)
+            engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+        out.append(rec)
     # whole steps (the state advances; e2e re-uploads its own inputs afterwards)
     dt_host = torch.zeros(1, dtype=torch.float32).pin_memory()
-    for rec, (theta, mode) in zip(out, configs):
+    for rec in out:
+        mode = {v: k for k, v in FAR_NAMES.items()}[rec["far_field"]]
+        if mode == 2:
+            engine.ff_configure(theta_far=rec["theta_far"], gamma=rec["gamma"], gate_tolerance=0.0)
         engine.set_far_field(mode)
         engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
         engine.invalidate_step_cache(sim.bvh)
         for _ in range(2):
-            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, theta, dt_host.data_ptr())
+            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, rec["theta"], dt_host.data_ptr())
         torch.cuda.synchronize()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
         k = max(3, args.steps // 2)
         ev[0].record()
         for _ in range(k):
-            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, theta, dt_host.data_ptr())
+            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, rec["theta"], dt_host.data_ptr())
         ev[1].record()
         torch.cuda.synchronize()
         ms = ev[0].elapsed_time(ev[1]) / k
@@ -492,12 +535,14 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth,
     base = out[0]
     ok = [r for r in out[1:] if r["force_rms_vs_fp64"] <= base["force_rms_vs_fp64"]]
     best = max(ok, key=lambda r: r["particle_steps_per_s"]) if ok else None
-    return {"runs": out,
+    lr = [r for r in out if r["far_field"] == FAR_NAMES[2]]
+    return {"runs": out, "learned_training": learned,
             "equal_error_choice": best and {"theta": best["theta"], "far_field": best["far_field"],
+                                            "theta_far": best.get("theta_far"),
                                             "speedup_vs_plain_theta05": best["particle_steps_per_s"] /
                                             base["particle_steps_per_s"]},
-            "note": "quadrupole far field (analytic, from refitted second moments); "
-                    "a learned correction is not built"}
+            "learned_best_vs_plain": (max(r["particle_steps_per_s"] for r in lr) / base["particle_steps_per_s"])
+                                     if lr else None}
 
 
 def run_e2e(sim, engine, torch, args, max_dt, world, dist):
@@ -597,8 +642,15 @@ def run_c3(args):
     acc64, _ = engine.direct_gravity_f64(sim.p, tgt)
     torch.cuda.synchronize()
     truth_s = time.perf_counter() - t0
+    learned = train_learned(engine, torch, [scenarios.plummer_sphere(524_288, seed=s) for s in (901, 902)])
+    params, scale = engine.ff_get_params()
     runs = []
-    for theta, mode in ((0.5, 0), (0.6, 0), (0.7, 0), (0.8, 0), (0.6, 1), (0.7, 1), (0.8, 1), (0.9, 1)):
+    configs = [(t, m, None, None) for t, m in ((0.5, 0), (0.6, 0), (0.7, 0), (0.8, 0), (0.6, 1), (0.7, 1), (0.8, 1),
+                                                (0.9, 1))]
+    configs += [(0.5, 2, tf, gm) for tf, gm in ((0.9, 0.3), (1.2, 0.3), (0.9, 0.5))]
+    for theta, mode, theta_far, gamma in configs:
+        if mode == 2:
+            engine.ff_configure(theta_far=theta_far, gamma=gamma, gate_tolerance=0.0)
         engine.set_far_field(mode)
         engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
         engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
@@ -616,11 +668,20 @@ def run_c3(args):
         A = sim.p.arrays
         bh = torch.stack([A["accX"][:n][tgt], A["accY"][:n][tgt], A["accZ"][:n][tgt]], 1).double()
         rel = (bh - acc64).norm(dim=1) / acc64.norm(dim=1)
-        runs.append({"theta": theta, "far_field": "monopole" if mode == 0 else "monopole+quadrupole",
-                     "gravity_ms": ms, "particles_per_s": n / (ms * 1e-3),
-                     "interactions_per_particle": c["gravity_interactions"] / reps / n,
-                     "force_rms_vs_fp64": float(torch.sqrt((rel * rel).mean())),
-                     "force_p99_vs_fp64": float(torch.quantile(rel.float(), 0.99))})
+        rec = {"theta": theta, "far_field": FAR_NAMES[mode],
+               "gravity_ms": ms, "particles_per_s": n / (ms * 1e-3),
+               "interactions_per_particle": c["gravity_interactions"] / reps / n,
+               "force_rms_vs_fp64": float(torch.sqrt((rel * rel).mean())),
+               "force_p99_vs_fp64": float(torch.quantile(rel.float(), 0.99))}
+        if mode == 2:
+            rec.update({"theta_far": theta_far, "gamma": gamma})
+            engine.ff_set_params(np.zeros_like(params), scale)
+            engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
+            bh0 = torch.stack([A["accX"][:n][tgt], A["accY"][:n][tgt], A["accZ"][:n][tgt]], 1).double()
+            rel0 = (bh0 - acc64).norm(dim=1) / acc64.norm(dim=1)
+            rec["force_rms_without_correction"] = float(torch.sqrt((rel0 * rel0).mean()))
+            engine.ff_set_params(params, scale)
+        runs.append(rec)
     engine.set_far_field(0)
     base = runs[0]
     ok = [r for r in runs[1:] if r["force_rms_vs_fp64"] <= base["force_rms_vs_fp64"]]
@@ -629,8 +690,9 @@ def run_c3(args):
         "workload": "c3", "metric": "gravity traversals: particles/s at equal force error", "unit": "particles/s",
         "config": {"workload": "Plummer sphere N=%d (a=1, G=1 via m/G_PSU, softening 1e-3 => h0=1.25e-3), "
                                "gravity only" % n, "targets_fp64": int(tgt.numel()), "truth_seconds": truth_s},
-        "runs": runs,
+        "runs": runs, "learned_training": learned,
         "equal_error_choice": best and {"theta": best["theta"], "far_field": best["far_field"],
+                                        "theta_far": best.get("theta_far"),
                                         "speedup_vs_plain_theta05": best["particles_per_s"] /
                                         base["particles_per_s"]}}))
 
