@@ -144,7 +144,7 @@ def test_gpu_quadrupole_needs_moments_tree():
     finally:
         engine.set_far_field(0)
     with pytest.raises(abi.AstraeaError):
-        engine.set_far_field(2)
+        engine.set_far_field(3)
 
 
 @pytest.mark.gpu
