@@ -62,9 +62,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None,
                     help="particles (default: 1M for c2, 4M for c3, 16M for c5)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "planet"],
                     help="c2: the 1M differentiated impact (the headline line); c3: 4M Plummer sphere, "
-                         "gravity only, plain vs quadrupole and learned far field; c5: 16M gas-giant core impact")
+                         "gravity only, plain vs quadrupole and learned far field; c5: 16M gas-giant core impact; "
+                         "planet: scenario construction only (the planet_builder field)")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--max-dt-sec", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -776,12 +777,18 @@ def run_reference(args):
 if __name__ == "__main__":
     a = parse()
     if a.n is None:
-        a.n = {"c2": 1_000_000, "c3": 4_000_000, "c5": 16_000_000}[a.workload]
+        a.n = {"c2": 1_000_000, "c3": 4_000_000, "c5": 16_000_000}.get(a.workload, 0)
     if a.workload != "c2":
-        a.no_cpu_baseline = a.no_ensemble = a.no_far_field = True
+        a.no_cpu_baseline = a.no_ensemble = a.no_far_field = a.no_planet = True
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "c3":
         run_c3(a)
+    elif a.workload == "planet":
+        import numpy as np
+        import torch
+        from astraea_gb300 import engine
+        print(json.dumps({"workload": "planet", "metric": "particles placed per second (wall)",
+                          "planet_builder": planet_stage(engine, torch, np, reps=max(1, a.steps // 3))}))
     else:
         run_gpu(a)
