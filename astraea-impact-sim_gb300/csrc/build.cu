@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(256) permuteLeavesKarrasKernel(AstraeaParticle
         } while (t > 1);
         const int g = ii + s * d + ((d < 0) ? d : 0);
         const int first = min(ii, j), last = max(ii, j);
+        w.nodeRange[ii] = make_uint2(static_cast<uint32_t>(first), static_cast<uint32_t>(last));
         bvh.leftChild[ii] = (first == g) ? ~g : g;
         bvh.rightChild[ii] = (last == g + 1) ? ~(g + 1) : (g + 1);
         bvh.parent[(first == g) ? (nn - 1 + g) : g] = ii;
@@ -166,145 +167,289 @@ __global__ void __launch_bounds__(256) refreshLeavesKernel(AstraeaParticles p, W
 }
 
 // ------------------------------------------------------------- refit ----
-struct ChildData {
-    float mnx, mny, mnz, mxx, mxy, mxz, maxH, maxHs;
-    NodeMom mom;
-    float cx, cy, cz;
-    float s[6];            // central second moments xx yy zz xy xz yz (moments refit only)
-};
+// Replaces bottomUpBvhMomentsKernel (engine/sph_gravity.cu:531-620).  Every
+// internal node of a Karras tree covers a contiguous range [first, last] of
+// sorted leaves (stored by the build), so a node's box, maxH and mass
+// moments are reductions over that range and need no climb through the
+// tree, no arrival counters and no fences:
+//   1. per block of 256 leaves: prefix and suffix min/max of the box and h
+//      values, inclusive FP64 prefix sums of the moments, the block's
+//      totals; then every node whose range lies inside the block, from
+//      shared memory;
+//   2. one block: exclusive FP64 scan of the block totals and a sparse table
+//      of block extremes;
+//   3. per node spanning blocks: box = suffix (first's block) + prefix
+//      (last's block) + one table query over the blocks between; moments =
+//      difference of two global prefix sums.
+// Min/max are exact in any order, so boxes, dNode and maxH equal the
+// engine's; COM and mass come from FP64 sums (as before, rounded to float
+// once).  kMoments adds the central second moments S = sum m x x^T - M c c^T
+// from FP64 sums of m x_a x_b.
+constexpr int kRefitBlock = 256;
+constexpr int kMomW = 10;     // m, mx, my, mz, mxx, myy, mzz, mxy, mxz, myz
 
-template <bool kMoments>
-__device__ __forceinline__ ChildData loadChild(const Work& w, int c, int n) {
-    ChildData d;
+struct Ext8 {                 // min x y z, max x y z, max 2h, max Hs
+    float mnx, mny, mnz, mxx, mxy, mxz, h, hs;
+};
+__device__ __forceinline__ Ext8 extEmpty() {
+    return Ext8{3.0e38f, 3.0e38f, 3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};
+}
+__device__ __forceinline__ Ext8 extJoin(const Ext8& a, const Ext8& b) {
+    return Ext8{fminf(a.mnx, b.mnx), fminf(a.mny, b.mny), fminf(a.mnz, b.mnz), fmaxf(a.mxx, b.mxx),
+                fmaxf(a.mxy, b.mxy), fmaxf(a.mxz, b.mxz), fmaxf(a.h, b.h), fmaxf(a.hs, b.hs)};
+}
+__device__ __forceinline__ void extStore(float4* dst, const Ext8& e) {
+    dst[0] = make_float4(e.mnx, e.mny, e.mnz, e.h);
+    dst[1] = make_float4(e.mxx, e.mxy, e.mxz, e.hs);
+}
+__device__ __forceinline__ Ext8 extLoad(const float4* src) {
+    const float4 a = __ldcg(&src[0]), b = __ldcg(&src[1]);
+    return Ext8{a.x, a.y, a.z, b.x, b.y, b.z, a.w, b.w};
+}
+__device__ __forceinline__ Ext8 extShfl(const Ext8& e, int delta, bool up) {
+    Ext8 o;
+    float* d = reinterpret_cast<float*>(&o);
+    const float* s = reinterpret_cast<const float*>(&e);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) d.s[k] = 0.0f;
-    if (c < 0) {
-        const int leaf = ~c;
-        const float4 pm = __ldg(&w.leafPM[leaf]);
-        const float4 ax = __ldg(&w.leafAux[leaf]);
-        d.mnx = d.mxx = d.cx = pm.x;
-        d.mny = d.mxy = d.cy = pm.y;
-        d.mnz = d.mxz = d.cz = pm.z;
-        d.maxH = ax.z;
-        d.maxHs = ax.x;
-        const double m = pm.w;
-        d.mom = NodeMom{m * static_cast<double>(pm.x), m * static_cast<double>(pm.y), m * static_cast<double>(pm.z), m};
-    } else {
-        const float4* rec = w.node + 4 * static_cast<size_t>(c);
-        const float4 r0 = __ldcg(&rec[0]);
-        const float4 r1 = __ldcg(&rec[1]);
-        const float4 r2 = __ldcg(&rec[2]);
-        const float4 r3 = __ldcg(&rec[3]);
-        d.cx = r0.x; d.cy = r0.y; d.cz = r0.z;
-        d.maxHs = r1.w;
-        d.mnx = r2.x; d.mny = r2.y; d.mnz = r2.z; d.maxH = r2.w;
-        d.mxx = r3.x; d.mxy = r3.y; d.mxz = r3.z;
-        const double2* mp = reinterpret_cast<const double2*>(w.nodeMom + c);
-        const double2 a = __ldcg(&mp[0]);
-        const double2 b = __ldcg(&mp[1]);
-        d.mom = NodeMom{a.x, a.y, b.x, b.y};
-        if (kMoments) {
-            const float4 q0 = __ldcg(&w.nodeQuad[2 * static_cast<size_t>(c)]);
-            const float4 q1 = __ldcg(&w.nodeQuad[2 * static_cast<size_t>(c) + 1]);
-            d.s[0] = q0.x; d.s[1] = q0.y; d.s[2] = q0.z; d.s[3] = q0.w; d.s[4] = q1.x; d.s[5] = q1.y;
-        }
-    }
-    (void)n;
-    return d;
+    for (int k = 0; k < 8; ++k)
+        d[k] = up ? __shfl_up_sync(0xffffffffu, s[k], delta) : __shfl_down_sync(0xffffffffu, s[k], delta);
+    return o;
 }
 
-// kMoments: also the central second moments S = sum m (x - c)(x - c)^T of
-// every node, combined with the parallel-axis rule
-//   S = S_L + S_R + m_L d_L d_L^T + m_R d_R d_R^T,   d = c_child - c,
-// in FP32 (no cancellation: every term is non-negative or a small offset).
+// Node records from a node's box, h extremes and FP64 moments.
 template <bool kMoments>
-__global__ void __launch_bounds__(256) refitKernel(AstraeaRadixBvh bvh, Work w, uint32_t n) {
-    const uint32_t leafIdx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (leafIdx >= n || n < 2u) return;
-    // The data of the node this thread just finished stays in registers; at
-    // each level only the sibling is loaded (the engine reloads both children).
-    int curr = ~static_cast<int>(leafIdx);          // child reference of the leaf
-    ChildData mine = loadChild<kMoments>(w, curr, static_cast<int>(n));
-    int pNode = __ldcg(&bvh.parent[(n - 1u) + leafIdx]);
-    // A radix tree over 63-bit keys + 32-bit index ties is at most 96 deep;
-    // the bound only matters for a tree built from a failed sort.
-    for (int level = 0; pNode >= 0; ++level) {
-        if (level >= 256 || pNode >= static_cast<int>(n) - 1) {
-            atomicOr(&w.status->flags, kFlagStackOverflow);
-            return;
-        }
-        // loads that do not depend on the arrival order, issued before the atomic
-        const int lc = __ldcg(&bvh.leftChild[pNode]);
-        const int rc = __ldcg(&bvh.rightChild[pNode]);
-        const int grand = __ldcg(&bvh.parent[pNode]);
-        // Arrival counter with release (this thread's node records, written
-        // with st.cg, become visible to the second arrival) and acquire (the
-        // sibling's records are read after it) in one atomic, instead of two
-        // full fences.
-        uint32_t before;
-        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
-                     : "=r"(before)
-                     : "l"(&bvh.atomicVisited[pNode])
-                     : "memory");
-        if (before == 0u) return;   // first arrival stops
-        const bool fromLeft = (lc == curr);
-        const ChildData other = loadChild<kMoments>(w, fromLeft ? rc : lc, static_cast<int>(n));
-        const ChildData& L = fromLeft ? mine : other;
-        const ChildData& R = fromLeft ? other : mine;
-        ChildData out;
-        out.mnx = fminf(L.mnx, R.mnx); out.mny = fminf(L.mny, R.mny); out.mnz = fminf(L.mnz, R.mnz);
-        out.mxx = fmaxf(L.mxx, R.mxx); out.mxy = fmaxf(L.mxy, R.mxy); out.mxz = fmaxf(L.mxz, R.mxz);
-        out.maxH = fmaxf(L.maxH, R.maxH);
-        out.maxHs = fmaxf(L.maxHs, R.maxHs);
-        out.mom = NodeMom{L.mom.sx + R.mom.sx, L.mom.sy + R.mom.sy, L.mom.sz + R.mom.sz, L.mom.m + R.mom.m};
-        if (out.mom.m > 0.0) {
-            const double im = 1.0 / out.mom.m;
-            out.cx = static_cast<float>(out.mom.sx * im);
-            out.cy = static_cast<float>(out.mom.sy * im);
-            out.cz = static_cast<float>(out.mom.sz * im);
-        } else {                                   // massless subtree (sph_gravity.cu:591-595)
-            out.cx = 0.5f * (L.cx + R.cx);
-            out.cy = 0.5f * (L.cy + R.cy);
-            out.cz = 0.5f * (L.cz + R.cz);
-        }
-        if (kMoments) {
-            const float mL = static_cast<float>(L.mom.m), mR = static_cast<float>(R.mom.m);
-            const float lx = L.cx - out.cx, ly = L.cy - out.cy, lz = L.cz - out.cz;
-            const float rx = R.cx - out.cx, ry = R.cy - out.cy, rz = R.cz - out.cz;
-            out.s[0] = L.s[0] + R.s[0] + mL * lx * lx + mR * rx * rx;
-            out.s[1] = L.s[1] + R.s[1] + mL * ly * ly + mR * ry * ry;
-            out.s[2] = L.s[2] + R.s[2] + mL * lz * lz + mR * rz * rz;
-            out.s[3] = L.s[3] + R.s[3] + mL * lx * ly + mR * rx * ry;
-            out.s[4] = L.s[4] + R.s[4] + mL * lx * lz + mR * rx * rz;
-            out.s[5] = L.s[5] + R.s[5] + mL * ly * lz + mR * ry * rz;
-            __stcg(&w.nodeQuad[2 * static_cast<size_t>(pNode)], make_float4(out.s[0], out.s[1], out.s[2], out.s[3]));
-            __stcg(&w.nodeQuad[2 * static_cast<size_t>(pNode) + 1], make_float4(out.s[4], out.s[5], 0.0f, 0.0f));
-        }
-        const float mSum = static_cast<float>(out.mom.m);
-        const float dNode = fmaxf(out.mxx - out.mnx, fmaxf(out.mxy - out.mny, out.mxz - out.mnz));
-        float4* rec = w.node + 4 * static_cast<size_t>(pNode);
-        __stcg(&rec[0], make_float4(out.cx, out.cy, out.cz, mSum));
-        __stcg(&rec[1], make_float4(__fmul_rn(dNode, dNode), __int_as_float(lc), __int_as_float(rc), out.maxHs));
-        __stcg(&rec[2], make_float4(out.mnx, out.mny, out.mnz, out.maxH));
-        __stcg(&rec[3], make_float4(out.mxx, out.mxy, out.mxz, 0.0f));
-        double2* mp = reinterpret_cast<double2*>(w.nodeMom + pNode);
-        __stcg(&mp[0], make_double2(out.mom.sx, out.mom.sy));
-        __stcg(&mp[1], make_double2(out.mom.sz, out.mom.m));
-        if (bvh.aabbMinX != nullptr) {
-            bvh.aabbMinX[pNode] = out.mnx; bvh.aabbMinY[pNode] = out.mny; bvh.aabbMinZ[pNode] = out.mnz;
-            bvh.aabbMaxX[pNode] = out.mxx; bvh.aabbMaxY[pNode] = out.mxy; bvh.aabbMaxZ[pNode] = out.mxz;
-            bvh.nodeMaxH[pNode] = out.maxH; bvh.nodeMass[pNode] = mSum;
-            bvh.comX[pNode] = out.cx; bvh.comY[pNode] = out.cy; bvh.comZ[pNode] = out.cz;
-        }
-        if (bvh.nodeComMass != nullptr) {
-            bvh.nodeComMass[pNode] = AstraeaFloat4{out.cx, out.cy, out.cz, mSum};
-            bvh.nodeMinExtent[pNode] = AstraeaFloat4{out.mnx, out.mny, out.mnz, dNode};
-            bvh.nodeMaxHPacked[pNode] = AstraeaFloat4{out.mxx, out.mxy, out.mxz, out.maxH};
-        }
-        mine = out;
-        curr = pNode;
-        pNode = grand;
+__device__ void writeNode(const AstraeaRadixBvh& bvh, const Work& w, int node, const Ext8& e, const double* M) {
+    const int lc = __ldg(&bvh.leftChild[node]), rc = __ldg(&bvh.rightChild[node]);
+    float cx, cy, cz;
+    if (M[0] > 0.0) {
+        const double im = 1.0 / M[0];
+        cx = static_cast<float>(M[1] * im);
+        cy = static_cast<float>(M[2] * im);
+        cz = static_cast<float>(M[3] * im);
+    } else {                                       // massless subtree: the box centre
+        cx = 0.5f * (e.mnx + e.mxx);
+        cy = 0.5f * (e.mny + e.mxy);
+        cz = 0.5f * (e.mnz + e.mxz);
     }
+    const float mSum = static_cast<float>(M[0]);
+    const float dNode = fmaxf(e.mxx - e.mnx, fmaxf(e.mxy - e.mny, e.mxz - e.mnz));
+    float4* rec = w.node + 4 * static_cast<size_t>(node);
+    __stcg(&rec[0], make_float4(cx, cy, cz, mSum));
+    __stcg(&rec[1], make_float4(__fmul_rn(dNode, dNode), __int_as_float(lc), __int_as_float(rc), e.hs));
+    __stcg(&rec[2], make_float4(e.mnx, e.mny, e.mnz, e.h));
+    __stcg(&rec[3], make_float4(e.mxx, e.mxy, e.mxz, 0.0f));
+    if (kMoments) {
+        float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (M[0] > 0.0) {
+            const double c[3] = {M[1] / M[0], M[2] / M[0], M[3] / M[0]};
+            s[0] = static_cast<float>(fmax(0.0, M[4] - M[0] * c[0] * c[0]));
+            s[1] = static_cast<float>(fmax(0.0, M[5] - M[0] * c[1] * c[1]));
+            s[2] = static_cast<float>(fmax(0.0, M[6] - M[0] * c[2] * c[2]));
+            s[3] = static_cast<float>(M[7] - M[0] * c[0] * c[1]);
+            s[4] = static_cast<float>(M[8] - M[0] * c[0] * c[2]);
+            s[5] = static_cast<float>(M[9] - M[0] * c[1] * c[2]);
+        }
+        __stcg(&w.nodeQuad[2 * static_cast<size_t>(node)], make_float4(s[0], s[1], s[2], s[3]));
+        __stcg(&w.nodeQuad[2 * static_cast<size_t>(node) + 1], make_float4(s[4], s[5], 0.0f, 0.0f));
+    }
+    if (bvh.aabbMinX != nullptr) {
+        bvh.aabbMinX[node] = e.mnx; bvh.aabbMinY[node] = e.mny; bvh.aabbMinZ[node] = e.mnz;
+        bvh.aabbMaxX[node] = e.mxx; bvh.aabbMaxY[node] = e.mxy; bvh.aabbMaxZ[node] = e.mxz;
+        bvh.nodeMaxH[node] = e.h; bvh.nodeMass[node] = mSum;
+        bvh.comX[node] = cx; bvh.comY[node] = cy; bvh.comZ[node] = cz;
+    }
+    if (bvh.nodeComMass != nullptr) {
+        bvh.nodeComMass[node] = AstraeaFloat4{cx, cy, cz, mSum};
+        bvh.nodeMinExtent[node] = AstraeaFloat4{e.mnx, e.mny, e.mnz, dNode};
+        bvh.nodeMaxHPacked[node] = AstraeaFloat4{e.mxx, e.mxy, e.mxz, e.h};
+    }
+}
+
+template <bool kMoments>
+__global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh bvh, Work w, uint32_t n) {
+    constexpr int kW = kMoments ? kMomW : 4;
+    __shared__ float sx[kRefitBlock], sy[kRefitBlock], sz[kRefitBlock], sh[kRefitBlock], shs[kRefitBlock];
+    __shared__ double sP[kW][kRefitBlock];         // inclusive block prefix of the moments
+    __shared__ Ext8 warpPre[kRefitBlock / 32], warpSuf[kRefitBlock / 32];
+    __shared__ double warpTot[kW][kRefitBlock / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t b0 = blockIdx.x * kRefitBlock;
+    const uint32_t i = b0 + static_cast<uint32_t>(t);
+    const bool valid = i < n;
+    Ext8 e = extEmpty();
+    double v[kW];
+#pragma unroll
+    for (int k = 0; k < kW; ++k) v[k] = 0.0;
+    if (valid) {
+        const float4 pm = __ldg(&w.leafPM[i]);
+        const float4 ax = __ldg(&w.leafAux[i]);
+        e = Ext8{pm.x, pm.y, pm.z, pm.x, pm.y, pm.z, ax.z, ax.x};
+        const double m = pm.w, x = pm.x, y = pm.y, z = pm.z;
+        v[0] = m; v[1] = m * x; v[2] = m * y; v[3] = m * z;
+        if constexpr (kMoments) {
+            v[4] = m * x * x; v[5] = m * y * y; v[6] = m * z * z;
+            v[7] = m * x * y; v[8] = m * x * z; v[9] = m * y * z;
+        }
+    }
+    sx[t] = e.mnx; sy[t] = e.mny; sz[t] = e.mnz; sh[t] = e.h; shs[t] = e.hs;
+    // warp-inclusive scans: prefix (up), suffix (down), moments (up)
+    Ext8 pre = e, suf = e;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const Ext8 u = extShfl(pre, d, true);
+        if (lane >= d) pre = extJoin(pre, u);
+        const Ext8 q = extShfl(suf, d, false);
+        if (lane + d < 32) suf = extJoin(suf, q);
+#pragma unroll
+        for (int k = 0; k < kW; ++k) {
+            const double o = __shfl_up_sync(0xffffffffu, v[k], d);
+            if (lane >= d) v[k] += o;
+        }
+    }
+    if (lane == 31) {
+        warpPre[warp] = pre;
+#pragma unroll
+        for (int k = 0; k < kW; ++k) warpTot[k][warp] = v[k];
+    }
+    if (lane == 0) warpSuf[warp] = suf;
+    __syncthreads();
+    for (int q = 0; q < warp; ++q) {
+        pre = extJoin(pre, warpPre[q]);
+#pragma unroll
+        for (int k = 0; k < kW; ++k) v[k] += warpTot[k][q];
+    }
+    for (int q = warp + 1; q < kRefitBlock / 32; ++q) suf = extJoin(suf, warpSuf[q]);
+#pragma unroll
+    for (int k = 0; k < kW; ++k) sP[k][t] = v[k];
+    if (valid) {
+        float4* ls = w.leafScan + 4 * static_cast<size_t>(i);
+        extStore(ls, pre);
+        extStore(ls + 2, suf);
+        double* ms = w.momScan + static_cast<size_t>(kMomW) * i;
+#pragma unroll
+        for (int k = 0; k < kW; ++k) ms[k] = v[k];
+    }
+    if (t == kRefitBlock - 1) {                    // block totals (level 0 of the table)
+        Ext8 all = pre;
+        extStore(w.blockTable + 2 * static_cast<size_t>(blockIdx.x), all);
+#pragma unroll
+        for (int k = 0; k < kW; ++k) w.blockMom[static_cast<size_t>(kMomW) * blockIdx.x + k] = v[k];
+    }
+    __syncthreads();
+    // internal nodes whose range lies inside this block
+    if (i + 1u < n) {
+        const uint2 r = __ldg(&w.nodeRange[i]);
+        if (r.x >= b0 && r.y < b0 + kRefitBlock && r.x <= r.y) {
+            const int f = static_cast<int>(r.x - b0), l = static_cast<int>(r.y - b0);
+            Ext8 a = extEmpty();
+            for (int k = f; k <= l; ++k)
+                a = extJoin(a, Ext8{sx[k], sy[k], sz[k], sx[k], sy[k], sz[k], sh[k], shs[k]});
+            double M[kMomW];
+#pragma unroll
+            for (int k = 0; k < kW; ++k) M[k] = sP[k][l] - (f > 0 ? sP[k][f - 1] : 0.0);
+#pragma unroll
+            for (int k = kW; k < kMomW; ++k) M[k] = 0.0;
+            writeNode<kMoments>(bvh, w, static_cast<int>(i), a, M);
+        }
+    }
+}
+
+// Block offsets (exclusive FP64 scan of the totals, in place) and the
+// sparse table of block extremes; one block of 1024 threads.
+template <bool kMoments>
+__global__ void __launch_bounds__(1024) refitTableKernel(Work w, uint32_t nb, uint32_t levels) {
+    constexpr int kW = kMoments ? kMomW : 4;
+    __shared__ double warpSum[kW][32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint32_t per = (nb + 1023u) / 1024u;
+    const uint32_t lo = min(nb, t * per), hi = min(nb, lo + per);
+    double acc[kW];
+#pragma unroll
+    for (int k = 0; k < kW; ++k) acc[k] = 0.0;
+    for (uint32_t b = lo; b < hi; ++b)
+#pragma unroll
+        for (int k = 0; k < kW; ++k) acc[k] += w.blockMom[static_cast<size_t>(kMomW) * b + k];
+    // exclusive scan of the per-thread sums: warp shuffles, then warp totals
+    double inc[kW];
+#pragma unroll
+    for (int k = 0; k < kW; ++k) inc[k] = acc[k];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+#pragma unroll
+        for (int k = 0; k < kW; ++k) {
+            const double o = __shfl_up_sync(0xffffffffu, inc[k], d);
+            if (lane >= static_cast<uint32_t>(d)) inc[k] += o;
+        }
+    if (lane == 31u)
+#pragma unroll
+        for (int k = 0; k < kW; ++k) warpSum[k][warp] = inc[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < kW; ++k) {
+            double x = warpSum[k][lane];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const double o = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= static_cast<uint32_t>(d)) x += o;
+            }
+            warpSum[k][lane] = x;                  // inclusive over warps
+        }
+    }
+    __syncthreads();
+    double run[kW];
+#pragma unroll
+    for (int k = 0; k < kW; ++k) run[k] = inc[k] - acc[k] + (warp > 0 ? warpSum[k][warp - 1] : 0.0);
+    for (uint32_t b = lo; b < hi; ++b)
+#pragma unroll
+        for (int k = 0; k < kW; ++k) {
+            double* slot = &w.blockMom[static_cast<size_t>(kMomW) * b + k];
+            const double x = *slot;
+            *slot = run[k];
+            run[k] += x;
+        }
+    for (uint32_t lev = 1; lev < levels; ++lev) {
+        __syncthreads();
+        const uint32_t span = 1u << (lev - 1);
+        const float4* src = w.blockTable + 2 * static_cast<size_t>(lev - 1) * nb;
+        float4* dst = w.blockTable + 2 * static_cast<size_t>(lev) * nb;
+        for (uint32_t b = t; b + 2u * span <= nb; b += 1024u)
+            extStore(dst + 2 * b, extJoin(extLoad(src + 2 * b), extLoad(src + 2 * (b + span))));
+    }
+}
+
+// Nodes whose range spans blocks.
+template <bool kMoments>
+__global__ void __launch_bounds__(256) refitCrossKernel(AstraeaRadixBvh bvh, Work w, uint32_t n, uint32_t nb) {
+    constexpr int kW = kMoments ? kMomW : 4;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1u >= n) return;
+    const uint2 r = __ldg(&w.nodeRange[i]);
+    const uint32_t bf = r.x / kRefitBlock, bl = r.y / kRefitBlock;
+    if (bf == bl || r.y >= n || r.x > r.y) return;
+    Ext8 e = extJoin(extLoad(w.leafScan + 4 * static_cast<size_t>(r.x) + 2),   // suffix in first's block
+                     extLoad(w.leafScan + 4 * static_cast<size_t>(r.y)));      // prefix in last's block
+    if (bl > bf + 1u) {
+        const uint32_t lo = bf + 1u, hi = bl - 1u, len = hi - lo + 1u;
+        const uint32_t lev = 31u - static_cast<uint32_t>(__clz(len));
+        const float4* tab = w.blockTable + 2 * static_cast<size_t>(lev) * nb;
+        e = extJoin(e, extJoin(extLoad(tab + 2 * lo), extLoad(tab + 2 * (hi + 1u - (1u << lev)))));
+    }
+    double M[kMomW];
+    const double* ml = w.momScan + static_cast<size_t>(kMomW) * r.y;
+    const double* ol = w.blockMom + static_cast<size_t>(kMomW) * bl;
+#pragma unroll
+    for (int k = 0; k < kW; ++k) M[k] = __ldcg(&ol[k]) + __ldcg(&ml[k]);
+    if (r.x > 0u) {
+        const uint32_t f1 = r.x - 1u;
+        const double* mf = w.momScan + static_cast<size_t>(kMomW) * f1;
+        const double* of = w.blockMom + static_cast<size_t>(kMomW) * (f1 / kRefitBlock);
+#pragma unroll
+        for (int k = 0; k < kW; ++k) M[k] -= __ldcg(&of[k]) + __ldcg(&mf[k]);
+    }
+#pragma unroll
+    for (int k = kW; k < kMomW; ++k) M[k] = 0.0;
+    writeNode<kMoments>(bvh, w, static_cast<int>(i), e, M);
 }
 
 inline unsigned gridFor(uint32_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
@@ -338,12 +483,26 @@ cudaError_t launchRefreshLeaves(const AstraeaParticles& p, const Work& w, uint32
     return cudaGetLastError();
 }
 
+uint32_t refitBlocks(uint32_t n) { return (n + kRefitBlock - 1) / kRefitBlock; }
+uint32_t refitLevels(uint32_t nb) {
+    uint32_t lev = 1;
+    while ((2u << (lev - 1)) <= nb) ++lev;      // levels 0 .. floor(log2 nb)
+    return lev;
+}
+
 cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, bool moments, cudaStream_t st) {
     if (n < 2u) return cudaSuccess;
-    if (moments)
-        refitKernel<true><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n);
-    else
-        refitKernel<false><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n);
+    const uint32_t nb = refitBlocks(n);
+    const uint32_t levels = refitLevels(nb);
+    if (moments) {
+        refitBlockKernel<true><<<nb, kRefitBlock, 0, st>>>(bvh, w, n);
+        refitTableKernel<true><<<1, 1024, 0, st>>>(w, nb, levels);
+        refitCrossKernel<true><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
+    } else {
+        refitBlockKernel<false><<<nb, kRefitBlock, 0, st>>>(bvh, w, n);
+        refitTableKernel<false><<<1, 1024, 0, st>>>(w, nb, levels);
+        refitCrossKernel<false><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
+    }
     return cudaGetLastError();
 }
 

@@ -128,7 +128,10 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     size_t off = 0;
     auto take = [&](size_t bytes) { const size_t o = off; off += alignUp(bytes); return o; };
     const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 16 * kRec2Width);
-    const size_t oNode = take(C * 64), oMom = take(C * 32), oQuad = take(C * 32), oDrift = take(C * 16);
+    const size_t nbMax = refitBlocks(static_cast<uint32_t>(C)), levMax = refitLevels(static_cast<uint32_t>(nbMax));
+    const size_t oNode = take(C * 64), oRange = take(C * 8), oLScan = take(C * 64), oMScan = take(C * 80);
+    const size_t oTable = take(levMax * nbMax * 32), oBMom = take(nbMax * 80), oQuad = take(C * 32);
+    const size_t oDrift = take(C * 16);
     const size_t oDRec = take(C * 16), oDAux = take(C * 8);
     const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
     const size_t oSort = take(sortWords * 4), oDt = take(64);
@@ -147,7 +150,11 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     w.velRho = reinterpret_cast<float4*>(b + oVR);
     w.rec2 = reinterpret_cast<float4*>(b + oRec);
     w.node = reinterpret_cast<float4*>(b + oNode);
-    w.nodeMom = reinterpret_cast<NodeMom*>(b + oMom);
+    w.nodeRange = reinterpret_cast<uint2*>(b + oRange);
+    w.leafScan = reinterpret_cast<float4*>(b + oLScan);
+    w.momScan = reinterpret_cast<double*>(b + oMScan);
+    w.blockTable = reinterpret_cast<float4*>(b + oTable);
+    w.blockMom = reinterpret_cast<double*>(b + oBMom);
     w.nodeQuad = reinterpret_cast<float4*>(b + oQuad);
     w.driftPos = reinterpret_cast<float4*>(b + oDrift);
     w.driftRec = reinterpret_cast<float4*>(b + oDRec);

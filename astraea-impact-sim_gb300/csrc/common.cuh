@@ -13,7 +13,7 @@
 //        r1 {dNode^2 (dNode = largest box side), left (int bits), right (int bits), maxHs}
 //        r2 {minX, minY, minZ, maxH}             maxH = max 2h (engine field)
 //        r3 {maxX, maxY, maxZ, 0}
-//   nodeMom [N-1] NodeMom {sum m x, sum m y, sum m z, sum m}  FP64 refit
+//   nodeRange [N-1] uint2 {first, last} sorted leaf range of the node (refit)
 //
 // Search radius: pass 1 (engine/sph_gravity.cu:713) needs r < 2 h_old,
 // pass 2 and the next drift (:1071, :1439) need r < max(2 h_i, 2 h_j) with
@@ -375,7 +375,11 @@ struct Work {
     float4* velRho;
     float4* rec2;          // kRec2Width float4 per particle: the pass-2 record
     float4* node;          // 4 x float4 per internal node
-    NodeMom* nodeMom;
+    uint2* nodeRange;      // [N-1] {first, last}: the sorted leaf range of each internal node
+    float4* leafScan;      // [4N] per leaf: block prefix and block suffix {min xyz, max 2h}, {max xyz, max Hs}
+    double* momScan;       // [10N] per leaf: inclusive block prefix of m, m x (3), m x x^T (6)
+    float4* blockTable;    // [2 levels nb] sparse table of block extremes (level 0: the blocks)
+    double* blockMom;      // [10 nb] block totals, then exclusive block offsets
     float4* nodeQuad;      // 2 x float4 per internal node: central second moments
                            // {Sxx, Syy, Szz, Sxy}, {Sxz, Syz, 0, 0} (far-field mode 1)
     float4* driftPos;      // {x, y, z, 0} after the drift

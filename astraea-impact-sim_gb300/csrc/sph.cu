@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w
             const float4 b4 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 4]);
             const float4 b5 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 5]);
             const float mj = b1.w, rhoJ = b2.x, pOverRho2J = b2.y, csJ = b2.z, fBalJ = b2.w;
-            const float volJ = b5.x, invRhoJ2 = b5.z;
+            const float volJ = b5.x;
             const float dvx = vxi - b1.x, dvy = vyi - b1.y, dvz = vzi - b1.z;
             const float vDotR = dvx * dx + dvy * dy + dvz * dz;
             const float r = sqrtf(r2);
