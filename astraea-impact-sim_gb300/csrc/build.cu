@@ -268,10 +268,12 @@ __device__ void writeNode(const AstraeaRadixBvh& bvh, const Work& w, int node, c
 template <bool kMoments>
 __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh bvh, Work w, uint32_t n) {
     constexpr int kW = kMoments ? kMomW : 4;
-    __shared__ float sx[kRefitBlock], sy[kRefitBlock], sz[kRefitBlock], sh[kRefitBlock], shs[kRefitBlock];
-    __shared__ double sP[kW][kRefitBlock];         // inclusive block prefix of the moments
-    __shared__ Ext8 warpPre[kRefitBlock / 32], warpSuf[kRefitBlock / 32];
-    __shared__ double warpTot[kW][kRefitBlock / 32];
+    constexpr int kWarps = kRefitBlock / 32;
+    __shared__ Ext8 wPre[kRefitBlock], wSuf[kRefitBlock];   // warp-inclusive prefix / suffix extremes
+    __shared__ Ext8 warpAgg[kWarps];
+    __shared__ Ext8 sLeaf[kRefitBlock];                     // each leaf's own extremes
+    __shared__ double sP[kW][kRefitBlock];                  // inclusive block prefix of the moments
+    __shared__ double warpOff[kW][kWarps];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t b0 = blockIdx.x * kRefitBlock;
     const uint32_t i = b0 + static_cast<uint32_t>(t);
@@ -291,7 +293,6 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
             v[7] = m * x * y; v[8] = m * x * z; v[9] = m * y * z;
         }
     }
-    sx[t] = e.mnx; sy[t] = e.mny; sz[t] = e.mnz; sh[t] = e.h; shs[t] = e.hs;
     // warp-inclusive scans: prefix (up), suffix (down), moments (up)
     Ext8 pre = e, suf = e;
 #pragma unroll
@@ -306,21 +307,34 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
             if (lane >= d) v[k] += o;
         }
     }
+    sLeaf[t] = e;
+    wPre[t] = pre;
+    wSuf[t] = suf;
     if (lane == 31) {
-        warpPre[warp] = pre;
+        warpAgg[warp] = pre;
 #pragma unroll
-        for (int k = 0; k < kW; ++k) warpTot[k][warp] = v[k];
+        for (int k = 0; k < kW; ++k) warpOff[k][warp] = v[k];
     }
-    if (lane == 0) warpSuf[warp] = suf;
     __syncthreads();
-    for (int q = 0; q < warp; ++q) {
-        pre = extJoin(pre, warpPre[q]);
+    if (t == 0) {                                   // exclusive offsets of the warps' moment sums
 #pragma unroll
-        for (int k = 0; k < kW; ++k) v[k] += warpTot[k][q];
+        for (int k = 0; k < kW; ++k) {
+            double run = 0.0;
+            for (int q = 0; q < kWarps; ++q) {
+                const double x = warpOff[k][q];
+                warpOff[k][q] = run;
+                run += x;
+            }
+        }
     }
-    for (int q = warp + 1; q < kRefitBlock / 32; ++q) suf = extJoin(suf, warpSuf[q]);
+    __syncthreads();
+    for (int q = 0; q < warp; ++q) pre = extJoin(pre, warpAgg[q]);
+    for (int q = warp + 1; q < kWarps; ++q) suf = extJoin(suf, warpAgg[q]);
 #pragma unroll
-    for (int k = 0; k < kW; ++k) sP[k][t] = v[k];
+    for (int k = 0; k < kW; ++k) {
+        v[k] += warpOff[k][warp];
+        sP[k][t] = v[k];
+    }
     if (valid) {
         float4* ls = w.leafScan + 4 * static_cast<size_t>(i);
         extStore(ls, pre);
@@ -330,8 +344,7 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
         for (int k = 0; k < kW; ++k) ms[k] = v[k];
     }
     if (t == kRefitBlock - 1) {                    // block totals (level 0 of the table)
-        Ext8 all = pre;
-        extStore(w.blockTable + 2 * static_cast<size_t>(blockIdx.x), all);
+        extStore(w.blockTable + 2 * static_cast<size_t>(blockIdx.x), pre);
 #pragma unroll
         for (int k = 0; k < kW; ++k) w.blockMom[static_cast<size_t>(kMomW) * blockIdx.x + k] = v[k];
     }
@@ -341,9 +354,19 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
         const uint2 r = __ldg(&w.nodeRange[i]);
         if (r.x >= b0 && r.y < b0 + kRefitBlock && r.x <= r.y) {
             const int f = static_cast<int>(r.x - b0), l = static_cast<int>(r.y - b0);
-            Ext8 a = extEmpty();
-            for (int k = f; k <= l; ++k)
-                a = extJoin(a, Ext8{sx[k], sy[k], sz[k], sx[k], sy[k], sz[k], sh[k], shs[k]});
+            const int wf = f >> 5, wl = l >> 5;
+            Ext8 a;
+            if (wf != wl) {                         // suffix + prefix + whole warps between
+                a = extJoin(wSuf[f], wPre[l]);
+                for (int q = wf + 1; q < wl; ++q) a = extJoin(a, warpAgg[q]);
+            } else if ((f & 31) == 0) {
+                a = wPre[l];
+            } else if ((l & 31) == 31) {
+                a = wSuf[f];
+            } else {                                // inside one warp, off both ends: <= 30 leaves
+                a = extEmpty();
+                for (int k = f; k <= l; ++k) a = extJoin(a, sLeaf[k]);
+            }
             double M[kMomW];
 #pragma unroll
             for (int k = 0; k < kW; ++k) M[k] = sP[k][l] - (f > 0 ? sP[k][f - 1] : 0.0);
@@ -354,10 +377,10 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
     }
 }
 
-// Block offsets (exclusive FP64 scan of the totals, in place) and the
-// sparse table of block extremes; one block of 1024 threads.
+// Block offsets: exclusive FP64 scan of the block totals, in place; one
+// block of 1024 threads.
 template <bool kMoments>
-__global__ void __launch_bounds__(1024) refitTableKernel(Work w, uint32_t nb, uint32_t levels) {
+__global__ void __launch_bounds__(1024) refitScanKernel(Work w, uint32_t nb) {
     constexpr int kW = kMoments ? kMomW : 4;
     __shared__ double warpSum[kW][32];
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
@@ -369,7 +392,6 @@ __global__ void __launch_bounds__(1024) refitTableKernel(Work w, uint32_t nb, ui
     for (uint32_t b = lo; b < hi; ++b)
 #pragma unroll
         for (int k = 0; k < kW; ++k) acc[k] += w.blockMom[static_cast<size_t>(kMomW) * b + k];
-    // exclusive scan of the per-thread sums: warp shuffles, then warp totals
     double inc[kW];
 #pragma unroll
     for (int k = 0; k < kW; ++k) inc[k] = acc[k];
@@ -408,14 +430,17 @@ __global__ void __launch_bounds__(1024) refitTableKernel(Work w, uint32_t nb, ui
             *slot = run[k];
             run[k] += x;
         }
-    for (uint32_t lev = 1; lev < levels; ++lev) {
-        __syncthreads();
-        const uint32_t span = 1u << (lev - 1);
-        const float4* src = w.blockTable + 2 * static_cast<size_t>(lev - 1) * nb;
-        float4* dst = w.blockTable + 2 * static_cast<size_t>(lev) * nb;
-        for (uint32_t b = t; b + 2u * span <= nb; b += 1024u)
-            extStore(dst + 2 * b, extJoin(extLoad(src + 2 * b), extLoad(src + 2 * (b + span))));
-    }
+}
+
+// One level of the sparse table of block extremes: T[lev][b] = T[lev-1][b]
+// joined with T[lev-1][b + 2^(lev-1)].
+__global__ void __launch_bounds__(256) refitLevelKernel(Work w, uint32_t nb, uint32_t lev) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t span = 1u << (lev - 1);
+    if (b + 2u * span > nb) return;
+    const float4* src = w.blockTable + 2 * static_cast<size_t>(lev - 1) * nb;
+    extStore(w.blockTable + 2 * (static_cast<size_t>(lev) * nb + b),
+             extJoin(extLoad(src + 2 * b), extLoad(src + 2 * (b + span))));
 }
 
 // Nodes whose range spans blocks.
@@ -496,13 +521,17 @@ cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, b
     const uint32_t levels = refitLevels(nb);
     if (moments) {
         refitBlockKernel<true><<<nb, kRefitBlock, 0, st>>>(bvh, w, n);
-        refitTableKernel<true><<<1, 1024, 0, st>>>(w, nb, levels);
-        refitCrossKernel<true><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
+        refitScanKernel<true><<<1, 1024, 0, st>>>(w, nb);
     } else {
         refitBlockKernel<false><<<nb, kRefitBlock, 0, st>>>(bvh, w, n);
-        refitTableKernel<false><<<1, 1024, 0, st>>>(w, nb, levels);
-        refitCrossKernel<false><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
+        refitScanKernel<false><<<1, 1024, 0, st>>>(w, nb);
     }
+    for (uint32_t lev = 1; lev < levels; ++lev)
+        refitLevelKernel<<<gridFor(nb, 256), 256, 0, st>>>(w, nb, lev);
+    if (moments)
+        refitCrossKernel<true><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
+    else
+        refitCrossKernel<false><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
     return cudaGetLastError();
 }
 
