@@ -42,8 +42,14 @@ sys.path.insert(0, os.path.join(ROOT, "astraea-impact-sim_gb300"))
 METRIC = "particle-steps/s at N=1M, learned-θ vs plain BH at equal force error"
 UNIT = "particle-steps/s"
 FLOP_PER_INTERACTION = 23        # 20 force + 3 potential (rsqrt counted once)
-KERNELS_PER_STEP = 19            # kick, drift, histogram, 8 onesweep, permute, refit,
-                                 # neighbour lists, pass 1, EOS, gravity, pass 2, kick
+def kernels_per_step(n):
+    """Launches of one fused step: kick, drift, histogram, 8 onesweep,
+    permute + Karras, the refit (block, scan, one per sparse-table level
+    above the first, cross), neighbour lists, pass 1, EOS, gravity, pass 2,
+    kick."""
+    nb = max(1, (n + 255) // 256)
+    levels = nb.bit_length()                   # levels 0 .. floor(log2 nb)
+    return 18 + 3 + (levels - 1)
 # Fields a fused step reads (uploaded every e2e step) and the fields the
 # engine's per-step telemetry reads back (engine/simulation.cpp:948-1000).
 E2E_IN = ["posX", "posY", "posZ", "velX", "velY", "velZ", "accX", "accY", "accZ", "mass", "h", "h0", "rho",
@@ -259,7 +265,7 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 in drift, refit moments)",
         "data": "synthetic (seeded hydrostatic bodies)",
         "config": workload_config(n, args.theta, args.far_field, args.workload),
-        "gpu_launches": KERNELS_PER_STEP * args.steps,
+        "gpu_launches": kernels_per_step(n) * args.steps,
         "clocks": clk,
         "roofline": {"kernel": "gravity (Barnes-Hut group walk + pair evaluation)", "bound": "fp32",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
