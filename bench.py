@@ -68,10 +68,11 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None,
                     help="particles (default: 1M for c2, 4M for c3, 16M for c5)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "planet"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "planet", "verify"],
                     help="c2: the 1M differentiated impact (the headline line); c3: 4M Plummer sphere, "
                          "gravity only, plain vs quadrupole and learned far field; c5: 16M gas-giant core impact; "
-                         "planet: scenario construction only (the planet_builder field)")
+                         "planet: scenario construction only (the planet_builder field); verify: the engine's "
+                         "headless --verify-conservation run (preset scenario, 100 steps) on the device path")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--max-dt-sec", type=float, default=5.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -790,6 +791,12 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.workload == "c3":
         run_c3(a)
+    elif a.workload == "verify":
+        from astraea_gb300 import headless
+        res = headless.run_headless("LivingGaiaAsteroidCataclysm", particles=a.n or 100000, steps=100)
+        print(json.dumps({"workload": "verify", "metric": "conservation over 100 steps (engine thresholds)",
+                          **res}))
+        sys.exit(0 if res["ok"] else 1)
     elif a.workload == "planet":
         import numpy as np
         import torch

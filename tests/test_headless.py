@@ -1,0 +1,82 @@
+"""The engine's scenario loading and conservation audits, run end to end on
+the library's device path (astraea_gb300.headless): preset configuration
+(engine/presets.cpp:147-210), bodies built and relaxed on the device,
+Kepler approach orbit and merge (engine/simulation.cpp:1300-1470), fused
+steps with the device telemetry reduction.
+
+* AC-5 of tests/cpp/test_conservation.cpp:123-158: EarthTheiaMoonForming,
+  20,000 particles, 150 steps of at most 5 s: |energy drift| < 1 %,
+  |dP| / (M v_esc(1.4 R_earth)) < 1e-4, |dL| / |L0| < 0.5 %;
+* the --verify-conservation thresholds of engine/headless_main.cpp:263-281
+  on the runner's default preset;
+* AC-9 of tests/cpp/test_conservation.cpp:197-258: the surface tracers of the
+  LivingTerra target stay a permutation of 0 .. 6 G^2 - 1 across re-sorts.
+CPU: the preset table and the Kepler placement's contact speed.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from astraea_gb300 import headless
+
+
+def test_presets_match_the_engine_table():
+    cfg = headless.preset_config("LivingGaiaAsteroidCataclysm", 100000)
+    assert cfg["target"].archetype == 0 and cfg["impactor"].archetype == 5
+    assert cfg["impactor"].massKg == pytest.approx(0.025 * headless.M_EARTH)
+    assert cfg["impactor"].coreTempK == 1800.0 and cfg["impactor"].spinOmegaRadS == 0.0
+    assert cfg["target"].relaxSteps == 80 and cfg["grid"] == 16 and cfg["seed"] == 42
+    assert (cfg["v_ratio"], cfg["b"], cfg["sep"]) == (1.65, 0.30, 3.2)
+    m = headless.preset_config("MercuryMantleStrip", 10)
+    assert m["target"].surfaceTempK == 440.0 and m["impactor"].archetype == 1
+    assert headless.preset_config("EarthTheiaMoonForming", 10, relax_steps=3)["impactor"].relaxSteps == 3
+
+
+def kepler_contact_speed(mtot, rc, d0, vrad, vperp):
+    """Speed at separation rc on the two-body orbit starting at d0 with
+    relative velocity (vrad, vperp): energy conservation."""
+    v2 = vrad * vrad + vperp * vperp + 2.0 * headless.G_PSU * mtot * (1.0 / rc - 1.0 / d0)
+    return math.sqrt(v2)
+
+
+def test_kepler_placement_reaches_the_requested_contact_speed():
+    G = headless.G_PSU
+    mtot, rc, vr, b, sep = 6.1, 9.4, 1.65, 0.30, 3.2
+    vesc = math.sqrt(2.0 * G * mtot / rc)
+    vc = vr * vesc
+    d0 = sep * rc
+    v0 = math.sqrt(vc * vc - 2.0 * G * mtot * (1.0 / rc - 1.0 / d0))
+    vperp = rc * vc * b / d0
+    vrad = -math.sqrt(v0 * v0 - vperp * vperp)
+    assert kepler_contact_speed(mtot, rc, d0, vrad, vperp) == pytest.approx(vc, rel=1e-12)
+
+
+@pytest.mark.gpu
+def test_gpu_conservation_audit_earth_theia_20k():
+    res = headless.run_headless("EarthTheiaMoonForming", particles=20000, steps=150, dt_max_sec=5.0, verify=True)
+    print(res)
+    assert res["particles"] == 20000 and res["finite"]
+    assert abs(res["energy_drift_rel"]) < 0.01
+    assert res["dp_rel"] < 1.0e-4 and res["dl_rel"] < 0.005
+    assert res["ok"]
+
+
+@pytest.mark.gpu
+def test_gpu_verify_conservation_default_preset():
+    res = headless.run_headless("LivingGaiaAsteroidCataclysm", particles=30000, steps=100, verify=True)
+    print(res)
+    assert res["ok"], res
+    assert res["tracers"] == 6 * 16 * 16
+
+
+@pytest.mark.gpu
+def test_gpu_tracers_survive_resorts():
+    cfg = headless.preset_config("LivingGaiaAsteroidCataclysm", 30000, relax_steps=5)
+    sim, info = headless.load_scenario(cfg)
+    T = info["tracers"]
+    assert T == 6 * 16 * 16
+    for _ in range(10):
+        sim.step(5.0e-3)
+    t = sim.state(["tracerIndex"])["tracerIndex"]
+    assert np.array_equal(np.sort(t[t >= 0]), np.arange(T))
