@@ -157,6 +157,11 @@ class FarFieldStats(ctypes.Structure):
 FF_PARAMS = 6288
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("gravityWarps", _U32), ("neighborWarps", _U32), ("gravityMs", ctypes.c_float),
+                ("neighborMs", ctypes.c_float)]
+
+
 SIGNATURES = [
     ("astraea_gb300_last_error", [], ctypes.c_char_p),
     ("astraea_gb300_abi_version", [], ctypes.c_int),
@@ -198,6 +203,9 @@ SIGNATURES = [
     ("astraea_gb300_ff_get_params", [_VP, _U32, _VP], ctypes.c_int),
     ("astraea_gb300_ff_set_params", [_VP, _U32, _VP], ctypes.c_int),
     ("astraea_gb300_ff_stats", [ctypes.POINTER(FarFieldStats)], ctypes.c_int),
+    ("astraea_gb300_autotune", [_P, _B, _F, ctypes.POINTER(Tuning)], ctypes.c_int),
+    ("astraea_gb300_get_tuning", [_U32, ctypes.POINTER(Tuning)], ctypes.c_int),
+    ("astraea_gb300_set_tuning", [_U32, ctypes.POINTER(Tuning)], ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

@@ -447,6 +447,32 @@ def train_far_field(states, theta=0.5, group_stride=1, steps=600, batch=8192, lr
     return X.shape[0], hist
 
 
+# ------------------------------------------------------------- autotuning
+def _tuning_dict(t):
+    return {f: getattr(t, f) for f, _ in abi.Tuning._fields_}
+
+
+def autotune(p, bvh, theta=0.5):
+    """Chooses the warps per block of the gravity and neighbour walks on the
+    current tree (built for p) and keeps the choice for this particle-count
+    bucket; returns it."""
+    t = abi.Tuning()
+    s = p.struct()
+    abi.check(lib().astraea_gb300_autotune(ctypes.byref(s), ctypes.byref(bvh.s), float(theta), ctypes.byref(t)))
+    return _tuning_dict(t)
+
+
+def get_tuning(count):
+    t = abi.Tuning()
+    abi.check(lib().astraea_gb300_get_tuning(int(count), ctypes.byref(t)))
+    return _tuning_dict(t)
+
+
+def set_tuning(count, gravity_warps=4, neighbor_warps=4):
+    t = abi.Tuning(int(gravity_warps), int(neighbor_warps), 0.0, 0.0)
+    abi.check(lib().astraea_gb300_set_tuning(int(count), ctypes.byref(t)))
+
+
 def invalidate_step_cache(bvh):
     abi.check(lib().astraea_gb300_invalidate_step_cache(ctypes.byref(bvh.s)))
 

@@ -244,6 +244,24 @@ AstraeaStatus checkLaunch(cudaError_t e, const char* what) {
         if (agS != ASTRAEA_OK) return agS;                           \
     } while (0)
 
+// ------------------------------------------------------------ autotuning
+// Warps per block of the two tree walks, per device and power-of-two
+// particle count (bucket floor(log2 n)); {4, 4} until tuned.
+std::mutex g_tuneMutex;
+std::map<std::pair<int, int>, AstraeaTuning> g_tuning;
+
+int tuneBucket(uint32_t n) {
+    int b = 0;
+    while (b < 31 && (2u << b) <= n) ++b;
+    return b;
+}
+
+AstraeaTuning tuningFor(uint32_t n) {
+    std::lock_guard<std::mutex> lock(g_tuneMutex);
+    const auto it = g_tuning.find(std::make_pair(currentDevice(), tuneBucket(n)));
+    return (it == g_tuning.end()) ? AstraeaTuning{4u, 4u, 0.0f, 0.0f} : it->second;
+}
+
 // ------------------------------------------- far-field mode 2 (learned)
 struct FfState {
     ff::Net net{};
@@ -352,7 +370,8 @@ AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, flo
         f->stats.lastPairs = std::min(pairs, f->pairCap);
         f->stats.lastGateRms = rms;
         if (!(rms <= f->cfg.gateTolerance)) {      // the gate failed: plain walk at theta
-            AG_LAUNCH(launchGravity(*p, ws->w, n, theta, false, smCount(), st));
+            AG_LAUNCH(launchGravity(*p, ws->w, n, theta, false, smCount(), st, nullptr,
+                                    static_cast<int>(tuningFor(n).gravityWarps)));
             f->stats.fallbacks++;
         }
     }
@@ -610,7 +629,7 @@ AstraeaStatus astraea_gb300_sph_pass1_neighbors(AstraeaParticles* p, const Astra
     if (s != ASTRAEA_OK) return s;
     cudaStream_t st = stream();
     AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, true, st));
-    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st));
+    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st, static_cast<int>(tuningFor(n).neighborWarps)));
     AG_LAUNCH(launchPass1(*p, ws->w, n, st));
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
@@ -638,7 +657,8 @@ AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const Astrae
         s = learnedGravity(p, ws, n, theta, true);
         if (s != ASTRAEA_OK) return s;
     } else {
-        AG_LAUNCH(launchGravity(*p, ws->w, n, theta, mode == 1, smCount(), stream()));
+        AG_LAUNCH(launchGravity(*p, ws->w, n, theta, mode == 1, smCount(), stream(), nullptr,
+                                static_cast<int>(tuningFor(n).gravityWarps)));
     }
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
@@ -656,7 +676,7 @@ AstraeaStatus astraea_gb300_sph_pass2_forces(AstraeaParticles* p, const AstraeaR
     if (s != ASTRAEA_OK) return s;
     cudaStream_t st = stream();
     AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, true, st));
-    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st));
+    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st, static_cast<int>(tuningFor(n).neighborWarps)));
     AG_LAUNCH(launchPackPass2Records(*p, ws->w, n, st));
     const uint32_t* living = (bvh->livingFlags != nullptr) ? bvh->livingFlags : ds->zeroWords;   // :2104
     AG_LAUNCH(launchPass2(*p, ws->w, n, living, st));
@@ -692,7 +712,7 @@ AstraeaStatus astraea_gb300_leapfrog_drift(AstraeaParticles* p, float dtPsu, con
     AstraeaStatus s = builtWorkspace(bvh, n, &ws);
     if (s != ASTRAEA_OK) return s;
     AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, true, st));
-    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st));
+    AG_LAUNCH(launchBuildNeighbors(ws->w, n, smCount(), st, static_cast<int>(tuningFor(n).neighborWarps)));
     AG_LAUNCH(launchDrift(*p, ws->w, n, nullptr, dtPsu, true, false, nullptr, st));
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
@@ -1037,6 +1057,78 @@ AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out) {
     return ASTRAEA_OK;
 }
 
+// ------------------------------------------------------------- autotune
+AstraeaStatus astraea_gb300_autotune(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                     AstraeaTuning* out) {
+    if (p == nullptr || bvh == nullptr || out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const uint32_t n = p->count;
+    *out = tuningFor(n);
+    if (n < 2u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    cudaStream_t st = stream();
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, st));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    AG_CUDA(cudaEventCreate(&e0));
+    AG_CUDA(cudaEventCreate(&e1));
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } guard{e0, e1};
+    const int sms = smCount();
+    auto best3 = [&](auto launch, float* ms) -> cudaError_t {
+        cudaError_t e = launch();                  // warm-up
+        if (e != cudaSuccess) return e;
+        float best = 3.0e38f;
+        for (int r = 0; r < 3; ++r) {
+            if ((e = cudaEventRecord(e0, st)) != cudaSuccess) return e;
+            if ((e = launch()) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(e1, st)) != cudaSuccess) return e;
+            if ((e = cudaEventSynchronize(e1)) != cudaSuccess) return e;
+            float t = 0.0f;
+            if ((e = cudaEventElapsedTime(&t, e0, e1)) != cudaSuccess) return e;
+            best = std::min(best, t);
+        }
+        *ms = best;
+        return cudaSuccess;
+    };
+    AstraeaTuning t{4u, 4u, 3.0e38f, 3.0e38f};
+    for (int wv : {2, 4, 8}) {
+        float ms = 0.0f;
+        AG_CUDA(best3([&] { return launchGravity(*p, ws->w, n, theta, false, sms, st, nullptr, wv); }, &ms));
+        if (ms < t.gravityMs) { t.gravityMs = ms; t.gravityWarps = static_cast<uint32_t>(wv); }
+    }
+    for (int wv : {2, 4, 8}) {
+        float ms = 0.0f;
+        AG_CUDA(best3([&] { return launchBuildNeighbors(ws->w, n, sms, st, wv); }, &ms));
+        if (ms < t.neighborMs) { t.neighborMs = ms; t.neighborWarps = static_cast<uint32_t>(wv); }
+    }
+    ws->stepCacheValid = false;
+    {
+        std::lock_guard<std::mutex> lock(g_tuneMutex);
+        g_tuning[std::make_pair(currentDevice(), tuneBucket(n))] = t;
+    }
+    *out = t;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_get_tuning(uint32_t count, AstraeaTuning* out) {
+    if (out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    *out = tuningFor(count);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_set_tuning(uint32_t count, const AstraeaTuning* tuning) {
+    if (tuning == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    auto ok = [](uint32_t v) { return v == 2u || v == 4u || v == 8u; };
+    if (!ok(tuning->gravityWarps) || !ok(tuning->neighborWarps))
+        return fail(ASTRAEA_ERR_INVALID, "set_tuning: warps per block must be 2, 4 or 8");
+    std::lock_guard<std::mutex> lock(g_tuneMutex);
+    g_tuning[std::make_pair(currentDevice(), tuneBucket(count))] = *tuning;
+    return ASTRAEA_OK;
+}
+
 // ------------------------------------------------------ planet building
 static planet::BodySpec toBodySpec(const AstraeaBodySpec& s) {
     return planet::BodySpec{static_cast<int>(s.archetype > 5u ? 99u : s.archetype), s.massKg, s.surfaceTempK,
@@ -1118,6 +1210,7 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
         return fail(ASTRAEA_ERR_INVALID, "step: build the tree once with astraea_gb300_sort_and_build_bvh first");
     cudaStream_t st = stream();
     Work& w = ws->w;
+    const AstraeaTuning tune = tuningFor(n);
     const int sms = smCount();
     int q = ws->parity;
     const bool useBvh = bvh->leftChild != nullptr && bvh->rightChild != nullptr && n >= 2u;
@@ -1127,7 +1220,7 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
         AG_LAUNCH(launchSetDtSlots(ws->dtSlots, q, prevDtPsu, ws->rawMin, st));
         AG_LAUNCH(launchReduceDt(*p, n, ws->rawMin + q, sms, st));
         AG_LAUNCH(launchRefreshLeaves(*p, w, n, false, st));
-        if (useBvh) AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
+        if (useBvh) AG_LAUNCH(launchBuildNeighbors(w, n, sms, st, static_cast<int>(tune.neighborWarps)));
     }
     // 1. opening half kick; dt resolved on the device
     KickArgs k1{};
@@ -1146,14 +1239,15 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     s = buildTree(p, alt, bvh, ws, w.driftPos, false);
     if (s != ASTRAEA_OK) return s;
     // 4. neighbour lists for pass 1, pass 2 and the next drift
-    AG_LAUNCH(launchBuildNeighbors(w, n, sms, st));
+    AG_LAUNCH(launchBuildNeighbors(w, n, sms, st, static_cast<int>(tune.neighborWarps)));
     AG_LAUNCH(launchPass1(*p, w, n, st));
     AG_LAUNCH(launchEos(*p, &w, n, st));
     if (ws->momentsBuilt && g_farField.load() == 2) {
         s = learnedGravity(p, ws, n, theta, true);
         if (s != ASTRAEA_OK) return s;
     } else {
-        AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt && g_farField.load() == 1, sms, st));
+        AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt && g_farField.load() == 1, sms, st, nullptr,
+                                static_cast<int>(tune.gravityWarps)));
     }
     AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));
     // 5. closing half kick + EOS + next dt minimum

@@ -194,11 +194,11 @@ __device__ __forceinline__ void getMono(const float* list, int slot, float (&e)[
 // 1 / |s| for a direction s in {-1, 0, 1}^3 with nz non-zero components.
 __device__ __forceinline__ float invDirNorm(int nz) { return nz == 3 ? 0.57735027f : (nz == 2 ? 0.70710678f : 1.0f); }
 
-template <bool kInside, bool kQuad, bool kLearned>
-__global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
+template <int kWarps, bool kInside, bool kQuad, bool kLearned>
+__global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
                                                                  float theta2, uint32_t numGroups,
                                                                  uint32_t* groupCounter, FarCapture ff) {
-    __shared__ GravWarpSmem<kInside, kQuad> smem[kGravWarps];
+    __shared__ GravWarpSmem<kInside, kQuad> smem[kWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GravWarpSmem<kInside, kQuad>& S = smem[warp];
     unsigned long long nInter = 0, nTests = 0, nUndecided = 0, nRounds = 0;
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(kGravWarps * 32) gravityKernel(AstraeaParticle
 }  // namespace
 
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
-                          cudaStream_t st, const FarCapture* far) {
+                          cudaStream_t st, const FarCapture* far, int warps) {
     if (n == 0) return cudaSuccess;
     const float th = fmaxf(0.0f, theta);
     const float theta2 = th * th;
@@ -505,19 +505,30 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     FarCapture ff{};
-    auto kernel = checkInside ? (quadrupole ? gravityKernel<true, true, false> : gravityKernel<true, false, false>)
-                              : (quadrupole ? gravityKernel<false, true, false> : gravityKernel<false, false, false>);
+    using GravFn = void (*)(AstraeaParticles, Work, uint32_t, float, uint32_t, uint32_t*, FarCapture);
+    GravFn kernel = nullptr;
+    int wps = kGravWarps;
     if (far != nullptr) {
         ff = *far;
         if (ff.groupStride == 0u) ff.groupStride = 1u;
-        kernel = checkInside ? gravityKernel<true, false, true> : gravityKernel<false, false, true>;
+        kernel = checkInside ? gravityKernel<kGravWarps, true, false, true> : gravityKernel<kGravWarps, false, false, true>;
+    } else if (quadrupole) {
+        kernel = checkInside ? gravityKernel<kGravWarps, true, true, false> : gravityKernel<kGravWarps, false, true, false>;
+    } else if (warps == 2) {
+        kernel = checkInside ? gravityKernel<2, true, false, false> : gravityKernel<2, false, false, false>;
+        wps = 2;
+    } else if (warps == 8) {
+        kernel = checkInside ? gravityKernel<8, true, false, false> : gravityKernel<8, false, false, false>;
+        wps = 8;
+    } else {
+        kernel = checkInside ? gravityKernel<kGravWarps, true, false, false> : gravityKernel<kGravWarps, false, false, false>;
     }
     int perSm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, kGravWarps * 32, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, wps * 32, 0);
     if (e != cudaSuccess) return e;
     const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(std::max(1, perSm) * sms),
-                                               (groups + kGravWarps - 1) / kGravWarps);
-    kernel<<<blocks, kGravWarps * 32, 0, st>>>(p, w, n, theta2, groups, counter, ff);
+                                               (groups + wps - 1) / wps);
+    kernel<<<blocks, wps * 32, 0, st>>>(p, w, n, theta2, groups, counter, ff);
     return cudaGetLastError();
 }
 

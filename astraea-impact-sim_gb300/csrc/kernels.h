@@ -102,8 +102,10 @@ struct FarCapture {
     float gamma2;
     uint32_t groupStride;  // only groups g % stride == 0 apply the far test
 };
+// warps: 2, 4 or 8 warps per block for the plain walk (the autotuner's
+// choice; the far-field walks use 4); results do not depend on it.
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
-                          cudaStream_t st, const FarCapture* far = nullptr);
+                          cudaStream_t st, const FarCapture* far = nullptr, int warps = 4);
 
 // ---------------------------------------------------------------- ff.cu ---
 namespace ff {
@@ -133,7 +135,8 @@ cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uin
 }  // namespace ff
 
 // -------------------------------------------------------------- sph.cu ---
-cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st);
+// warps: 2, 4 or 8 warps per block (the autotuner's choice; results do not depend on it)
+cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st, int warps = 4);
 cudaError_t launchPass1(const AstraeaParticles& p, const Work& w, uint32_t n, cudaStream_t st);
 cudaError_t launchPass2(const AstraeaParticles& p, const Work& w, uint32_t n, const uint32_t* livingFlags,
                         cudaStream_t st);

@@ -45,9 +45,10 @@ __device__ __forceinline__ uint32_t laneMaskLt() {
     return m;
 }
 
-__global__ void __launch_bounds__(kNbWarps * 32) buildNeighborsKernel(Work w, uint32_t n, uint32_t numGroups,
-                                                                      uint32_t* groupCounter) {
-    __shared__ NbWarpSmem smem[kNbWarps];
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint32_t n, uint32_t numGroups,
+                                                                    uint32_t* groupCounter) {
+    __shared__ NbWarpSmem smem[kWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     NbWarpSmem& S = smem[warp];
     unsigned long long nEntries = 0, nCand = 0;
@@ -595,18 +596,22 @@ inline unsigned gridFor(uint32_t n, int block) { return static_cast<unsigned>((n
 
 }  // namespace
 
-cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st) {
+cudaError_t launchBuildNeighbors(const Work& w, uint32_t n, int sms, cudaStream_t st, int warps) {
     if (n == 0) return cudaSuccess;
     const uint32_t groups = (n + 31u) / 32u;
     uint32_t* counter = w.words + kWNbrCounter;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
+    using NbFn = void (*)(Work, uint32_t, uint32_t, uint32_t*);
+    const int wps = (warps == 2 || warps == 8) ? warps : kNbWarps;
+    const NbFn kernel = (wps == 2) ? buildNeighborsKernel<2> : (wps == 8) ? buildNeighborsKernel<8>
+                                                                         : buildNeighborsKernel<kNbWarps>;
     int perSm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, buildNeighborsKernel, kNbWarps * 32, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, wps * 32, 0);
     if (e != cudaSuccess) return e;
     const uint32_t blocks = std::min<uint32_t>(static_cast<uint32_t>(std::max(1, perSm) * sms),
-                                               (groups + kNbWarps - 1) / kNbWarps);
-    buildNeighborsKernel<<<blocks, kNbWarps * 32, 0, st>>>(w, n, groups, counter);
+                                               (groups + wps - 1) / wps);
+    kernel<<<blocks, wps * 32, 0, st>>>(w, n, groups, counter);
     return cudaGetLastError();
 }
 

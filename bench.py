@@ -80,6 +80,7 @@ def parse():
     ap.add_argument("--no-far-field", action="store_true", help="skip the far-field comparison (quadrupole and learned)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-planet", action="store_true", help="skip the planet-construction measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default block shape of the tree walks")
     ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
                     help="far-field model of the timed steps: 0 monopole (the engine's), 1 + quadrupole")
     ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
@@ -188,6 +189,10 @@ def run_gpu(args):
     sim.load_state(st)
     engine.reserve(sim.bvh, n)
     sim.evaluate_initial_forces(args.theta)
+    tuning = None
+    if not args.no_autotune:                   # block shape of the two walks, then fresh forces
+        tuning = engine.autotune(sim.p, sim.bvh, args.theta)
+        sim.evaluate_initial_forces(args.theta)
     for _ in range(max(args.warmup, 0)):
         sim.step(max_dt, args.theta)
     torch.cuda.synchronize()
@@ -287,6 +292,7 @@ def run_gpu(args):
         "e2e": e2e,
     }
     out["config"]["max_dt_psu"] = max_dt
+    out["config"]["autotuned_walks"] = tuning
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(st, args, max_dt)
     if rank == 0:

@@ -444,6 +444,33 @@ AstraeaStatus astraea_gb300_reserve(const AstraeaRadixBvh* bvh, uint32_t capacit
  * (the engine's fallback scratch lives until process exit). */
 AstraeaStatus astraea_gb300_release_scratch(const AstraeaRadixBvh* bvh);
 
+/* ---- autotuning (no engine counterpart) --------------------------------- */
+
+/* Block shape of the two tree walks: warps per block (2, 4 or 8) of the
+ * gravity walk and of the neighbour-list walk, and the times that chose
+ * them.  The walks' results do not depend on the block shape (each group of
+ * 32 particles is walked by one warp); the shape sets how many warps share
+ * an SM's registers and shared memory. */
+typedef struct AstraeaTuning {
+    uint32_t gravityWarps;
+    uint32_t neighborWarps;
+    float gravityMs;         /* best time of the chosen gravity variant (0 when set by hand) */
+    float neighborMs;        /* best time of the chosen neighbour-walk variant */
+} AstraeaTuning;
+
+/* Times the gravity walk (at theta) and the neighbour-list walk with 2, 4
+ * and 8 warps per block on the tree of bvh as built for p (after
+ * astraea_gb300_sort_and_build_bvh), best of three launches each, and keeps
+ * the fastest for every later call on this device whose particle count has
+ * the same floor(log2 count).  Overwrites p's gravity outputs and the
+ * neighbour lists (the next stage calls or step recompute both).  Blocks. */
+AstraeaStatus astraea_gb300_autotune(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                     AstraeaTuning* out);
+/* The tuning used for `count` particles on this device ({4, 4} untuned). */
+AstraeaStatus astraea_gb300_get_tuning(uint32_t count, AstraeaTuning* out);
+/* Sets it by hand (warps 2, 4 or 8), e.g. from a saved autotune result. */
+AstraeaStatus astraea_gb300_set_tuning(uint32_t count, const AstraeaTuning* tuning);
+
 /* ---- library primitives and diagnostics --------------------------------- */
 
 /* Stable LSD radix sort of (u64 key, u32 value) pairs over key bits
