@@ -336,7 +336,7 @@ __device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32
 }
 
 // ---------------------------------------------------------------- pass 1 ---
-__global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
+__global__ void __launch_bounds__(128, 8) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 me = __ldg(&w.leafPM[i]);
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(128) pass1Kernel(AstraeaParticles p, Work w, u
 // Reads the pass-2 records written by the EOS kernel (layout and derived
 // values: integrate.cu, writePass2Record): one 16-byte load per group of
 // fields, and no per-pair division for quantities of the neighbour alone.
-__global__ void __launch_bounds__(128, 5) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
+__global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
                                                    const uint32_t* livingFlags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
