@@ -600,15 +600,21 @@ class Ensemble:
     particle buffers: after two the graph's pointers and slots are where
     they started, so the same graph can be replayed again and again."""
 
-    def __init__(self, states, max_dt, theta=0.5):
+    def __init__(self, states, max_dt, theta=0.5, autotune_walks=True):
         self.max_dt, self.theta = max_dt, theta
         self.sims = []
+        self.tuning = {}
         for st in states:
             n = len(st["posX"])
             sim = Simulation(n)
             sim.load_state(st)
             reserve(sim.bvh, n)
             sim.evaluate_initial_forces(theta)
+            bucket = n.bit_length() - 1
+            if autotune_walks and bucket not in self.tuning:
+                # the first instance of each power-of-two size tunes the walks for all of them
+                self.tuning[bucket] = autotune(sim.p, sim.bvh, theta)
+                sim.evaluate_initial_forces(theta)
             self.sims.append(sim)
         self.dt = torch.zeros(2 * len(states), dtype=torch.float32).pin_memory()
         self.streams = [torch.cuda.Stream() for _ in states]

@@ -327,13 +327,15 @@ def ensemble_run(engine, scenarios, torch, max_dt, theta, replays=4):
     eager_ms = ev[0].elapsed_time(ev[1]) / steps
     graph_ms = ev[2].elapsed_time(ev[3]) / steps
     total = ens.particles
+    tuned = {"2^%d" % k: v for k, v in sorted(ens.tuning.items())}
     del ens
     torch.cuda.empty_cache()
     return {"instances": len(states), "particles": total, "steps": steps,
             "eager_ms_per_step": eager_ms, "graph_ms_per_step": graph_ms,
             "eager_particle_steps_per_s": total / (eager_ms * 1e-3),
             "graph_particle_steps_per_s": total / (graph_ms * 1e-3),
-            "graph_speedup": eager_ms / graph_ms}
+            "graph_speedup": eager_ms / graph_ms,
+            "autotuned_walks": tuned}
 
 
 def planet_stage(engine, torch, np, reps=3):
