@@ -185,6 +185,17 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 if (undecided) open = (bits >> slot) & 1u;
                 __syncwarp();
             }
+            // An opened node of at most 32 particles is not descended: its
+            // sorted leaf range is read whole below (one coalesced load).
+            uint2 rng = make_uint2(1u, 0u);               // empty unless a small node is expanded
+            if (open) {
+                const uint2 r = __ldg(&w.nodeRange[c]);
+                if (r.x <= r.y && r.y < n && r.y - r.x < 32u) {
+                    rng = r;
+                    open = false;
+                }
+            }
+            unsigned expandMask = __ballot_sync(0xffffffffu, rng.x <= rng.y);
             unsigned openMask = __ballot_sync(0xffffffffu, open);
             if (sp + 2 * __popc(openMask) > kNbStack) {
                 stackOverflow = true;     // cannot happen for trees of depth < 32
@@ -223,6 +234,39 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 cCount -= 32;
                 flush(cCount, 32);
                 __syncwarp();
+            }
+            while (expandMask) {                // small opened nodes: their particles, lane by lane
+                const int src = __ffs(expandMask) - 1;
+                expandMask &= expandMask - 1u;
+                const uint32_t first = __shfl_sync(0xffffffffu, rng.x, src);
+                const uint32_t last = __shfl_sync(0xffffffffu, rng.y, src);
+                const uint32_t j = first + static_cast<uint32_t>(lane);
+                bool keepJ = false;
+                float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+                float hj = 0.0f;
+                if (j <= last) {
+                    pj = __ldg(&w.leafPM[j]);
+                    hj = __ldg(&w.leafAux[j]).x;
+                    const float dx = fmaxf(0.0f, fmaxf(gminx - pj.x, pj.x - gmaxx));
+                    const float dy = fmaxf(0.0f, fmaxf(gminy - pj.y, pj.y - gmaxy));
+                    const float dz = fmaxf(0.0f, fmaxf(gminz - pj.z, pj.z - gmaxz));
+                    const float R = fmaxf(gHs, hj);
+                    keepJ = dx * dx + dy * dy + dz * dz <= R * R * 1.00001f;
+                }
+                const unsigned km = __ballot_sync(0xffffffffu, keepJ);
+                if (keepJ) {
+                    const int slot = cCount + __popc(km & laneMaskLt());
+                    S.cand[slot] = make_float4(pj.x, pj.y, pj.z, hj);
+                    S.candIdx[slot] = static_cast<int>(j);
+                }
+                cCount += __popc(km);
+                nCand += __popc(km);
+                __syncwarp();
+                if (cCount >= 32) {
+                    cCount -= 32;
+                    flush(cCount, 32);
+                    __syncwarp();
+                }
             }
         }
         flush(0, cCount);
