@@ -24,6 +24,7 @@ namespace {
 constexpr int kNbWarps = 4;
 constexpr int kNbStack = 1024;
 constexpr int kNbList = 64;
+constexpr uint32_t kNbExpand = 32;   // an opened node of at most this many particles is read as its leaf range
 
 // dirMem[k] (k = 4 [sx > 0] + 2 [sy > 0] + [sz > 0], s in {-1, 1}^3, the
 // octant diagonals): the member {x, y, z, Hs} with the largest projection
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
             uint2 rng = make_uint2(1u, 0u);               // empty unless a small node is expanded
             if (open) {
                 const uint2 r = __ldg(&w.nodeRange[c]);
-                if (r.x <= r.y && r.y < n && r.y - r.x < 32u) {
+                if (r.x <= r.y && r.y < n && r.y - r.x < kNbExpand) {
                     rng = r;
                     open = false;
                 }
@@ -240,7 +241,8 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 expandMask &= expandMask - 1u;
                 const uint32_t first = __shfl_sync(0xffffffffu, rng.x, src);
                 const uint32_t last = __shfl_sync(0xffffffffu, rng.y, src);
-                const uint32_t j = first + static_cast<uint32_t>(lane);
+                for (uint32_t base = first; base <= last; base += 32u) {
+                const uint32_t j = base + static_cast<uint32_t>(lane);
                 bool keepJ = false;
                 float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
                 float hj = 0.0f;
@@ -266,6 +268,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                     cCount -= 32;
                     flush(cCount, 32);
                     __syncwarp();
+                }
                 }
             }
         }
