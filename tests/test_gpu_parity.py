@@ -278,3 +278,31 @@ def test_capacity_error_like_engine():
     with pytest.raises(abi.AstraeaError) as ei:
         engine.sort_and_build_bvh(p, alt, small)
     assert ei.value.status == 2
+
+
+def test_c1_twenty_steps_track_oracle():
+    """The small benchmark configuration end to end: two granite spheres,
+    12,288 + 4,096 particles, 20 fused KDK steps against 20 oracle steps
+    (trajectory level: FP32 summation order and the race-free drift
+    both enter, so the bound is wider than one step's), with momentum
+    conserved on both."""
+    st = c1_state()
+    n = len(st["posX"])
+    sim = engine.Simulation(n)
+    sim.load_state(st)
+    sim.evaluate_initial_forces()
+    o = oracle.Oracle(st)
+    o.initial_forces()
+    for k in range(20):
+        dt_g = sim.step(5e-3)
+        dt_o = o.step(5e-3)
+        assert abs(dt_g - dt_o) <= 1e-4 * dt_o, (k, dt_g, dt_o)
+    g, c = sim.state(), o.state()
+    assert np.array_equal(g["originalId"], c["originalId"])
+    e = report("c1-20-steps", g, c, ["posX", "posY", "posZ", "velX", "velY", "velZ", "rho", "u", "h", "pressure"])
+    assert max(e.values()) < 5e-4, e        # measured 7.2e-5 (h) on GB300
+    for s in (g, c):
+        m = s["mass"].astype(np.float64)
+        mom = [np.sum(m * s[k].astype(np.float64)) for k in ("velX", "velY", "velZ")]
+        scale = np.sum(m * np.sqrt(sum(s[k].astype(np.float64) ** 2 for k in ("velX", "velY", "velZ"))))
+        assert max(abs(x) for x in mom) < 1e-4 * scale
