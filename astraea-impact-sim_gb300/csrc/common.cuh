@@ -120,6 +120,33 @@ __device__ __forceinline__ float wendlandC2N(float r, float H, float norm) {   /
     return norm * omq2 * omq2 * (1.0f + 4.0f * q);
 }
 __device__ __forceinline__ float wendlandNorm(float H) { return 21.0f / (2.0f * kPiF * H * H * H); }
+
+// Pair-loop forms of the kernels above.  The neighbour loops evaluate them
+// once per pair; the IEEE quotient r / H (a dozen instructions with its
+// special-case path) becomes three operations with y = 1 / H taken once per
+// particle (or stored in its record): q0 = r y, the exact residual
+// e = fma(-q0, H, r), q = fma(e, y, q0).  With y the correctly rounded
+// reciprocal this one correction step returns the correctly rounded quotient
+// (Markstein's theorem: P. Markstein, IBM J. Res. Dev. 34 (1990) 111-119;
+// J.-M. Muller et al., Handbook of Floating-Point Arithmetic, ch. 4), so the
+// kernel values are the ones the engine's division gives; it holds while no
+// operand or residual is subnormal (r, H >= 2e-6 here, r = 0 gives q = 0).
+__device__ __forceinline__ float quotRN(float r, float H, float invH) {
+    const float q0 = __fmul_rn(r, invH);
+    return __fmaf_rn(__fmaf_rn(-q0, H, r), invH, q0);
+}
+__device__ __forceinline__ float wendlandC2I(float r, float H, float invH, float norm) {
+    if (r >= H) return 0.0f;
+    const float q = quotRN(r, H, invH);
+    const float omq = 1.0f - q;
+    const float omq2 = omq * omq;
+    return norm * omq2 * omq2 * (1.0f + 4.0f * q);
+}
+__device__ __forceinline__ float wendlandC2GradI(float r, float H, float invH, float norm) {
+    if (r >= H) return 0.0f;
+    const float omq = 1.0f - quotRN(r, H, invH);
+    return -norm * omq * omq * omq;
+}
 __device__ __forceinline__ float wendlandC2GradN(float r, float H, float norm) {
     if (r >= H || H <= 0.0f) return 0.0f;
     const float omq = 1.0f - r / H;

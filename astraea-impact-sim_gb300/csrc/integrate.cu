@@ -63,10 +63,11 @@ __device__ __forceinline__ float resolveDt(uint32_t rawBits, float prevDt, float
 // neighbour j):
 //   q0 {x, y, z, h}  q1 {vx, vy, vz, m}  q2 {rho, P_eff / rho^2, cs, f_Balsara}
 //   q3 {sXX, sYY, sZZ, sXY} / rho^2   q4 {sXZ / rho^2, sYZ / rho^2, material, R_tensile}
-//   q5 {m / rho, 210 / (pi H^5), 1 / rho^2, 0}    (H = 2h)
+//   q5 {m / rho, 210 / (pi H^5), 1 / rho^2, 1 / H}    (H = 2h)
 // with h, rho and cs clamped as the engine clamps them on load.  Every
-// derived value is the IEEE operation the engine's pair loop performs on
-// the same inputs (sph_gravity.cu:1076-1142), done once per particle.
+// derived value but 1 / H is the IEEE operation the engine's pair loop
+// performs on the same inputs (sph_gravity.cu:1076-1142), done once per
+// particle; 1 / H replaces the pair loop's quotient r / H by a product.
 __device__ __forceinline__ void writePass2Record(float4* R, float x, float y, float z, float hRaw, float vx, float vy,
                                                  float vz, float m, float rhoRaw, float pEff, float csRaw, float fBalIn,
                                                  float sxx, float syy, float szz, float sxy, float sxz, float syz,
@@ -84,7 +85,7 @@ __device__ __forceinline__ void writePass2Record(float4* R, float x, float y, fl
     R[2] = make_float4(rho, pEff * invRho2, csRaw, fBalIn);
     R[3] = make_float4(sxx * invRho2, syy * invRho2, szz * invRho2, sxy * invRho2);
     R[4] = make_float4(sxz * invRho2, syz * invRho2, __int_as_float(mat), rTens);
-    R[5] = make_float4(m / rho, gradNorm, invRho2, 0.0f);
+    R[5] = make_float4(m / rho, gradNorm, invRho2, 1.0f / H);
 }
 
 __global__ void __launch_bounds__(256) eosKernel(AstraeaParticles p, Work w, bool withRecords, uint32_t n) {

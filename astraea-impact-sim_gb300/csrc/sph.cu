@@ -395,6 +395,9 @@ __global__ void __launch_bounds__(128, 8) pass1Kernel(AstraeaParticles p, Work w
     const float Hi = 2.0f * hi;
     const float Hi2 = __fmul_rn(Hi, Hi);
     const float w0 = 21.0f / (2.0f * kPiF * Hi * Hi * Hi);
+    const float Hi5 = (Hi * Hi) * (Hi * Hi) * Hi;
+    const float gNormI = 210.0f / (kPiF * Hi5);
+    const float invHi = 1.0f / Hi;
     float shep = (mi / rhoI) * w0;
     int ngb = 1;
     float nsX = 0.f, nsY = 0.f, nsZ = 0.f;
@@ -407,13 +410,13 @@ __global__ void __launch_bounds__(128, 8) pass1Kernel(AstraeaParticles p, Work w
             ++ngb;
             const float4 vj = __ldg(&w.velRho[j]);
             const float r = sqrtf(r2);
-            const float volJ = q.w / fmaxf(vj.w, 1.0e-9f);
-            const float wij = wendlandC2(r, Hi);
+            const float volJ = __fdividef(q.w, fmaxf(vj.w, 1.0e-9f));
+            const float wij = wendlandC2I(r, Hi, invHi, w0);
             shep += volJ * wij;
             nsX -= volJ * dx * wij;
             nsY -= volJ * dy * wij;
             nsZ -= volJ * dz * wij;
-            const float gc = wendlandC2Grad(r, Hi);
+            const float gc = wendlandC2GradI(r, Hi, invHi, gNormI);
             const float gx = gc * dx, gy = gc * dy, gz = gc * dz;
             const float dvx = vj.x - vr.x, dvy = vj.y - vr.y, dvz = vj.z - vr.z;
             gXX += volJ * dvx * gx; gXY += volJ * dvx * gy; gXZ += volJ * dvx * gz;
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
     const float sXYi = __ldg(&p.sXY[i]), sXZi = __ldg(&p.sXZ[i]), sYZi = __ldg(&p.sYZ[i]);
     const int matI = __float_as_int(a4.z);
     const float Ri = a4.w;
-    const float gradNormI = a5.y, invRhoI2 = a5.z;
+    const float gradNormI = a5.y, invRhoI2 = a5.z, invHi = a5.w;
     const float pI = effectivePressure(__ldg(&p.pressure[i]), __ldg(&p.phaseId[i]));   // the record's P_eff
     const float sXXr = sXXi * invRhoI2, sYYr = sYYi * invRhoI2, sZZr = sZZi * invRhoI2;
     const float sXYr = sXYi * invRhoI2, sXZr = sXZi * invRhoI2, sYZr = sYZi * invRhoI2;
@@ -488,7 +491,7 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
             const float dvx = vxi - b1.x, dvy = vyi - b1.y, dvz = vzi - b1.z;
             const float vDotR = dvx * dx + dvy * dy + dvz * dz;
             const float r = sqrtf(r2);
-            const float gI = wendlandC2GradN(r, Hi, gradNormI), gJ = wendlandC2GradN(r, Hj, b5.y);
+            const float gI = wendlandC2GradI(r, Hi, invHi, gradNormI), gJ = wendlandC2GradI(r, Hj, b5.w, b5.y);
             const float gb = 0.5f * (gI + gJ);
             const float gx = gb * dx, gy = gb * dy, gz = gb * dz;
             const float vDotG = dvx * gx + dvy * gy + dvz * gz;
@@ -501,15 +504,15 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
             float piIJ = 0.0f;                                 // Monaghan AV x Balsara (:1121-1128)
             if (vDotR < 0.0f) {
                 const float hB = 0.5f * (hi + hj), cB = 0.5f * (csI + csJ), rB = 0.5f * (rhoI + rhoJ);
-                const float muIJ = (hB * vDotR) / (r2 + 0.01f * hB * hB);
-                piIJ = ((-1.0f * cB * muIJ + 2.0f * muIJ * muIJ) / rB) * (0.5f * (fBalI + fBalJ));
+                const float muIJ = __fdividef(hB * vDotR, r2 + 0.01f * hB * hB);
+                piIJ = __fdividef(-1.0f * cB * muIJ + 2.0f * muIJ * muIJ, rB) * (0.5f * (fBalI + fBalJ));
             }
             float tens = 0.0f;                                 // tensile correction (:1130-1142)
             const float Rj = b4.w;
             if (Ri + Rj > 0.0f) {
                 const float Hb = 0.5f * (Hi + Hj);
                 if (r < Hb) {
-                    const float qb = r / Hb, om = 1.0f - qb, om2 = om * om;
+                    const float qb = __fdividef(r, Hb), om = 1.0f - qb, om2 = om * om;
                     const float fr = (om2 * om2 * (1.0f + 4.0f * qb)) * (1.0f / 0.6328125f);
                     const float fr2 = fr * fr;
                     tens = (Ri + Rj) * (fr2 * fr2);
@@ -605,6 +608,7 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
         const float4 vr = __ldg(&w.velRho[i]);
         const float Hi = me.w;
         const float normI = __ldg(&w.driftAux[i]).y;
+        const float invHi = 1.0f / Hi;
         const float rhoI = fmaxf(vr.w, 1.0e-9f);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         if (useList && n >= 2u) {
@@ -617,9 +621,9 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
                 const float4 vj = __ldg(&w.velRho[j]);
                 const float2 aj = __ldg(&w.driftAux[j]);          // {m, Wendland norm of H_j}
                 const float r = sqrtf(r2);
-                const float wb = 0.5f * (wendlandC2N(r, Hi, normI) + wendlandC2N(r, Hj, aj.y));
+                const float wb = 0.5f * (wendlandC2I(r, Hi, invHi, normI) + wendlandC2N(r, Hj, aj.y));
                 const float rb = 0.5f * (rhoI + fmaxf(vj.w, 1.0e-9f));
-                const float co = (aj.x / rb) * wb;
+                const float co = __fdividef(aj.x, rb) * wb;
                 sx += co * (vj.x - vr.x);
                 sy += co * (vj.y - vr.y);
                 sz += co * (vj.z - vr.z);
