@@ -127,12 +127,12 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     const size_t sortWords = sortScratchWords(static_cast<uint32_t>(C), &maxTiles);
     size_t off = 0;
     auto take = [&](size_t bytes) { const size_t o = off; off += alignUp(bytes); return o; };
-    const size_t oPM = take(C * 16), oAux = take(C * 16), oVR = take(C * 16), oRec = take(C * 16 * kRec2Width);
+    const size_t oLeaf = take(C * 32), oAux = take(C * 16), oRec = take(C * 16 * kRec2Width);
     const size_t nbMax = refitBlocks(static_cast<uint32_t>(C)), levMax = refitLevels(static_cast<uint32_t>(nbMax));
     const size_t oNode = take(C * 64), oRange = take(C * 8), oLScan = take(C * 64), oMScan = take(C * 80);
     const size_t oTable = take(levMax * nbMax * 32), oBMom = take(nbMax * 80), oQuad = take(C * 32);
     const size_t oDrift = take(C * 16);
-    const size_t oDRec = take(C * 16), oDAux = take(C * 8);
+    const size_t oDRec = take(C * 32), oDAux = take(C * 8);
     const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
     const size_t oSort = take(sortWords * 4), oDt = take(64);
     void* block = nullptr;
@@ -145,9 +145,8 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     Work& w = ws->w;
     w.capacity = static_cast<uint32_t>(C);
     w.maxNbr = maxNbr;
-    w.leafPM = reinterpret_cast<float4*>(b + oPM);
+    w.leaf = reinterpret_cast<Rec32*>(b + oLeaf);
     w.leafAux = reinterpret_cast<float4*>(b + oAux);
-    w.velRho = reinterpret_cast<float4*>(b + oVR);
     w.rec2 = reinterpret_cast<float4*>(b + oRec);
     w.node = reinterpret_cast<float4*>(b + oNode);
     w.nodeRange = reinterpret_cast<uint2*>(b + oRange);
@@ -157,7 +156,7 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     w.blockMom = reinterpret_cast<double*>(b + oBMom);
     w.nodeQuad = reinterpret_cast<float4*>(b + oQuad);
     w.driftPos = reinterpret_cast<float4*>(b + oDrift);
-    w.driftRec = reinterpret_cast<float4*>(b + oDRec);
+    w.drift = reinterpret_cast<Rec32*>(b + oDRec);
     w.driftAux = reinterpret_cast<float2*>(b + oDAux);
     w.nbrCount = reinterpret_cast<uint32_t*>(b + oCnt);
     w.nbrList = reinterpret_cast<uint32_t*>(b + oList);
@@ -1231,7 +1230,7 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     k1.maxDt = maxDtPsu;
     k1.resetWord = ws->rawMin + (q ^ 1);
     k1.boundsWordsInit = w.words;
-    k1.velRhoOut = w.velRho;
+    k1.driftOut = w.drift;
     AG_LAUNCH(launchKick(*p, n, k1, st));
     // 2. XSPH drift on the previous step's neighbour lists -> scratch positions + bounds
     AG_LAUNCH(launchDrift(*p, w, n, ws->dtSlots + (q ^ 1), 0.0f, useBvh, true, w.words, st));

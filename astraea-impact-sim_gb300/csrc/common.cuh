@@ -4,9 +4,9 @@
 // the reference kernel they restate (engine/sph_gravity.cu, engine/eos.cu of
 // Ananasjik/astraea-impact-sim).  Data layout (HBM, per particle / per node):
 //
-//   leafPM  [N]   float4 {x, y, z, m}            sorted positions + mass
+//   leaf    [N]   32-byte record {x, y, z, m}, {vx, vy, vz, rho}   sorted positions, mass, velocity, density
 //   leafAux [N]   float4 {Hs, eps, 2h, 0}        Hs = search radius (below)
-//   velRho  [N]   float4 {vx, vy, vz, rho}       neighbour velocity + density
+//   drift   [N]   32-byte record {x, y, z, H}, {vx, vy, vz, rho}   the next drift's neighbour record
 //   rec2    [6N]  float4 x6 per particle          pass-2 neighbour record
 //   node    [4(N-1)] float4 x4 per internal node:
 //        r0 {comX, comY, comZ, mass}
@@ -75,6 +75,20 @@ __device__ __forceinline__ uint64_t spreadBits21(uint64_t v) {
     v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
     v = (v | (v << 2)) & 0x1249249249249249ULL;
     return v;
+}
+
+// 32-byte read-only load (the 256-bit vector load of sm_100 and later): the
+// two float4 halves of a 32-byte aligned record.  The SPH pair loops are
+// bound by the L1 data pipe, which works per 32-byte sector per lane: one
+// 32-byte load costs what a 16-byte load costs, so a record read in 32-byte
+// pieces moves half the sectors of the same record read in 16-byte pieces.
+struct F8 { float4 a, b; };
+__device__ __forceinline__ F8 ldg256(const float4* p) {
+    F8 r;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y), "=f"(r.b.z), "=f"(r.b.w)
+        : "l"(p));
+    return r;
 }
 
 // Squared length with explicit IEEE rounding and no multiply-add fusion:
@@ -387,6 +401,12 @@ __device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, fl
 
 constexpr int kRec2Width = 6;   // float4 per pass-2 record
 
+// Two float4 of one particle in one 32-byte aligned record, read whole by
+// ldg256 in the SPH pair loops.
+struct __align__(32) Rec32 {
+    float4 a, b;
+};
+
 // FP64 mass moments of one internal node (32 bytes, 16-byte aligned).
 struct __align__(16) NodeMom {
     double sx, sy, sz, m;
@@ -397,9 +417,8 @@ struct __align__(16) NodeMom {
 struct Work {
     uint32_t capacity;
     uint32_t maxNbr;
-    float4* leafPM;
+    Rec32* leaf;           // sorted order: a {x, y, z, m}, b {vx, vy, vz, rho} (permutation / leaf refresh)
     float4* leafAux;
-    float4* velRho;
     float4* rec2;          // kRec2Width float4 per particle: the pass-2 record
     float4* node;          // 4 x float4 per internal node
     uint2* nodeRange;      // [N-1] {first, last}: the sorted leaf range of each internal node
@@ -410,7 +429,8 @@ struct Work {
     float4* nodeQuad;      // 2 x float4 per internal node: central second moments
                            // {Sxx, Syy, Szz, Sxy}, {Sxz, Syz, 0, 0} (far-field mode 1)
     float4* driftPos;      // {x, y, z, 0} after the drift
-    float4* driftRec;      // {x, y, z, H = 2 max(h, 1e-6)} for the next drift (pass 1 / leaf refresh)
+    Rec32* drift;          // for the next drift: a {x, y, z, H = 2 max(h, 1e-6)} (pass 1 / leaf refresh),
+                           // b {vx, vy, vz, rho} (opening kick / leaf refresh)
     float2* driftAux;      // {m, 21 / (2 pi H^3)} (the Wendland norm of H)
     uint32_t* nbrCount;
     uint32_t* nbrList;     // particle-major, maxNbr per particle

@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kLabelWarps * 32) labelKernel(Work w, uint32_t
     const double cx = grp.x, cy = grp.y, cz = grp.z;
     double a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (uint32_t j = first + static_cast<uint32_t>(lane); j <= last && j < n; j += 32u) {
-        const float4 pm = __ldg(&w.leafPM[j]);
+        const float4 pm = __ldg(&w.leaf[j].a);
         const double dx = cx - pm.x, dy = cy - pm.y, dz = cz - pm.z;
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (!(r2 > 0.0)) continue;
@@ -409,12 +409,12 @@ __global__ void __launch_bounds__(kGateThreads) gateKernel(AstraeaParticles p, W
                                                            float* out) {
     __shared__ float red[3][kGateThreads / 32];
     const uint32_t t = (K > 1u) ? static_cast<uint32_t>((static_cast<uint64_t>(blockIdx.x) * (n - 1u)) / (K - 1u)) : 0u;
-    const float4 me = __ldg(&w.leafPM[t]);
+    const float4 me = __ldg(&w.leaf[t].a);
     const float ei = __ldg(&w.leafAux[t]).y;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     for (uint32_t j = threadIdx.x; j < n; j += kGateThreads) {
         if (j == t) continue;
-        const float4 pm = __ldg(&w.leafPM[j]);
+        const float4 pm = __ldg(&w.leaf[j].a);
         const float e = 0.5f * (ei + __ldg(&w.leafAux[j]).y);
         const float dx = me.x - pm.x, dy = me.y - pm.y, dz = me.z - pm.z;
         const float den = dx * dx + dy * dy + dz * dz + e * e + 1.0e-20f;

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         float4 me = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         float epsI = 0.8e-6f;
         if (active) {
-            me = __ldg(&w.leafPM[i]);
+            me = __ldg(&w.leaf[i].a);
             epsI = __ldg(&w.leafAux[i]).y;
         }
         const float xi = me.x, yi = me.y, zi = me.z;
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             unsigned selfBit = 0u;
             if (isLeaf) {
                 const int j = ~c;
-                const float4 pm = __ldg(&w.leafPM[j]);
+                const float4 pm = __ldg(&w.leaf[j].a);
                 const float ej = __ldg(&w.leafAux[j]).y;
                 const int slot = pCount + __popc(leafMask & laneMaskLt());
                 putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(256) kickKernel(AstraeaParticles p, uint32_t n
             p.pressure[i] = e.P; p.soundSpeed[i] = e.cs; p.tempK[i] = e.T; p.phaseId[i] = e.phase;
             cs = e.cs;
         }
-        if (a.velRhoOut != nullptr) a.velRhoOut[i] = make_float4(vx, vy, vz, rhoNew);
+        if (a.driftOut != nullptr) a.driftOut[i].b = make_float4(vx, vy, vz, rhoNew);
         if (a.rawMinOut != nullptr) {
             const float d = dtCandidate(p.h[i], cs, vx, vy, vz, p.accX[i], p.accY[i], p.accZ[i], uNew, p.duDt[i],
                                         matRaw);

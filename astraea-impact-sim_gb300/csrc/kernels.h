@@ -166,7 +166,7 @@ struct KickArgs {
     uint32_t* rawMinOut;       // when non-null: reduce the next dt minimum into it
     uint32_t* resetWord;       // when non-null: block 0 writes 0x7f7f7f7f here
     uint32_t* boundsWordsInit; // when non-null: block 0 re-arms bounds + living flags
-    float4* velRhoOut;         // when non-null: write {v, rho} records
+    Rec32* driftOut;           // when non-null: write the {v, rho} half of the drift records
 };
 cudaError_t launchKick(const AstraeaParticles& p, uint32_t n, const KickArgs& a, cudaStream_t st);
 cudaError_t launchReduceDt(const AstraeaParticles& p, uint32_t n, uint32_t* rawMinOut, int sms, cudaStream_t st);

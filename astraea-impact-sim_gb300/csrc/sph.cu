@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
         float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
         float Hs = 0.0f;
         if (active) {
-            me = __ldg(&w.leafPM[i]);
+            me = __ldg(&w.leaf[i].a);
             Hs = __ldg(&w.leafAux[i]).x;
         }
         const float gminx = warpMinF(active ? me.x : 3.0e38f), gmaxx = warpMaxF(active ? me.x : -3.0e38f);
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
             float hsj = 0.0f;
             bool keep = false;
             if (isLeaf) {
-                pm = __ldg(&w.leafPM[~c]);
+                pm = __ldg(&w.leaf[~c].a);
                 hsj = __ldg(&w.leafAux[~c]).x;
                 const float dx = fmaxf(0.0f, fmaxf(gminx - pm.x, pm.x - gmaxx));
                 const float dy = fmaxf(0.0f, fmaxf(gminy - pm.y, pm.y - gmaxy));
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
                 float hj = 0.0f;
                 if (j <= last) {
-                    pj = __ldg(&w.leafPM[j]);
+                    pj = __ldg(&w.leaf[j].a);
                     hj = __ldg(&w.leafAux[j]).x;
                     const float dx = fmaxf(0.0f, fmaxf(gminx - pj.x, pj.x - gmaxx));
                     const float dy = fmaxf(0.0f, fmaxf(gminy - pj.y, pj.y - gmaxy));
@@ -306,7 +306,7 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
         return;
     }
     atomicAdd(&w.status->counters[kCntFallbackWalks], 1ull);
-    const float4 me = __ldg(&w.leafPM[i]);
+    const float4 me = __ldg(&w.leaf[i].a);
     const float Hs = __ldg(&w.leafAux[i]).x;
     int stack[kTreeStack];
     int sp = 0;
@@ -324,7 +324,7 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
         if (c2 < 0) {
             const uint32_t j = static_cast<uint32_t>(~c2);
             if (j == i) continue;
-            const float4 q = __ldg(&w.leafPM[j]);
+            const float4 q = __ldg(&w.leaf[j].a);
             const float R = fmaxf(Hs, __ldg(&w.leafAux[j]).x);
             if (len2Exact(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z)) < __fmul_rn(R, R)) f(j);
             continue;
@@ -369,7 +369,7 @@ __device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32
         uint4 q = c >= 4 ? ldListNoL1(list) : make_uint4(0u, 0u, 0u, 0u);
         for (; k + 4 <= c; k += 4) {
             const uint4 next = (k + 8 <= c) ? ldListNoL1(list + k + 4) : q;
-            const float4 r0 = load(q.x), r1 = load(q.y), r2 = load(q.z), r3 = load(q.w);
+            const auto r0 = load(q.x), r1 = load(q.y), r2 = load(q.z), r3 = load(q.w);
             body(q.x, r0); body(q.y, r1); body(q.z, r2); body(q.w, r3);
             q = next;
         }
@@ -383,11 +383,11 @@ __device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32
 }
 
 // ---------------------------------------------------------------- pass 1 ---
-__global__ void __launch_bounds__(128, 8) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
+__global__ void __launch_bounds__(128, 7) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 me = __ldg(&w.leafPM[i]);
-    const float4 vr = __ldg(&w.velRho[i]);
+    const F8 rec = ldg256(&w.leaf[i].a);
+    const float4 me = rec.a, vr = rec.b;
     const float mi = me.w;
     const float hi = fmaxf(__ldg(&p.h[i]), 1.0e-6f);
     const float h0i = fmaxf(__ldg(&p.h0[i]), 1.0e-6f);
@@ -403,12 +403,14 @@ __global__ void __launch_bounds__(128, 8) pass1Kernel(AstraeaParticles p, Work w
     float nsX = 0.f, nsY = 0.f, nsZ = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
     if (n >= 2u) {
-        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&w.leafPM[j]); }, [&](uint32_t j, float4 q) {
+        // one 32-byte record per candidate: {x, y, z, m}, {vx, vy, vz, rho}
+        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&w.leaf[j].a); }, [&](uint32_t j, const F8& rj) {
+            const float4 q = rj.a;
             const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
             const float r2 = len2Exact(dx, dy, dz);
             if (!(r2 < Hi2)) return;                       // sph_gravity.cu:713
             ++ngb;
-            const float4 vj = __ldg(&w.velRho[j]);
+            const float4 vj = rj.b;
             const float r = sqrtf(r2);
             const float volJ = __fdividef(q.w, fmaxf(vj.w, 1.0e-9f));
             const float wij = wendlandC2I(r, Hi, invHi, w0);
@@ -439,7 +441,7 @@ __global__ void __launch_bounds__(128, 8) pass1Kernel(AstraeaParticles p, Work w
     p.h[i] = hNew;
     // records of the next drift (positions and h do not change before it)
     const float Hd = 2.0f * fmaxf(hNew, 1.0e-6f);
-    w.driftRec[i] = make_float4(me.x, me.y, me.z, Hd);
+    w.drift[i].a = make_float4(me.x, me.y, me.z, Hd);
     w.driftAux[i] = make_float2(mi, wendlandNorm(Hd));
 }
 
@@ -475,17 +477,19 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
     float axS = 0.f, ayS = 0.f, azS = 0.f, drC = 0.f, drD = 0.f, duP = 0.f, duAv = 0.f, duT = 0.f, duS = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
     if (n >= 2u) {
-        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&R[kRec2Width * static_cast<size_t>(j) + 0]); }, [&](uint32_t j, float4 b0) {
+        // records in 32-byte pieces: {q0, q1} for every candidate (one sector),
+        // {q2, q3} and {q4, q5} for the candidates in range
+        forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&R[kRec2Width * static_cast<size_t>(j)]); },
+                                   [&](uint32_t j, const F8& q01) {
+            const float4 b0 = q01.a;
             const float dx = __fsub_rn(xi, b0.x), dy = __fsub_rn(yi, b0.y), dz = __fsub_rn(zi, b0.z);
             const float r2 = len2Exact(dx, dy, dz);
             const float hj = b0.w, Hj = 2.0f * hj;
             const float Hm = fmaxf(Hi, Hj);
             if (!(r2 < __fmul_rn(Hm, Hm))) return;          // sph_gravity.cu:1071
-            const float4 b1 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 1]);
-            const float4 b2 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 2]);
-            const float4 b3 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 3]);
-            const float4 b4 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 4]);
-            const float4 b5 = __ldg(&R[kRec2Width * static_cast<size_t>(j) + 5]);
+            const F8 q23 = ldg256(&R[kRec2Width * static_cast<size_t>(j) + 2]);
+            const F8 q45 = ldg256(&R[kRec2Width * static_cast<size_t>(j) + 4]);
+            const float4 b1 = q01.b, b2 = q23.a, b3 = q23.b, b4 = q45.a, b5 = q45.b;
             const float mj = b1.w, rhoJ = b2.x, pOverRho2J = b2.y, csJ = b2.z, fBalJ = b2.w;
             const float volJ = b5.x;
             const float dvx = vxi - b1.x, dvy = vyi - b1.y, dvz = vzi - b1.z;
@@ -604,21 +608,23 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
     float mn[3] = {1.0e30f, 1.0e30f, 1.0e30f}, mx[3] = {-1.0e30f, -1.0e30f, -1.0e30f};
     if (i < n) {
         const float dt = (dtDev != nullptr) ? *dtDev : dtHost;
-        const float4 me = __ldg(&w.driftRec[i]);            // {x, y, z, H}
-        const float4 vr = __ldg(&w.velRho[i]);
+        const F8 rec = ldg256(&w.drift[i].a);
+        const float4 me = rec.a, vr = rec.b;               // {x, y, z, H}, {vx, vy, vz, rho}
         const float Hi = me.w;
         const float normI = __ldg(&w.driftAux[i]).y;
         const float invHi = 1.0f / Hi;
         const float rhoI = fmaxf(vr.w, 1.0e-9f);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         if (useList && n >= 2u) {
-            forEachCandidatePrefetched(w, i, [&](uint32_t j) { return __ldg(&w.driftRec[j]); }, [&](uint32_t j, float4 q) {
+            // one 32-byte record per candidate: {x, y, z, H}, {vx, vy, vz, rho}
+            forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&w.drift[j].a); }, [&](uint32_t j, const F8& rj) {
+                const float4 q = rj.a;
                 const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
                 const float r2 = len2Exact(dx, dy, dz);
                 const float Hj = q.w;
                 const float Hm = fmaxf(Hi, Hj);
                 if (!(r2 < __fmul_rn(Hm, Hm))) return;
-                const float4 vj = __ldg(&w.velRho[j]);
+                const float4 vj = rj.b;
                 const float2 aj = __ldg(&w.driftAux[j]);          // {m, Wendland norm of H_j}
                 const float r = sqrtf(r2);
                 const float wb = 0.5f * (wendlandC2I(r, Hi, invHi, normI) + wendlandC2N(r, Hj, aj.y));
