@@ -563,28 +563,29 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
 
 def run_e2e(sim, engine, torch, args, max_dt, world, dist):
     """The same fused step through the C-ABI with host-resident inputs and
-    outputs.  Every step copies its input fields from pinned host memory and
-    its result fields (the engine's telemetry fields) and dt back to pinned
-    host memory.  The copies run on their own streams (H2D and D2H in both
-    copy engines) and overlap the previous / next step's kernels: inputs are
-    staged into a second device buffer while the step before computes, then
-    moved into the particle arrays with a device-to-device copy; results are
-    copied device-to-device into a staging buffer and read back while the
-    next step computes."""
+    outputs.  Every step copies its input fields from pinned host memory into
+    the particle arrays and its result fields (the engine's telemetry fields)
+    and dt back to pinned host memory.  Two device states alternate, so the
+    copies run on their own streams (H2D and D2H in both copy engines) and
+    overlap the kernels of the step on the other state: step k uploads into
+    state k mod 2 while step k-1 computes on the other one, and reads its
+    results back while step k+1 computes."""
     n = sim.p.count
+    sims = [sim, engine.Simulation(n)]
+    sims[1].load_state(sim.p.download())
+    engine.reserve(sims[1].bvh, n)
+    sims[1].evaluate_initial_forces(args.theta)
     host_in = {f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in E2E_IN}
     host_out = [{f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in E2E_OUT}
                 for _ in range(2)]
     for f in E2E_IN:
         host_in[f].copy_(sim.p.arrays[f][:n])
-    stage_in = [{f: torch.empty_like(sim.p.arrays[f][:n]) for f in E2E_IN} for _ in range(2)]
-    stage_out = [{f: torch.empty_like(sim.p.arrays[f][:n]) for f in E2E_OUT} for _ in range(2)]
     dt_host = torch.zeros(2, dtype=torch.float32).pin_memory()
     bi = sum(t.numel() * t.element_size() for t in host_in.values())
     bo = sum(t.numel() * t.element_size() for t in host_out[0].values()) + 4
     comp, h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
     ev = lambda: torch.cuda.Event()
-    in_ready, in_used, out_ready, out_read = [ev(), ev()], [ev(), ev()], [ev(), ev()], [ev(), ev()]
+    in_ready, out_ready, out_read = [ev(), ev()], [ev(), ev()], [ev(), ev()]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -596,9 +597,9 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
         with torch.cuda.stream(h2d):
             h2d.wait_event(e0)
             if k >= 2:
-                h2d.wait_event(in_used[b])          # staging buffer b consumed by step k-2
+                h2d.wait_event(out_read[b])         # state b read back after step k-2
             for f in E2E_IN:
-                stage_in[b][f].copy_(host_in[f], non_blocking=True)
+                sims[b].p.arrays[f][:n].copy_(host_in[f], non_blocking=True)
             in_ready[b].record(h2d)
 
     upload(0, 0)
@@ -606,22 +607,16 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
         b = k & 1
         if k + 1 < args.steps:
             upload(b ^ 1, k + 1)
+        st = sims[b]
         with torch.cuda.stream(comp):
             comp.wait_event(in_ready[b])
-            for f in E2E_IN:
-                sim.p.arrays[f][:n].copy_(stage_in[b][f])
-            in_used[b].record(comp)
-            engine.invalidate_step_cache(sim.bvh)
-            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, args.theta, dt_host[b:].data_ptr())
-            if k >= 2:
-                comp.wait_event(out_read[b])        # staging buffer b read back (step k-2)
-            for f in E2E_OUT:
-                stage_out[b][f].copy_(sim.p.arrays[f][:n])
+            engine.invalidate_step_cache(st.bvh)
+            engine.step(st.p, st.alt, st.bvh, sim.prev_dt, max_dt, args.theta, dt_host[b:].data_ptr())
             out_ready[b].record(comp)
         with torch.cuda.stream(d2h):
             d2h.wait_event(out_ready[b])
             for f in E2E_OUT:
-                host_out[b][f].copy_(stage_out[b][f], non_blocking=True)
+                host_out[b][f].copy_(st.p.arrays[f][:n], non_blocking=True)
             out_read[b].record(d2h)
     comp.wait_stream(d2h)
     e1.record(comp)
@@ -629,12 +624,14 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
     engine.set_stream(None)
     ms = e0.elapsed_time(e1)
     rate, _ = replica_rate(n * args.steps, ms, dist, "cuda")
+    sims[1].bvh.free()
+    del sims[1], st
     return {"value": rate, "unit": UNIT,
             "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
-            "note": "every step: H2D of the step's input fields from pinned memory, fused step (step cache "
-                    "invalidated: neighbour lists and dt recomputed from the uploaded state), D2H of the "
-                    "engine telemetry fields and dt; copies on their own streams, overlapping the "
-                    "neighbouring steps' kernels"}
+            "note": "every step: H2D of the step's input fields from pinned memory into the particle arrays, "
+                    "fused step (step cache invalidated: neighbour lists and dt recomputed from the uploaded "
+                    "state), D2H of the engine telemetry fields and dt; two device states alternate so the "
+                    "copies run on their own streams beside the other state's step"}
 
 
 def run_c3(args):
