@@ -59,11 +59,12 @@ namespace astraea_gb300 {
 namespace {
 constexpr int kDirectThreads = 128;
 constexpr double kGPsuDirect = 6.67430e-11 * 1.0e24 * 1.0e3 * 1.0e3 / (1.0e6 * 1.0e6 * 1.0e6);
+struct Src4 { double x, y, z, w; };   // one staged source: position, mass
 
 __global__ void __launch_bounds__(kDirectThreads) directGravityF64Kernel(AstraeaParticles p, uint32_t n,
                                                                         const uint32_t* targets, uint32_t nt,
                                                                         double* acc3, double* phiOut) {
-    __shared__ double4 src[kDirectThreads];   // x, y, z, m
+    __shared__ Src4 src[kDirectThreads];      // x, y, z, m
     __shared__ double srcEps[kDirectThreads];
     const uint32_t t = blockIdx.x * kDirectThreads + threadIdx.x;
     const bool live = t < nt;
@@ -79,17 +80,17 @@ __global__ void __launch_bounds__(kDirectThreads) directGravityF64Kernel(Astraea
         const uint32_t j = base + threadIdx.x;
         __syncthreads();
         if (j < n) {
-            src[threadIdx.x] = make_double4(p.posX[j], p.posY[j], p.posZ[j], p.mass[j]);
+            src[threadIdx.x] = Src4{p.posX[j], p.posY[j], p.posZ[j], p.mass[j]};
             srcEps[threadIdx.x] = 0.8 * static_cast<double>(fmaxf(p.h0[j], 1.0e-6f));
         } else {
-            src[threadIdx.x] = make_double4(0.0, 0.0, 0.0, 0.0);
+            src[threadIdx.x] = Src4{0.0, 0.0, 0.0, 0.0};
             srcEps[threadIdx.x] = 1.0;
         }
         __syncthreads();
         const int cnt = static_cast<int>(min(static_cast<uint32_t>(kDirectThreads), n - base));
         for (int k = 0; k < cnt; ++k) {
             if (base + static_cast<uint32_t>(k) == i) continue;
-            const double4 s = src[k];
+            const Src4 s = src[k];
             const double dx = xi - s.x, dy = yi - s.y, dz = zi - s.z;
             const double e = 0.5 * (ei + srcEps[k]);
             const double r2 = dx * dx + dy * dy + dz * dz + e * e;
