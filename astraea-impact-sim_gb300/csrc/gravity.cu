@@ -512,6 +512,12 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
         ff = *far;
         if (ff.groupStride == 0u) ff.groupStride = 1u;
         kernel = checkInside ? gravityKernel<kGravWarps, true, false, true> : gravityKernel<kGravWarps, false, false, true>;
+    } else if (quadrupole && warps == 2) {
+        kernel = checkInside ? gravityKernel<2, true, true, false> : gravityKernel<2, false, true, false>;
+        wps = 2;
+    } else if (quadrupole && warps == 8) {
+        kernel = checkInside ? gravityKernel<8, true, true, false> : gravityKernel<8, false, true, false>;
+        wps = 8;
     } else if (quadrupole) {
         kernel = checkInside ? gravityKernel<kGravWarps, true, true, false> : gravityKernel<kGravWarps, false, true, false>;
     } else if (warps == 2) {

@@ -102,8 +102,9 @@ struct FarCapture {
     float gamma2;
     uint32_t groupStride;  // only groups g % stride == 0 apply the far test
 };
-// warps: 2, 4 or 8 warps per block for the plain walk (the autotuner's
-// choice; the far-field walks use 4); results do not depend on it.
+// warps: 2, 4 or 8 warps per block for the plain and quadrupole walks (the
+// autotuner's choice; the learned far-field walk uses 4); results do not
+// depend on it.
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
                           cudaStream_t st, const FarCapture* far = nullptr, int warps = 4);
 
