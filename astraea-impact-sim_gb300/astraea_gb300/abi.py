@@ -76,6 +76,11 @@ DEVFLAG_STACK_OVERFLOW = 0x4
 
 COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "gravity_rounds",
             "gravity_stack_peak", "fallback_walks", "neighbor_candidates", "gravity_undecided"]
+# astraea_gb300_read_device_counters: the eight above, then the SPH pair counts
+ALL_COUNTERS = COUNTERS + ["pass1_pairs", "pass2_pairs", "drift_pairs"]
+# astraea_gb300_read_stage_times order (ASTRAEA_STAGE_*)
+STAGES = ["refresh", "kick", "drift", "sort", "permute", "refit", "neighbours", "pass1", "eos", "gravity",
+          "pass2", "kick_eos"]
 
 # (symbol, argtypes) of every exported entry point, in header order.
 class PclsFrameInfo(ctypes.Structure):
@@ -213,6 +218,9 @@ SIGNATURES = [
     ("astraea_gb300_radix_sort_pairs", [_VP, _VP, _VP, _VP, _U32, ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_radix_sort_pairs_noalloc", [_VP, _VP, _VP, _VP, _U32, ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_read_device_status", [ctypes.POINTER(_U32), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    ("astraea_gb300_read_device_counters", [ctypes.POINTER(ctypes.c_uint64), _U32, ctypes.POINTER(_U32)], ctypes.c_int),
+    ("astraea_gb300_set_stage_timing", [ctypes.c_int], ctypes.c_int),
+    ("astraea_gb300_read_stage_times", [_B, ctypes.POINTER(_F), _U32, ctypes.POINTER(_U32)], ctypes.c_int),
     ("astraea_gb300_reset_device_status", [], ctypes.c_int),
     ("astraea_gb300_direct_gravity_f64", [_P, _VP, _U32, _VP, _VP], ctypes.c_int),
     ("astraea_gb300_measure_fp32_tflops", [ctypes.POINTER(_F)], ctypes.c_int),

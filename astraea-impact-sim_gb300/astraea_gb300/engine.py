@@ -498,6 +498,27 @@ def read_device_status():
     return flags.value, dict(zip(abi.COUNTERS, list(counters)))
 
 
+def read_device_counters():
+    """Every device counter since the last reset (ASTRAEA_COUNTER_* order)."""
+    out = (ctypes.c_uint64 * len(abi.ALL_COUNTERS))()
+    cnt = ctypes.c_uint32(0)
+    abi.check(lib().astraea_gb300_read_device_counters(out, len(abi.ALL_COUNTERS), ctypes.byref(cnt)))
+    return dict(zip(abi.ALL_COUNTERS, list(out)[: cnt.value]))
+
+
+def set_stage_timing(enable):
+    """Events between the fused step's stages (off by default; not during graph capture)."""
+    abi.check(lib().astraea_gb300_set_stage_timing(1 if enable else 0))
+
+
+def read_stage_times(bvh):
+    """Stage times (ms) of the last timed fused step on this BVH, by stage name."""
+    out = (ctypes.c_float * len(abi.STAGES))()
+    cnt = ctypes.c_uint32(0)
+    abi.check(lib().astraea_gb300_read_stage_times(ctypes.byref(bvh.s), out, len(abi.STAGES), ctypes.byref(cnt)))
+    return dict(zip(abi.STAGES, list(out)[: cnt.value]))
+
+
 def measure_fp32_tflops():
     out = ctypes.c_float(0.0)
     abi.check(lib().astraea_gb300_measure_fp32_tflops(ctypes.byref(out)))

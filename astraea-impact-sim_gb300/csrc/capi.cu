@@ -29,6 +29,8 @@ thread_local std::string g_lastError;
 std::atomic<cudaStream_t> g_stream{nullptr};
 std::atomic<uint32_t> g_spinLimit{1u << 22};
 std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: + quadrupole, 2: + learned correction
+std::atomic<bool> g_stageTiming{false};   // events between the fused step's stages
+constexpr int kStageCount = ASTRAEA_STAGE_COUNT;
 std::mutex g_mutex;
 
 AstraeaStatus fail(AstraeaStatus s, const std::string& msg) {
@@ -101,6 +103,10 @@ struct Workspace {
     const void* stepToken = nullptr;
     uint32_t stepCount = 0;
     int parity = 0;
+    // stage timing: event k is recorded where stage k of the fused step
+    // starts, event kStageCount where the step ends (created on first use)
+    cudaEvent_t stageEv[kStageCount + 1] = {};
+    bool stageRecorded = false;
 };
 std::map<std::pair<int, const void*>, Workspace*> g_work;
 
@@ -200,6 +206,8 @@ void dropWorkspace(const void* leftChild) {
     for (auto it = g_work.begin(); it != g_work.end(); ++it) {
         if (it->first.second == leftChild) {
             cudaFree(it->second->block);
+            for (cudaEvent_t e : it->second->stageEv)
+                if (e) cudaEventDestroy(e);
             delete it->second;
             g_work.erase(it);
             return;
@@ -382,8 +390,17 @@ uint32_t* livingPtr(const AstraeaRadixBvh* bvh, Workspace* ws) {
 }
 
 // Sort + permutation + Karras + refit shared by the stage call and the step.
+// Events between the stages of one fused step (null events: timing off).
+struct StageMarks {
+    cudaEvent_t* ev = nullptr;
+    cudaStream_t st = nullptr;
+    void mark(int k) const {
+        if (ev != nullptr) cudaEventRecord(ev[k], st);
+    }
+};
+
 AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh, Workspace* ws,
-                        const float4* driftPos, bool allFields) {
+                        const float4* driftPos, bool allFields, const StageMarks& marks = StageMarks{}) {
     const uint32_t n = p->count;
     cudaStream_t st = stream();
     Work& w = ws->w;
@@ -410,6 +427,7 @@ AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadix
     if (bvh->sceneBoundsOrdered != nullptr)
         AG_CUDA(cudaMemcpyAsync(bvh->sceneBoundsOrdered, w.words + kWBounds, 6 * sizeof(uint32_t),
                                 cudaMemcpyDeviceToDevice, st));
+    marks.mark(ASTRAEA_STAGE_PERMUTE);
     // The fused step (allFields == false) keeps its tree in the library's node
     // records only; the descriptor's node arrays (SoA and packed) are written
     // by the stage call, whose callers may read them.
@@ -421,6 +439,7 @@ AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadix
     AG_LAUNCH(launchPermuteLeavesKarras(*p, *alt, kb, driftPos, w, n, living, allFields, st));
     swapParticlePointers(*p, *alt);
     alt->count = p->count;
+    marks.mark(ASTRAEA_STAGE_REFIT);
     const bool moments = g_farField.load() != 0;
     AG_LAUNCH(launchRefit(kb, w, n, moments, st));
     ws->treeBuilt = true;
@@ -486,7 +505,7 @@ AstraeaStatus astraea_gb300_read_device_status(uint32_t* flags, uint64_t* counte
     AG_CUDA(cudaMemcpy(&h, ds->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
     if (flags) *flags = h.flags;
     if (counters8)
-        for (int k = 0; k < kCntCount; ++k) counters8[k] = h.counters[k];
+        for (int k = 0; k < 8; ++k) counters8[k] = h.counters[k];
     return ASTRAEA_OK;
 }
 
@@ -1214,6 +1233,15 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     int q = ws->parity;
     const bool useBvh = bvh->leftChild != nullptr && bvh->rightChild != nullptr && n >= 2u;
     const bool cacheOk = ws->stepCacheValid && ws->stepToken == static_cast<const void*>(p->posX);
+    StageMarks marks;
+    if (g_stageTiming.load()) {
+        for (cudaEvent_t& e : ws->stageEv)
+            if (e == nullptr) AG_CUDA(cudaEventCreate(&e));
+        marks.ev = ws->stageEv;
+        marks.st = st;
+        ws->stageRecorded = true;
+    }
+    marks.mark(ASTRAEA_STAGE_REFRESH);
     if (!cacheOk) {
         // Device dt state from the caller's previous dt and the current state.
         AG_LAUNCH(launchSetDtSlots(ws->dtSlots, q, prevDtPsu, ws->rawMin, st));
@@ -1222,6 +1250,7 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
         if (useBvh) AG_LAUNCH(launchBuildNeighbors(w, n, sms, st, static_cast<int>(tune.neighborWarps)));
     }
     // 1. opening half kick; dt resolved on the device
+    marks.mark(ASTRAEA_STAGE_KICK);
     KickArgs k1{};
     k1.dtMode = 1;
     k1.rawMinIn = ws->rawMin + q;
@@ -1233,14 +1262,20 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     k1.driftOut = w.drift;
     AG_LAUNCH(launchKick(*p, n, k1, st));
     // 2. XSPH drift on the previous step's neighbour lists -> scratch positions + bounds
+    marks.mark(ASTRAEA_STAGE_DRIFT);
     AG_LAUNCH(launchDrift(*p, w, n, ws->dtSlots + (q ^ 1), 0.0f, useBvh, true, w.words, st));
     // 3. sort + permutation (live fields) + Karras + refit
-    s = buildTree(p, alt, bvh, ws, w.driftPos, false);
+    marks.mark(ASTRAEA_STAGE_SORT);
+    s = buildTree(p, alt, bvh, ws, w.driftPos, false, marks);
     if (s != ASTRAEA_OK) return s;
     // 4. neighbour lists for pass 1, pass 2 and the next drift
+    marks.mark(ASTRAEA_STAGE_NEIGHBOURS);
     AG_LAUNCH(launchBuildNeighbors(w, n, sms, st, static_cast<int>(tune.neighborWarps)));
+    marks.mark(ASTRAEA_STAGE_PASS1);
     AG_LAUNCH(launchPass1(*p, w, n, st));
+    marks.mark(ASTRAEA_STAGE_EOS);
     AG_LAUNCH(launchEos(*p, &w, n, st));
+    marks.mark(ASTRAEA_STAGE_GRAVITY);
     if (ws->momentsBuilt && g_farField.load() == 2) {
         s = learnedGravity(p, ws, n, theta, true);
         if (s != ASTRAEA_OK) return s;
@@ -1248,8 +1283,10 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
         AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt && g_farField.load() == 1, sms, st, nullptr,
                                 static_cast<int>(tune.gravityWarps)));
     }
+    marks.mark(ASTRAEA_STAGE_PASS2);
     AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));
     // 5. closing half kick + EOS + next dt minimum
+    marks.mark(ASTRAEA_STAGE_KICK_EOS);
     KickArgs k2{};
     k2.dtMode = 2;
     k2.dtSlots = ws->dtSlots;
@@ -1257,12 +1294,50 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
     k2.withEos = true;
     k2.rawMinOut = ws->rawMin + (q ^ 1);
     AG_LAUNCH(launchKick(*p, n, k2, st));
+    marks.mark(kStageCount);
     if (outDtPsu != nullptr)
         AG_CUDA(cudaMemcpyAsync(outDtPsu, ws->dtSlots + (q ^ 1), sizeof(float), cudaMemcpyDeviceToHost, st));
     ws->parity = q ^ 1;
     ws->stepCacheValid = true;
     ws->stepToken = static_cast<const void*>(p->posX);
     ws->stepCount += 1;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_set_stage_timing(int enable) {
+    g_stageTiming.store(enable != 0);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_read_stage_times(const AstraeaRadixBvh* bvh, float* outMs, uint32_t capacity,
+                                             uint32_t* outCount) {
+    if (bvh == nullptr || outMs == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    Workspace* ws = nullptr;
+    AstraeaStatus s = workspaceFor(bvh, 0u, false, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (!ws->stageRecorded) return fail(ASTRAEA_ERR_INVALID, "read_stage_times: no timed fused step on this BVH");
+    AG_CUDA(cudaEventSynchronize(ws->stageEv[kStageCount]));
+    const uint32_t m = std::min<uint32_t>(capacity, static_cast<uint32_t>(kStageCount));
+    for (uint32_t k = 0; k < m; ++k) {
+        float t = 0.0f;
+        AG_CUDA(cudaEventElapsedTime(&t, ws->stageEv[k], ws->stageEv[k + 1]));
+        outMs[k] = t;
+    }
+    if (outCount != nullptr) *outCount = m;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_read_device_counters(uint64_t* outCounters, uint32_t capacity, uint32_t* outCount) {
+    if (outCounters == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    DeviceState* ds = nullptr;
+    AstraeaStatus s = deviceState(&ds);
+    if (s != ASTRAEA_OK) return s;
+    DevStatus h{};
+    AG_CUDA(cudaStreamSynchronize(stream()));
+    AG_CUDA(cudaMemcpy(&h, ds->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    const uint32_t m = std::min<uint32_t>(capacity, static_cast<uint32_t>(kCntCount));
+    for (uint32_t k = 0; k < m; ++k) outCounters[k] = h.counters[k];
+    if (outCount != nullptr) *outCount = m;
     return ASTRAEA_OK;
 }
 

@@ -49,7 +49,10 @@ enum Counter : int {
     kCntFallbackWalks = 5,         // particles served by the per-thread walk
     kCntNeighborCandidates = 6,    // leaves tested by the neighbour build (after the group-box filter)
     kCntGravityUndecided = 7,      // nodes the whole group had to test in the gravity walk
-    kCntCount = 8
+    kCntPass1Pairs = 8,            // pairs inside pass 1's radius (r < 2 h_i)
+    kCntPass2Pairs = 9,            // pairs inside pass 2's radius (r < max(2 h_i, 2 h_j))
+    kCntDriftPairs = 10,           // pairs inside the drift's radius
+    kCntCount = 11
 };
 
 struct DevStatus {

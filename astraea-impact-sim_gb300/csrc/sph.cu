@@ -382,6 +382,15 @@ __device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32
     forEachCandidate(w, i, [&](uint32_t j) { body(j, load(j)); });
 }
 
+// Adds a per-thread count to a device counter with one atomic per group of
+// threads that reach the call together (the running threads of a warp).
+__device__ __forceinline__ void addCount(DevStatus* st, int which, uint32_t v) {
+    const unsigned m = __activemask();
+    const unsigned tot = __reduce_add_sync(m, v);
+    if ((threadIdx.x & 31u) == static_cast<unsigned>(__ffs(m) - 1))
+        atomicAdd(&st->counters[which], static_cast<unsigned long long>(tot));
+}
+
 // ---------------------------------------------------------------- pass 1 ---
 __global__ void __launch_bounds__(128, 7) pass1Kernel(AstraeaParticles p, Work w, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,6 +435,7 @@ __global__ void __launch_bounds__(128, 7) pass1Kernel(AstraeaParticles p, Work w
             gZX += volJ * dvz * gx; gZY += volJ * dvz * gy; gZZ += volJ * dvz * gz;
         });
     }
+    addCount(w.status, kCntPass1Pairs, static_cast<uint32_t>(ngb - 1));
     p.shepardC[i] = shep;                                   // sph_gravity.cu:772-787
     const float normNs = sqrtf(nsX * nsX + nsY * nsY + nsZ * nsZ);
     float fs = fminf(1.0f, fmaxf(0.0f, 1.6f * fmaxf(1.0f - shep, normNs / hi) - 0.15f));
@@ -476,6 +486,7 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
 
     float axS = 0.f, ayS = 0.f, azS = 0.f, drC = 0.f, drD = 0.f, duP = 0.f, duAv = 0.f, duT = 0.f, duS = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
+    uint32_t nPairs = 0;
     if (n >= 2u) {
         // records in 32-byte pieces: {q0, q1} for every candidate (one sector),
         // {q2, q3} and {q4, q5} for the candidates in range
@@ -487,6 +498,7 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
             const float hj = b0.w, Hj = 2.0f * hj;
             const float Hm = fmaxf(Hi, Hj);
             if (!(r2 < __fmul_rn(Hm, Hm))) return;          // sph_gravity.cu:1071
+            ++nPairs;
             const F8 q23 = ldg256(&R[kRec2Width * static_cast<size_t>(j) + 2]);
             const F8 q45 = ldg256(&R[kRec2Width * static_cast<size_t>(j) + 4]);
             const float4 b1 = q01.b, b2 = q23.a, b3 = q23.b, b4 = q45.a, b5 = q45.b;
@@ -541,6 +553,7 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
             gZX += volJ * wz * gxi; gZY += volJ * wz * gyi; gZZ += volJ * wz * gzi;
         });
     }
+    addCount(w.status, kCntPass2Pairs, nPairs);
     p.accX[i] += axS;                                          // sph_gravity.cu:1213-1218
     p.accY[i] += ayS;
     p.accZ[i] += azS;
@@ -615,6 +628,7 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
         const float invHi = 1.0f / Hi;
         const float rhoI = fmaxf(vr.w, 1.0e-9f);
         float sx = 0.f, sy = 0.f, sz = 0.f;
+        uint32_t nPairs = 0;
         if (useList && n >= 2u) {
             // one 32-byte record per candidate: {x, y, z, H}, {vx, vy, vz, rho}
             forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&w.drift[j].a); }, [&](uint32_t j, const F8& rj) {
@@ -624,6 +638,7 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
                 const float Hj = q.w;
                 const float Hm = fmaxf(Hi, Hj);
                 if (!(r2 < __fmul_rn(Hm, Hm))) return;
+                ++nPairs;
                 const float4 vj = rj.b;
                 const float2 aj = __ldg(&w.driftAux[j]);          // {m, Wendland norm of H_j}
                 const float r = sqrtf(r2);
@@ -635,6 +650,7 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
                 sz += co * (vj.z - vr.z);
             });
         }
+        addCount(w.status, kCntDriftPairs, nPairs);
         const double d = static_cast<double>(dt);
         const float nx = static_cast<float>(static_cast<double>(me.x) + d * (static_cast<double>(vr.x) + 0.25 * static_cast<double>(sx)));
         const float ny = static_cast<float>(static_cast<double>(me.y) + d * (static_cast<double>(vr.y) + 0.25 * static_cast<double>(sy)));

@@ -247,6 +247,9 @@ def run_gpu(args):
         except ValueError:
             traffic = None
 
+    # ---- per-stage times of the fused step (events between its stages)
+    stages = stage_breakdown(sim, engine, torch, args, max_dt, n, fp32_peak)
+
     # ---- force error of the plain path vs an FP64 direct sum (sampled targets)
     truth = fp64_truth(sim, torch, samples=1024)
     err_rms = force_error_fp64(sim, engine, torch, np, truth=truth, theta=args.theta)
@@ -280,6 +283,7 @@ def run_gpu(args):
                                     "MEASURED_PEAKS.json do not bound this kernel",
                      "interactions_per_launch": inter, "launch_ms": grav_ms},
         "step_hbm": step_hbm_roofline(n, ms_max / args.steps),
+        "stages": stages,
         "force_error_rms_vs_fp64": err_rms,
         "step_counters_per_particle": {k: v / (args.steps * n) for k, v in counters.items()
                                        if k != "gravity_stack_peak"},
@@ -407,18 +411,74 @@ def frame_stages(sim, engine, torch, np, n, reps=5):
             "pcls_frame_ms": pm, "pcls_frame_bytes": size, "pcls_frame_gbs": 68.0 * n / (pm * 1e-3) / 1e9}
 
 
+def hbm_peak():
+    """Measured STREAM-style copy bandwidth of the GB300s (GB/s)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
+
+
 def step_hbm_roofline(n, ms):
     """Compulsory bytes per particle-step of the reference SoA (1.58 KB, the
     per-stage sum of the engine's reads/writes) against measured HBM."""
-    peak = None
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
-            peak = json.load(fh)["hbm_gbs"]
-    except (OSError, ValueError, KeyError):
-        peak = 6800.0
+    peak = hbm_peak()
     achieved = 1580.0 * n / (ms * 1e-3) / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "bytes_per_particle_step": 1580.0}
+
+
+# Compulsory bytes per particle of each fused-step stage for the reference SoA
+# (drift 44; bounds 12 + Morton 24 + sort 200; permute 428; build + refit 172;
+# pass 1 68; EOS 26 per evaluation; gravity 32; pass 2 171; kick 169 per
+# half kick; dt 41 with the closing kick): 1,582 B per particle-step.
+STAGE_BYTES = {"kick": 169, "drift": 44, "sort": 236, "permute": 428, "refit": 172, "pass1": 68, "eos": 26,
+               "gravity": 32, "pass2": 171, "kick_eos": 236}
+# FP32 operations per in-range pair, counted from the restated formulas
+# (every term; a sqrt, a quotient and a Wendland evaluation count as the
+# operations written): pass 1 65, pass 2 189 (with the viscosity, delta-SPH
+# and tensile terms), XSPH drift 41.
+PAIR_FLOP = {"pass1": 65, "pass2": 189, "drift": 41}
+
+
+def stage_breakdown(sim, engine, torch, args, max_dt, n, fp32_peak, steps=3):
+    """CUDA-event time of every stage of the fused step (astraea_gb300_
+    set_stage_timing), averaged over a few steps after the timed region, with
+    each stage's compulsory bytes against measured HBM and, for the SPH pair
+    loops, the in-range pairs (device counters) times their FLOP count
+    against the measured FP32 FMA peak."""
+    from astraea_gb300 import abi
+    acc = dict.fromkeys(abi.STAGES, 0.0)
+    # one untimed step first: the stage calls before this may have left the
+    # step cache invalid, which would put a refresh into the first timed step
+    engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, args.theta, None)
+    engine.reset_device_status()
+    engine.set_stage_timing(True)
+    try:
+        for _ in range(steps):
+            engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, args.theta, None)
+            for k, v in engine.read_stage_times(sim.bvh).items():
+                acc[k] += v / steps
+    finally:
+        engine.set_stage_timing(False)
+    counters = engine.read_device_counters()
+    peak = hbm_peak()
+    out = {}
+    for k, ms in acc.items():
+        e = {"ms": ms}
+        if k in STAGE_BYTES and ms > 0.0:
+            gbs = STAGE_BYTES[k] * n / (ms * 1e-3) / 1e9
+            e.update(bytes_per_particle=STAGE_BYTES[k], gbs=gbs, frac_hbm=gbs / peak)
+        if k in PAIR_FLOP and ms > 0.0:
+            pairs = counters[k + "_pairs"] / steps
+            tf = PAIR_FLOP[k] * pairs / (ms * 1e-3) / 1e12
+            e.update(pairs_per_particle=pairs / n, flop_per_pair=PAIR_FLOP[k], tflops=tf,
+                     frac_fp32=tf / fp32_peak if fp32_peak else None)
+        out[k] = e
+    out["hbm_peak_gbs"] = peak
+    out["total_ms"] = sum(acc.values())
+    return out
 
 
 def force_error_fp64(sim, engine, torch, np, samples=1024, truth=None, theta=0.5):

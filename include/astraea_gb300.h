@@ -499,6 +499,49 @@ AstraeaStatus astraea_gb300_radix_sort_pairs_noalloc(uint64_t* keysIn, uint64_t*
 #define ASTRAEA_DEVFLAG_STACK_OVERFLOW     0x4u
 #define ASTRAEA_DEVFLAG_GROUP_FALLBACK     0x8u
 AstraeaStatus astraea_gb300_read_device_status(uint32_t* outFlags, uint64_t* outCounters8);
+/* Every device counter accumulated since the last reset, in this order (the
+ * first eight are the counters of astraea_gb300_read_device_status); up to
+ * `capacity` of them, *outCount = how many were written.  Blocks.  No engine
+ * counterpart. */
+#define ASTRAEA_COUNTER_GRAVITY_INTERACTIONS  0u
+#define ASTRAEA_COUNTER_GRAVITY_NODE_TESTS    1u
+#define ASTRAEA_COUNTER_NEIGHBOR_ENTRIES      2u
+#define ASTRAEA_COUNTER_GRAVITY_ROUNDS        3u
+#define ASTRAEA_COUNTER_GRAVITY_STACK_PEAK    4u   /* maximum, not a sum */
+#define ASTRAEA_COUNTER_FALLBACK_WALKS        5u
+#define ASTRAEA_COUNTER_NEIGHBOR_CANDIDATES   6u
+#define ASTRAEA_COUNTER_GRAVITY_UNDECIDED     7u
+#define ASTRAEA_COUNTER_PASS1_PAIRS           8u   /* pairs with r < 2 h_i in SPH pass 1 */
+#define ASTRAEA_COUNTER_PASS2_PAIRS           9u   /* pairs with r < max(2 h_i, 2 h_j) in SPH pass 2 */
+#define ASTRAEA_COUNTER_DRIFT_PAIRS          10u   /* pairs inside the XSPH drift's radius */
+#define ASTRAEA_COUNTER_COUNT                11u
+AstraeaStatus astraea_gb300_read_device_counters(uint64_t* outCounters, uint32_t capacity, uint32_t* outCount);
+/* Stage timing of the fused step (no engine counterpart; the engine times
+ * the whole step, gpuStepMs, engine/simulation.cpp:1719-1739).  While
+ * enabled, astraea_gb300_step records a CUDA event on its stream where each
+ * stage begins and where the step ends; astraea_gb300_read_stage_times
+ * returns the stage times of the last such step on this BVH in milliseconds,
+ * in the order ASTRAEA_STAGE_* (blocks until that step has finished).  The
+ * refresh stage is the leaf refresh, drift neighbour lists and dt reduction
+ * of a step whose cache was invalid (near 0 otherwise).  Off by default; the
+ * events add a few microseconds per step.  Do not enable it while a CUDA
+ * graph is being captured. */
+#define ASTRAEA_STAGE_REFRESH      0
+#define ASTRAEA_STAGE_KICK         1    /* opening half kick, dt resolved on the device */
+#define ASTRAEA_STAGE_DRIFT        2
+#define ASTRAEA_STAGE_SORT         3    /* bounds + Morton codes + radix sort */
+#define ASTRAEA_STAGE_PERMUTE      4    /* permutation + Karras build */
+#define ASTRAEA_STAGE_REFIT        5
+#define ASTRAEA_STAGE_NEIGHBOURS   6
+#define ASTRAEA_STAGE_PASS1        7
+#define ASTRAEA_STAGE_EOS          8
+#define ASTRAEA_STAGE_GRAVITY      9
+#define ASTRAEA_STAGE_PASS2       10
+#define ASTRAEA_STAGE_KICK_EOS    11    /* closing half kick + EOS + next dt candidate */
+#define ASTRAEA_STAGE_COUNT       12
+AstraeaStatus astraea_gb300_set_stage_timing(int enable);
+AstraeaStatus astraea_gb300_read_stage_times(const AstraeaRadixBvh* bvh, float* outMs, uint32_t capacity,
+                                             uint32_t* outCount);
 /* Measured FP32 FMA throughput of the current device in TFLOP/s (the
  * denominator of the gravity kernel's roofline).  Blocks; no engine
  * counterpart. */
