@@ -33,7 +33,9 @@ constexpr uint32_t kNbExpand = 32;   // an opened node of at most this many part
 // undMin while dirMem is computed.
 struct NbWarpSmem {
     int stack[kNbStack];
-    float4 cand[kNbList];    // {x, y, z, Hs}
+    // candidate leaves, pair-interleaved for the f32x2 pipes:
+    // cand[8k..8k+7] = {xA, xB, yA, yB, zA, zB, HsA, HsB} of entries 2k, 2k+1
+    float cand[8 * (kNbList / 2)];
     int candIdx[kNbList];
     float4 dirMem[8];
     float4 undMin[32];
@@ -108,18 +110,41 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
             if (cnt < maxNbr) myList[cnt] = j;
             ++cnt;
         };
-        // Superset test r < max(Hs_i, Hs_j) in plain FMA arithmetic: every
-        // pass re-tests its own radius exactly, and Hs exceeds those radii by
-        // 0.9 %, far more than any rounding difference.
-        auto flush = [&](int base, int num) {
+        auto putCand = [&](int slot, float x, float y, float z, float hs, int j) {
+            float* b = S.cand + 8 * (slot >> 1) + (slot & 1);
+            b[0] = x; b[2] = y; b[4] = z; b[6] = hs;
+            S.candIdx[slot] = j;
+        };
+        // Superset test r < max(Hs_i, Hs_j) in plain FMA arithmetic, two
+        // candidates per instruction: every pass re-tests its own radius
+        // exactly, and Hs exceeds those radii by 0.9 %, far more than any
+        // rounding difference.  Tests candidates 0 .. 2 pairs - 1 in order.
+        const f2 X2 = pack2(me.x, me.x), Y2 = pack2(me.y, me.y), Z2 = pack2(me.z, me.z);
+        auto flush = [&](int pairs) {
             if (active) {
-                for (int e = 0; e < num; ++e) {
-                    const float4 q = S.cand[base + e];
-                    const int j = S.candIdx[base + e];
-                    const float dx = me.x - q.x, dy = me.y - q.y, dz = me.z - q.z;
-                    const float R = fmaxf(Hs, q.w);
-                    if (dx * dx + dy * dy + dz * dz < R * R && j != static_cast<int>(i)) put(static_cast<uint32_t>(j));
+                for (int k = 0; k < pairs; ++k) {
+                    const float* b = S.cand + 8 * k;
+                    const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(b);       // (x), (y)
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(b + 4);   // (z), (Hs)
+                    const int2 jj = *reinterpret_cast<const int2*>(S.candIdx + 2 * k);
+                    const f2 dx = sub2(X2, u.x), dy = sub2(Y2, u.y), dz = sub2(Z2, v.x);
+                    float r2a, r2b, ha, hb;
+                    unpack2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))), r2a, r2b);
+                    unpack2(v.y, ha, hb);
+                    const float Ra = fmaxf(Hs, ha), Rb = fmaxf(Hs, hb);
+                    if (r2a < Ra * Ra && jj.x != static_cast<int>(i)) put(static_cast<uint32_t>(jj.x));
+                    if (r2b < Rb * Rb && jj.y != static_cast<int>(i)) put(static_cast<uint32_t>(jj.y));
                 }
+            }
+        };
+        // after a flush of entries 0..31: entries 32 .. cCount-1 move down
+        auto shiftDown = [&]() {
+            if (lane < cCount - 32) {
+                const int src = 32 + lane;
+                const float* b = S.cand + 8 * (src >> 1) + (src & 1);
+                const float x = b[0], y = b[2], z = b[4], hs = b[6];
+                const int j = S.candIdx[src];
+                putCand(lane, x, y, z, hs, j);
             }
         };
 
@@ -223,17 +248,15 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 keep = dx * dx + dy * dy + dz * dz <= R * R * 1.00001f;
             }
             const unsigned leafMask = __ballot_sync(0xffffffffu, keep);
-            if (keep) {
-                const int slot = cCount + __popc(leafMask & laneMaskLt());
-                S.cand[slot] = make_float4(pm.x, pm.y, pm.z, hsj);
-                S.candIdx[slot] = ~c;
-            }
+            if (keep) putCand(cCount + __popc(leafMask & laneMaskLt()), pm.x, pm.y, pm.z, hsj, ~c);
             cCount += __popc(leafMask);
             nCand += __popc(leafMask);
             __syncwarp();
             if (cCount >= 32) {
+                flush(16);
+                __syncwarp();
+                shiftDown();
                 cCount -= 32;
-                flush(cCount, 32);
                 __syncwarp();
             }
             while (expandMask) {                // small opened nodes: their particles, lane by lane
@@ -256,23 +279,25 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                     keepJ = dx * dx + dy * dy + dz * dz <= R * R * 1.00001f;
                 }
                 const unsigned km = __ballot_sync(0xffffffffu, keepJ);
-                if (keepJ) {
-                    const int slot = cCount + __popc(km & laneMaskLt());
-                    S.cand[slot] = make_float4(pj.x, pj.y, pj.z, hj);
-                    S.candIdx[slot] = static_cast<int>(j);
-                }
+                if (keepJ) putCand(cCount + __popc(km & laneMaskLt()), pj.x, pj.y, pj.z, hj, static_cast<int>(j));
                 cCount += __popc(km);
                 nCand += __popc(km);
                 __syncwarp();
                 if (cCount >= 32) {
+                    flush(16);
+                    __syncwarp();
+                    shiftDown();
                     cCount -= 32;
-                    flush(cCount, 32);
                     __syncwarp();
                 }
                 }
             }
         }
-        flush(0, cCount);
+        if (cCount & 1) {                  // odd tail: a pad entry no member can reach
+            if (lane == 0) putCand(cCount, 3.0e38f, 3.0e38f, 3.0e38f, 0.0f, -1);
+            __syncwarp();
+        }
+        flush((cCount + 1) >> 1);
         if (active) {
             w.nbrCount[i] = cnt;
             if (cnt > maxNbr) overflow = true;
