@@ -323,19 +323,42 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 const int nu = __popc(und);
                 nUndecided += nu;
                 const int slot = __popc(und & laneMaskLt());
+                // pair-interleaved in und's storage: {comxA, comxB, comyA,
+                // comyB, comzA, comzB, ddA, ddB} for undecided nodes 2k, 2k+1
+                float* undP = reinterpret_cast<float*>(S.und);
                 if (undecided) {
-                    S.und[slot] = make_float4(r0.x, r0.y, r0.z, dd);
+                    float* ub = undP + 8 * (slot >> 1) + (slot & 1);
+                    ub[0] = r0.x; ub[2] = r0.y; ub[4] = r0.z; ub[6] = dd;
                     if (kInside) { S.undMin[slot] = bmin; S.undMax[slot] = bmax; }
                 }
                 __syncwarp();
                 unsigned bits = 0u;
-#pragma unroll 2
-                for (int k = 0; k < nu; ++k) {
-                    const float4 q = S.und[k];
-                    float4 mn = q, mx = q;
-                    if (kInside) { mn = S.undMin[k]; mx = S.undMax[k]; }
-                    const bool ok = !active || acceptsMember(xi, yi, zi, q, q.w, theta2, kInside, mn, mx);
-                    bits |= (__all_sync(0xffffffffu, ok) ? 1u : 0u) << k;
+                // the engine's member test (acceptsMember) for two nodes per
+                // instruction: the same IEEE operations in the same order
+                const f2 T2 = pack2(theta2, theta2);
+                for (int k = 0; k < nu; k += 2) {
+                    const float* ub = undP + 4 * k;
+                    const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(ub);       // (com x), (com y)
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(ub + 4);   // (com z), (dd)
+                    const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
+                    const f2 r2 = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+                    float r2a, r2b, ta, tb, dda, ddb;
+                    unpack2(r2, r2a, r2b);
+                    unpack2(mul2(T2, r2), ta, tb);
+                    unpack2(v.y, dda, ddb);
+                    bool okA = dda < ta && r2a > 1.0e-20f, okB = ddb < tb && r2b > 1.0e-20f;
+                    if (kInside) {
+                        const float4 mnA = S.undMin[k], mxA = S.undMax[k];
+                        const float4 mnB = S.undMin[k + 1], mxB = S.undMax[k + 1];
+                        if (okA && xi >= mnA.x && xi <= mxA.x && yi >= mnA.y && yi <= mxA.y && zi >= mnA.z &&
+                            zi <= mxA.z)
+                            okA = false;
+                        if (okB && xi >= mnB.x && xi <= mxB.x && yi >= mnB.y && yi <= mxB.y && zi >= mnB.z &&
+                            zi <= mxB.z)
+                            okB = false;
+                    }
+                    bits |= (__all_sync(0xffffffffu, !active || okA) ? 1u : 0u) << k;
+                    if (k + 1 < nu) bits |= (__all_sync(0xffffffffu, !active || okB) ? 1u : 0u) << (k + 1);
                 }
                 if (undecided) accept = (bits >> slot) & 1u;
                 __syncwarp();
