@@ -129,26 +129,8 @@ __device__ __forceinline__ float pointBoxDist2(float px, float py, float pz, flo
 }
 
 // ---------------------------------------------------------- SPH kernels ---
-// Wendland C2 in 3-D with support H (sph_gravity.cu:199-208).
-__device__ __forceinline__ float wendlandC2(float r, float H) {
-    if (r >= H || H <= 0.0f) return 0.0f;
-    const float q = r / H;
-    const float omq = 1.0f - q;
-    const float omq2 = omq * omq;
-    const float norm = 21.0f / (2.0f * kPiF * H * H * H);
-    return norm * omq2 * omq2 * (1.0f + 4.0f * q);
-}
-// g with grad_i W(r_i - r_j, H) = g (r_i - r_j) (sph_gravity.cu:211-220).
-// wendlandC2GradN takes norm = 210 / (pi H^5), computed once per particle
-// with the same expression.
-__device__ __forceinline__ float wendlandC2Grad(float r, float H) {
-    if (r >= H || H <= 0.0f) return 0.0f;
-    const float q = r / H;
-    const float omq = 1.0f - q;
-    const float H2 = H * H;
-    const float H5 = H2 * H2 * H;
-    return -(210.0f / (kPiF * H5)) * omq * omq * omq;
-}
+// Wendland C2 in 3-D with support H (sph_gravity.cu:199-208), its norm
+// 21 / (2 pi H^3) computed once per particle with the engine's expression.
 __device__ __forceinline__ float wendlandC2N(float r, float H, float norm) {   // norm = 21 / (2 pi H^3)
     if (r >= H || H <= 0.0f) return 0.0f;
     const float q = r / H;
@@ -158,7 +140,9 @@ __device__ __forceinline__ float wendlandC2N(float r, float H, float norm) {   /
 }
 __device__ __forceinline__ float wendlandNorm(float H) { return 21.0f / (2.0f * kPiF * H * H * H); }
 
-// Pair-loop forms of the kernels above.  The neighbour loops evaluate them
+// Pair-loop forms of the Wendland C2 kernel and of its gradient factor g,
+// grad_i W(r_i - r_j, H) = g (r_i - r_j) (sph_gravity.cu:211-220, norm
+// 210 / (pi H^5) computed once per particle).  The neighbour loops evaluate them
 // once per pair; the IEEE quotient r / H (a dozen instructions with its
 // special-case path) becomes three operations with y = 1 / H taken once per
 // particle (or stored in its record): q0 = r y, the exact residual
@@ -182,11 +166,6 @@ __device__ __forceinline__ float wendlandC2I(float r, float H, float invH, float
 __device__ __forceinline__ float wendlandC2GradI(float r, float H, float invH, float norm) {
     if (r >= H) return 0.0f;
     const float omq = 1.0f - quotRN(r, H, invH);
-    return -norm * omq * omq * omq;
-}
-__device__ __forceinline__ float wendlandC2GradN(float r, float H, float norm) {
-    if (r >= H || H <= 0.0f) return 0.0f;
-    const float omq = 1.0f - r / H;
     return -norm * omq * omq * omq;
 }
 // Balsara switch (sph_gravity.cu:222-228).

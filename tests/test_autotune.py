@@ -36,6 +36,30 @@ def test_gpu_walk_results_do_not_depend_on_block_shape():
 
 
 @pytest.mark.gpu
+def test_gpu_quadrupole_walk_does_not_depend_on_block_shape():
+    from astraea_gb300 import engine
+    st, _ = scenarios.differentiated_impact(n_total=131072, seed=19)
+    n = len(st["posX"])
+    p, alt, bvh = engine.DeviceParticles(n), engine.DeviceParticles(n), engine.DeviceBvh(n)
+    p.upload(st)
+    alt.count = n
+    outs = []
+    engine.set_far_field(1)
+    try:
+        engine.sort_and_build_bvh(p, alt, bvh)           # builds the second moments too
+        for gw in (4, 2, 8):
+            engine.set_tuning(n, gw, 4)
+            engine.gravity_barnes_hut(p, bvh, 0.7)
+            outs.append(p.download(["accX", "accY", "accZ", "phiGrav"]))
+    finally:
+        engine.set_far_field(0)
+        engine.set_tuning(n, 4, 4)
+    for o in outs[1:]:
+        for f, v in o.items():
+            assert np.array_equal(v, outs[0][f]), f
+
+
+@pytest.mark.gpu
 def test_gpu_autotune_records_a_valid_choice():
     from astraea_gb300 import engine
     st, _ = scenarios.differentiated_impact(n_total=65536, seed=18)
