@@ -110,8 +110,10 @@ def test_pass1_eos_gravity_pass2_parity():
     e = report("eos", g, c, ["pressure", "soundSpeed", "tempK"])
     assert max(e.values()) < TOL
     assert np.mean(g["phaseId"] == c["phaseId"]) > 0.999
+    engine.reset_device_status()
     engine.gravity_barnes_hut(p, bvh, 0.5)
-    o.gravity(0.5)
+    _, counters = engine.read_device_status()
+    assert counters["gravity_interactions"] == o.gravity(0.5)       # the same interaction set
     g, c = p.download(), o.state()
     e = report("gravity", g, c, ["accX", "accY", "accZ", "phiGrav"])
     assert max(e.values()) < TOL
@@ -151,13 +153,17 @@ def test_gravity_parity_and_ac3_error(theta):
     st["originalId"] = np.arange(4096, dtype=np.uint32)
     p, alt, bvh = gpu_setup(st, packed=False)
     engine.sort_and_build_bvh(p, alt, bvh)
+    engine.reset_device_status()
     engine.gravity_barnes_hut(p, bvh, theta)
+    _, counters = engine.read_device_status()
     o = oracle.Oracle(st)
     o.sort_and_build()
-    o.gravity(theta)
+    inter = o.gravity(theta)
     g, c = p.download(), o.state()
     e = report("gravity theta=%.1f" % theta, g, c, ["accX", "accY", "accZ", "phiGrav"])
     assert max(e.values()) < TOL
+    # the same interaction set: the number of (particle, monopole or leaf) terms is an integer result
+    assert counters["gravity_interactions"] == inter
     acc, _ = oracle.direct_gravity_f64(g, np.arange(4096))
     bh = np.stack([g["accX"], g["accY"], g["accZ"]], 1).astype(np.float64)
     err = np.linalg.norm(bh - acc, axis=1) / np.linalg.norm(acc, axis=1)
