@@ -139,7 +139,7 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     const size_t oTable = take(levMax * nbMax * 32), oBMom = take(nbMax * 80), oQuad = take(C * 32);
     const size_t oDrift = take(C * 16);
     const size_t oDRec = take(C * 32), oDAux = take(C * 8);
-    const size_t oCnt = take(C * 4), oList = take(C * maxNbr * 4), oWords = take(kWCount * 4);
+    const size_t oCnt = take(C * 4), oList = take((C + 31) / 32 * 32 * maxNbr * 4), oWords = take(kWCount * 4);
     const size_t oSort = take(sortWords * 4), oDt = take(64);
     void* block = nullptr;
     AG_CUDA(cudaMalloc(&block, off));

@@ -435,7 +435,7 @@ struct Work {
                            // b {vx, vy, vz, rho} (opening kick / leaf refresh)
     float2* driftAux;      // {m, 21 / (2 pi H^3)} (the Wendland norm of H)
     uint32_t* nbrCount;
-    uint32_t* nbrList;     // particle-major, maxNbr per particle
+    uint32_t* nbrList;     // group-interleaved: entry k of particle i at ((i/32) maxNbr + k) 32 + i%32
     uint32_t* words;       // small words, see WordIndex
     uint32_t* sortScratch; // histograms + look-back + tile counters
     size_t sortScratchWords;

@@ -103,11 +103,11 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, cCount = 0;
         uint32_t cnt = 0, rounds = 0;
-        uint32_t* myList = w.nbrList + static_cast<size_t>(active ? i : 0u) * maxNbr;
+        uint32_t* myList = w.nbrList + static_cast<size_t>(g) * maxNbr * 32u + static_cast<uint32_t>(lane);
         __syncwarp();
 
         auto put = [&](uint32_t j) {
-            if (cnt < maxNbr) myList[cnt] = j;
+            if (cnt < maxNbr) myList[static_cast<size_t>(cnt) * 32u] = j;
             ++cnt;
         };
         auto putCand = [&](int slot, float x, float y, float z, float hs, int j) {
@@ -315,19 +315,22 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
     }
 }
 
+// Neighbour lists are group-interleaved: entry k of particle i is word
+// ((i / 32) maxNbr + k) 32 + i % 32, so the 32 particles of a group (the
+// lanes of one warp in every pass) read their k-th entries as one 128-byte
+// row and a lane's list never shares a sector with another lane's.
+__device__ __forceinline__ const uint32_t* listOf(const Work& w, uint32_t i) {
+    return w.nbrList + static_cast<size_t>(i >> 5) * w.maxNbr * 32u + (i & 31u);
+}
+
 // Visit every j of particle i's superset list; when the list overflowed,
 // walk the tree depth-first with the same superset test instead.
 template <class F>
 __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& f) {
     const uint32_t c = __ldg(&w.nbrCount[i]);
     if (c <= w.maxNbr) {
-        const uint32_t* list = w.nbrList + static_cast<size_t>(i) * w.maxNbr;
-        uint32_t k = 0;
-        for (; k + 4 <= c; k += 4) {
-            const uint4 q = __ldg(reinterpret_cast<const uint4*>(list + k));
-            f(q.x); f(q.y); f(q.z); f(q.w);
-        }
-        for (; k < c; ++k) f(__ldg(&list[k]));
+        const uint32_t* list = listOf(w, i);
+        for (uint32_t k = 0; k < c; ++k) f(__ldg(&list[static_cast<size_t>(k) * 32u]));
         return;
     }
     atomicAdd(&w.status->counters[kCntFallbackWalks], 1ull);
@@ -372,13 +375,16 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
 
 // List words are read once per pass and the lists (308 B per particle) do
 // not fit in L1: read them without allocating in L1, which keeps L1 for the
-// neighbour records.
-__device__ __forceinline__ uint4 ldListNoL1(const uint32_t* p) {
-    uint4 v;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p));
+// neighbour records.  Four consecutive entries of one particle (32 words
+// apart in the group-interleaved layout).
+__device__ __forceinline__ uint32_t ldWordNoL1(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
+}
+__device__ __forceinline__ uint4 ldListNoL1(const uint32_t* list, uint32_t k) {
+    const uint32_t* p = list + static_cast<size_t>(k) * 32u;
+    return make_uint4(ldWordNoL1(p), ldWordNoL1(p + 32), ldWordNoL1(p + 64), ldWordNoL1(p + 96));
 }
 
 // Same candidate set as forEachCandidate, with each candidate's first record
@@ -389,17 +395,17 @@ template <class L, class B>
 __device__ __forceinline__ void forEachCandidatePrefetched(const Work& w, uint32_t i, L&& load, B&& body) {
     const uint32_t c = __ldg(&w.nbrCount[i]);
     if (c <= w.maxNbr) {
-        const uint32_t* list = w.nbrList + static_cast<size_t>(i) * w.maxNbr;
+        const uint32_t* list = listOf(w, i);
         uint32_t k = 0;
-        uint4 q = c >= 4 ? ldListNoL1(list) : make_uint4(0u, 0u, 0u, 0u);
+        uint4 q = c >= 4 ? ldListNoL1(list, 0u) : make_uint4(0u, 0u, 0u, 0u);
         for (; k + 4 <= c; k += 4) {
-            const uint4 next = (k + 8 <= c) ? ldListNoL1(list + k + 4) : q;
+            const uint4 next = (k + 8 <= c) ? ldListNoL1(list, k + 4) : q;
             const auto r0 = load(q.x), r1 = load(q.y), r2 = load(q.z), r3 = load(q.w);
             body(q.x, r0); body(q.y, r1); body(q.z, r2); body(q.w, r3);
             q = next;
         }
         for (; k < c; ++k) {
-            const uint32_t j = __ldg(&list[k]);
+            const uint32_t j = __ldg(&list[static_cast<size_t>(k) * 32u]);
             body(j, load(j));
         }
         return;
