@@ -133,31 +133,40 @@ __global__ void __launch_bounds__(256) kickKernel(AstraeaParticles p, uint32_t n
     }
     float dtCand = 1.0e30f;
     if (i < n) {
-        const float vx = p.velX[i] + halfDt * p.accX[i];
-        const float vy = p.velY[i] + halfDt * p.accY[i];
-        const float vz = p.velZ[i] + halfDt * p.accZ[i];
+        // every input first (the fields are plain pointers, so loads after a
+        // store could not be moved ahead of it): all reads in flight at once
+        const float ax0 = p.accX[i], ay0 = p.accY[i], az0 = p.accZ[i];
+        const float vx0 = p.velX[i], vy0 = p.velY[i], vz0 = p.velZ[i];
+        const float rho0 = p.rho[i], drho = p.drhoDt[i], u0 = p.u[i], du = p.duDt[i];
+        const float dOld = p.damageCbrt[i], dDam = p.dDamageCbrtDt[i];
+        const float temp0 = p.tempK[i], pres0 = p.pressure[i], cs0 = p.soundSpeed[i];
+        const float s0xx = p.sXX[i], s0yy = p.sYY[i], s0zz = p.sZZ[i], s0xy = p.sXY[i], s0xz = p.sXZ[i], s0yz = p.sYZ[i];
+        const float dsxx = p.dSXX[i], dsyy = p.dSYY[i], dszz = p.dSZZ[i], dsxy = p.dSXY[i], dsxz = p.dSXZ[i], dsyz = p.dSYZ[i];
+        const float hI = (a.rawMinOut != nullptr) ? p.h[i] : 0.0f;
+        const float vx = vx0 + halfDt * ax0;
+        const float vy = vy0 + halfDt * ay0;
+        const float vz = vz0 + halfDt * az0;
         p.velX[i] = vx; p.velY[i] = vy; p.velZ[i] = vz;
         p.velHalfX[i] = vx; p.velHalfY[i] = vy; p.velHalfZ[i] = vz;
-        const float rhoNew = fmaxf(p.rho[i] + halfDt * p.drhoDt[i], 1.0e-9f);
+        const float rhoNew = fmaxf(rho0 + halfDt * drho, 1.0e-9f);
         p.rho[i] = rhoNew;
         const uint8_t matRaw = p.materialId[i];
         const int mi = matIndex(matRaw);
         const MatConst& st = c_mat[mi];
-        float uNew = p.u[i] + halfDt * p.duDt[i];
+        float uNew = u0 + halfDt * du;
         if (a.clampThermal) {
             uNew = fmaxf(uNew, coldEnergyF32(mi, rhoNew) + 3.0f * st.cv);
         } else {
             uNew = fmaxf(uNew, 0.0f);
         }
         p.u[i] = uNew;
-        const float dOld = p.damageCbrt[i];
-        float dCbrt = dOld + halfDt * p.dDamageCbrtDt[i];
+        float dCbrt = dOld + halfDt * dDam;
         dCbrt = fminf(1.0f, fmaxf(dOld, dCbrt));
         const float D = dCbrt * dCbrt * dCbrt;
         p.damageCbrt[i] = dCbrt;
         p.damage[i] = D;
-        float tempK = p.tempK[i];
-        float pres = p.pressure[i];
+        float tempK = temp0;
+        float pres = pres0;
         EosOut e{};
         if (a.clampThermal || a.withEos) e = evaluateEosF32(static_cast<uint8_t>(mi), rhoNew, uNew, D);
         if (a.clampThermal) {                      // EOS before the strength update (:1334-1340)
@@ -166,12 +175,12 @@ __global__ void __launch_bounds__(256) kickKernel(AstraeaParticles p, uint32_t n
         }
         float sXX = 0.f, sYY = 0.f, sZZ = 0.f, sXY = 0.f, sXZ = 0.f, sYZ = 0.f;
         if (!(st.muShear <= 0.0f || st.tMelt <= 0.0f || tempK >= st.tMelt)) {   // :1342-1373
-            sXX = p.sXX[i] + halfDt * p.dSXX[i];
-            sYY = p.sYY[i] + halfDt * p.dSYY[i];
-            sZZ = p.sZZ[i] + halfDt * p.dSZZ[i];
-            sXY = p.sXY[i] + halfDt * p.dSXY[i];
-            sXZ = p.sXZ[i] + halfDt * p.dSXZ[i];
-            sYZ = p.sYZ[i] + halfDt * p.dSYZ[i];
+            sXX = s0xx + halfDt * dsxx;
+            sYY = s0yy + halfDt * dsyy;
+            sZZ = s0zz + halfDt * dszz;
+            sXY = s0xy + halfDt * dsxy;
+            sXZ = s0xz + halfDt * dsxz;
+            sYZ = s0yz + halfDt * dsyz;
             const float tr3 = (sXX + sYY + sZZ) * (1.0f / 3.0f);
             sXX -= tr3; sYY -= tr3; sZZ -= tr3;
             const float tRatio = tempK / st.tMelt;
@@ -184,15 +193,14 @@ __global__ void __launch_bounds__(256) kickKernel(AstraeaParticles p, uint32_t n
             sXX *= scale; sYY *= scale; sZZ *= scale; sXY *= scale; sXZ *= scale; sYZ *= scale;
         }
         p.sXX[i] = sXX; p.sYY[i] = sYY; p.sZZ[i] = sZZ; p.sXY[i] = sXY; p.sXZ[i] = sXZ; p.sYZ[i] = sYZ;
-        float cs = p.soundSpeed[i];
+        float cs = a.clampThermal ? e.cs : cs0;
         if (a.withEos && !a.clampThermal) {        // the engine's EOS launch after the kick
             p.pressure[i] = e.P; p.soundSpeed[i] = e.cs; p.tempK[i] = e.T; p.phaseId[i] = e.phase;
             cs = e.cs;
         }
         if (a.driftOut != nullptr) a.driftOut[i].b = make_float4(vx, vy, vz, rhoNew);
         if (a.rawMinOut != nullptr) {
-            const float d = dtCandidate(p.h[i], cs, vx, vy, vz, p.accX[i], p.accY[i], p.accZ[i], uNew, p.duDt[i],
-                                        matRaw);
+            const float d = dtCandidate(hI, cs, vx, vy, vz, ax0, ay0, az0, uNew, du, matRaw);
             if (isfinite(d) && d > 0.0f) dtCand = d;
         }
     }
