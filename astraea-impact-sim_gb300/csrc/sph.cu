@@ -10,10 +10,11 @@
 //   * pass 1, pass 2 and the drift run one thread per particle over its own
 //     list, re-applying the engine's exact FP32 range test, so every lane
 //     works on its own pairs;
-//   * neighbour data is read from packed float4 records (positions + mass,
-//     velocity + density, and a five-float4 pass-2 record written by the EOS
-//     kernel), one 16-byte load per group of fields instead of one gather per
-//     field.
+//   * neighbour data is read from packed records (pass 1: position + mass
+//     and velocity + density in one 32-byte record; drift: position + H and
+//     velocity + density; pass 2: a 96-byte record written by the EOS
+//     kernel, read in three 32-byte pieces), one 256-bit load per piece
+//     instead of one gather per field.
 // A particle whose list overflowed the per-particle capacity is served by a
 // per-thread depth-first walk with the same superset test (rare path).
 #include "kernels.h"
@@ -488,8 +489,8 @@ __global__ void __launch_bounds__(128, 7) pass1Kernel(AstraeaParticles p, Work w
 
 // ---------------------------------------------------------------- pass 2 ---
 // Reads the pass-2 records written by the EOS kernel (layout and derived
-// values: integrate.cu, writePass2Record): one 16-byte load per group of
-// fields, and no per-pair division for quantities of the neighbour alone.
+// values: integrate.cu, writePass2Record): one 256-bit load per 32-byte
+// piece, and no per-pair division for quantities of the neighbour alone.
 __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w, uint32_t n,
                                                    const uint32_t* livingFlags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
