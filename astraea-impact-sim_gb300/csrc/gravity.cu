@@ -16,8 +16,9 @@
 //     26-direction bounding polytope) accepts most far nodes; (2) the exact
 //     test of the member that lies furthest towards the node (looked up per
 //     group for 26 directions) opens most near ones; (3) the few nodes still
-//     undecided are tested by all 32 members at once, one node per warp
-//     iteration from a shared-memory list, so no lane loops over the group;
+//     undecided are tested by all 32 members at once, two nodes per warp
+//     iteration (f32x2) from a shared-memory list, so no lane loops over the
+//     group;
 //   * accepted monopoles and reached leaves are appended to two per-warp
 //     interaction lists in shared memory; every 32 entries the warp evaluates
 //     them with each lane summing its own particle's force from broadcast
