@@ -31,7 +31,7 @@ namespace astraea_gb300 {
 namespace {
 
 constexpr int kGravWarps = 4;
-constexpr int kGravStack = 1024;
+constexpr int kGravStack = 768;           // entries per warp (peak use: 274 at 1M, 322 at 16M)
 constexpr int kGravList = 64;
 
 // Interaction lists are stored pair-interleaved so that one 16-byte shared
