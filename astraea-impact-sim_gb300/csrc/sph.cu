@@ -23,7 +23,7 @@ namespace astraea_gb300 {
 namespace {
 
 constexpr int kNbWarps = 4;
-constexpr int kNbStack = 1024;
+constexpr int kNbStack = 384;   // entries per warp (peak use: 80 at 1M, 88 at 16M)
 constexpr int kNbList = 64;
 constexpr uint32_t kNbExpand = 32;   // an opened node of at most this many particles is read as its leaf range
 
