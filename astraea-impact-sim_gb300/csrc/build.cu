@@ -22,7 +22,7 @@ __global__ void initBoundsKernel(uint32_t* words) {
         const uint32_t hi = orderedFromFloat(1.0e30f), lo = orderedFromFloat(-1.0e30f);
         words[kWBounds + 0] = hi; words[kWBounds + 1] = hi; words[kWBounds + 2] = hi;
         words[kWBounds + 3] = lo; words[kWBounds + 4] = lo; words[kWBounds + 5] = lo;
-        words[kWLiving + 0] = 0u; words[kWLiving + 1] = 0u;
+        words[kWLiving + 0] = 0u; words[kWLiving + 1] = 0u; words[kWMassMax] = 0u;
     }
 }
 
@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(256) permuteLeavesKarrasKernel(AstraeaParticle
                                                                  Work w, uint32_t n, uint32_t* livingFlags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool tracer = false, intact = false;
+    uint32_t massBits = 0u;                         // |m| as bits: ordered like the values
     if (i < n) {
         // min(): keeps the gather in bounds even if a failed sort (look-back
         // timeout, flagged in the status word) left a non-permutation here.
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(256) permuteLeavesKarrasKernel(AstraeaParticle
         }
 #undef AG_GATHER
         const float m = __ldg(&p.mass[s]);
+        massBits = __float_as_uint(fabsf(m));
         const float hRaw = __ldg(&p.h[s]);
         const float hI = fmaxf(hRaw, 1.0e-6f);
         const float h0I = fmaxf(__ldg(&p.h0[s]), 1.0e-6f);
@@ -116,9 +118,11 @@ __global__ void __launch_bounds__(256) permuteLeavesKarrasKernel(AstraeaParticle
     }
     const unsigned anyTracer = __ballot_sync(0xffffffffu, tracer);
     const unsigned anyIntact = __ballot_sync(0xffffffffu, intact);
+    const uint32_t warpMassBits = __reduce_max_sync(0xffffffffu, massBits);
     if ((threadIdx.x & 31) == 0) {
         if (anyTracer) atomicOr(&livingFlags[0], 1u);
         if (anyIntact) atomicOr(&livingFlags[1], 1u);
+        if (warpMassBits != 0u) atomicMax(&w.words[kWMassMax], warpMassBits);   // scale of the refit's sums
     }
     if (i + 1u < n) {                               // internal node i (Karras 2012)
         const int ii = static_cast<int>(i);
@@ -176,20 +180,96 @@ __global__ void __launch_bounds__(256) refreshLeavesKernel(AstraeaParticles p, W
 // moments are reductions over that range and need no climb through the
 // tree, no arrival counters and no fences:
 //   1. per block of 256 leaves: prefix and suffix min/max of the box and h
-//      values, inclusive FP64 prefix sums of the moments, the block's
-//      totals; then every node whose range lies inside the block, from
-//      shared memory;
-//   2. one block: exclusive FP64 scan of the block totals and a sparse table
-//      of block extremes;
+//      values, inclusive prefix sums of the moments, the block's totals;
+//      then every node whose range lies inside the block, from shared memory;
+//   2. one block: exclusive scan of the block totals; a sparse table of
+//      block extremes;
 //   3. per node spanning blocks: box = suffix (first's block) + prefix
 //      (last's block) + one table query over the blocks between; moments =
 //      difference of two global prefix sums.
 // Min/max are exact in any order, so boxes, dNode and maxH equal the
-// engine's; COM and mass come from FP64 sums (as before, rounded to float
-// once).  kMoments adds the central second moments S = sum m x x^T - M c c^T
-// from FP64 sums of m x_a x_b.
+// engine's.  The moments are summed as 64-bit fixed-point integers: with
+// |m| < 2^em (the largest mass, reduced by the permutation), |x| < 2^ex (the
+// scene bounds) and n <= 2^lg, the unit of m x is 2^(em + ex + lg - 61), so
+// no partial sum reaches 2^62.  Integer sums are exact in any order and a
+// node's sum is the exact difference of two prefix sums (FP64 prefix sums
+// lose a small node's digits to the cancellation), and they take the
+// integer pipes instead of the FP64 pipe, which runs at 1/64 of the FP32
+// rate on this GPU.  The leaf terms m x are FP32 products (one rounding);
+// the node COM is the quotient of two sums in FP32 with one correction
+// step, the mass the sum rounded to float once.  kMoments (the quadrupole
+// far field) forms its terms m, m x, m x_a x_b in FP64 and the central
+// second moments S = sum m x x^T - M c c^T in FP64 from the exact sums.
 constexpr int kRefitBlock = 256;
 constexpr int kMomW = 10;     // m, mx, my, mz, mxx, myy, mzz, mxy, mxz, myz
+
+__device__ __forceinline__ float pow2f(int e) {           // 2^e, e clamped to the normal range
+    return __int_as_float((max(-126, min(127, e)) + 127) << 23);
+}
+__device__ __forceinline__ double pow2d(int e) {          // 2^e for |e| < 1000
+    return __longlong_as_double(static_cast<long long>(e + 1023) << 52);
+}
+__device__ __forceinline__ int expAbove(float v) {        // least e with |v| < 2^e; -126 for 0 and subnormals
+    const int b = static_cast<int>((__float_as_uint(v) >> 23) & 0xffu);
+    return b == 0 ? -126 : b - 126;
+}
+
+// Units of one build's fixed-point sums; every thread derives the same
+// values from the bounds and largest-mass words.
+struct MomScale {
+    int em, ex, lg;           // |m| < 2^em, |x| < 2^ex, n <= 2^lg
+    float mIn, xIn, kIn;      // leaf term of m x: (m 2^-em) (x 2^-ex) 2^(61 - lg)
+};
+__device__ __forceinline__ MomScale momScale(const Work& w, uint32_t n) {
+    float X = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) X = fmaxf(X, fabsf(floatFromOrdered(__ldcg(&w.words[kWBounds + k]))));
+    MomScale s;
+    s.em = min(expAbove(__uint_as_float(__ldcg(&w.words[kWMassMax]))), 127);
+    s.ex = min(expAbove(X), 127);
+    s.lg = n > 1u ? 32 - __clz(static_cast<int>(n - 1u)) : 0;
+    s.mIn = pow2f(-s.em);
+    s.xIn = pow2f(-s.ex);
+    s.kIn = pow2f(61 - s.lg);
+    return s;
+}
+
+template <bool kMoments>
+__device__ __forceinline__ void leafTerms(const float4& pm, const MomScale& S, long long* v) {
+    if constexpr (kMoments) {
+        const double m = pm.w, x = pm.x, y = pm.y, z = pm.z;
+        const double u0 = pow2d(61 - S.lg - S.em), u1 = pow2d(61 - S.lg - S.em - S.ex),
+                     u2 = pow2d(61 - S.lg - S.em - 2 * S.ex);
+        v[0] = __double2ll_rn(m * u0);
+        v[1] = __double2ll_rn(m * x * u1);
+        v[2] = __double2ll_rn(m * y * u1);
+        v[3] = __double2ll_rn(m * z * u1);
+        v[4] = __double2ll_rn(m * x * x * u2);
+        v[5] = __double2ll_rn(m * y * y * u2);
+        v[6] = __double2ll_rn(m * z * z * u2);
+        v[7] = __double2ll_rn(m * x * y * u2);
+        v[8] = __double2ll_rn(m * x * z * u2);
+        v[9] = __double2ll_rn(m * y * z * u2);
+    } else {
+        const float ms = pm.w * S.mIn;                      // the scalings by 2^k are exact
+        v[0] = __float2ll_rn(ms * S.kIn);
+        v[1] = __float2ll_rn(ms * (pm.x * S.xIn) * S.kIn);
+        v[2] = __float2ll_rn(ms * (pm.y * S.xIn) * S.kIn);
+        v[3] = __float2ll_rn(ms * (pm.z * S.xIn) * S.kIn);
+    }
+}
+
+// a / b with b = bh + bl (bh = RN(b), r = RN(1 / bh)): the quotient ah r
+// and one correction step from the FMA residual (Markstein, IBM J. Res.
+// Dev. 34 (1990)), a split into two floats the same way.
+__device__ __forceinline__ float llQuot(long long a, float bh, float bl, float r) {
+    const float ah = __ll2float_rn(a);
+    const float al = __ll2float_rn(a - __float2ll_rz(ah));
+    const float q0 = ah * r;
+    float res = fmaf(-q0, bh, ah);
+    res = fmaf(-q0, bl, res + al);
+    return fmaf(res, r, q0);
+}
 
 struct Ext8 {                 // min x y z, max x y z, max 2h, max Hs
     float mnx, mny, mnz, mxx, mxy, mxz, h, hs;
@@ -219,31 +299,52 @@ __device__ __forceinline__ Ext8 extShfl(const Ext8& e, int delta, bool up) {
     return o;
 }
 
-// Node records from a node's box, h extremes and FP64 moments.
+// Node records from a node's box, h extremes and fixed-point moment sums.
 template <bool kMoments>
-__device__ void writeNode(const AstraeaRadixBvh& bvh, const Work& w, int node, const Ext8& e, const double* M) {
+__device__ void writeNode(const AstraeaRadixBvh& bvh, const Work& w, int node, const Ext8& e, const long long* Q,
+                          const MomScale& S) {
     const int lc = __ldg(&bvh.leftChild[node]), rc = __ldg(&bvh.rightChild[node]);
-    float cx, cy, cz;
-    if (M[0] > 0.0) {
-        const double im = 1.0 / M[0];
-        cx = static_cast<float>(M[1] * im);
-        cy = static_cast<float>(M[2] * im);
-        cz = static_cast<float>(M[3] * im);
+    float cx, cy, cz, mSum;
+    double M[kMomW];
+    if constexpr (kMoments) {
+        const double u1 = pow2d(S.em + S.ex + S.lg - 61), u2 = pow2d(S.em + 2 * S.ex + S.lg - 61);
+        M[0] = static_cast<double>(Q[0]) * pow2d(S.em + S.lg - 61);
+#pragma unroll
+        for (int k = 1; k < 4; ++k) M[k] = static_cast<double>(Q[k]) * u1;
+#pragma unroll
+        for (int k = 4; k < kMomW; ++k) M[k] = static_cast<double>(Q[k]) * u2;
+        mSum = static_cast<float>(M[0]);
+    } else {
+        mSum = (__ll2float_rn(Q[0]) * pow2f(S.lg - 61)) * pow2f(S.em);
+    }
+    if (Q[0] > 0) {
+        if constexpr (kMoments) {
+            const double im = 1.0 / M[0];
+            cx = static_cast<float>(M[1] * im);
+            cy = static_cast<float>(M[2] * im);
+            cz = static_cast<float>(M[3] * im);
+        } else {                                   // c = (Q_x / Q_m) 2^ex
+            const float bh = __ll2float_rn(Q[0]);
+            const float bl = __ll2float_rn(Q[0] - __float2ll_rz(bh));
+            const float r = __frcp_rn(bh), sc = pow2f(S.ex);
+            cx = llQuot(Q[1], bh, bl, r) * sc;
+            cy = llQuot(Q[2], bh, bl, r) * sc;
+            cz = llQuot(Q[3], bh, bl, r) * sc;
+        }
     } else {                                       // massless subtree: the box centre
         cx = 0.5f * (e.mnx + e.mxx);
         cy = 0.5f * (e.mny + e.mxy);
         cz = 0.5f * (e.mnz + e.mxz);
     }
-    const float mSum = static_cast<float>(M[0]);
     const float dNode = fmaxf(e.mxx - e.mnx, fmaxf(e.mxy - e.mny, e.mxz - e.mnz));
     float4* rec = w.node + 4 * static_cast<size_t>(node);
     __stcg(&rec[0], make_float4(cx, cy, cz, mSum));
     __stcg(&rec[1], make_float4(__fmul_rn(dNode, dNode), __int_as_float(lc), __int_as_float(rc), e.hs));
     __stcg(&rec[2], make_float4(e.mnx, e.mny, e.mnz, e.h));
     __stcg(&rec[3], make_float4(e.mxx, e.mxy, e.mxz, 0.0f));
-    if (kMoments) {
+    if constexpr (kMoments) {
         float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (M[0] > 0.0) {
+        if (Q[0] > 0) {
             const double c[3] = {M[1] / M[0], M[2] / M[0], M[3] / M[0]};
             s[0] = static_cast<float>(fmax(0.0, M[4] - M[0] * c[0] * c[0]));
             s[1] = static_cast<float>(fmax(0.0, M[5] - M[0] * c[1] * c[1]));
@@ -275,26 +376,22 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
     __shared__ Ext8 wPre[kRefitBlock], wSuf[kRefitBlock];   // warp-inclusive prefix / suffix extremes
     __shared__ Ext8 warpAgg[kWarps];
     __shared__ Ext8 sLeaf[kRefitBlock];                     // each leaf's own extremes
-    __shared__ double sP[kW][kRefitBlock];                  // inclusive block prefix of the moments
-    __shared__ double warpOff[kW][kWarps];
+    __shared__ long long sP[kW][kRefitBlock];               // inclusive block prefix of the moments
+    __shared__ long long warpOff[kW][kWarps];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t b0 = blockIdx.x * kRefitBlock;
     const uint32_t i = b0 + static_cast<uint32_t>(t);
     const bool valid = i < n;
+    const MomScale S = momScale(w, n);
     Ext8 e = extEmpty();
-    double v[kW];
+    long long v[kW];
 #pragma unroll
-    for (int k = 0; k < kW; ++k) v[k] = 0.0;
+    for (int k = 0; k < kW; ++k) v[k] = 0;
     if (valid) {
         const float4 pm = __ldg(&w.leaf[i].a);
         const float4 ax = __ldg(&w.leafAux[i]);
         e = Ext8{pm.x, pm.y, pm.z, pm.x, pm.y, pm.z, ax.z, ax.x};
-        const double m = pm.w, x = pm.x, y = pm.y, z = pm.z;
-        v[0] = m; v[1] = m * x; v[2] = m * y; v[3] = m * z;
-        if constexpr (kMoments) {
-            v[4] = m * x * x; v[5] = m * y * y; v[6] = m * z * z;
-            v[7] = m * x * y; v[8] = m * x * z; v[9] = m * y * z;
-        }
+        leafTerms<kMoments>(pm, S, v);
     }
     // warp-inclusive scans: prefix (up), suffix (down), moments (up)
     Ext8 pre = e, suf = e;
@@ -306,7 +403,7 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
         if (lane + d < 32) suf = extJoin(suf, q);
 #pragma unroll
         for (int k = 0; k < kW; ++k) {
-            const double o = __shfl_up_sync(0xffffffffu, v[k], d);
+            const long long o = __shfl_up_sync(0xffffffffu, v[k], d);
             if (lane >= d) v[k] += o;
         }
     }
@@ -322,9 +419,9 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
     if (t == 0) {                                   // exclusive offsets of the warps' moment sums
 #pragma unroll
         for (int k = 0; k < kW; ++k) {
-            double run = 0.0;
+            long long run = 0;
             for (int q = 0; q < kWarps; ++q) {
-                const double x = warpOff[k][q];
+                const long long x = warpOff[k][q];
                 warpOff[k][q] = run;
                 run += x;
             }
@@ -342,7 +439,7 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
         float4* ls = w.leafScan + 4 * static_cast<size_t>(i);
         extStore(ls, pre);
         extStore(ls + 2, suf);
-        double* ms = w.momScan + static_cast<size_t>(kMomW) * i;
+        long long* ms = w.momScan + static_cast<size_t>(kMomW) * i;
 #pragma unroll
         for (int k = 0; k < kW; ++k) ms[k] = v[k];
     }
@@ -370,39 +467,37 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
                 a = extEmpty();
                 for (int k = f; k <= l; ++k) a = extJoin(a, sLeaf[k]);
             }
-            double M[kMomW];
+            long long Q[kW];
 #pragma unroll
-            for (int k = 0; k < kW; ++k) M[k] = sP[k][l] - (f > 0 ? sP[k][f - 1] : 0.0);
-#pragma unroll
-            for (int k = kW; k < kMomW; ++k) M[k] = 0.0;
-            writeNode<kMoments>(bvh, w, static_cast<int>(i), a, M);
+            for (int k = 0; k < kW; ++k) Q[k] = sP[k][l] - (f > 0 ? sP[k][f - 1] : 0);
+            writeNode<kMoments>(bvh, w, static_cast<int>(i), a, Q, S);
         }
     }
 }
 
-// Block offsets: exclusive FP64 scan of the block totals, in place; one
-// block of 1024 threads.
+// Block offsets: exclusive scan of the block totals, in place; one block of
+// 1024 threads.
 template <bool kMoments>
 __global__ void __launch_bounds__(1024) refitScanKernel(Work w, uint32_t nb) {
     constexpr int kW = kMoments ? kMomW : 4;
-    __shared__ double warpSum[kW][32];
+    __shared__ long long warpSum[kW][32];
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint32_t per = (nb + 1023u) / 1024u;
     const uint32_t lo = min(nb, t * per), hi = min(nb, lo + per);
-    double acc[kW];
+    long long acc[kW];
 #pragma unroll
-    for (int k = 0; k < kW; ++k) acc[k] = 0.0;
+    for (int k = 0; k < kW; ++k) acc[k] = 0;
     for (uint32_t b = lo; b < hi; ++b)
 #pragma unroll
         for (int k = 0; k < kW; ++k) acc[k] += w.blockMom[static_cast<size_t>(kMomW) * b + k];
-    double inc[kW];
+    long long inc[kW];
 #pragma unroll
     for (int k = 0; k < kW; ++k) inc[k] = acc[k];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1)
 #pragma unroll
         for (int k = 0; k < kW; ++k) {
-            const double o = __shfl_up_sync(0xffffffffu, inc[k], d);
+            const long long o = __shfl_up_sync(0xffffffffu, inc[k], d);
             if (lane >= static_cast<uint32_t>(d)) inc[k] += o;
         }
     if (lane == 31u)
@@ -412,24 +507,24 @@ __global__ void __launch_bounds__(1024) refitScanKernel(Work w, uint32_t nb) {
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < kW; ++k) {
-            double x = warpSum[k][lane];
+            long long x = warpSum[k][lane];
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                const double o = __shfl_up_sync(0xffffffffu, x, d);
+                const long long o = __shfl_up_sync(0xffffffffu, x, d);
                 if (lane >= static_cast<uint32_t>(d)) x += o;
             }
             warpSum[k][lane] = x;                  // inclusive over warps
         }
     }
     __syncthreads();
-    double run[kW];
+    long long run[kW];
 #pragma unroll
-    for (int k = 0; k < kW; ++k) run[k] = inc[k] - acc[k] + (warp > 0 ? warpSum[k][warp - 1] : 0.0);
+    for (int k = 0; k < kW; ++k) run[k] = inc[k] - acc[k] + (warp > 0 ? warpSum[k][warp - 1] : 0);
     for (uint32_t b = lo; b < hi; ++b)
 #pragma unroll
         for (int k = 0; k < kW; ++k) {
-            double* slot = &w.blockMom[static_cast<size_t>(kMomW) * b + k];
-            const double x = *slot;
+            long long* slot = &w.blockMom[static_cast<size_t>(kMomW) * b + k];
+            const long long x = *slot;
             *slot = run[k];
             run[k] += x;
         }
@@ -463,21 +558,19 @@ __global__ void __launch_bounds__(256) refitCrossKernel(AstraeaRadixBvh bvh, Wor
         const float4* tab = w.blockTable + 2 * static_cast<size_t>(lev) * nb;
         e = extJoin(e, extJoin(extLoad(tab + 2 * lo), extLoad(tab + 2 * (hi + 1u - (1u << lev)))));
     }
-    double M[kMomW];
-    const double* ml = w.momScan + static_cast<size_t>(kMomW) * r.y;
-    const double* ol = w.blockMom + static_cast<size_t>(kMomW) * bl;
+    long long Q[kW];
+    const long long* ml = w.momScan + static_cast<size_t>(kMomW) * r.y;
+    const long long* ol = w.blockMom + static_cast<size_t>(kMomW) * bl;
 #pragma unroll
-    for (int k = 0; k < kW; ++k) M[k] = __ldcg(&ol[k]) + __ldcg(&ml[k]);
+    for (int k = 0; k < kW; ++k) Q[k] = __ldcg(&ol[k]) + __ldcg(&ml[k]);
     if (r.x > 0u) {
         const uint32_t f1 = r.x - 1u;
-        const double* mf = w.momScan + static_cast<size_t>(kMomW) * f1;
-        const double* of = w.blockMom + static_cast<size_t>(kMomW) * (f1 / kRefitBlock);
+        const long long* mf = w.momScan + static_cast<size_t>(kMomW) * f1;
+        const long long* of = w.blockMom + static_cast<size_t>(kMomW) * (f1 / kRefitBlock);
 #pragma unroll
-        for (int k = 0; k < kW; ++k) M[k] -= __ldcg(&of[k]) + __ldcg(&mf[k]);
+        for (int k = 0; k < kW; ++k) Q[k] -= __ldcg(&of[k]) + __ldcg(&mf[k]);
     }
-#pragma unroll
-    for (int k = kW; k < kMomW; ++k) M[k] = 0.0;
-    writeNode<kMoments>(bvh, w, static_cast<int>(i), e, M);
+    writeNode<kMoments>(bvh, w, static_cast<int>(i), e, Q, momScale(w, n));
 }
 
 inline unsigned gridFor(uint32_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }

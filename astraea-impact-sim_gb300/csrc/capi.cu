@@ -157,9 +157,9 @@ AstraeaStatus allocWorkspace(Workspace* ws, uint32_t capacity) {
     w.node = reinterpret_cast<float4*>(b + oNode);
     w.nodeRange = reinterpret_cast<uint2*>(b + oRange);
     w.leafScan = reinterpret_cast<float4*>(b + oLScan);
-    w.momScan = reinterpret_cast<double*>(b + oMScan);
+    w.momScan = reinterpret_cast<long long*>(b + oMScan);
     w.blockTable = reinterpret_cast<float4*>(b + oTable);
-    w.blockMom = reinterpret_cast<double*>(b + oBMom);
+    w.blockMom = reinterpret_cast<long long*>(b + oBMom);
     w.nodeQuad = reinterpret_cast<float4*>(b + oQuad);
     w.driftPos = reinterpret_cast<float4*>(b + oDrift);
     w.drift = reinterpret_cast<Rec32*>(b + oDRec);

@@ -425,9 +425,9 @@ struct Work {
     float4* node;          // 4 x float4 per internal node
     uint2* nodeRange;      // [N-1] {first, last}: the sorted leaf range of each internal node
     float4* leafScan;      // [4N] per leaf: block prefix and block suffix {min xyz, max 2h}, {max xyz, max Hs}
-    double* momScan;       // [10N] per leaf: inclusive block prefix of m, m x (3), m x x^T (6)
+    long long* momScan;    // [10N] per leaf: inclusive block prefix of m, m x (3), m x x^T (6), fixed point
     float4* blockTable;    // [2 levels nb] sparse table of block extremes (level 0: the blocks)
-    double* blockMom;      // [10 nb] block totals, then exclusive block offsets
+    long long* blockMom;   // [10 nb] block totals, then exclusive block offsets
     float4* nodeQuad;      // 2 x float4 per internal node: central second moments
                            // {Sxx, Syy, Szz, Sxy}, {Sxz, Syz, 0, 0} (far-field mode 1)
     float4* driftPos;      // {x, y, z, 0} after the drift
@@ -451,6 +451,7 @@ enum WordIndex : int {
     kWDtState = 10,      // 2 float dt slots (step parity)
     kWGroupCounter = 12, // persistent-grid work counter (gravity)
     kWNbrCounter = 13,   // persistent-grid work counter (neighbour build)
+    kWMassMax = 14,      // bits of the largest |mass| (set by the permutation, read by the refit)
     kWBoundsF = 16,      // 6 floats: decoded bounds
     kWCount = 32
 };

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) kickKernel(AstraeaParticles p, uint32_t n
             uint32_t* wds = a.boundsWordsInit;
             wds[kWBounds + 0] = hi; wds[kWBounds + 1] = hi; wds[kWBounds + 2] = hi;
             wds[kWBounds + 3] = lo; wds[kWBounds + 4] = lo; wds[kWBounds + 5] = lo;
-            wds[kWLiving + 0] = 0u; wds[kWLiving + 1] = 0u;
+            wds[kWLiving + 0] = 0u; wds[kWLiving + 1] = 0u; wds[kWMassMax] = 0u;
         }
     }
     float dtCand = 1.0e30f;
