@@ -195,9 +195,11 @@ __global__ void __launch_bounds__(256) refreshLeavesKernel(AstraeaParticles p, W
 // node's sum is the exact difference of two prefix sums (FP64 prefix sums
 // lose a small node's digits to the cancellation), and they take the
 // integer pipes instead of the FP64 pipe, which runs at 1/64 of the FP32
-// rate on this GPU.  The leaf terms m x are FP32 products (one rounding);
-// the node COM is the quotient of two sums in FP32 with one correction
-// step, the mass the sum rounded to float once.  kMoments (the quadrupole
+// rate on this GPU.  A leaf term m x is the exact product (24 x 24-bit
+// integer mantissa product) rounded once to the unit, so each sum is at
+// least as precise as an FP64 accumulation; the node COM is the quotient of
+// two sums in FP32 with one correction step, the mass the sum rounded to
+// float once.  kMoments (the quadrupole
 // far field) forms its terms m, m x, m x_a x_b in FP64 and the central
 // second moments S = sum m x x^T - M c c^T in FP64 from the exact sums.
 constexpr int kRefitBlock = 256;
@@ -218,7 +220,7 @@ __device__ __forceinline__ int expAbove(float v) {        // least e with |v| < 
 // values from the bounds and largest-mass words.
 struct MomScale {
     int em, ex, lg;           // |m| < 2^em, |x| < 2^ex, n <= 2^lg
-    float mIn, xIn, kIn;      // leaf term of m x: (m 2^-em) (x 2^-ex) 2^(61 - lg)
+    float mIn, xIn;           // leaf term of m x: (m 2^(61 - lg - em)) (x 2^-ex)
 };
 __device__ __forceinline__ MomScale momScale(const Work& w, uint32_t n) {
     float X = 0.0f;
@@ -228,10 +230,26 @@ __device__ __forceinline__ MomScale momScale(const Work& w, uint32_t n) {
     s.em = min(expAbove(__uint_as_float(__ldcg(&w.words[kWMassMax]))), 127);
     s.ex = min(expAbove(X), 127);
     s.lg = n > 1u ? 32 - __clz(static_cast<int>(n - 1u)) : 0;
-    s.mIn = pow2f(-s.em);
+    s.mIn = pow2f(61 - s.lg - s.em);
     s.xIn = pow2f(-s.ex);
-    s.kIn = pow2f(61 - s.lg);
     return s;
+}
+
+// a b rounded to the nearest integer (ties away from zero), exact before
+// that rounding: the product of the two 24-bit significands is formed in a
+// 64-bit integer.  |a b| < 2^62 by the choice of units.
+__device__ __forceinline__ long long fixProd(float a, float b) {
+    const uint32_t ua = __float_as_uint(a), ub = __float_as_uint(b);
+    const int ea = static_cast<int>((ua >> 23) & 0xffu), eb = static_cast<int>((ub >> 23) & 0xffu);
+    const uint64_t ma = (ua & 0x7fffffu) | (ea != 0 ? 0x800000u : 0u);
+    const uint64_t mb = (ub & 0x7fffffu) | (eb != 0 ? 0x800000u : 0u);
+    const uint64_t P = ma * mb;                                    // < 2^48
+    const int sh = max(ea, 1) + max(eb, 1) - 300;                  // a b = P 2^sh
+    uint64_t q;
+    if (sh >= 0) q = P << min(sh, 15);
+    else if (sh > -60) q = (P + (1ull << (-sh - 1))) >> (-sh);
+    else q = 0u;
+    return ((ua ^ ub) >> 31) != 0u ? -static_cast<long long>(q) : static_cast<long long>(q);
 }
 
 template <bool kMoments>
@@ -252,10 +270,10 @@ __device__ __forceinline__ void leafTerms(const float4& pm, const MomScale& S, l
         v[9] = __double2ll_rn(m * y * z * u2);
     } else {
         const float ms = pm.w * S.mIn;                      // the scalings by 2^k are exact
-        v[0] = __float2ll_rn(ms * S.kIn);
-        v[1] = __float2ll_rn(ms * (pm.x * S.xIn) * S.kIn);
-        v[2] = __float2ll_rn(ms * (pm.y * S.xIn) * S.kIn);
-        v[3] = __float2ll_rn(ms * (pm.z * S.xIn) * S.kIn);
+        v[0] = __float2ll_rn(ms);
+        v[1] = fixProd(ms, pm.x * S.xIn);
+        v[2] = fixProd(ms, pm.y * S.xIn);
+        v[3] = fixProd(ms, pm.z * S.xIn);
     }
 }
 

@@ -73,6 +73,54 @@ def test_sort_and_build_bit_exact(packed):
         assert rel_rms(ncm[:, 3], b["nodeMass"]) < 1e-6
 
 
+def test_refit_moments_against_exact_sums():
+    """Node mass and COM against exact rational sums over each node's leaves.
+
+    The refit sums m and m x as 64-bit fixed-point integers (exact products,
+    one rounding to the unit each) and divides once: every node mass is
+    within one float ulp of the exact sum, every COM within one ulp plus the
+    fixed-point floor (2^-40 of the scene's largest coordinate).
+    """
+    from fractions import Fraction
+    st = c1_state()
+    n = len(st["posX"])
+    p, alt, bvh = gpu_setup(st, True)
+    engine.sort_and_build_bvh(p, alt, bvh)
+    torch.cuda.synchronize()
+    g = p.download()
+    lc, rc = tnp(bvh.t["leftChild"], n - 1), tnp(bvh.t["rightChild"], n - 1)
+    first, last = np.zeros(n - 1, np.int64), np.zeros(n - 1, np.int64)
+    order, stack = [], [0]
+    while stack:
+        v = stack.pop()
+        order.append(v)
+        stack += [int(c) for c in (lc[v], rc[v]) if c >= 0]
+    for v in reversed(order):
+        first[v] = ~lc[v] if lc[v] < 0 else first[lc[v]]
+        last[v] = ~rc[v] if rc[v] < 0 else last[rc[v]]
+    m = [Fraction(float(v)) for v in g["mass"]]
+    pm, acc = [Fraction(0)], Fraction(0)
+    for v in m:
+        acc += v
+        pm.append(acc)
+    gm = tnp(bvh.t["nodeMass"], n - 1)
+    X = max(float(np.abs(g[k]).max()) for k in ("posX", "posY", "posZ"))
+    for f in ("nodeMass", "comX", "comY", "comZ"):
+        assert np.all(np.isfinite(tnp(bvh.t[f], n - 1))), f
+    for v in range(n - 1):
+        s = pm[last[v] + 1] - pm[first[v]]
+        assert abs(float(gm[v]) - float(s)) <= np.spacing(np.float32(float(s))), v
+    for k, f in (("posX", "comX"), ("posY", "comY"), ("posZ", "comZ")):
+        px, acc = [Fraction(0)], Fraction(0)
+        for mi, xi in zip(m, g[k]):
+            acc += mi * Fraction(float(xi))
+            px.append(acc)
+        gc = tnp(bvh.t[f], n - 1)
+        for v in range(n - 1):
+            c = float((px[last[v] + 1] - px[first[v]]) / (pm[last[v] + 1] - pm[first[v]]))
+            assert abs(float(gc[v]) - c) <= np.spacing(np.float32(abs(c))) + 2.0 ** -40 * X, (f, v)
+
+
 @pytest.mark.parametrize("n,end_bit", [(1, 64), (5, 64), (4096, 63), (4097, 64), (300001, 64), (1 << 20, 63)])
 def test_radix_sort_pairs_stable(n, end_bit):
     rng = np.random.Generator(np.random.PCG64(n))
