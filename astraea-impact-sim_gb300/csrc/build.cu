@@ -9,8 +9,9 @@
 //   * the tree walks read 64-byte AoS node records (common.cuh) instead of
 //     eleven SoA arrays; the engine's SoA / packed node arrays are still
 //     written when the caller's descriptor has them;
-//   * node mass and centre of mass are accumulated as FP64 moments
-//     (sum m, sum m x) and rounded to FP32 once per node.
+//   * node mass and centre of mass come from exact 64-bit fixed-point sums
+//     (sum m, sum m x) over the node's leaf range, rounded to FP32 once
+//     per node.
 #include "kernels.h"
 
 namespace astraea_gb300 {

@@ -409,11 +409,6 @@ struct __align__(32) Rec32 {
     float4 a, b;
 };
 
-// FP64 mass moments of one internal node (32 bytes, 16-byte aligned).
-struct __align__(16) NodeMom {
-    double sx, sy, sz, m;
-};
-
 // ----------------------------------------------------------- workspace ---
 // Device pointers of the library-owned scratch of one BVH (see capi.cu).
 struct Work {

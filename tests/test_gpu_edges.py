@@ -98,7 +98,7 @@ def test_fully_coincident_cloud():
     g, c = run_pipeline(small)
     assert np.array_equal(g["originalId"], c["originalId"])
     # Every separation is zero, so the true gravity and SPH accelerations are
-    # zero.  The library's node COM comes from FP64 moments and equals the
+    # zero.  The library's node COM comes from exact moment sums and equals the
     # common position: it opens every node and adds exact zeros.  The
     # engine's FP32 COM lands an ulp away, so its tiny nodes pass the opening
     # test and give a spurious monopole force (the oracle shows ~1.7e-6).

@@ -65,7 +65,7 @@ def test_sort_and_build_bit_exact(packed):
         assert np.array_equal(g[f], c[f]), f
     for f in ("aabbMinX", "aabbMinY", "aabbMinZ", "aabbMaxX", "aabbMaxY", "aabbMaxZ", "nodeMaxH"):
         assert np.array_equal(tnp(bvh.t[f], 2 * n - 1), b[f]), f
-    for f in ("nodeMass", "comX", "comY", "comZ"):  # FP64 moments vs FP32 refit
+    for f in ("nodeMass", "comX", "comY", "comZ"):  # exact moment sums vs FP32 refit
         assert rel_rms(tnp(bvh.t[f], 2 * n - 1), b[f]) < 1e-6, f
     if packed:
         assert np.array_equal(tnp(bvh.t["sceneBoundsFloat"], 6), o.bounds)
