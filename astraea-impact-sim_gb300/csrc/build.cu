@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(256) permuteLeavesKarrasKernel(AstraeaParticle
     if ((threadIdx.x & 31) == 0) {
         if (anyTracer) atomicOr(&livingFlags[0], 1u);
         if (anyIntact) atomicOr(&livingFlags[1], 1u);
-        if (warpMassBits != 0u) atomicMax(&w.words[kWMassMax], warpMassBits);   // scale of the refit's sums
+        // scale of the refit's sums; the word only grows, so a stale read costs one extra atomic at most
+        if (warpMassBits > __ldcg(&w.words[kWMassMax])) atomicMax(&w.words[kWMassMax], warpMassBits);
     }
     if (i + 1u < n) {                               // internal node i (Karras 2012)
         const int ii = static_cast<int>(i);
@@ -549,15 +550,27 @@ __global__ void __launch_bounds__(1024) refitScanKernel(Work w, uint32_t nb) {
         }
 }
 
-// One level of the sparse table of block extremes: T[lev][b] = T[lev-1][b]
-// joined with T[lev-1][b + 2^(lev-1)].
-__global__ void __launch_bounds__(256) refitLevelKernel(Work w, uint32_t nb, uint32_t lev) {
+// Up to three levels of the sparse table of block extremes per launch
+// (the levels are latency-bound, so the extra loads are cheap): with
+// s = 2^(lev-1) and A_k = T[lev-1][b + k s], T[lev-1+j][b] joins
+// A_0 .. A_(2^j - 1) (it covers blocks b .. b + 2^j s - 1), j = 1 .. count.
+__global__ void __launch_bounds__(256) refitLevelKernel(Work w, uint32_t nb, uint32_t lev, uint32_t count) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t span = 1u << (lev - 1);
-    if (b + 2u * span > nb) return;
+    const uint32_t s = 1u << (lev - 1);
+    if (b + 2u * s > nb) return;
     const float4* src = w.blockTable + 2 * static_cast<size_t>(lev - 1) * nb;
-    extStore(w.blockTable + 2 * (static_cast<size_t>(lev) * nb + b),
-             extJoin(extLoad(src + 2 * b), extLoad(src + 2 * (b + span))));
+    Ext8 a[8];
+#pragma unroll
+    for (uint32_t k = 0; k < 8u; ++k)
+        a[k] = (k < (2u << (count - 1)) && b + (k + 1u) * s <= nb) ? extLoad(src + 2 * (b + k * s)) : extEmpty();
+    Ext8 acc = a[0];
+#pragma unroll
+    for (uint32_t j = 1; j <= 3u; ++j) {
+        const uint32_t width = 1u << j;
+        if (j > count || b + width * s > nb) break;
+        for (uint32_t k = width >> 1; k < width; ++k) acc = extJoin(acc, a[k]);
+        extStore(w.blockTable + 2 * (static_cast<size_t>(lev - 1 + j) * nb + b), acc);
+    }
 }
 
 // Nodes whose range spans blocks.
@@ -641,8 +654,8 @@ cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, b
         refitBlockKernel<false><<<nb, kRefitBlock, 0, st>>>(bvh, w, n);
         refitScanKernel<false><<<1, 1024, 0, st>>>(w, nb);
     }
-    for (uint32_t lev = 1; lev < levels; ++lev)
-        refitLevelKernel<<<gridFor(nb, 256), 256, 0, st>>>(w, nb, lev);
+    for (uint32_t lev = 1; lev < levels; lev += 3)
+        refitLevelKernel<<<gridFor(nb, 256), 256, 0, st>>>(w, nb, lev, std::min(3u, levels - lev));
     if (moments)
         refitCrossKernel<true><<<gridFor(n, 256), 256, 0, st>>>(bvh, w, n, nb);
     else
