@@ -44,12 +44,12 @@ UNIT = "particle-steps/s"
 FLOP_PER_INTERACTION = 23        # 20 force + 3 potential (rsqrt counted once)
 def kernels_per_step(n):
     """Launches of one fused step: kick, drift, histogram, 8 onesweep,
-    permute + Karras, the refit (block, scan, one per sparse-table level
-    above the first, cross), neighbour lists, pass 1, EOS, gravity, pass 2,
-    kick."""
+    permute + Karras, the refit (block, scan, one launch per three
+    sparse-table levels above the first, cross), neighbour lists, pass 1,
+    EOS, gravity, pass 2, kick."""
     nb = max(1, (n + 255) // 256)
     levels = nb.bit_length()                   # levels 0 .. floor(log2 nb)
-    return 18 + 3 + (levels - 1)
+    return 18 + 3 + (levels - 1 + 2) // 3
 # Fields a fused step reads (uploaded every e2e step) and the fields the
 # engine's per-step telemetry reads back (engine/simulation.cpp:948-1000).
 E2E_IN = ["posX", "posY", "posZ", "velX", "velY", "velZ", "accX", "accY", "accZ", "mass", "h", "h0", "rho",
