@@ -496,58 +496,62 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
 }
 
 // Block offsets: exclusive scan of the block totals, in place; one block of
-// 1024 threads.
+// 1024 threads over chunks of 1024 blocks (coalesced), the next chunk's
+// loads in flight while the current one is scanned.
 template <bool kMoments>
 __global__ void __launch_bounds__(1024) refitScanKernel(Work w, uint32_t nb) {
     constexpr int kW = kMoments ? kMomW : 4;
     __shared__ long long warpSum[kW][32];
+    __shared__ long long carry[kW];
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
-    const uint32_t per = (nb + 1023u) / 1024u;
-    const uint32_t lo = min(nb, t * per), hi = min(nb, lo + per);
-    long long acc[kW];
+    if (t < static_cast<uint32_t>(kW)) carry[t] = 0;
+    long long cur[kW], nxt[kW];
 #pragma unroll
-    for (int k = 0; k < kW; ++k) acc[k] = 0;
-    for (uint32_t b = lo; b < hi; ++b)
-#pragma unroll
-        for (int k = 0; k < kW; ++k) acc[k] += w.blockMom[static_cast<size_t>(kMomW) * b + k];
-    long long inc[kW];
-#pragma unroll
-    for (int k = 0; k < kW; ++k) inc[k] = acc[k];
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1)
-#pragma unroll
-        for (int k = 0; k < kW; ++k) {
-            const long long o = __shfl_up_sync(0xffffffffu, inc[k], d);
-            if (lane >= static_cast<uint32_t>(d)) inc[k] += o;
-        }
-    if (lane == 31u)
-#pragma unroll
-        for (int k = 0; k < kW; ++k) warpSum[k][warp] = inc[k];
+    for (int k = 0; k < kW; ++k) cur[k] = t < nb ? __ldcg(&w.blockMom[static_cast<size_t>(kMomW) * t + k]) : 0;
     __syncthreads();
-    if (warp == 0) {
+    for (uint32_t base = 0; base < nb; base += 1024u) {
+        const uint32_t bn = base + 1024u + t;
 #pragma unroll
-        for (int k = 0; k < kW; ++k) {
-            long long x = warpSum[k][lane];
+        for (int k = 0; k < kW; ++k) nxt[k] = bn < nb ? __ldcg(&w.blockMom[static_cast<size_t>(kMomW) * bn + k]) : 0;
+        long long inc[kW];
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const long long o = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane >= static_cast<uint32_t>(d)) x += o;
+        for (int k = 0; k < kW; ++k) inc[k] = cur[k];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1)
+#pragma unroll
+            for (int k = 0; k < kW; ++k) {
+                const long long o = __shfl_up_sync(0xffffffffu, inc[k], d);
+                if (lane >= static_cast<uint32_t>(d)) inc[k] += o;
             }
-            warpSum[k][lane] = x;                  // inclusive over warps
+        if (lane == 31u)
+#pragma unroll
+            for (int k = 0; k < kW; ++k) warpSum[k][warp] = inc[k];
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int k = 0; k < kW; ++k) {
+                long long x = warpSum[k][lane];
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const long long o = __shfl_up_sync(0xffffffffu, x, d);
+                    if (lane >= static_cast<uint32_t>(d)) x += o;
+                }
+                warpSum[k][lane] = x;              // inclusive over warps
+            }
         }
+        __syncthreads();
+        const uint32_t b = base + t;
+        if (b < nb)
+#pragma unroll
+            for (int k = 0; k < kW; ++k)
+                w.blockMom[static_cast<size_t>(kMomW) * b + k] =
+                    carry[k] + (warp > 0 ? warpSum[k][warp - 1] : 0) + inc[k] - cur[k];
+        __syncthreads();                           // carry and warpSum read by all
+        if (t < static_cast<uint32_t>(kW)) carry[t] += warpSum[t][31];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kW; ++k) cur[k] = nxt[k];
     }
-    __syncthreads();
-    long long run[kW];
-#pragma unroll
-    for (int k = 0; k < kW; ++k) run[k] = inc[k] - acc[k] + (warp > 0 ? warpSum[k][warp - 1] : 0);
-    for (uint32_t b = lo; b < hi; ++b)
-#pragma unroll
-        for (int k = 0; k < kW; ++k) {
-            long long* slot = &w.blockMom[static_cast<size_t>(kMomW) * b + k];
-            const long long x = *slot;
-            *slot = run[k];
-            run[k] += x;
-        }
 }
 
 // Up to three levels of the sparse table of block extremes per launch
