@@ -208,6 +208,7 @@ SIGNATURES = [
     ("astraea_gb300_ff_get_params", [_VP, _U32, _VP], ctypes.c_int),
     ("astraea_gb300_ff_set_params", [_VP, _U32, _VP], ctypes.c_int),
     ("astraea_gb300_ff_stats", [ctypes.POINTER(FarFieldStats)], ctypes.c_int),
+    ("astraea_gb300_ff_profile", [_P, _B, _F, ctypes.POINTER(_F)], ctypes.c_int),
     ("astraea_gb300_autotune", [_P, _B, _F, ctypes.POINTER(Tuning)], ctypes.c_int),
     ("astraea_gb300_get_tuning", [_U32, ctypes.POINTER(Tuning)], ctypes.c_int),
     ("astraea_gb300_set_tuning", [_U32, ctypes.POINTER(Tuning)], ctypes.c_int),
@@ -224,6 +225,9 @@ SIGNATURES = [
     ("astraea_gb300_reset_device_status", [], ctypes.c_int),
     ("astraea_gb300_direct_gravity_f64", [_P, _VP, _U32, _VP, _VP], ctypes.c_int),
     ("astraea_gb300_measure_fp32_tflops", [ctypes.POINTER(_F)], ctypes.c_int),
+    ("astraea_gb300_measure_fp32_peaks", [ctypes.POINTER(_F), ctypes.POINTER(_F)], ctypes.c_int),
+    ("astraea_gb300_debug_gravity_group_counts", [_P, _B, _F, _VP], ctypes.c_int),
+    ("astraea_gb300_debug_gravity_group_trace", [_P, _B, _F, _U32, _VP, _U32], ctypes.c_int),
     ("astraea_gb300_set_lookback_spin_limit", [_U32], ctypes.c_int),
     ("astraea_gb300_set_far_field", [ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_debug_lookback_probe", [_U32, ctypes.POINTER(_U32)], ctypes.c_int),

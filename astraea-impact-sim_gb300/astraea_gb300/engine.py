@@ -182,6 +182,28 @@ def gravity_barnes_hut(p, bvh, theta=0.5):
     abi.check(lib().astraea_gb300_gravity_barnes_hut(ctypes.byref(s), ctypes.byref(bvh.s), float(theta)))
 
 
+def gravity_group_counts(p, bvh, theta=0.5):
+    """The gravity stage with each group's interaction count (int64 numpy
+    array, one entry per group of 32 sorted particles)."""
+    groups = (p.count + 31) // 32
+    out = torch.zeros(max(groups, 1), dtype=torch.int32, device=p.device)
+    sp = p.struct()
+    abi.check(lib().astraea_gb300_debug_gravity_group_counts(ctypes.byref(sp), ctypes.byref(bvh.s), float(theta),
+                                                            out.data_ptr()))
+    return out[:groups].cpu().numpy().view(np.uint32).astype(np.int64)
+
+
+def gravity_group_trace(p, bvh, group, theta=0.5, capacity=1 << 16):
+    """The gravity stage recording what one group takes: the nodes it accepts
+    as monopoles (>= 0) and the leaves it reaches (~particle), in walk order."""
+    out = torch.zeros(capacity + 1, dtype=torch.int32, device=p.device)
+    sp = p.struct()
+    abi.check(lib().astraea_gb300_debug_gravity_group_trace(ctypes.byref(sp), ctypes.byref(bvh.s), float(theta),
+                                                           int(group), out.data_ptr(), int(capacity)))
+    a = out.cpu().numpy()
+    return a[1:1 + min(int(a[0]), capacity)].astype(np.int64)
+
+
 def sph_pass2_forces(p, bvh):
     s = p.struct()
     abi.check(lib().astraea_gb300_sph_pass2_forces(ctypes.byref(s), ctypes.byref(bvh.s)))
@@ -404,6 +426,15 @@ def ff_set_params(params, scale=None):
     abi.check(lib().astraea_gb300_ff_set_params(p.ctypes.data, p.size, None if sc is None else sc.ctypes.data))
 
 
+def ff_profile(p, bvh, theta=0.5):
+    """Times (ms) of the parts of one mode-2 gravity call: walk, network,
+    correction, gate spot check, fallback walk."""
+    out = (ctypes.c_float * 5)()
+    sp = p.struct()
+    abi.check(lib().astraea_gb300_ff_profile(ctypes.byref(sp), ctypes.byref(bvh.s), float(theta), out))
+    return dict(zip(("walk", "network", "correct", "gate", "fallback"), list(out)))
+
+
 def ff_stats():
     st = abi.FarFieldStats()
     abi.check(lib().astraea_gb300_ff_stats(ctypes.byref(st)))
@@ -523,6 +554,13 @@ def measure_fp32_tflops():
     out = ctypes.c_float(0.0)
     abi.check(lib().astraea_gb300_measure_fp32_tflops(ctypes.byref(out)))
     return out.value
+
+
+def measure_fp32_peaks():
+    """(scalar fmaf, packed fma.rn.f32x2) FP32 throughput in TFLOP/s."""
+    a, b = ctypes.c_float(0.0), ctypes.c_float(0.0)
+    abi.check(lib().astraea_gb300_measure_fp32_peaks(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def reset_device_status():

@@ -281,7 +281,8 @@ struct FfState {
     float* groupCorr = nullptr;
     uint32_t groupCap = 0;
     uint32_t* word = nullptr;      // [0]: pair count
-    float* gateSum = nullptr;
+    ff::GateDev* gate = nullptr;   // the gate's device state (spot-check sum, decision, statistics)
+    bool lastCallGated = false;
     float* pinned = nullptr;       // 4 floats / words for read-backs
     AstraeaFarFieldStats stats{0ull, 0ull, 0u, 0u, -1.0f, 0.0f};
 };
@@ -297,7 +298,8 @@ AstraeaStatus ffState(FfState** out) {
         AG_CUDA(cudaMalloc(&f.net.outScale, ff::kOut * sizeof(float)));
         AG_CUDA(cudaMalloc(&f.net.loss, sizeof(float)));
         AG_CUDA(cudaMalloc(&f.word, 4 * sizeof(uint32_t)));
-        AG_CUDA(cudaMalloc(&f.gateSum, sizeof(float)));
+        AG_CUDA(cudaMalloc(&f.gate, sizeof(ff::GateDev)));
+        AG_CUDA(cudaMemset(f.gate, 0, sizeof(ff::GateDev)));
         AG_CUDA(cudaMallocHost(&f.pinned, 4 * sizeof(float)));
         AG_CUDA(cudaMemset(f.net.params, 0, ff::kParams * sizeof(float)));
         AG_CUDA(cudaMemset(f.net.grads, 0, ff::kParams * sizeof(float)));
@@ -348,40 +350,45 @@ AstraeaStatus ffWalk(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta
 }
 
 // Gravity of far-field mode 2: walk, network on the recorded pairs,
-// per-member correction, and (gateTolerance > 0) the direct-sum gate with
-// fallback to the plain walk at theta.  Blocks when the gate runs.
-AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta, bool gate) {
+// per-member correction, and (gateTolerance > 0) the gate: an FP64 direct-sum
+// spot check of gateTargets particles decides on the device whether the plain
+// walk at theta that follows runs or returns at once.  No host round trip, so
+// a gated step can be captured in a CUDA graph.
+// ev (optional, 6 events): recorded before the walk, the network, the
+// correction, the spot check, the fallback walk and at the end.
+AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta, bool gate,
+                             cudaEvent_t* ev = nullptr) {
     FfState* f = nullptr;
     AstraeaStatus s = ffState(&f);
     if (s != ASTRAEA_OK) return s;
     if (!f->ready) return fail(ASTRAEA_ERR_INVALID, "far-field mode 2 needs network parameters (ff_init / ff_set_params)");
+    cudaStream_t st = stream();
+    auto mark = [&](int k) { if (ev != nullptr) cudaEventRecord(ev[k], st); };
+    mark(0);
     s = ffWalk(p, ws, n, theta, f, 1u);
     if (s != ASTRAEA_OK) return s;
-    cudaStream_t st = stream();
     const uint32_t groups = (n + 31u) / 32u;
+    mark(1);
     AG_CUDA(cudaMemsetAsync(f->groupCorr, 0, 12ull * groups * sizeof(float), st));
     AG_LAUNCH(ff::launchApply(f->net, ws->w, f->pairs, f->word, f->pairCap, f->groups, f->groupCorr, smCount(), st));
+    mark(2);
     AG_LAUNCH(ff::launchCorrect(*p, f->groups, f->groupCorr, n, st));
+    mark(3);
     f->stats.calls++;
-    f->stats.lastGateRms = -1.0f;
+    f->lastCallGated = false;
     if (gate && f->cfg.gateTolerance > 0.0f && n >= 2u) {
         const uint32_t K = std::max<uint32_t>(1u, std::min(f->cfg.gateTargets, n));
-        AG_CUDA(cudaMemsetAsync(f->gateSum, 0, sizeof(float), st));
-        AG_LAUNCH(ff::launchGate(*p, ws->w, n, K, f->gateSum, st));
-        AG_CUDA(cudaMemcpyAsync(f->pinned, f->gateSum, sizeof(float), cudaMemcpyDeviceToHost, st));
-        AG_CUDA(cudaMemcpyAsync(f->pinned + 1, f->word, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        AG_CUDA(cudaStreamSynchronize(st));
-        const float rms = std::sqrt(f->pinned[0] / static_cast<float>(K));
-        uint32_t pairs = 0;
-        std::memcpy(&pairs, f->pinned + 1, sizeof(uint32_t));
-        f->stats.lastPairs = std::min(pairs, f->pairCap);
-        f->stats.lastGateRms = rms;
-        if (!(rms <= f->cfg.gateTolerance)) {      // the gate failed: plain walk at theta
-            AG_LAUNCH(launchGravity(*p, ws->w, n, theta, false, smCount(), st, nullptr,
-                                    static_cast<int>(tuningFor(n).gravityWarps)));
-            f->stats.fallbacks++;
-        }
+        AG_LAUNCH(ff::launchGate(*p, ws->w, n, K, f->cfg.gateTolerance, f->word, f->pairCap, f->gate, st));
+        mark(4);
+        Work w = ws->w;
+        w.runIf = &f->gate->runFallback;       // the plain walk at theta, run only when the gate failed
+        AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), st, nullptr,
+                                static_cast<int>(tuningFor(n).gravityWarps)));
+        f->lastCallGated = true;
+    } else {
+        mark(4);
     }
+    mark(5);
     return ASTRAEA_OK;
 }
 
@@ -473,6 +480,7 @@ namespace astraea_gb300 {
 cudaStream_t capiStream() { return stream(); }
 void capiSetLastError(const std::string& msg) { g_lastError = msg; }
 uint32_t capiSpinLimit() { return g_spinLimit.load(); }
+uint32_t* noallocStatusFlagsAddress();   // noalloc.cu
 }  // namespace astraea_gb300
 
 extern "C" {
@@ -503,6 +511,11 @@ AstraeaStatus astraea_gb300_read_device_status(uint32_t* flags, uint64_t* counte
     DevStatus h{};
     AG_CUDA(cudaStreamSynchronize(stream()));
     AG_CUDA(cudaMemcpy(&h, ds->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    if (uint32_t* na = noallocStatusFlagsAddress()) {   // the no-allocation sort's own status block
+        uint32_t f = 0;
+        AG_CUDA(cudaMemcpy(&f, na, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        h.flags |= f;
+    }
     if (flags) *flags = h.flags;
     if (counters8)
         for (int k = 0; k < 8; ++k) counters8[k] = h.counters[k];
@@ -514,6 +527,7 @@ AstraeaStatus astraea_gb300_reset_device_status(void) {
     AstraeaStatus s = deviceState(&ds);
     if (s != ASTRAEA_OK) return s;
     AG_CUDA(cudaMemsetAsync(ds->status, 0, sizeof(DevStatus), stream()));
+    if (uint32_t* na = noallocStatusFlagsAddress()) AG_CUDA(cudaMemsetAsync(na, 0, sizeof(uint32_t), stream()));
     return ASTRAEA_OK;
 }
 
@@ -682,6 +696,45 @@ AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const Astrae
     return ASTRAEA_OK;
 }
 
+AstraeaStatus astraea_gb300_debug_gravity_group_trace(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                                     uint32_t group, int32_t* trace, uint32_t capacity) {
+    if (p == nullptr || bvh == nullptr || trace == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (g_farField.load() != 0) return fail(ASTRAEA_ERR_INVALID, "the trace is taken in far-field mode 0");
+    AG_CUDA(cudaMemsetAsync(trace, 0, sizeof(int32_t), stream()));
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
+    Work w = ws->w;
+    w.traceList = trace;
+    w.traceGroup = group;
+    w.traceCap = capacity;
+    AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), stream(), nullptr,
+                            static_cast<int>(tuningFor(n).gravityWarps)));
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_debug_gravity_group_counts(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                                      uint32_t* groupCounts) {
+    if (p == nullptr || bvh == nullptr || groupCounts == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (g_farField.load() != 0) return fail(ASTRAEA_ERR_INVALID, "group counts are taken in far-field mode 0");
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
+    Work w = ws->w;
+    w.groupCounts = groupCounts;
+    AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), stream(), nullptr,
+                            static_cast<int>(tuningFor(n).gravityWarps)));
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_sph_pass2_forces(AstraeaParticles* p, const AstraeaRadixBvh* bvh) {
     if (p == nullptr || bvh == nullptr) return fail(ASTRAEA_ERR_INVALID, "null descriptor");
     const uint32_t n = p->count;
@@ -749,8 +802,11 @@ AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevD
     AG_LAUNCH(launchReduceDt(*p, p->count, dtWord, smCount(), st));
     // flags + dt bits in one copy: the blocking read the engine does anyway
     AG_CUDA(cudaMemcpyAsync(ds->hostWord, ds->status, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    ds->hostWord[2] = 0u;
+    if (uint32_t* na = noallocStatusFlagsAddress())
+        AG_CUDA(cudaMemcpyAsync(ds->hostWord + 2, na, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     AG_CUDA(cudaStreamSynchronize(st));
-    if (ds->hostWord[0] & kFlagLookbackTimeout)
+    if ((ds->hostWord[0] | ds->hostWord[2]) & kFlagLookbackTimeout)
         return fail(ASTRAEA_ERR_DEVICE_TIMEOUT, "a radix-sort look-back wait timed out; results since the last status "
                                                 "reset are invalid (astraea_gb300_reset_device_status clears it)");
     *outDt = hostClampDt(ds->hostWord[1], prevDtPsu, maxDtPsu);
@@ -1066,11 +1122,39 @@ AstraeaStatus astraea_gb300_ff_set_params(const float* params, uint32_t count, c
     return ASTRAEA_OK;
 }
 
+AstraeaStatus astraea_gb300_ff_profile(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta, float* outMs5) {
+    if (p == nullptr || bvh == nullptr || outMs5 == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const uint32_t n = p->count;
+    if (n == 0u) return ASTRAEA_OK;
+    if (g_farField.load() != 2) return fail(ASTRAEA_ERR_INVALID, "ff_profile runs far-field mode 2");
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (!ws->momentsBuilt) return fail(ASTRAEA_ERR_INVALID, "far-field mode 2 needs a tree built in that mode");
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
+    cudaEvent_t ev[6] = {};
+    for (auto& e : ev) AG_CUDA(cudaEventCreate(&e));
+    s = learnedGravity(p, ws, n, theta, true, ev);
+    cudaError_t e = cudaEventSynchronize(ev[5]);
+    for (int k = 0; k < 5 && e == cudaSuccess && s == ASTRAEA_OK; ++k) e = cudaEventElapsedTime(&outMs5[k], ev[k], ev[k + 1]);
+    for (auto& x : ev) cudaEventDestroy(x);
+    ws->stepCacheValid = false;
+    if (s != ASTRAEA_OK) return s;
+    AG_CUDA(e);
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out) {
     if (out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
     FfState* f = nullptr;
     AstraeaStatus s = ffState(&f);
     if (s != ASTRAEA_OK) return s;
+    ff::GateDev g{};
+    AG_CUDA(cudaStreamSynchronize(stream()));
+    AG_CUDA(cudaMemcpy(&g, f->gate, sizeof(g), cudaMemcpyDeviceToHost));
+    f->stats.fallbacks = g.fallbacks;
+    f->stats.lastPairs = g.lastPairs;
+    f->stats.lastGateRms = f->lastCallGated ? g.lastRms : -1.0f;
     *out = f->stats;
     return ASTRAEA_OK;
 }
@@ -1344,6 +1428,13 @@ AstraeaStatus astraea_gb300_read_device_counters(uint64_t* outCounters, uint32_t
 AstraeaStatus astraea_gb300_measure_fp32_tflops(float* outTflops) {
     if (outTflops == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
     AG_LAUNCH(measureFp32Tflops(smCount(), outTflops, stream()));
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_measure_fp32_peaks(float* outScalarTflops, float* outPackedTflops) {
+    if (outScalarTflops == nullptr || outPackedTflops == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    float peak = 0.f;
+    AG_LAUNCH(measureFp32TflopsBoth(smCount(), outScalarTflops, outPackedTflops, &peak, stream()));
     return ASTRAEA_OK;
 }
 

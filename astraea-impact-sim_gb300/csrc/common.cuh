@@ -205,7 +205,6 @@ struct MatConst {
     float cv;              // MJ/(kg K)
     float cvTrefHi, cvTrefLo;   // cv * tRef as a float pair (hi + lo)
     float cMinCondensed;   // max(0.05, sqrt(A / rho0))
-    float rho0KgTimes08;   // 0.8 * rho0 in kg/m^3 (vapour test)
     float u0Ref;           // cv * 300 K (sph_gravity.cu:27-33)
     float kH2, gamma;      // HydrogenHelium polytrope + ideal gas
 };
@@ -233,7 +232,7 @@ constexpr MatConst makeMat(double rho0Kg, double a, double b, double APa, double
                     static_cast<float>(alpha), static_cast<float>(beta),
                     static_cast<float>(rho0 - static_cast<double>(static_cast<float>(rho0))), static_cast<float>(cv), hi,
                     static_cast<float>(cvTref - static_cast<double>(hi)),
-                    static_cast<float>(cMin > 0.05 ? cMin : 0.05), static_cast<float>(0.8 * rho0Kg),
+                    static_cast<float>(cMin > 0.05 ? cMin : 0.05),
                     static_cast<float>((cvSI * 300.0) / 1.0e6), static_cast<float>(kH2), static_cast<float>(gamma)};
 }
 // Strength columns (mu, T_melt, K, Y0) of the HydrogenHelium row are zero in
@@ -251,6 +250,83 @@ static __constant__ MatConst c_mat[5] = {
 };
 
 __device__ __forceinline__ int matIndex(uint8_t m) { return (m <= 4u) ? static_cast<int>(m) : 1; }
+
+// FP64 constants of the engine's FP64 temperature and phase classification
+// (eos.cu:229-266, 283-318, 320-350), formed as the engine forms them: PSU
+// values by one division by the unit, 0.8 rho0 in kg/m^3 by one product.
+// Each float threshold is the smallest float x for which the engine's FP64
+// test on x passes, so the FP32 test of a float input decides exactly as the
+// engine's FP64 test does.
+struct MatConstD {
+    double rho0, A, B, kH2, cv, tMelt;
+    float ecvUp;        // smallest float u with (double)u >= E_cv (PSU)
+    float rhoVapUp;     // smallest float rho with rho * 1e6 >= 0.8 rho0 [kg/m^3]
+};
+constexpr double cxUlpOfFloat(double f) {   // spacing of the floats in [2^e, 2^(e+1)) that holds f > 0
+    double p = 1.0;
+    while (p > f) p *= 0.5;
+    while (p * 2.0 <= f) p *= 2.0;
+    return p * (1.0 / 8388608.0);
+}
+constexpr float cxFloatNext(float f) { return static_cast<float>(static_cast<double>(f) + cxUlpOfFloat(f)); }
+constexpr float cxFloatPrev(float f) {       // largest float below f > 0 (half the spacing below a power of two)
+    const double u = cxUlpOfFloat(f);
+    const bool pow2 = static_cast<double>(f) == u * 8388608.0;
+    return static_cast<float>(static_cast<double>(f) - (pow2 ? 0.5 * u : u));
+}
+constexpr float cxFloatUp(double x) {       // smallest float >= x, x > 0 normal
+    const float f = static_cast<float>(x);   // the nearest float: the next one up is >= x
+    return (static_cast<double>(f) < x) ? cxFloatNext(f) : f;
+}
+constexpr float cxRhoUp(double kgPerM3) {   // smallest float rho with rho * 1e6 >= kgPerM3 (exact product)
+    float f = cxFloatUp(kgPerM3 / 1.0e6);
+    while (static_cast<double>(f) * 1.0e6 < kgPerM3) f = cxFloatNext(f);
+    while (static_cast<double>(cxFloatPrev(f)) * 1.0e6 >= kgPerM3) f = cxFloatPrev(f);
+    return f;
+}
+constexpr MatConstD makeMatD(double rho0Kg, double APa, double BPa, double Ecv, double cvSI, double tMelt, double kH2) {
+    return MatConstD{rho0Kg / 1.0e6, APa / 1.0e12, BPa / 1.0e12, kH2, cvSI / 1.0e6, tMelt,
+                     Ecv > 0.0 ? cxFloatUp(Ecv / 1.0e6) : 0.0f, rho0Kg > 0.0 ? cxRhoUp(0.8 * rho0Kg) : 0.0f};
+}
+static __constant__ MatConstD c_matD[5] = {
+    makeMatD(7800.0, 1.28e11, 1.05e11, 8.67e6, 449.0, 1811.0, 0.0),     // Iron
+    makeMatD(2680.0, 1.80e10, 1.80e10, 1.80e7, 790.0, 1600.0, 0.0),     // Granite
+    makeMatD(1000.0, 2.18e9, 1.325e10, 2.68e6, 4184.0, 273.15, 0.0),    // WaterIce
+    makeMatD(0.178, 0.0, 0.0, 0.0, 8260.0, 0.0, 2.08e5),                // HydrogenHelium
+    makeMatD(2000.0, 1.20e10, 1.20e10, 1.80e7, 800.0, 1500.0, 0.0),     // Regolith
+};
+constexpr float kRhoWaterVapUp = cxRhoUp(322.0);   // eos.cu:247: rho [kg/m^3] < 322
+
+// computeColdEnergyPsu (eos.cu:283-318) in FP64, in the engine's operation order.
+__device__ __forceinline__ double coldEnergyF64(int mat, double rho) {
+    const MatConstD& c = c_matD[mat];
+    rho = rho > 0.0 ? rho : 0.0;
+    if (mat == 3) return c.kH2 * rho;
+    const double eta = rho / c.rho0;
+    if (eta <= 1.0) return 0.0;
+    const double mu = eta - 1.0;
+    double ta, tb;
+    if (mu < 1.0e-5) {
+        const double m2 = mu * mu, m3 = m2 * mu, m4 = m3 * mu, m5 = m4 * mu;
+        ta = 0.5 * m2 - (2.0 / 3.0) * m3 + 0.75 * m4 - 0.8 * m5;
+        tb = (1.0 / 3.0) * m3 - 0.5 * m4 + 0.6 * m5;
+    } else {
+        const double le = log1p(mu);
+        ta = le - (mu / eta);
+        tb = (mu * (2.0 + mu)) / eta - 2.0 * le;
+    }
+    return (c.A * ta + c.B * tb) / c.rho0;
+}
+
+// The engine's FP64 temperature (eos.cu:320-330, 342).
+static __device__ __noinline__ double temperatureF64(int mi, float rhoIn, float uIn) {
+    const MatConstD& c = c_matD[mi];
+    const double rho = fmax(static_cast<double>(rhoIn), 1.0e-12);
+    const double u = static_cast<double>(uIn);
+    const double uCold = coldEnergyF64(mi, rho);
+    if (mi == 3) return fmax(3.0, fmax(0.0, u - uCold) / c.cv);
+    return fmax(3.0, (u - uCold) / c.cv);
+}
 
 // ---------------------------------------------------------------- EOS -----
 // FP32 evaluation of engine/eos.cu:283-388.  The reference evaluates in FP64;
@@ -340,19 +416,46 @@ __device__ __forceinline__ PD tillotsonExpandedF32(const MatConst& c, float rho,
     return r;
 }
 
-__device__ __forceinline__ uint8_t classifyPhaseF32(int mi, const MatConst& c, float rho, float u, float T) {
-    if (mi == 3) return (T > 10000.0f) ? 3u : 5u;                 // eos.cu:235-238
-    const float rhoKg = rho * 1.0e6f;
+// classifyPhase (eos.cu:229-266) on the engine's FP64 temperature T: the
+// density and energy tests compare the float inputs with exact float
+// thresholds (c_matD), the temperature tests are FP64.
+__device__ __forceinline__ uint8_t classifyPhaseExact(int mi, float rho, float u, double T) {
+    if (mi == 3) return (T > 10000.0) ? 3u : 5u;                  // eos.cu:235-238
+    const MatConstD& d = c_matD[mi];
     if (mi == 2) {                                               // eos.cu:243-254
-        if (T > 15000.0f) return 3u;
-        if (u >= c.Ecv || (T > 647.0f && rhoKg < 322.0f)) return 2u;
-        if (T >= 273.15f) return 4u;
+        if (T > 15000.0) return 3u;
+        if (u >= d.ecvUp || (T > 647.0 && rho < kRhoWaterVapUp)) return 2u;
+        if (T >= 273.15) return 4u;
         return 0u;
     }
-    if (T > 12000.0f) return 3u;                                 // eos.cu:257-266
-    if (u >= c.Ecv && rhoKg < c.rho0KgTimes08) return 2u;
-    if (T >= c.tMelt) return 1u;
+    if (T > 12000.0) return 3u;                                  // eos.cu:257-266
+    if (u >= d.ecvUp && rho < d.rhoVapUp) return 2u;
+    if (T >= d.tMelt) return 1u;
     return 0u;
+}
+
+// True when the FP32 temperature T (from u and an FP32 cold energy uCold)
+// may lie on the other side of a phase threshold than the engine's FP64 one:
+// within 1e-5 T plus 4e-6 (|u| + |uCold|) / c_v of a threshold of the
+// material (the FP32 T is within about a tenth of that of the FP64 T).
+__device__ __forceinline__ bool nearPhaseTemperature(int mi, float T, float u, float uCold, float cv) {
+    const float tol = 1.0e-5f * T + 4.0e-6f * (fabsf(u) + fabsf(uCold)) / cv;
+    if (mi == 3) return fabsf(T - 10000.0f) <= tol;
+    if (mi == 2)
+        return fabsf(T - 15000.0f) <= tol || fabsf(T - 647.0f) <= tol || fabsf(T - 273.15f) <= tol;
+    return fabsf(T - 12000.0f) <= tol || fabsf(T - static_cast<float>(c_matD[mi].tMelt)) <= tol;
+}
+
+// Phase and stored temperature: far from every threshold the FP32 T decides
+// as the FP64 one would; near one, the engine's FP64 T is formed and both
+// the phase and the stored temperature (float(T)) are the engine's.
+__device__ __forceinline__ void phaseAndTemperature(int mi, float rhoIn, float u, float uCold, float cv, EosOut& o) {
+    double T = static_cast<double>(o.T);
+    if (nearPhaseTemperature(mi, o.T, u, uCold, cv)) {
+        T = temperatureF64(mi, rhoIn, u);
+        o.T = static_cast<float>(T);
+    }
+    o.phase = classifyPhaseExact(mi, rhoIn < 1.0e-12f ? 1.0e-12f : rhoIn, u, T);
 }
 
 __device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, float u, float dIn) {
@@ -367,7 +470,7 @@ __device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, fl
         const float P = c.kH2 * rho * rho + (c.gamma - 1.0f) * rho * uTh;
         const float cs2 = 2.0f * c.kH2 * rho + c.gamma * (c.gamma - 1.0f) * uTh;
         o.P = P; o.cs = fmaxf(0.05f, sqrtf(fmaxf(0.0f, cs2))); o.T = T;
-        o.phase = classifyPhaseF32(mi, c, rho, u, T);
+        phaseAndTemperature(mi, rhoIn, u, c.kH2 * rho, c.cv, o);
         return o;
     }
     const float mu = ((rho - c.rho0) - c.rho0Lo) / c.rho0;   // additive uses
@@ -397,7 +500,7 @@ __device__ __forceinline__ EosOut evaluateEosF32(uint8_t matRaw, float rhoIn, fl
     o.P = r.p;
     o.cs = fmaxf(cMin, sqrtf(fmaxf(0.0f, cs2)));
     o.T = T;
-    o.phase = classifyPhaseF32(mi, c, rho, u, T);
+    phaseAndTemperature(mi, rhoIn, u, uCold, c.cv, o);
     return o;
 }
 
@@ -436,6 +539,11 @@ struct Work {
     size_t sortScratchWords;
     uint32_t sortMaxTiles;
     DevStatus* status;
+    uint32_t* groupCounts; // null, or [groups]: each group's gravity interaction count (diagnostic)
+    int32_t* traceList;    // null, or {count, entries...}: the nodes (>= 0) and leaves (~j) the group
+    uint32_t traceGroup;   //   traceGroup accepts in the gravity walk, appended in walk order (diagnostic)
+    uint32_t traceCap;
+    const uint32_t* runIf; // null, or a device word: the gravity kernel returns at once while it is 0
 };
 
 // Indices into Work::words.

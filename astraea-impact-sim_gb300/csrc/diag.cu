@@ -1,7 +1,9 @@
 // diag.cu -- measured FP32 CUDA-core throughput, the denominator of the
 // gravity kernel's roofline (the pair interactions are FP32 FMA/MUFU work,
-// not tensor-core work).  Every thread runs 8 independent FMA chains so the
-// pipes, not dependencies, bound the rate.
+// not tensor-core work).  Two forms are timed: scalar fmaf chains and packed
+// fma.rn.f32x2 chains (two FP32 FMAs per instruction, the form the gravity
+// pair evaluation issues); the larger rate is the peak.  Every thread runs 8
+// independent chains so the pipes, not dependencies, bound the rate.
 #include "kernels.h"
 
 namespace astraea_gb300 {
@@ -22,29 +24,62 @@ __global__ void __launch_bounds__(256) fmaPeakKernel(float* out, int iters, floa
     if (s == 123.456f) out[blockIdx.x] = s;   // keeps the chains live; never true in practice
 }
 
-}  // namespace
+__global__ void __launch_bounds__(256) fma2PeakKernel(float* out, int iters, float seed) {
+    const float b0 = seed + threadIdx.x;
+    f2 a0 = pack2(b0, b0 + 0.5f), a1 = pack2(b0 + 1.f, b0 + 1.5f), a2 = pack2(b0 + 2.f, b0 + 2.5f),
+       a3 = pack2(b0 + 3.f, b0 + 3.5f), a4 = pack2(b0 + 4.f, b0 + 4.5f), a5 = pack2(b0 + 5.f, b0 + 5.5f),
+       a6 = pack2(b0 + 6.f, b0 + 6.5f), a7 = pack2(b0 + 7.f, b0 + 7.5f);
+    const f2 m = pack2(0.999999f, 0.999999f), c = pack2(1.0e-7f, 1.0e-7f);
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            a0 = fma2(a0, m, c); a1 = fma2(a1, m, c); a2 = fma2(a2, m, c); a3 = fma2(a3, m, c);
+            a4 = fma2(a4, m, c); a5 = fma2(a5, m, c); a6 = fma2(a6, m, c); a7 = fma2(a7, m, c);
+        }
+    }
+    f2 s2 = add2(add2(add2(a0, a1), add2(a2, a3)), add2(add2(a4, a5), add2(a6, a7)));
+    float lo, hi;
+    unpack2(s2, lo, hi);
+    if (lo + hi == 123.456f) out[blockIdx.x] = lo;   // keeps the chains live; never true in practice
+}
 
-cudaError_t measureFp32Tflops(int sms, float* tflops, cudaStream_t st) {
-    float* dummy = nullptr;
-    cudaError_t e = cudaMalloc(&dummy, 4096 * sizeof(float));
-    if (e != cudaSuccess) return e;
+template <typename K>
+float timeFmaKernel(K kernel, int blocks, int iters, float* dummy, double fmaPerThreadIter, cudaStream_t st,
+                    cudaError_t* err) {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    const int blocks = sms * 8, iters = 2048;
-    fmaPeakKernel<<<blocks, 256, 0, st>>>(dummy, 64, 1.0f);   // warm-up
+    kernel<<<blocks, 256, 0, st>>>(dummy, 64, 1.0f);   // warm-up
     cudaEventRecord(a, st);
-    fmaPeakKernel<<<blocks, 256, 0, st>>>(dummy, iters, 1.0f);
+    kernel<<<blocks, 256, 0, st>>>(dummy, iters, 1.0f);
     cudaEventRecord(b, st);
-    e = cudaEventSynchronize(b);
+    *err = cudaEventSynchronize(b);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    const double flops = 2.0 * fmaPerThreadIter * iters * static_cast<double>(blocks) * 256.0;
+    return (*err == cudaSuccess && ms > 0.f) ? static_cast<float>(flops / (ms * 1.0e-3) / 1.0e12) : 0.f;
+}
+
+}  // namespace
+
+cudaError_t measureFp32Tflops(int sms, float* tflops, cudaStream_t st) {
+    float scalar = 0.f, packed = 0.f;
+    return measureFp32TflopsBoth(sms, &scalar, &packed, tflops, st);
+}
+
+cudaError_t measureFp32TflopsBoth(int sms, float* scalarOut, float* packedOut, float* peakOut, cudaStream_t st) {
+    float* dummy = nullptr;
+    cudaError_t e = cudaMalloc(&dummy, 4096 * sizeof(float));
+    if (e != cudaSuccess) return e;
+    const int blocks = sms * 8, iters = 2048;
+    cudaError_t e1 = cudaSuccess, e2 = cudaSuccess;
+    *scalarOut = timeFmaKernel(fmaPeakKernel, blocks, iters, dummy, 8.0 * 16.0, st, &e1);
+    *packedOut = timeFmaKernel(fma2PeakKernel, blocks, iters, dummy, 2.0 * 8.0 * 16.0, st, &e2);
+    *peakOut = *scalarOut > *packedOut ? *scalarOut : *packedOut;
     cudaFree(dummy);
-    const double flops = 2.0 * 8.0 * 16.0 * iters * static_cast<double>(blocks) * 256.0;
-    *tflops = static_cast<float>(flops / (ms * 1.0e-3) / 1.0e12);
-    return e;
+    return e1 != cudaSuccess ? e1 : e2;
 }
 
 }  // namespace astraea_gb300

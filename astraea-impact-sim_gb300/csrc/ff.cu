@@ -405,21 +405,25 @@ __global__ void __launch_bounds__(kLabelWarps * 32) labelKernel(Work w, uint32_t
 // spread sorted particles against the accelerations in p; accumulates
 // sum |a - a_ref|^2 / |a_ref|^2 into out[0].
 constexpr int kGateThreads = 256;
+// The gate's spot check: block k takes the k-th of K evenly spaced sorted
+// particles and sums its acceleration over every other particle in FP64
+// (positions widened before the subtraction, the softened kernel in double),
+// then adds |a - a_FP64|^2 / |a_FP64|^2 to gate->errSum.
 __global__ void __launch_bounds__(kGateThreads) gateKernel(AstraeaParticles p, Work w, uint32_t n, uint32_t K,
-                                                           float* out) {
-    __shared__ float red[3][kGateThreads / 32];
+                                                           GateDev* gate) {
+    __shared__ double red[3][kGateThreads / 32];
     const uint32_t t = (K > 1u) ? static_cast<uint32_t>((static_cast<uint64_t>(blockIdx.x) * (n - 1u)) / (K - 1u)) : 0u;
     const float4 me = __ldg(&w.leaf[t].a);
-    const float ei = __ldg(&w.leafAux[t]).y;
-    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    const double xi = me.x, yi = me.y, zi = me.z, ei = __ldg(&w.leafAux[t]).y;
+    double ax = 0.0, ay = 0.0, az = 0.0;
     for (uint32_t j = threadIdx.x; j < n; j += kGateThreads) {
         if (j == t) continue;
         const float4 pm = __ldg(&w.leaf[j].a);
-        const float e = 0.5f * (ei + __ldg(&w.leafAux[j]).y);
-        const float dx = me.x - pm.x, dy = me.y - pm.y, dz = me.z - pm.z;
-        const float den = dx * dx + dy * dy + dz * dz + e * e + 1.0e-20f;
-        const float ir = rsqrtf(den);
-        const float f = -kG * pm.w * ir * ir * ir;
+        const double e = 0.5 * (ei + static_cast<double>(__ldg(&w.leafAux[j]).y));
+        const double dx = xi - pm.x, dy = yi - pm.y, dz = zi - pm.z;
+        const double den = dx * dx + dy * dy + dz * dz + e * e;
+        const double ir = 1.0 / sqrt(den);
+        const double f = -static_cast<double>(kG) * pm.w * ir * ir * ir;
         ax += f * dx; ay += f * dy; az += f * dz;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -431,12 +435,26 @@ __global__ void __launch_bounds__(kGateThreads) gateKernel(AstraeaParticles p, W
     if (lane == 0) { red[0][warp] = ax; red[1][warp] = ay; red[2][warp] = az; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        double sx = 0.0, sy = 0.0, sz = 0.0;
         for (int k = 0; k < kGateThreads / 32; ++k) { sx += red[0][k]; sy += red[1][k]; sz += red[2][k]; }
-        const float ex = p.accX[t] - sx, ey = p.accY[t] - sy, ez = p.accZ[t] - sz;
-        const float ref = sx * sx + sy * sy + sz * sz;
-        if (ref > 0.0f) atomicAdd(out, (ex * ex + ey * ey + ez * ez) / ref);
+        const double ex = p.accX[t] - sx, ey = p.accY[t] - sy, ez = p.accZ[t] - sz;
+        const double ref = sx * sx + sy * sy + sz * sz;
+        if (ref > 0.0) atomicAdd(&gate->errSum, (ex * ex + ey * ey + ez * ez) / ref);
     }
+}
+
+// The gate's decision, on the device: RMS of the spot check against the
+// tolerance; runFallback = 1 makes the following plain walk run, 0 makes it
+// return at once.  Also the statistics ff_stats reads.
+__global__ void gateDecideKernel(GateDev* gate, uint32_t K, float tolerance, const uint32_t* pairCount,
+                                 uint32_t pairCap) {
+    const double rms = sqrt(gate->errSum / static_cast<double>(K));
+    const bool pass = rms <= static_cast<double>(tolerance);
+    gate->runFallback = pass ? 0u : 1u;
+    gate->lastRms = static_cast<float>(rms);
+    gate->lastPairs = min(*pairCount, pairCap);
+    if (!pass) gate->fallbacks += 1ull;
+    gate->errSum = 0.0;                      // ready for the next gate
 }
 
 inline unsigned blocks(size_t n, unsigned t) { return static_cast<unsigned>((n + t - 1) / t); }
@@ -503,10 +521,12 @@ cudaError_t launchCorrect(const AstraeaParticles& p, const float4* groups, const
     return cudaGetLastError();
 }
 
-cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float* out,
-                       cudaStream_t st) {
-    if (n < 2 || K == 0) return cudaSuccess;
-    gateKernel<<<K, kGateThreads, 0, st>>>(p, w, n, K, out);
+cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float tolerance,
+                       const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, cudaStream_t st) {
+    gateKernel<<<K, kGateThreads, 0, st>>>(p, w, n, K, gate);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    gateDecideKernel<<<1, 1, 0, st>>>(gate, K, tolerance, pairCount, pairCap);
     return cudaGetLastError();
 }
 

@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
     int spPeak = 0;
     bool overflowed = false;
 
+    if (w.runIf != nullptr && *w.runIf == 0u) return;   // the gate of the learned mode passed
     if (n == 1u) {                                   // sph_gravity.cu:824-832
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             p.accX[0] = 0.0f; p.accY[0] = 0.0f; p.accZ[0] = 0.0f; p.phiGrav[0] = 0.0f;
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         const uint32_t i = g * 32u + static_cast<uint32_t>(lane);
         const bool active = i < n;                  // active members are lanes 0 .. act-1
         const int act = static_cast<int>(min(32u, n - g * 32u));
+        const unsigned long long interBefore = nInter;
         float4 me = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         float epsI = 0.8e-6f;
         if (active) {
@@ -334,19 +336,18 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 }
                 __syncwarp();
                 unsigned bits = 0u;
-                // the engine's member test (acceptsMember) for two nodes per
-                // instruction: the same IEEE operations in the same order
-                const f2 T2 = pack2(theta2, theta2);
+                // the engine's member test (acceptsMember) on two nodes per
+                // iteration, in scalar IEEE operations (__fmul_rn / __fadd_rn
+                // are never contracted into multiply-adds, so a member exactly
+                // on the theta boundary is decided as the engine decides it)
                 for (int k = 0; k < nu; k += 2) {
                     const float* ub = undP + 4 * k;
-                    const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(ub);       // (com x), (com y)
-                    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(ub + 4);   // (com z), (dd)
-                    const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
-                    const f2 r2 = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
-                    float r2a, r2b, ta, tb, dda, ddb;
-                    unpack2(r2, r2a, r2b);
-                    unpack2(mul2(T2, r2), ta, tb);
-                    unpack2(v.y, dda, ddb);
+                    const float4 pa = *reinterpret_cast<const float4*>(ub);       // com xA, xB, yA, yB
+                    const float4 pb = *reinterpret_cast<const float4*>(ub + 4);   // com zA, zB, ddA, ddB
+                    const float r2a = len2Exact(__fsub_rn(xi, pa.x), __fsub_rn(yi, pa.z), __fsub_rn(zi, pb.x));
+                    const float r2b = len2Exact(__fsub_rn(xi, pa.y), __fsub_rn(yi, pa.w), __fsub_rn(zi, pb.y));
+                    const float ta = __fmul_rn(theta2, r2a), tb = __fmul_rn(theta2, r2b);
+                    const float dda = pb.z, ddb = pb.w;
                     bool okA = dda < ta && r2a > 1.0e-20f, okB = ddb < tb && r2b > 1.0e-20f;
                     if (kInside) {
                         const float4 mnA = S.undMin[k], mxA = S.undMax[k];
@@ -398,6 +399,10 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             }
             sp += 2 * __popc(openMask);
             const unsigned accMask = __ballot_sync(0xffffffffu, accept);
+            if (w.traceList != nullptr && g == w.traceGroup && (accept || isLeaf)) {
+                const uint32_t k = atomicAdd(reinterpret_cast<uint32_t*>(w.traceList), 1u);
+                if (k < w.traceCap) w.traceList[1 + k] = c;
+            }
             if (accept) {
                 float e[10] = {r0.x, r0.y, r0.z, -kGPsuF * r0.w, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 if (kQuad) {
@@ -484,7 +489,10 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         }
         nRounds += rounds;
         nInter += static_cast<unsigned long long>(act) * static_cast<unsigned>(mCount + pCount);
-        if (lane == 0) nInter -= static_cast<unsigned long long>(__popc(selfSeen));
+        if (lane == 0) {
+            nInter -= static_cast<unsigned long long>(__popc(selfSeen));
+            if (w.groupCounts != nullptr) w.groupCounts[g] = static_cast<uint32_t>(nInter - interBefore);
+        }
         __syncwarp();
     }
     if (lane == 0) {

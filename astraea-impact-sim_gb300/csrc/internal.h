@@ -18,6 +18,17 @@ constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
 constexpr int kSortBins = 256;
 constexpr int kSortMaxPasses = 8;
 
+// Onesweep scratch layout (32-bit words):
+//   [0, kSortHistWords)                              digit histograms, one per pass
+//   [kSortHistWords, + kSortCounterWords)            tile counters, one per pass
+//   then kSortMaxPasses * tiles * kSortBins          look-back status words
+constexpr size_t kSortHistWords = static_cast<size_t>(kSortMaxPasses) * kSortBins;
+constexpr size_t kSortCounterWords = 8;
+constexpr uint32_t sortTiles(uint32_t n) { return n == 0u ? 1u : (n + kSortTile - 1u) / kSortTile; }
+constexpr size_t sortScratchWordsFor(uint32_t n) {
+    return kSortHistWords + kSortCounterWords + static_cast<size_t>(kSortMaxPasses) * sortTiles(n) * kSortBins;
+}
+
 // Number of 32-bit words of onesweep scratch for n keys.
 size_t sortScratchWords(uint32_t n, uint32_t* maxTilesOut);
 

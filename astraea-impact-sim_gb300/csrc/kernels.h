@@ -132,7 +132,18 @@ cudaError_t launchApply(const Net& net, const Work& w, const uint2* pairs, const
                         const float4* groups, float* groupCorr, int sms, cudaStream_t st);
 cudaError_t launchCorrect(const AstraeaParticles& p, const float4* groups, const float* groupCorr, uint32_t n,
                           cudaStream_t st);
-cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float* out, cudaStream_t st);
+// Device state of the learned mode's gate (one per device).
+struct GateDev {
+    double errSum;                 // sum of relative squared errors of the spot check (reset by the decision)
+    unsigned long long fallbacks;  // gated calls that fell back to the plain walk
+    uint32_t runFallback;          // 1: the plain walk after the gate runs, 0: it returns at once
+    uint32_t lastPairs;            // (group, node) pairs of the last gated call
+    float lastRms;                 // RMS relative error of the last gate
+    uint32_t reserved;
+};
+// FP64 spot check of K sampled particles and the decision (gate->runFallback).
+cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float tolerance,
+                       const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, cudaStream_t st);
 }  // namespace ff
 
 // -------------------------------------------------------------- sph.cu ---
@@ -181,6 +192,8 @@ cudaError_t launchDriftPlain(const AstraeaParticles& p, uint32_t n, float dt, cu
 
 // -------------------------------------------------------------- diag.cu ---
 cudaError_t measureFp32Tflops(int sms, float* tflops, cudaStream_t st);
+// Scalar fmaf and packed fma.rn.f32x2 throughput, and the larger of the two.
+cudaError_t measureFp32TflopsBoth(int sms, float* scalarOut, float* packedOut, float* peakOut, cudaStream_t st);
 
 // ------------------------------------------------------------ planet.cu ---
 namespace planet {

@@ -15,12 +15,19 @@
 //     ASTRAEA_ERR_CAPACITY without touching the GPU;
 //   * every GPU that loads the library holds the array (about 2.1 MB) until
 //     the process exits;
-//   * the array is shared by all calls: each call clears the parts that must
-//     start at zero before its kernels run, but two calls whose work overlaps
-//     on the GPU (different streams, or different host threads) race on it;
+//   * the array is shared by all calls: each call clears the sort's parts that
+//     must start at zero before its kernels run, but two calls whose work
+//     overlaps on the GPU (different streams, or different host threads) race
+//     on it;
+//   * a look-back wait that gives up sets a flag in a status block kept in the
+//     same array; the flag stays set until astraea_gb300_reset_device_status,
+//     and astraea_gb300_read_device_status and astraea_gb300_reduce_dt_psu
+//     report it like the allocating sort's (the result of such a call is not
+//     sorted);
 //   * the first call on each device looks up the array's device address with
 //     cudaGetSymbolAddress (set-up, once per device); make that first call
-//     before any stream capture.
+//     before any stream capture.  The address is kept for the life of the
+//     process, so cudaDeviceReset between calls is not supported.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -39,17 +46,34 @@ namespace {
 
 constexpr uint32_t kNoAllocMaxKeys = 1u << 20;
 constexpr size_t kStatusWords = (sizeof(DevStatus) + 255) / 256 * 64;   // 256-byte aligned status block
-constexpr size_t kSortWordsMax =
-    static_cast<size_t>(kSortMaxPasses) * kSortBins + 8 +
-    static_cast<size_t>(kSortMaxPasses) * ((kNoAllocMaxKeys + kSortTile - 1) / kSortTile) * kSortBins;
+constexpr size_t kSortWordsMax = sortScratchWordsFor(kNoAllocMaxKeys);   // the sort's own layout
 
-// [0, kStatusWords): a DevStatus for the look-back flag; then the sort scratch.
+// [0, kStatusWords): a DevStatus for the look-back flag (zero at load, cleared
+// only by astraea_gb300_reset_device_status); then the sort scratch.
 static __device__ __align__(256) uint32_t g_noallocScratch[kStatusWords + kSortWordsMax];
+static_assert(sizeof(g_noallocScratch) / sizeof(uint32_t) >= kStatusWords + sortScratchWordsFor(kNoAllocMaxKeys),
+              "the fixed array must hold the sort's scratch for the largest call");
 
 std::mutex g_setupMutex;
 uint32_t* g_scratchAddr[64] = {};
 
+uint32_t* scratchAddressIfSetUp() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(g_setupMutex);
+    return g_scratchAddr[dev];
+}
+
 }  // namespace
+
+// Device address of the flags word of the no-allocation sort's status block on
+// the current device, or null while no call has set the device up (its flags
+// are then zero).  Used by the status entry points of capi.cu.
+uint32_t* noallocStatusFlagsAddress() {
+    uint32_t* base = scratchAddressIfSetUp();
+    return base == nullptr ? nullptr : &reinterpret_cast<DevStatus*>(base)->flags;
+}
+
 }  // namespace astraea_gb300
 
 using namespace astraea_gb300;
@@ -90,13 +114,11 @@ extern "C" AstraeaStatus astraea_gb300_radix_sort_pairs_noalloc(uint64_t* keysIn
     }
     cudaStream_t st = capiStream();
     DevStatus* status = reinterpret_cast<DevStatus*>(base);
-    e = cudaMemsetAsync(status, 0, sizeof(DevStatus), st);
     uint32_t* sortScratch = base + kStatusWords;
-    const uint32_t maxTiles = (kNoAllocMaxKeys + kSortTile - 1) / kSortTile;
+    const uint32_t maxTiles = sortTiles(kNoAllocMaxKeys);
     bool inA = true;
-    if (e == cudaSuccess)
-        e = radixSortPairs(keysIn, valsIn, keysOut, valsOut, n, endBit, sortScratch, kSortWordsMax, maxTiles, status,
-                           capiSpinLimit(), KeySource::Array, nullptr, &inA, st);
+    e = radixSortPairs(keysIn, valsIn, keysOut, valsOut, n, endBit, sortScratch, kSortWordsMax, maxTiles, status,
+                       capiSpinLimit(), KeySource::Array, nullptr, &inA, st);
     if (e == cudaSuccess && inA) {
         e = cudaMemcpyAsync(keysOut, keysIn, n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(valsOut, valsIn, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);

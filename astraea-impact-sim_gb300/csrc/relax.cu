@@ -26,40 +26,6 @@ constexpr int kRelaxMaxBlocks = 512;
 constexpr int kRelaxSlots = 8;
 constexpr double kGPsuD = 6.67430e-11 * 1.0e24 * 1.0e3 * 1.0e3 / (1.0e6 * 1.0e6 * 1.0e6);   // engine/units.hpp:27
 
-// Cold-energy and heat-capacity constants in PSU (published Tillotson /
-// polytrope values, eos.cu:10-116): rho0, A, B, k_H2, c_v.
-struct ColdParams {
-    double rho0, A, B, kH2, cv;
-};
-__constant__ ColdParams c_cold[5] = {
-    {7800.0 / 1.0e6, 1.28e11 / 1.0e12, 1.05e11 / 1.0e12, 0.0, 449.0 / 1.0e6},     // Iron
-    {2680.0 / 1.0e6, 1.80e10 / 1.0e12, 1.80e10 / 1.0e12, 0.0, 790.0 / 1.0e6},     // Granite
-    {1000.0 / 1.0e6, 2.18e9 / 1.0e12, 1.325e10 / 1.0e12, 0.0, 4184.0 / 1.0e6},    // WaterIce
-    {0.178 / 1.0e6, 0.0, 0.0, 2.08e5, 8260.0 / 1.0e6},                            // HydrogenHelium
-    {2000.0 / 1.0e6, 1.20e10 / 1.0e12, 1.20e10 / 1.0e12, 0.0, 800.0 / 1.0e6},     // Regolith
-};
-
-// computeColdEnergyPsu (eos.cu:283-318) in FP64, as the engine's host code.
-__device__ double coldEnergyF64(int mat, double rho) {
-    const ColdParams& c = c_cold[mat];
-    rho = rho > 0.0 ? rho : 0.0;
-    if (mat == 3) return c.kH2 * rho;
-    const double eta = rho / c.rho0;
-    if (eta <= 1.0) return 0.0;
-    const double mu = eta - 1.0;
-    double ta, tb;
-    if (mu < 1.0e-5) {
-        const double m2 = mu * mu, m3 = m2 * mu, m4 = m3 * mu, m5 = m4 * mu;
-        ta = 0.5 * m2 - (2.0 / 3.0) * m3 + 0.75 * m4 - 0.8 * m5;
-        tb = (1.0 / 3.0) * m3 - 0.5 * m4 + 0.6 * m5;
-    } else {
-        const double le = log1p(mu);
-        ta = le - (mu / eta);
-        tb = (mu * (2.0 + mu)) / eta - 2.0 * le;
-    }
-    return (c.A * ta + c.B * tb) / c.rho0;
-}
-
 struct RelaxState {
     uint32_t ticket;
     double com[3], vcom[3];
@@ -141,7 +107,7 @@ __device__ __forceinline__ float anchoredU(const AstraeaParticles& p, uint32_t i
     const double tAnchor = (anchorT != nullptr && oid < anchorCount) ? anchorT[oid] : 288.0;
     const uint8_t m8 = p.materialId[i];
     const int mat = m8 <= 4u ? static_cast<int>(m8) : 1;
-    return static_cast<float>(coldEnergyF64(mat, static_cast<double>(p.rho[i])) + c_cold[mat].cv * tAnchor);
+    return static_cast<float>(coldEnergyF64(mat, static_cast<double>(p.rho[i])) + c_matD[mat].cv * tAnchor);
 }
 
 __device__ __forceinline__ void zeroStrength(const AstraeaParticles& p, uint32_t i) {

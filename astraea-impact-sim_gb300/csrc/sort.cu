@@ -12,9 +12,12 @@
 //     decoupled look-back, and keys/values are scattered through a
 //     shared-memory staging buffer so global writes stay coalesced per bin.
 // Every look-back spin is bounded; a timeout sets a device status flag and
-// the tile proceeds with the prefix gathered so far, which keeps every write
-// inside [0, n) (the tile's destinations stay below the bin's end offset).
+// the tile proceeds with the prefix gathered so far (an underestimate, so the
+// tile's destinations stay inside its bin).  The result is then not sorted,
+// and later passes see keys that no longer match the digit histograms, so
+// every store is also checked against n.
 #include <algorithm>
+#include <atomic>
 
 #include "internal.h"
 
@@ -25,12 +28,9 @@ constexpr uint32_t kFlagAggregate = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 
-// Scratch layout (32-bit words):
-//   [0, 8*256)                    digit histograms
-//   [8*256, 8*256+8)              tile counters, one per pass
-//   [2056, 2056 + 8*maxTiles*256) look-back status words
-constexpr size_t kHistWords = kSortMaxPasses * kSortBins;
-constexpr size_t kCounterWords = 8;
+// Scratch layout: internal.h (sortScratchWordsFor).
+constexpr size_t kHistWords = kSortHistWords;
+constexpr size_t kCounterWords = kSortCounterWords;
 
 __device__ __forceinline__ uint32_t lanemaskLt() {
     uint32_t m;
@@ -274,8 +274,13 @@ __global__ void __launch_bounds__(kSortThreads) onesweepKernel(const uint64_t* _
         const uint64_t kk = s.keys[slot];
         const uint32_t d = static_cast<uint32_t>((kk >> shift) & 0xFFu);
         const uint32_t dst = s.globalBase[d] + slot;
-        keysOut[dst] = kk;
-        valsOut[dst] = s.vals[slot];
+        // Always true for a consistent input.  After a look-back timeout in an
+        // earlier pass the keys are no longer a permutation of the histogram's,
+        // and a bin can overflow its range: the check keeps the writes in [0, n).
+        if (dst < n) {
+            keysOut[dst] = kk;
+            valsOut[dst] = s.vals[slot];
+        }
     }
 }
 
@@ -288,9 +293,8 @@ cudaError_t launchLookbackProbe(const uint32_t* neverSet, DevStatus* status, uin
 }
 
 size_t sortScratchWords(uint32_t n, uint32_t* maxTilesOut) {
-    const uint32_t tiles = std::max<uint32_t>(1u, (n + kSortTile - 1) / kSortTile);
-    if (maxTilesOut) *maxTilesOut = tiles;
-    return kHistWords + kCounterWords + static_cast<size_t>(kSortMaxPasses) * tiles * kSortBins;
+    if (maxTilesOut) *maxTilesOut = sortTiles(n);
+    return sortScratchWordsFor(n);
 }
 
 cudaError_t radixSortPairs(uint64_t* keysA, uint32_t* valsA, uint64_t* keysB, uint32_t* valsB, uint32_t n,
@@ -324,11 +328,14 @@ cudaError_t radixSortPairs(uint64_t* keysA, uint32_t* valsA, uint64_t* keysB, ui
     if (e != cudaSuccess) return e;
 
     const size_t smem = sizeof(SortSmem);
-    static bool attrSet[64] = {};
-    if (dev < 64 && !attrSet[dev]) {
+    // The shared-memory attribute is set once per device; host threads that
+    // sort on the same device at once may both set it (the same value), and
+    // the flag is atomic, so neither reads it torn.
+    static std::atomic<bool> attrSet[64] = {};
+    if (dev < 0 || dev >= 64 || !attrSet[dev].load(std::memory_order_acquire)) {
         e = cudaFuncSetAttribute(onesweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
-        attrSet[dev] = true;
+        if (dev >= 0 && dev < 64) attrSet[dev].store(true, std::memory_order_release);
     }
     uint64_t* kin = keysA;
     uint32_t* vin = valsA;

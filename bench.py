@@ -18,11 +18,14 @@ whole particle set, through the library's fused C-ABI step.
   roofline   the gravity kernel (dominant): 23 FLOP per evaluated pair
              interaction (device counter) / CUDA-event launch time, against
              the FP32 FMA throughput measured in this process
-  cpu_baseline  the CPU restatement of the reference algorithm (oracle/) on
-             the host cores, on a bounded sample of the same step
+  cpu_baseline  the reference algorithm's FP64 host path (oracle/, OpenMP
+             on the host cores): two full steps of the same workload
 
---impl reference prints the CPU reference arm (the oracle port) on the same
-workload and metric.  Under torchrun each rank runs an independent replica
+--impl reference prints the CPU reference arm on the same workload and
+metric: full FP64 host steps, W untimed and K timed; beside them, in
+"reference_cuda", the reference's own CUDA kernels (compiled for sm_100 from
+its checkout) stepping the same workload on this GPU, when that build is
+present.  Under torchrun each rank runs an independent replica
 (the path has no cross-GPU exchange; "replicas only"); value aggregates all
 ranks.
 """
@@ -83,7 +86,6 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default block shape of the tree walks")
     ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
                     help="far-field model of the timed steps: 0 monopole (the engine's), 1 + quadrupole")
-    ap.add_argument("--cpu-stride", type=int, default=0, help="group sample stride of the CPU leg (0: auto)")
     return ap.parse_args()
 
 
@@ -235,7 +237,8 @@ def run_gpu(args):
     _, gc = engine.read_device_status()
     grav_ms = g0.elapsed_time(g1) / reps
     inter = gc["gravity_interactions"] / reps
-    fp32_peak = engine.measure_fp32_tflops()
+    fp32_scalar, fp32_packed = engine.measure_fp32_peaks()
+    fp32_peak = max(fp32_scalar, fp32_packed)
     achieved = FLOP_PER_INTERACTION * inter / (grav_ms * 1e-3) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "gravity_traffic.json")
@@ -279,8 +282,9 @@ def run_gpu(args):
         "roofline": {"kernel": "gravity (Barnes-Hut group walk + pair evaluation)", "bound": "fp32",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if fp32_peak else None, "traffic": traffic,
-                     "peak_source": "measured in-process (FP32 FMA kernel); bf16/HBM peaks of "
-                                    "MEASURED_PEAKS.json do not bound this kernel",
+                     "peak_source": "measured in-process: the larger of scalar fmaf (%.1f) and packed "
+                                    "fma.rn.f32x2 (%.1f) FMA chains; the bf16/HBM peaks of MEASURED_PEAKS.json "
+                                    "do not bound this kernel" % (fp32_scalar, fp32_packed),
                      "interactions_per_launch": inter, "launch_ms": grav_ms},
         "step_hbm": step_hbm_roofline(n, ms_max / args.steps),
         "stages": stages,
@@ -777,48 +781,64 @@ def _oracle():
     return oracle
 
 
-def cpu_sampled_step_rate(st, stride, max_dt, steps=1, warmup=0):
-    """Particle-steps/s of the oracle (the reference algorithm restated for the
-    CPU, OpenMP over all host cores) on the full workload, with the four
-    tree-walking stages run on every stride-th group and their time scaled by
-    stride; the O(N) stages (sort, permutation, tree build, EOS, kicks, dt)
-    run in full.  Returns (rate, seconds of CPU work spent, detail)."""
+def cpu_fp64_step_rate(st, max_dt, steps=1, warmup=0):
+    """Particle-steps/s of the reference algorithm's FP64 host path
+    (oracle_step_f64: the reference's stage sequence restated for the CPU, the
+    tree walks with FP64 pair arithmetic and sums, the reference's FP64 EOS,
+    OpenMP over all host cores) on the full workload: every particle, every
+    stage, `warmup` untimed and `steps` timed full steps after the initial
+    forces.  Returns (rate, median step seconds, seconds of CPU work spent)."""
     oracle = _oracle()
     o = oracle.Oracle(st)
-    oracle.set_group_stride(stride)
+    oracle.set_group_stride(1)
     t_all = time.perf_counter()
     o.initial_forces()
-    walk, full = 0.0, 0.0
+    times = []
     for k in range(warmup + steps):
-        t = {}
         c = time.perf_counter()
-        dt, _ = o.reduce_dt(o.prev_dt, max_dt); o.prev_dt = dt
-        o.kick(0.5 * dt); t["kick1"] = time.perf_counter() - c; c = time.perf_counter()
-        o.drift(dt); t["drift"] = time.perf_counter() - c; c = time.perf_counter()
-        o.sort_and_build(); t["build"] = time.perf_counter() - c; c = time.perf_counter()
-        o.pass1(); t["pass1"] = time.perf_counter() - c; c = time.perf_counter()
-        o.eos(); t["eos"] = time.perf_counter() - c; c = time.perf_counter()
-        o.gravity(); t["gravity"] = time.perf_counter() - c; c = time.perf_counter()
-        o.pass2(); t["pass2"] = time.perf_counter() - c; c = time.perf_counter()
-        o.kick(0.5 * dt); o.eos(); t["kick2"] = time.perf_counter() - c
+        o.step_f64(max_dt)
         if k >= warmup:
-            walk += t["drift"] + t["pass1"] + t["gravity"] + t["pass2"]
-            full += t["kick1"] + t["build"] + t["eos"] + t["kick2"]
-    oracle.set_group_stride(1)
-    per_step = (full + stride * walk) / steps
+            times.append(time.perf_counter() - c)
     n = len(st["posX"])
-    return n / per_step, time.perf_counter() - t_all, {"walk_s": walk / steps, "linear_s": full / steps}
+    per_step = statistics.median(times)
+    return n / per_step, per_step, time.perf_counter() - t_all
+
+
+def host_threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
 
 def cpu_baseline(st, args, max_dt):
     n = len(st["posX"])
-    stride = args.cpu_stride or 2
-    rate, spent, det = cpu_sampled_step_rate(st, stride, max_dt, steps=1)
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "1 step of the same N=%d workload: tree walks (drift, pass 1, gravity, pass 2) on every "
-                      "%d-th group of 32, time scaled by %d; sort/permute/build/EOS/kicks/dt in full (%.1f s "
-                      "of CPU work)" % (n, stride, stride, spent)}
+    rate, per_step, spent = cpu_fp64_step_rate(st, max_dt, steps=2)
+    return {"value": rate, "unit": UNIT, "cores": host_threads(), "kind": "port",
+            "sample": "2 full steps (every particle, every stage) of the same N=%d workload after its initial "
+                      "forces, on the reference algorithm's FP64 host path (the oracle's restatement of the "
+                      "reference kernels, FP64 pair arithmetic, OpenMP); median step %.2f s, %.1f s of CPU work"
+                      % (n, per_step, spent)}
+
+
+def reference_cuda(n, st, steps=10, warmup=3):
+    """The reference's own CUDA kernels (engine/sph_gravity.cu + eos.cu,
+    compiled unmodified for sm_100 from the reference checkout into
+    oracle/_ref) stepping the same workload on this GPU, timed with CUDA
+    events over the gpuStepMs span (engine/simulation.cpp:1719-1739)."""
+    cubin = os.path.join(ROOT, "oracle", "_ref", "ref_kernels_sm100.cubin")
+    if not os.path.exists(cubin):
+        return "unavailable: oracle/_ref/ref_kernels_sm100.cubin is absent (it is compiled from the reference " \
+               "checkout, which this machine does not have)"
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return "unavailable: no CUDA device visible"
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import ref_gpu
+        rec = ref_gpu.bench(n, steps, warmup, st=st)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return rec
+    except Exception as exc:                    # report, never fail the CPU arm
+        return "unavailable: %s" % str(exc).splitlines()[0][:200]
 
 
 def run_reference(args):
@@ -829,20 +849,23 @@ def run_reference(args):
     n = args.n
     max_dt = max(1.0e-5, args.max_dt_sec) / 1.0e3
     st, _ = scenarios.differentiated_impact(n_total=n, seed=42)
-    stride = args.cpu_stride or 4
-    rate, spent, det = cpu_sampled_step_rate(st, stride, max_dt, steps=max(args.steps, 1), warmup=max(args.warmup, 0))
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    sample = ("%d warm-up + %d timed steps of the N=%d workload on the CPU restatement of the reference kernels "
-              "(the reference has no CPU kernels of its own): tree walks on every %d-th group of 32, scaled by %d"
-              % (args.warmup, args.steps, n, stride, stride))
+    ref_cuda = reference_cuda(n, st)
+    rate, per_step, spent = cpu_fp64_step_rate(st, max_dt, steps=max(args.steps, 1), warmup=max(args.warmup, 0))
+    cores = host_threads()
+    sample = ("%d warm-up + %d timed full steps (every particle, every stage) of the N=%d workload after its "
+              "initial forces, on the reference algorithm's FP64 host path: the oracle's restatement of the "
+              "reference kernels (the reference has no CPU kernels of its own) with FP64 pair arithmetic and "
+              "sums and the reference's FP64 EOS, OpenMP on %d host threads" % (args.warmup, args.steps, n, cores))
+    cfg = workload_config(n, args.theta)
+    cfg["max_dt_psu"] = max_dt
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": n / rate * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (reference kernels restated; FP64 EOS)", "data": "synthetic",
-        "config": workload_config(n, args.theta),
+        "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (reference algorithm restated; FP64 pair arithmetic and EOS)",
+        "data": "synthetic", "config": cfg,
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "detail": det, "cpu_seconds": spent,
+        "reference_cuda": ref_cuda, "cpu_seconds": spent,
     }))
 
 

@@ -356,8 +356,10 @@ AstraeaStatus astraea_gb300_build_planet(const AstraeaBodySpec* spec, uint32_t p
  * group's pairs of R + J (x_i - c).  Features: (COM - c)/r, dNode/r,
  * S/(M dNode^2) (central second moments), group extent/r.  With
  * gateTolerance > 0 every mode-2 gravity call checks the RMS relative error
- * of gateTargets sampled particles against an FP32 direct sum and, above the
- * tolerance, recomputes plain theta gravity (the call then blocks). */
+ * of gateTargets sampled particles against an FP64 direct sum and, above the
+ * tolerance, recomputes plain theta gravity; the decision is taken on the
+ * device (the plain walk is always launched and returns at once when the
+ * check passed), so the call does not block and can be graph-captured. */
 typedef struct AstraeaFarFieldConfig {
     float thetaFar;          /* opening angle of the far test (default 0.8) */
     float gamma;             /* far test: L1 group extent <= gamma r (default 0.3) */
@@ -408,6 +410,12 @@ AstraeaStatus astraea_gb300_ff_predict(const float* features, uint32_t count, fl
 AstraeaStatus astraea_gb300_ff_get_params(float* params, uint32_t capacity, float* outScale16);
 AstraeaStatus astraea_gb300_ff_set_params(const float* params, uint32_t count, const float* outScale16);
 AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out);
+/* One far-field mode-2 gravity call (current mode must be 2, tree built in
+ * it) with CUDA events between its parts; outMs5 (host) receives the times of
+ * the walk with its pair records, the network on the recorded pairs, the
+ * per-member correction, the FP64 spot check of the gate (0 without a gate)
+ * and the fallback walk (returns at once when the gate passed).  Blocks. */
+AstraeaStatus astraea_gb300_ff_profile(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta, float* outMs5);
 
 /* ---- fused step (no counterpart function in sph_gravity.cuh) ----------- */
 
@@ -486,9 +494,13 @@ AstraeaStatus astraea_gb300_radix_sort_pairs(uint64_t* keysIn, uint64_t* keysOut
  * scratch is a fixed ~2.1 MB array inside the library image, so the call
  * makes no cudaMalloc/cudaFree.  At most 1,048,576 keys (else
  * ASTRAEA_ERR_CAPACITY).  The first call on a device looks up the array's
- * address (once per device; make it before any stream capture).  Calls share
- * the array: calls whose GPU work overlaps race on it.  No counterpart in the
- * reference. */
+ * address (once per device; make it before any stream capture) and keeps it
+ * for the life of the process: cudaDeviceReset between calls is not
+ * supported.  Calls share the array: calls whose GPU work overlaps race on it.
+ * A look-back wait that gives up is reported like the allocating sort's
+ * (ASTRAEA_DEVFLAG_LOOKBACK_TIMEOUT in astraea_gb300_read_device_status, and
+ * ASTRAEA_ERR_DEVICE_TIMEOUT from astraea_gb300_reduce_dt_psu) until
+ * astraea_gb300_reset_device_status.  No counterpart in the reference. */
 AstraeaStatus astraea_gb300_radix_sort_pairs_noalloc(uint64_t* keysIn, uint64_t* keysOut,
                                                      uint32_t* valsIn, uint32_t* valsOut,
                                                      uint32_t n, int endBit);
@@ -543,9 +555,23 @@ AstraeaStatus astraea_gb300_set_stage_timing(int enable);
 AstraeaStatus astraea_gb300_read_stage_times(const AstraeaRadixBvh* bvh, float* outMs, uint32_t capacity,
                                              uint32_t* outCount);
 /* Measured FP32 FMA throughput of the current device in TFLOP/s (the
- * denominator of the gravity kernel's roofline).  Blocks; no engine
- * counterpart. */
+ * denominator of the gravity kernel's roofline): the larger of scalar fmaf
+ * chains and packed fma.rn.f32x2 chains.  Blocks; no engine counterpart. */
 AstraeaStatus astraea_gb300_measure_fp32_tflops(float* outTflops);
+/* The gravity stage (far-field mode 0) with each group's interaction count
+ * written to groupCounts[g] (device, ceil(count / 32) words): the per-group
+ * form of ASTRAEA_COUNTER_GRAVITY_INTERACTIONS, for locating a group whose
+ * interaction set differs from the oracle's.  No engine counterpart. */
+AstraeaStatus astraea_gb300_debug_gravity_group_counts(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                                      uint32_t* groupCounts);
+/* The gravity stage (far-field mode 0) recording, for one group, every node it
+ * takes as a monopole (node index >= 0) and every leaf it reaches (~particle)
+ * into trace[1 ..] in walk order, trace[0] = the number recorded (device,
+ * capacity + 1 words).  Diagnostic; no engine counterpart. */
+AstraeaStatus astraea_gb300_debug_gravity_group_trace(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                                     uint32_t group, int32_t* trace, uint32_t capacity);
+/* Both forms of that measurement (host outputs, TFLOP/s). */
+AstraeaStatus astraea_gb300_measure_fp32_peaks(float* outScalarTflops, float* outPackedTflops);
 AstraeaStatus astraea_gb300_reset_device_status(void);
 /* FP64 direct-sum gravity at `count` listed targets (device indices; device
  * outputs: acc3[3 count] as x, y, z, and phi[count]), over all p->count

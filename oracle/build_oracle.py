@@ -17,6 +17,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+# The reference checkout this recipe compiles from: ASTRAEA_REFERENCE_ENGINE
+# when set, else the checkout's usual place on the build machine.  It is
+# absent on GPU machines; every step that needs it is skipped there.
 REFERENCE_ENGINE = os.environ.get("ASTRAEA_REFERENCE_ENGINE", "/root/reference/engine")
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
@@ -115,6 +118,31 @@ def build_reference_planet(force=False):
         tmp = out + ".tmp%d" % os.getpid()
         _run(["g++"] + CXXFLAGS + ["-I", REFERENCE_ENGINE, srcs[0], srcs[1], "-x", "c++", srcs[2], "-x", "none",
                                    shim, "-o", tmp])
+        os.replace(tmp, out)
+    return out
+
+
+def build_reference_sim(force=False):
+    """The reference engine's own host code (engine/simulation.cpp with
+    planet_builder.cpp, presets.cpp and eos.cu as host C++) run on the CPU
+    behind oracle/ref_sim_harness.cpp: the CUDA runtime calls over host memory,
+    the kernels from the oracle library.  None where the checkout is absent."""
+    srcs = [os.path.join(REFERENCE_ENGINE, f) for f in ("simulation.cpp", "planet_builder.cpp", "presets.cpp",
+                                                         "eos.cu")]
+    cuda_inc = "/usr/local/cuda/include"
+    if not all(os.path.exists(x) for x in srcs) or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        return None
+    lib_dir = os.path.dirname(build_oracle())
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libref_sim.so")
+    shim = os.path.join(HERE, "ref_sim_harness.cpp")
+    if force or _stale(out, srcs + [shim, os.path.join(lib_dir, "liboracle.so")]):
+        tmp = out + ".tmp%d" % os.getpid()
+        flags = [f for f in CXXFLAGS if not f.startswith("-std=")] + ["-std=c++20"]
+        _run(["g++"] + flags + ["-I", os.path.join(ROOT, "include"), "-I", REFERENCE_ENGINE, "-I", cuda_inc, shim,
+                                srcs[1], srcs[2], "-x", "c++", srcs[3], "-x", "none", "-L", lib_dir, "-loracle",
+                                "-Wl,-rpath," + lib_dir, "-Wl,-Bsymbolic", "-o", tmp])
         os.replace(tmp, out)
     return out
 

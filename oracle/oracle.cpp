@@ -626,8 +626,14 @@ void oracle_evaluate_eos(AstraeaParticles* p) {
 // node's central second moments {xx, yy, zz, xy, xz, yz} from
 // oracle_node_moments: Q = 3 S - tr(S) I, r = x_i - COM, the softened 1/r of
 // the monopole, a += G [Q r / r^5 - 5/2 (r.Q.r) r / r^7], phi -= G (r.Q.r) / (2 r^5).
-void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, const float* S6,
-                       uint64_t* interactionsOut) {
+}  // extern "C"
+
+// R = float: the reference kernel's arithmetic.  R = double: the FP64 host
+// path -- the same tree, the same float acceptance tests (so the same
+// interaction set), each pair term and the sums in double.
+template <typename R>
+static void gravityImpl(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, const float* S6,
+                        uint64_t* interactionsOut, uint32_t* groupCounts = nullptr) {
     const uint32_t n = p->count;
     if (n == 0) return;
     if (n == 1) { p->accX[0] = p->accY[0] = p->accZ[0] = p->phiGrav[0] = 0.0f; return; }
@@ -641,8 +647,10 @@ void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float thet
         if (skipGroup(g)) continue;
         const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
         const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
+        const uint64_t totalBefore = total;
         float xi[kGroup], yi[kGroup], zi[kGroup], eI[kGroup], eI2[kGroup];
-        float ax[kGroup] = {}, ay[kGroup] = {}, az[kGroup] = {}, ph[kGroup] = {};
+        R ax[kGroup] = {}, ay[kGroup] = {}, az[kGroup] = {}, ph[kGroup] = {};
+        const R G = static_cast<R>(sizeof(R) == 4 ? static_cast<double>(kGPsuF) : kGPsuD);
         for (int l = 0; l < act; ++l) {
             const uint32_t i = i0 + l;
             xi[l] = p->posX[i]; yi[l] = p->posY[i]; zi[l] = p->posZ[i];
@@ -663,15 +671,15 @@ void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float thet
                     const float eJ = 0.8f * std::fmax(p->h0[j], 1.0e-6f);
                     for (int l = 0; l < act; ++l) {
                         if (i0 + l == j) continue;
-                        const float dx = xi[l] - pxj, dy = yi[l] - pyj, dz = zi[l] - pzj;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        const float eij = 0.5f * (eI[l] + eJ);
-                        const float den = r2 + eij * eij + 1.0e-20f;
-                        const float iR = 1.0f / std::sqrt(den);
-                        const float iR3 = iR * iR * iR;
-                        const float f = -kGPsuF * mj * iR3;
+                        const R dx = R(xi[l]) - R(pxj), dy = R(yi[l]) - R(pyj), dz = R(zi[l]) - R(pzj);
+                        const R r2 = dx * dx + dy * dy + dz * dz;
+                        const R eij = R(0.5f) * (R(eI[l]) + R(eJ));
+                        const R den = r2 + eij * eij + R(1.0e-20f);
+                        const R iR = R(1) / std::sqrt(den);
+                        const R iR3 = iR * iR * iR;
+                        const R f = -G * R(mj) * iR3;
                         ax[l] += f * dx; ay[l] += f * dy; az[l] += f * dz;
-                        ph[l] -= kGPsuF * mj * iR;
+                        ph[l] -= G * R(mj) * iR;
                         ++total;
                     }
                 } else {
@@ -689,13 +697,16 @@ void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float thet
                     }
                     if (!anyOpen || sp >= kStackSize) {
                         for (int l = 0; l < act; ++l) {
-                            const float den = r2s[l] + eI2[l] + 1.0e-20f;
-                            const float iR = 1.0f / std::sqrt(den);
-                            const float iR3 = iR * iR * iR;
-                            const float f = -kGPsuF * nb.m * iR3;
-                            ax[l] += f * dxs[l]; ay[l] += f * dys[l]; az[l] += f * dzs[l];
-                            ph[l] -= kGPsuF * nb.m * iR;
+                            const R dx = R(xi[l]) - R(nb.cx), dy = R(yi[l]) - R(nb.cy), dz = R(zi[l]) - R(nb.cz);
+                            const R r2 = (sizeof(R) == 4) ? R(r2s[l]) : dx * dx + dy * dy + dz * dz;
+                            const R den = r2 + R(eI2[l]) + R(1.0e-20f);
+                            const R iR = R(1) / std::sqrt(den);
+                            const R iR3 = iR * iR * iR;
+                            const R f = -G * R(nb.m) * iR3;
+                            ax[l] += f * dx; ay[l] += f * dy; az[l] += f * dz;
+                            ph[l] -= G * R(nb.m) * iR;
                             if (S6 != nullptr) {
+                                const float iRf = static_cast<float>(iR);
                                 const float* sc = S6 + 6 * static_cast<size_t>(c);
                                 const float tr = sc[0] + sc[1] + sc[2];
                                 const float qxx = kGPsuF * (3.0f * sc[0] - tr), qyy = kGPsuF * (3.0f * sc[1] - tr);
@@ -706,7 +717,7 @@ void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float thet
                                 const float qr1 = qxy * dx + qyy * dy + qyz * dz;
                                 const float qr2 = qxz * dx + qyz * dy + qzz * dz;
                                 const float rqr = dx * qr0 + dy * qr1 + dz * qr2;
-                                const float i2 = iR * iR, i5 = iR * i2 * i2, i7 = i5 * i2;
+                                const float i2 = iRf * iRf, i5 = iRf * i2 * i2, i7 = i5 * i2;
                                 const float t = -2.5f * rqr * i7;
                                 ax[l] += qr0 * i5 + t * dx;
                                 ay[l] += qr1 * i5 + t * dy;
@@ -721,16 +732,33 @@ void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float thet
                 }
             }
         }
+        if (groupCounts != nullptr) groupCounts[g] = static_cast<uint32_t>(total - totalBefore);
         for (int l = 0; l < act; ++l) {
             const uint32_t i = i0 + l;
-            p->accX[i] = ax[l]; p->accY[i] = ay[l]; p->accZ[i] = az[l]; p->phiGrav[i] = ph[l];
+            p->accX[i] = static_cast<float>(ax[l]); p->accY[i] = static_cast<float>(ay[l]);
+            p->accZ[i] = static_cast<float>(az[l]); p->phiGrav[i] = static_cast<float>(ph[l]);
         }
     }
     if (interactionsOut) *interactionsOut = total;
 }
 
+extern "C" {
+void oracle_gravity_ff(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, const float* S6,
+                       uint64_t* interactionsOut) {
+    gravityImpl<float>(p, b, theta, S6, interactionsOut);
+}
+
 void oracle_gravity(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, uint64_t* interactionsOut) {
-    oracle_gravity_ff(p, b, theta, nullptr, interactionsOut);
+    gravityImpl<float>(p, b, theta, nullptr, interactionsOut);
+}
+
+void oracle_gravity_f64(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, uint64_t* interactionsOut) {
+    gravityImpl<double>(p, b, theta, nullptr, interactionsOut);
+}
+
+// The reference kernel with each group's interaction count in groupCounts[g].
+void oracle_gravity_group_counts(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, uint32_t* groupCounts) {
+    gravityImpl<float>(p, b, theta, nullptr, nullptr, groupCounts);
 }
 
 // Central second moments of every internal node, S = sum m (x - c)(x - c)^T,
@@ -1047,10 +1075,15 @@ void oracle_kick_half(AstraeaParticles* p, float hdt, int clampThermal) {
     }
 }
 
+}  // extern "C"
+
 // ------------------------------------------------------------ XSPH drift ----
 // engine/sph_gravity.cu:1376-1489, with neighbours read from the pre-drift
 // positions (the reference kernel reads them while other threads write).
-void oracle_drift(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int useBvh) {
+// R = float: the reference kernel's arithmetic; R = double: the FP64 host
+// path (the same neighbour sets, sums and the position update in double).
+template <typename R>
+static void driftImpl(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int useBvh) {
     const uint32_t n = p->count;
     std::vector<float> nx(p->posX, p->posX + n), ny(p->posY, p->posY + n), nz(p->posZ, p->posZ + n);
     const int G = numGroups(n);
@@ -1060,7 +1093,7 @@ void oracle_drift(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int u
         const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
         const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
         float xi[kGroup], yi[kGroup], zi[kGroup], vxi[kGroup], vyi[kGroup], vzi[kGroup], Hi[kGroup], rhoI[kGroup];
-        float sx[kGroup] = {}, sy[kGroup] = {}, sz[kGroup] = {};
+        R sx[kGroup] = {}, sy[kGroup] = {}, sz[kGroup] = {};
         for (int l = 0; l < act; ++l) {
             const uint32_t i = i0 + l;
             xi[l] = p->posX[i]; yi[l] = p->posY[i]; zi[l] = p->posZ[i];
@@ -1087,24 +1120,33 @@ void oracle_drift(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int u
                         const float r2 = dx * dx + dy * dy + dz * dz;
                         const float Hm = std::fmax(Hi[l], Hj);
                         if (!(r2 < Hm * Hm)) continue;
-                        const float r = std::sqrt(r2);
-                        const float wb = 0.5f * (wendland<float>(r, Hi[l]) + wendland<float>(r, Hj));
-                        const float rb = 0.5f * (rhoI[l] + std::fmax(p->rho[j], 1.0e-9f));
-                        const float co = (p->mass[j] / rb) * wb;
-                        sx[l] += co * (p->velX[j] - vxi[l]);
-                        sy[l] += co * (p->velY[j] - vyi[l]);
-                        sz[l] += co * (p->velZ[j] - vzi[l]);
+                        const R r = (sizeof(R) == 4) ? R(std::sqrt(r2))
+                                                     : std::sqrt(R(dx) * R(dx) + R(dy) * R(dy) + R(dz) * R(dz));
+                        const R wb = R(0.5f) * (wendland<R>(r, R(Hi[l])) + wendland<R>(r, R(Hj)));
+                        const R rb = R(0.5f) * (R(rhoI[l]) + R(std::fmax(p->rho[j], 1.0e-9f)));
+                        const R co = (R(p->mass[j]) / rb) * wb;
+                        sx[l] += co * (R(p->velX[j]) - R(vxi[l]));
+                        sy[l] += co * (R(p->velY[j]) - R(vyi[l]));
+                        sz[l] += co * (R(p->velZ[j]) - R(vzi[l]));
                     }
                 });
         }
         for (int l = 0; l < act; ++l) {
             const uint32_t i = i0 + l;
-            nx[i] = xi[l] + dt * (vxi[l] + 0.25f * sx[l]);
-            ny[i] = yi[l] + dt * (vyi[l] + 0.25f * sy[l]);
-            nz[i] = zi[l] + dt * (vzi[l] + 0.25f * sz[l]);
+            nx[i] = static_cast<float>(R(xi[l]) + R(dt) * (R(vxi[l]) + R(0.25f) * sx[l]));
+            ny[i] = static_cast<float>(R(yi[l]) + R(dt) * (R(vyi[l]) + R(0.25f) * sy[l]));
+            nz[i] = static_cast<float>(R(zi[l]) + R(dt) * (R(vzi[l]) + R(0.25f) * sz[l]));
         }
     }
     std::memcpy(p->posX, nx.data(), n * 4); std::memcpy(p->posY, ny.data(), n * 4); std::memcpy(p->posZ, nz.data(), n * 4);
+}
+
+extern "C" {
+void oracle_drift(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int useBvh) {
+    driftImpl<float>(p, dt, b, useBvh);
+}
+void oracle_drift_f64(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, int useBvh) {
+    driftImpl<double>(p, dt, b, useBvh);
 }
 
 // --------------------------------------------------------------- dt ----
@@ -1147,6 +1189,26 @@ float oracle_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* b
     oracle_evaluate_eos(p);
     oracle_gravity(p, b, theta, nullptr);
     oracle_sph_pass2(p, b);
+    oracle_kick_half(p, 0.5f * dt, 0);
+    oracle_evaluate_eos(p);
+    return dt;
+}
+
+// The FP64 host path of the same step (the CPU baseline): the stages that
+// walk the tree (drift, pass 1, gravity, pass 2) in double over the same
+// neighbour and interaction sets; sort, tree and refit as above; the EOS is
+// the reference's FP64 EOS in both paths.
+float oracle_step_f64(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* b, float prevDt, float maxDt,
+                      float theta) {
+    const float dt = oracle_reduce_dt(p, prevDt, maxDt, nullptr);
+    oracle_kick_half(p, 0.5f * dt, 0);
+    const int useBvh = (b->capacity >= p->count && b->leftChild != nullptr && p->count >= 2u) ? 1 : 0;
+    oracle_drift_f64(p, dt, b, useBvh);
+    oracle_sort_and_build(p, alt, b, nullptr);
+    oracle_sph_pass1_f64(p, b);
+    oracle_evaluate_eos(p);
+    oracle_gravity_f64(p, b, theta, nullptr);
+    oracle_sph_pass2_f64(p, b);
     oracle_kick_half(p, 0.5f * dt, 0);
     oracle_evaluate_eos(p);
     return dt;

@@ -48,14 +48,18 @@ def load(build=True):
             "oracle_evaluate_eos": [P],
             "oracle_gravity": [P, B, f, vp],
             "oracle_gravity_ff": [P, B, f, vp, vp],
+            "oracle_gravity_f64": [P, B, f, vp],
+            "oracle_gravity_group_counts": [P, B, f, vp],
             "oracle_node_moments": [P, B, vp],
             "oracle_direct_gravity_f64": [u32, vp, vp, vp, vp, vp, u32, vp, vp, vp],
             "oracle_sph_pass2": [P, B],
             "oracle_sph_pass2_f64": [P, B],
             "oracle_kick_half": [P, f, ctypes.c_int],
             "oracle_drift": [P, f, B, ctypes.c_int],
+            "oracle_drift_f64": [P, f, B, ctypes.c_int],
             "oracle_reduce_dt": [P, f, f, vp],
             "oracle_step": [P, P, B, f, f, f],
+            "oracle_step_f64": [P, P, B, f, f, f],
             "oracle_pack_render_records": [P, vp, vp, f, f, f],
             "oracle_extract_tracers": [P, vp, u32, f, f, f, f, f, f],
             "oracle_pcls_frame": [P, ctypes.POINTER(abi.PclsFrameInfo), vp, ctypes.c_size_t],
@@ -70,6 +74,7 @@ def load(build=True):
             getattr(_lib, name).argtypes = args
         _lib.oracle_reduce_dt.restype = f
         _lib.oracle_step.restype = f
+        _lib.oracle_step_f64.restype = f
         _lib.oracle_pcls_frame.restype = ctypes.c_size_t
         _lib.oracle_set_group_stride.argtypes = [ctypes.c_int]
         _lib.oracle_cold_energy.restype = ctypes.c_double
@@ -400,16 +405,26 @@ class Oracle:
         s = self.p.struct()
         self.lib.oracle_evaluate_eos(ctypes.byref(s))
 
-    def gravity(self, theta=0.5, far_field=0):
-        """far_field 0: the reference kernel; 1: + quadrupole of accepted nodes."""
+    def gravity(self, theta=0.5, far_field=0, f64=False):
+        """far_field 0: the reference kernel; 1: + quadrupole of accepted nodes.
+        f64: the same interaction set with FP64 pair arithmetic and sums."""
         s = self.p.struct()
         cnt = np.zeros(1, np.uint64)
-        if far_field == 0:
+        if f64:
+            self.lib.oracle_gravity_f64(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(cnt))
+        elif far_field == 0:
             self.lib.oracle_gravity(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(cnt))
         else:
             S6 = self.node_moments()
             self.lib.oracle_gravity_ff(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(S6), _ptr(cnt))
         return int(cnt[0])
+
+    def gravity_group_counts(self, theta=0.5):
+        """The reference kernel; returns each group's interaction count."""
+        s = self.p.struct()
+        out = np.zeros(max((self.p.count + 31) // 32, 1), np.uint32)
+        self.lib.oracle_gravity_group_counts(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(out))
+        return out[: (self.p.count + 31) // 32].astype(np.int64)
 
     def node_moments(self):
         """Central second moments of the internal nodes, float32 (n-1, 6)."""
@@ -426,10 +441,11 @@ class Oracle:
         s = self.p.struct()
         self.lib.oracle_kick_half(ctypes.byref(s), float(half_dt), int(bool(clamp_thermal)))
 
-    def drift(self, dt):
+    def drift(self, dt, f64=False):
         s = self.p.struct()
         use = 1 if self.p.count >= 2 else 0
-        self.lib.oracle_drift(ctypes.byref(s), float(dt), ctypes.byref(self.bvh.s), use)
+        (self.lib.oracle_drift_f64 if f64 else self.lib.oracle_drift)(ctypes.byref(s), float(dt),
+                                                                      ctypes.byref(self.bvh.s), use)
 
     def reduce_dt(self, prev_dt, max_dt):
         s = self.p.struct()
@@ -444,6 +460,20 @@ class Oracle:
         self.eos()
         self.gravity(theta)
         self.pass2()
+
+    def step_f64(self, max_dt, theta=0.5):
+        """The FP64 host path of one step (oracle_step_f64), in C."""
+        sp, sa = self._pp()
+        dt = self.lib.oracle_step_f64(ctypes.byref(sp), ctypes.byref(sa), ctypes.byref(self.bvh.s),
+                                      float(self.prev_dt), float(max_dt), float(theta))
+        by_ptr = {}
+        for hp in (self.p, self.alt):
+            for a in hp.arrays.values():
+                by_ptr[a.ctypes.data] = a
+        self.p.rebind(sp, by_ptr)
+        self.alt.rebind(sa, by_ptr)
+        self.prev_dt = float(dt)
+        return float(dt)
 
     def step(self, max_dt, theta=0.5):
         dt, _ = self.reduce_dt(self.prev_dt, max_dt)

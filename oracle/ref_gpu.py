@@ -300,10 +300,13 @@ def golden(out_path):
     print("wrote", out_path, len(rec), "arrays")
 
 
-def bench(n, steps, warmup, theta=0.5):
+def bench(n, steps, warmup, theta=0.5, st=None):
+    """Step time of the reference's kernels on the workload; returns the
+    record that `python ref_gpu.py bench` prints."""
     import torch
     from astraea_gb300 import scenarios
-    st, _ = scenarios.differentiated_impact(n_total=n, seed=42)
+    if st is None:
+        st, _ = scenarios.differentiated_impact(n_total=n, seed=42)
     e = RefEngine(n)
     e.p.upload(st)
     e.alt.count = n
@@ -341,10 +344,10 @@ def bench(n, steps, warmup, theta=0.5):
     for k, nm in enumerate(names):
         stage_ms[nm] = ev[k].elapsed_time(ev[k + 1])
     med = float(np.median(times))
-    print(json.dumps({"impl": "reference CUDA kernels (sm_100 cubin) on this GPU", "n": n, "steps": steps,
-                      "warmup": warmup, "ms_per_step_median": med, "ms_per_step_mean": float(np.mean(times)),
-                      "particle_steps_per_s": n / (med / 1e3), "stage_ms": stage_ms,
-                      "note": "CUB SortPairs replaced by torch.sort(stable=True), the same stable order"}))
+    return {"impl": "reference CUDA kernels (sm_100 cubin) on this GPU", "n": n, "steps": steps,
+            "warmup": warmup, "ms_per_step_median": med, "ms_per_step_mean": float(np.mean(times)),
+            "particle_steps_per_s": n / (med / 1e3), "stage_ms": stage_ms,
+            "note": "CUB SortPairs replaced by torch.sort(stable=True), the same stable order"}
 
 
 if __name__ == "__main__":
@@ -353,4 +356,4 @@ if __name__ == "__main__":
     elif sys.argv[1] == "golden_render":
         golden_render(sys.argv[2])
     elif sys.argv[1] == "bench":
-        bench(int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))
+        print(json.dumps(bench(int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))))

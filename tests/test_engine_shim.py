@@ -1,8 +1,8 @@
 """The C++ drop-in for engine/sph_gravity.cu (csrc/shim/sph_gravity_gb300.cpp).
 
-Where the ASTRAEA engine's sources are available (their path is taken from
-ASTRAEA_REFERENCE_ENGINE, default the reference checkout of this build
-machine), this compiles the shim against the engine's own headers -- its
+Where the ASTRAEA engine's sources are available (their path comes from the
+oracle's build recipe, oracle/build_oracle.py: ASTRAEA_REFERENCE_ENGINE, else
+the checkout that recipe builds from), this compiles the shim against the engine's own headers -- its
 static_asserts check the descriptor layouts -- links it with
 libastraea_gb300, compiles the engine's Simulation (engine/simulation.cpp)
 to an object file, and checks that every astraea::cuda symbol that object
@@ -16,8 +16,9 @@ import subprocess
 
 import pytest
 
+from build_oracle import REFERENCE_ENGINE as ENGINE
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-ENGINE = os.environ.get("ASTRAEA_REFERENCE_ENGINE", "/root/reference/engine")
 CUDA_INC = "/usr/local/cuda/include"
 SHIM = os.path.join(ROOT, "astraea-impact-sim_gb300", "csrc", "shim", "sph_gravity_gb300.cpp")
 LIBDIR = os.path.join(ROOT, "astraea-impact-sim_gb300")

@@ -15,6 +15,7 @@ import pytest
 
 import oracle
 from astraea_gb300 import abi, scenarios
+from conftest import rel_rms
 
 
 def random_params(seed=3, scale=0.3):
@@ -139,6 +140,41 @@ def test_gpu_gate_falls_back_to_plain_walk():
     plain = p.download()
     for f in ("accX", "accY", "accZ", "phiGrav"):
         assert np.array_equal(gated[f], plain[f]), f
+
+
+@pytest.mark.gpu
+def test_gpu_gate_that_passes_keeps_the_learned_result():
+    """A gate whose tolerance the spot check meets: the plain walk launched
+    after it returns at once (the decision is on the device), so the result is
+    the learned mode's own and no fallback is counted."""
+    from astraea_gb300 import engine
+    st = impact(16384, 23)
+    n = len(st["posX"])
+    engine.ff_init(7)
+    p, alt, bvh = engine.DeviceParticles(n), engine.DeviceParticles(n), engine.DeviceBvh(n)
+    p.upload(st)
+    alt.count = n
+    before = engine.ff_stats()["fallbacks"]
+    try:
+        engine.set_far_field(2)
+        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=0.0)
+        engine.sort_and_build_bvh(p, alt, bvh)
+        engine.gravity_barnes_hut(p, bvh, 0.5)
+        ungated = p.download()
+        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=10.0, gate_targets=32)
+        engine.gravity_barnes_hut(p, bvh, 0.5)
+        gated = p.download()
+    finally:
+        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=0.0)
+        engine.set_far_field(0)
+    stats = engine.ff_stats()
+    assert stats["fallbacks"] == before and 0.0 < stats["lastGateRms"] < 10.0
+    engine.gravity_barnes_hut(p, bvh, 0.5)                    # the plain walk (mode 0 tree is the same)
+    plain = p.download()
+    for f in ("accX", "accY", "accZ"):
+        # the correction sums are float atomics (order-dependent in the last bits)
+        assert rel_rms(gated[f], ungated[f]) < 1e-6, f
+        assert rel_rms(gated[f], plain[f]) > 1e-5, f
 
 
 @pytest.mark.gpu

@@ -6,8 +6,10 @@ or a host that forbids allocation after start-up).  Its scratch is a fixed
 array inside the library image, shared by all calls.  These checks run it
 twice in a row on different inputs and compare with the allocating
 astraea_gb300_radix_sort_pairs (an integer sort: the outputs must be equal),
-show that a repeated call leaves free device memory unchanged, and that a
-call above the fixed limit is refused with ASTRAEA_ERR_CAPACITY.
+show that a repeated call leaves free device memory unchanged, that a call
+above the fixed limit is refused with ASTRAEA_ERR_CAPACITY, and that a
+look-back wait that gives up inside it is reported by the library's status
+calls (its result is then unsorted, so it must not pass silently).
 
 The file is named to be collected last, so a stop-at-first-failure run has
 already run every other test when it gets here.
@@ -18,7 +20,7 @@ import numpy as np
 import pytest
 import torch
 
-from astraea_gb300 import abi, engine
+from astraea_gb300 import abi, engine, scenarios
 
 pytestmark = pytest.mark.gpu
 MAX_KEYS = 1 << 20
@@ -78,3 +80,42 @@ def test_noalloc_sort_refuses_more_than_its_limit():
         dummy.data_ptr(), dummy.data_ptr(), dummy.data_ptr(), dummy.data_ptr(), MAX_KEYS + 1, 64)
     assert rc == 2
     assert b"limit" in abi.load_library().astraea_gb300_last_error()
+
+
+def test_noalloc_sort_reports_a_lookback_timeout():
+    """With a one-poll look-back limit some tiles give up waiting for their
+    predecessors; every store stays inside the output (the sort checks each
+    destination), the result is then not sorted, and the flag must reach
+    read_device_status and the blocking dt call.  A result without the flag
+    must be exactly sorted."""
+    lib = abi.load_library()
+    keys, vals = keys_and_values(14, MAX_KEYS, 64)
+    kn = keys.cpu().numpy().view(np.uint64)
+    expect = vals.cpu().numpy().view(np.uint32)[np.argsort(kn, kind="stable")]
+    engine.reset_device_status()
+    flagged_calls = 0
+    try:
+        abi.check(lib.astraea_gb300_set_lookback_spin_limit(1))
+        for _ in range(20):
+            _, v = sort_noalloc(keys, vals, 64)
+            flags, _ = engine.read_device_status()
+            if flags & abi.DEVFLAG_LOOKBACK_TIMEOUT:
+                flagged_calls += 1
+                break
+            assert np.array_equal(v.cpu().numpy().view(np.uint32), expect)
+    finally:
+        abi.check(lib.astraea_gb300_set_lookback_spin_limit(0))   # back to the default limit
+    assert flagged_calls == 1
+    st, _ = scenarios.two_granite_spheres(n_target=48, n_impactor=16, seed=3)
+    p = engine.DeviceParticles(64)
+    p.upload(st)
+    with pytest.raises(abi.AstraeaError) as ei:
+        engine.reduce_dt_psu(p, 0.0, 1e-3)
+    assert ei.value.status == 4
+    engine.reset_device_status()
+    flags, _ = engine.read_device_status()
+    assert not flags & abi.DEVFLAG_LOOKBACK_TIMEOUT
+    _, v = sort_noalloc(keys, vals, 64)
+    flags, _ = engine.read_device_status()
+    assert not flags & abi.DEVFLAG_LOOKBACK_TIMEOUT
+    assert np.array_equal(v.cpu().numpy().view(np.uint32), expect)
