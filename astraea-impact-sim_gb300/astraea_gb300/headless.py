@@ -231,6 +231,10 @@ def run_headless(preset="LivingGaiaAsteroidCataclysm", particles=100000, steps=1
     l_ref = max(float(np.linalg.norm(l0)), m_tot_kg * r_scale * v_esc * 1.0e-6)
     l_rel = float(np.linalg.norm(dl) / l_ref)
     res = {"preset": preset, "particles": sim.p.count, "tracers": info["tracers"], "steps": steps,
+           "energy_j_t0": e0, "energy_j_t1": energy(tel), "radiated_j": e_rad,
+           "momentum_t0": p0.tolist(), "momentum_t1": (np.array(tel["momentumPsu"]) * M_UNIT * V_UNIT).tolist(),
+           "angular_momentum_t0": l0.tolist(),
+           "angular_momentum_t1": (np.array(tel["angularMomentumPsu"]) * L_ANG_UNIT).tolist(),
            "sim_time_sec": sim.sim_time * T_UNIT, "energy_drift_rel": drift, "dp_rel": p_rel, "dl_rel": l_rel,
            "max_temp_k": tel["maxTempK"], "max_pressure_gpa": tel["maxPressureGPa"], "finite": finite,
            "load_s": load_s, "step_s": step_s}

@@ -17,7 +17,11 @@ the CUDA runtime, the oracle as its kernels).  Recorded:
   positions, velocities, density, energy, h and v_rms / v_esc;
 * AC-2 (tests/cpp/test_planet_builder.cpp:329-361): relaxBody(0, 80) of each
   of the six archetypes in the test's own two-body scenario, the engine's
-  v_rms / v_esc.
+  v_rms / v_esc;
+* AC-5 (tests/cpp/test_conservation.cpp:123-158): the engine's own
+  conservation audit -- EarthTheiaMoonForming, 20,000 particles, loadScenario
+  with its relaxation, 150 steps -- its snapshots at the start and the end and
+  the drifts the test and --verify-conservation compute from them.
 
 Usage: python tests/golden/make_sim_golden.py [out.npz]
 """
@@ -132,6 +136,16 @@ def main(out_path):
         ac2.append(vr)
         print("AC-2 archetype %d: v_rms / v_esc = %.3e" % (arch, vr))
     out["ac2_vrms"] = np.array(ac2)
+
+    cons = ref_sim.RefSimulation(25000)
+    cons.load_preset("EarthTheiaMoonForming", 20000, -1, 42)
+    t0 = cons.telemetry()
+    for _ in range(150):
+        cons.step(5.0)
+    t1 = cons.telemetry()
+    out["ac5_t0"] = np.array([t0[k] for k in ref_sim.SNAPSHOT_FIELDS])
+    out["ac5_t1"] = np.array([t1[k] for k in ref_sim.SNAPSHOT_FIELDS])
+    print("AC-5 engine: energy drift %.3e, sim time %.1f s" % (t1["energyDriftRel"], t1["simTimeSec"]))
     np.savez_compressed(out_path, **out)
     print("wrote", out_path, len(out), "arrays")
 

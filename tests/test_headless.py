@@ -52,14 +52,47 @@ def test_kepler_placement_reaches_the_requested_contact_speed():
     assert kepler_contact_speed(mtot, rc, d0, vrad, vperp) == pytest.approx(vc, rel=1e-12)
 
 
+def ac5_drifts(e0, e1, e_rad, p0, p1, l0, l1):
+    """The drifts tests/cpp/test_conservation.cpp:123-158 computes."""
+    cfg = headless.preset_config("EarthTheiaMoonForming", 20000)
+    m_kg = cfg["target"].massKg + cfg["impactor"].massKg
+    v_esc = math.sqrt(2.0 * 6.67430e-11 * m_kg / (1.4 * 6.371e6))
+    de = (e1 + e_rad - e0) / abs(e0)
+    dp = float(np.linalg.norm(np.subtract(p1, p0))) / (m_kg * v_esc)
+    dl = float(np.linalg.norm(np.subtract(l1, l0))) / float(np.linalg.norm(l0))
+    return de, dp, dl
+
+
 @pytest.mark.gpu
-def test_gpu_conservation_audit_earth_theia_20k():
+def test_gpu_conservation_audit_earth_theia_20k(golden_dir):
+    """AC-5 on the device path, against the engine's own audit of the same
+    scenario (tests/golden/sim_reference.npz: engine/simulation.cpp run on
+    the CPU with the oracle's kernels): both pass the test's thresholds, the
+    loaded scenarios have the same initial energy to 1e-3 and the drifts agree
+    to within a tenth of each threshold."""
     res = headless.run_headless("EarthTheiaMoonForming", particles=20000, steps=150, dt_max_sec=5.0, verify=True)
     print(res)
     assert res["particles"] == 20000 and res["finite"]
     assert abs(res["energy_drift_rel"]) < 0.01
     assert res["dp_rel"] < 1.0e-4 and res["dl_rel"] < 0.005
     assert res["ok"]
+    g = np.load(golden_dir + "/sim_reference.npz")
+    names = ["frameSeq", "simTimeSec", "dtSec", "outcome", "kineticEnergyJ", "potentialEnergyJ", "internalEnergyJ",
+             "radiatedEnergyJ", "totalEnergyJ", "initialTotalEnergyJ", "energyDriftRel", "momentumX", "momentumY",
+             "momentumZ", "angularMomentumX", "angularMomentumY", "angularMomentumZ"]
+    t0 = dict(zip(names, g["ac5_t0"]))
+    t1 = dict(zip(names, g["ac5_t1"]))
+    mom = lambda t: [t["momentumX"], t["momentumY"], t["momentumZ"]]
+    ang = lambda t: [t["angularMomentumX"], t["angularMomentumY"], t["angularMomentumZ"]]
+    engine_d = ac5_drifts(t0["totalEnergyJ"], t1["totalEnergyJ"], t1["radiatedEnergyJ"], mom(t0), mom(t1), ang(t0),
+                          ang(t1))
+    ours = ac5_drifts(res["energy_j_t0"], res["energy_j_t1"], res["radiated_j"], res["momentum_t0"],
+                      res["momentum_t1"], res["angular_momentum_t0"], res["angular_momentum_t1"])
+    print("AC-5 drifts (energy, dP, dL): device %s, engine %s" % (ours, engine_d))
+    assert abs(res["energy_j_t0"] - t0["totalEnergyJ"]) <= 1e-3 * abs(t0["totalEnergyJ"])
+    for mine, ref, thr in zip(ours, engine_d, (0.01, 1e-4, 0.005)):
+        assert abs(ref) < thr and abs(mine) < thr
+        assert abs(mine - ref) < 0.1 * thr
 
 
 @pytest.mark.gpu
