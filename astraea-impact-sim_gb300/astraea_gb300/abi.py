@@ -77,7 +77,8 @@ DEVFLAG_STACK_OVERFLOW = 0x4
 COUNTERS = ["gravity_interactions", "gravity_node_tests", "neighbor_entries", "gravity_rounds",
             "gravity_stack_peak", "fallback_walks", "neighbor_candidates", "gravity_undecided"]
 # astraea_gb300_read_device_counters: the eight above, then the SPH pair counts
-ALL_COUNTERS = COUNTERS + ["pass1_pairs", "pass2_pairs", "drift_pairs"]
+ALL_COUNTERS = COUNTERS + ["pass1_pairs", "pass2_pairs", "drift_pairs", "gravity_group_evals",
+                           "gravity_bucket_leaves"]
 # astraea_gb300_read_stage_times order (ASTRAEA_STAGE_*)
 STAGES = ["refresh", "kick", "drift", "sort", "permute", "refit", "neighbours", "pass1", "eos", "gravity",
           "pass2", "kick_eos"]
@@ -230,6 +231,9 @@ SIGNATURES = [
     ("astraea_gb300_debug_gravity_group_trace", [_P, _B, _F, _U32, _VP, _U32], ctypes.c_int),
     ("astraea_gb300_set_lookback_spin_limit", [_U32], ctypes.c_int),
     ("astraea_gb300_set_far_field", [ctypes.c_int], ctypes.c_int),
+    ("astraea_gb300_set_far_field_expansion", [_U32, _F], ctypes.c_int),
+    ("astraea_gb300_autotune_expansion", [_P, _B, _F, _VP, _U32, ctypes.POINTER(_U32), ctypes.POINTER(_F)],
+     ctypes.c_int),
     ("astraea_gb300_debug_lookback_probe", [_U32, ctypes.POINTER(_U32)], ctypes.c_int),
 ]
 EXPORTED_SYMBOLS = [name for name, _, _ in SIGNATURES]

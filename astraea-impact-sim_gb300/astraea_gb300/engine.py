@@ -574,8 +574,26 @@ def set_stream(stream):
 
 
 def set_far_field(mode):
-    """0: monopole (the engine's kernel), 1: + quadrupole, 2: + learned correction."""
+    """0: monopole (the engine's kernel), 1: + quadrupole, 2: + learned
+    correction, 3: quadrupole with leaf buckets and group expansion."""
     abi.check(lib().astraea_gb300_set_far_field(int(mode)))
+
+
+def autotune_expansion(p, bvh, theta, candidates=(8, 16, 24, 32)):
+    """Far-field mode 3: times the gravity for each candidate leaf bucket and
+    keeps the fastest; returns (bucket, {candidate: ms})."""
+    c = (ctypes.c_uint32 * len(candidates))(*candidates)
+    ms = (ctypes.c_float * len(candidates))()
+    out = ctypes.c_uint32(0)
+    sp = p.struct()
+    abi.check(lib().astraea_gb300_autotune_expansion(ctypes.byref(sp), ctypes.byref(bvh.s), float(theta), c,
+                                                    len(candidates), ctypes.byref(out), ms))
+    return out.value, dict(zip(candidates, list(ms)))
+
+
+def set_far_field_expansion(leaf_bucket=16, gamma=0.3):
+    """Far-field mode 3: leaf bucket size (0..32) and the group-expansion gamma."""
+    abi.check(lib().astraea_gb300_set_far_field_expansion(int(leaf_bucket), float(gamma)))
 
 
 def set_lookback_spin_limit(limit):

@@ -28,7 +28,10 @@ namespace {
 thread_local std::string g_lastError;
 std::atomic<cudaStream_t> g_stream{nullptr};
 std::atomic<uint32_t> g_spinLimit{1u << 22};
-std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: + quadrupole, 2: + learned correction
+std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: + quadrupole, 2: + learned correction,
+                                  // 3: quadrupole + leaf buckets + group expansion of far nodes
+std::atomic<uint32_t> g_leafBucket{16};      // mode 3: leaf bucket (particles)
+std::atomic<float> g_expandGamma{0.3f};      // mode 3: group radius <= gamma |c - COM| takes the expansion
 std::atomic<bool> g_stageTiming{false};   // events between the fused step's stages
 constexpr int kStageCount = ASTRAEA_STAGE_COUNT;
 std::mutex g_mutex;
@@ -350,9 +353,9 @@ AstraeaStatus ffWalk(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta
 }
 
 // Gravity of far-field mode 2: walk, network on the recorded pairs,
-// per-member correction, and (gateTolerance > 0) the gate: an FP64 direct-sum
-// spot check of gateTargets particles decides on the device whether the plain
-// walk at theta that follows runs or returns at once.  No host round trip, so
+// per-member correction, and (gateTolerance > 0) the gate: a direct-sum spot
+// check (FP32 pair terms, FP64 sums) of gateTargets particles decides on the
+// device whether the plain walk at theta that follows runs or returns at once.  No host round trip, so
 // a gated step can be captured in a CUDA graph.
 // ev (optional, 6 events): recorded before the walk, the network, the
 // correction, the spot check, the fallback walk and at the end.
@@ -390,6 +393,19 @@ AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, flo
     }
     mark(5);
     return ASTRAEA_OK;
+}
+
+// The gravity walk of far-field modes 0, 1 and 3 on a built workspace.
+cudaError_t modeGravity(const AstraeaParticles& p, const Work& w0, uint32_t n, float theta, int mode, bool moments,
+                        int sms, cudaStream_t st, int warps) {
+    if (mode == 3 && moments) {
+        Work w = w0;
+        w.leafBucket = g_leafBucket.load();
+        const float gm = g_expandGamma.load();
+        w.expandGamma2 = gm * gm;
+        return launchGravity(p, w, n, theta, true, sms, st, nullptr, warps, true);
+    }
+    return launchGravity(p, w0, n, theta, moments && mode == 1, sms, st, nullptr, warps);
 }
 
 uint32_t* livingPtr(const AstraeaRadixBvh* bvh, Workspace* ws) {
@@ -494,8 +510,16 @@ AstraeaStatus astraea_gb300_set_stream(void* s) {
 }
 
 AstraeaStatus astraea_gb300_set_far_field(int mode) {
-    if (mode < 0 || mode > 2) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0, 1 or 2");
+    if (mode < 0 || mode > 3) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0, 1, 2 or 3");
     g_farField.store(mode);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_set_far_field_expansion(uint32_t leafBucket, float gamma) {
+    if (leafBucket > 32u) return fail(ASTRAEA_ERR_INVALID, "leaf bucket must be at most 32 particles");
+    if (!(gamma >= 0.0f && gamma < 1.0f)) return fail(ASTRAEA_ERR_INVALID, "gamma must be in [0, 1)");
+    g_leafBucket.store(leafBucket);
+    g_expandGamma.store(gamma);
     return ASTRAEA_OK;
 }
 
@@ -684,13 +708,13 @@ AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const Astrae
     AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, stream()));
     const int mode = g_farField.load();
     if (mode != 0 && !ws->momentsBuilt)
-        return fail(ASTRAEA_ERR_INVALID, "far-field modes 1 and 2 need a tree built in that mode");
+        return fail(ASTRAEA_ERR_INVALID, "far-field modes 1, 2 and 3 need a tree built in that mode");
     if (mode == 2) {
         s = learnedGravity(p, ws, n, theta, true);
         if (s != ASTRAEA_OK) return s;
     } else {
-        AG_LAUNCH(launchGravity(*p, ws->w, n, theta, mode == 1, smCount(), stream(), nullptr,
-                                static_cast<int>(tuningFor(n).gravityWarps)));
+        AG_LAUNCH(modeGravity(*p, ws->w, n, theta, mode, true, smCount(), stream(),
+                              static_cast<int>(tuningFor(n).gravityWarps)));
     }
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
@@ -961,6 +985,8 @@ AstraeaStatus astraea_gb300_ff_configure(const AstraeaFarFieldConfig* cfg) {
     if (cfg == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
     if (!(cfg->thetaFar > 0.0f) || !(cfg->gamma > 0.0f) || !(cfg->gateTolerance >= 0.0f) || cfg->pairsPerGroup == 0u)
         return fail(ASTRAEA_ERR_INVALID, "ff_configure: thetaFar, gamma, pairsPerGroup must be > 0");
+    if (cfg->gateTargets > ff::kGateMaxTargets)
+        return fail(ASTRAEA_ERR_INVALID, "ff_configure: gateTargets must be <= 1024");
     FfState* f = nullptr;
     AstraeaStatus s = ffState(&f);
     if (s != ASTRAEA_OK) return s;
@@ -1215,6 +1241,55 @@ AstraeaStatus astraea_gb300_autotune(AstraeaParticles* p, const AstraeaRadixBvh*
     return ASTRAEA_OK;
 }
 
+AstraeaStatus astraea_gb300_autotune_expansion(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                               const uint32_t* candidates, uint32_t count, uint32_t* outBucket,
+                                               float* outMs) {
+    if (p == nullptr || bvh == nullptr || candidates == nullptr || count == 0u || outBucket == nullptr)
+        return fail(ASTRAEA_ERR_INVALID, "null argument");
+    const uint32_t n = p->count;
+    if (n < 2u) return ASTRAEA_OK;
+    Workspace* ws = nullptr;
+    AstraeaStatus s = builtWorkspace(bvh, n, &ws);
+    if (s != ASTRAEA_OK) return s;
+    if (!ws->momentsBuilt) return fail(ASTRAEA_ERR_INVALID, "far-field mode 3 needs a tree built in that mode");
+    for (uint32_t k = 0; k < count; ++k)
+        if (candidates[k] > 32u) return fail(ASTRAEA_ERR_INVALID, "leaf bucket must be at most 32 particles");
+    cudaStream_t st = stream();
+    AG_LAUNCH(launchRefreshLeaves(*p, ws->w, n, false, st));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    AG_CUDA(cudaEventCreate(&e0));
+    AG_CUDA(cudaEventCreate(&e1));
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } guard{e0, e1};
+    const int sms = smCount(), warps = static_cast<int>(tuningFor(n).gravityWarps);
+    const uint32_t keep = g_leafBucket.load();
+    float best = 3.0e38f;
+    uint32_t bestBucket = keep;
+    for (uint32_t k = 0; k < count; ++k) {
+        g_leafBucket.store(candidates[k]);
+        auto launch = [&] { return modeGravity(*p, ws->w, n, theta, 3, true, sms, st, warps); };
+        AG_LAUNCH(launch());                         // warm-up
+        float ms = 3.0e38f;
+        for (int r = 0; r < 3; ++r) {
+            AG_CUDA(cudaEventRecord(e0, st));
+            AG_LAUNCH(launch());
+            AG_CUDA(cudaEventRecord(e1, st));
+            AG_CUDA(cudaEventSynchronize(e1));
+            float t = 0.0f;
+            AG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+            ms = std::min(ms, t);
+        }
+        if (outMs != nullptr) outMs[k] = ms;
+        if (ms < best) { best = ms; bestBucket = candidates[k]; }
+    }
+    g_leafBucket.store(bestBucket);
+    *outBucket = bestBucket;
+    ws->stepCacheValid = false;
+    return ASTRAEA_OK;
+}
+
 AstraeaStatus astraea_gb300_get_tuning(uint32_t count, AstraeaTuning* out) {
     if (out == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
     *out = tuningFor(count);
@@ -1364,8 +1439,8 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
         s = learnedGravity(p, ws, n, theta, true);
         if (s != ASTRAEA_OK) return s;
     } else {
-        AG_LAUNCH(launchGravity(*p, w, n, theta, ws->momentsBuilt && g_farField.load() == 1, sms, st, nullptr,
-                                static_cast<int>(tune.gravityWarps)));
+        AG_LAUNCH(modeGravity(*p, w, n, theta, g_farField.load(), ws->momentsBuilt, sms, st,
+                              static_cast<int>(tune.gravityWarps)));
     }
     marks.mark(ASTRAEA_STAGE_PASS2);
     AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));

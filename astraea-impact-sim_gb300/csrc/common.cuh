@@ -52,7 +52,9 @@ enum Counter : int {
     kCntPass1Pairs = 8,            // pairs inside pass 1's radius (r < 2 h_i)
     kCntPass2Pairs = 9,            // pairs inside pass 2's radius (r < max(2 h_i, 2 h_j))
     kCntDriftPairs = 10,           // pairs inside the drift's radius
-    kCntCount = 11
+    kCntGravityGroupEvals = 11,    // far nodes taken by a group's expansion (far-field mode 3)
+    kCntGravityBucketLeaves = 12,  // particle-particle terms from leaf buckets (far-field mode 3)
+    kCntCount = 13
 };
 
 struct DevStatus {
@@ -544,6 +546,8 @@ struct Work {
     uint32_t traceGroup;   //   traceGroup accepts in the gravity walk, appended in walk order (diagnostic)
     uint32_t traceCap;
     const uint32_t* runIf; // null, or a device word: the gravity kernel returns at once while it is 0
+    uint32_t leafBucket;   // far-field mode 3: opened nodes of at most this many particles are evaluated P-P
+    float expandGamma2;    // far-field mode 3: gamma^2 of the group-expansion test
 };
 
 // Indices into Work::words.

@@ -46,7 +46,7 @@ constexpr int kGravList = 64;
 // member on ties) and, in .w, that projection measured from the group-box
 // centre.  und[] holds the compacted undecided nodes of one walk round; the
 // same storage holds the member positions while dirPos is computed.
-template <bool kInside, bool kQuad>
+template <bool kInside, bool kQuad, bool kExpand = false>
 struct __align__(16) GravWarpSmem {
     int stack[kGravStack];
     float mlist[(kQuad ? 20 : 8) * (kGravList / 2)];
@@ -56,7 +56,24 @@ struct __align__(16) GravWarpSmem {
     float4 und[32];                    // {com.x, com.y, com.z, dNode^2}
     float4 undMin[kInside ? 32 : 1];
     float4 undMax[kInside ? 32 : 1];
+    // far-field mode 3 only; last, and whole float4s, so the arrays above
+    // keep the 16-byte alignment of their vector loads in every variant
+    float4 flist4[kExpand ? 5 * (kGravList / 2) : 1];   // far nodes of the group expansion (mlist layout)
+    float4 facc4[kExpand ? 5 : 1];                      // the group's expansion coefficients (see farTaylor)
 };
+// the vector loads of the lists (16 bytes) and of peps (8 bytes)
+template <bool kInside, bool kQuad, bool kExpand>
+constexpr bool gravSmemAligned() {
+    using S = GravWarpSmem<kInside, kQuad, kExpand>;
+    return offsetof(S, mlist) % 16 == 0 && offsetof(S, plist) % 16 == 0 && offsetof(S, peps) % 16 == 0 &&
+           offsetof(S, dirPos) % 16 == 0 && offsetof(S, und) % 16 == 0 && offsetof(S, undMin) % 16 == 0 &&
+           offsetof(S, undMax) % 16 == 0 && offsetof(S, flist4) % 16 == 0 && offsetof(S, facc4) % 16 == 0 &&
+           sizeof(S) % 16 == 0;
+}
+static_assert(gravSmemAligned<false, false, false>() && gravSmemAligned<true, false, false>() &&
+              gravSmemAligned<false, true, false>() && gravSmemAligned<true, true, false>() &&
+              gravSmemAligned<false, true, true>() && gravSmemAligned<true, true, true>(),
+              "gravity shared-memory layout must keep 16-byte alignment");
 
 __device__ __forceinline__ uint32_t laneMaskLt() {
     uint32_t m;
@@ -174,17 +191,61 @@ __device__ __forceinline__ void getMono(const float* list, int slot, float (&e)[
     for (int k = 0; k < (kQuad ? 10 : 4); ++k) e[k] = b[2 * k];
 }
 
+// Far-field mode 3: the field of a far node about the group centre c, to
+// second order in d = x_i - c.  With r = c - COM, s^2 = r^2 + eps_g^2 (Plummer
+// softening with the group's mean eps^2), GM = G m:
+//   phi(c) = -GM/s - (r.Q.r)/(2 s^5),   a(c) = -GM r/s^3 + [Q r/s^5 - 5/2 (r.Q.r) r/s^7]
+// (monopole + quadrupole, Q = G (3S - tr S I), the expression of the member
+// evaluation), and the monopole's derivatives
+//   J_ij = da_i/dx_j = -GM (d_ij/s^3 - 3 r_i r_j/s^5)
+//   H_ijk = dJ_ij/dx_k = -GM (-3 (d_ij r_k + d_ik r_j + d_jk r_i)/s^5 + 15 r_i r_j r_k/s^7).
+// Coefficients (20): phi, a (3), J xx yy zz xy xz yz (6), H xxx yyy zzz xxy
+// xxz xyy yyz xzz yzz xyz (10).  A member then takes
+//   a_i = a + J d + 1/2 H:dd,   phi_i = phi - a.d - 1/2 d.J.d.
+__device__ __forceinline__ void farTaylor(const float (&e)[10], float cx, float cy, float cz, float epsG2,
+                                          float (&t)[20]) {
+    const float rx = cx - e[0], ry = cy - e[1], rz = cz - e[2];
+    const float s2 = rx * rx + ry * ry + rz * rz + epsG2;
+    const float is = rsqrtf(s2), is2 = is * is, is3 = is * is2, is5 = is3 * is2, is7 = is5 * is2;
+    const float gm = -e[3];                       // e[3] = -G m
+    // quadrupole part of phi and a
+    const float q0 = e[4] * rx + e[7] * ry + e[8] * rz;
+    const float q1 = e[7] * rx + e[5] * ry + e[9] * rz;
+    const float q2 = e[8] * rx + e[9] * ry + e[6] * rz;
+    const float rqr = rx * q0 + ry * q1 + rz * q2;
+    const float tq = -2.5f * rqr * is7;
+    t[0] = -gm * is - 0.5f * rqr * is5;
+    t[1] = -gm * is3 * rx + q0 * is5 + tq * rx;
+    t[2] = -gm * is3 * ry + q1 * is5 + tq * ry;
+    t[3] = -gm * is3 * rz + q2 * is5 + tq * rz;
+    const float a3 = -gm * is3, b5 = 3.0f * gm * is5;   // J = a3 I + b5 r r^T
+    t[4] = a3 + b5 * rx * rx; t[5] = a3 + b5 * ry * ry; t[6] = a3 + b5 * rz * rz;
+    t[7] = b5 * rx * ry; t[8] = b5 * rx * rz; t[9] = b5 * ry * rz;
+    const float c5 = 3.0f * gm * is5, c7 = -15.0f * gm * is7;   // H = c5 (sym d r) + c7 r r r
+    t[10] = 3.0f * c5 * rx + c7 * rx * rx * rx;          // xxx
+    t[11] = 3.0f * c5 * ry + c7 * ry * ry * ry;          // yyy
+    t[12] = 3.0f * c5 * rz + c7 * rz * rz * rz;          // zzz
+    t[13] = c5 * ry + c7 * rx * rx * ry;                  // xxy
+    t[14] = c5 * rz + c7 * rx * rx * rz;                  // xxz
+    t[15] = c5 * rx + c7 * rx * ry * ry;                  // xyy
+    t[16] = c5 * rz + c7 * ry * ry * rz;                  // yyz
+    t[17] = c5 * rx + c7 * rx * rz * rz;                  // xzz
+    t[18] = c5 * ry + c7 * ry * rz * rz;                  // yzz
+    t[19] = c7 * rx * ry * rz;                            // xyz
+}
+
 // 1 / |s| for a direction s in {-1, 0, 1}^3 with nz non-zero components.
 __device__ __forceinline__ float invDirNorm(int nz) { return nz == 3 ? 0.57735027f : (nz == 2 ? 0.70710678f : 1.0f); }
 
-template <int kWarps, bool kInside, bool kQuad, bool kLearned>
+template <int kWarps, bool kInside, bool kQuad, bool kLearned, bool kExpand = false>
 __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
                                                                  float theta2, uint32_t numGroups,
                                                                  uint32_t* groupCounter, FarCapture ff) {
-    __shared__ GravWarpSmem<kInside, kQuad> smem[kWarps];
+    static_assert(!kExpand || kQuad, "the group expansion is a quadrupole mode");
+    __shared__ GravWarpSmem<kInside, kQuad, kExpand> smem[kWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GravWarpSmem<kInside, kQuad>& S = smem[warp];
-    unsigned long long nInter = 0, nTests = 0, nUndecided = 0, nRounds = 0;
+    GravWarpSmem<kInside, kQuad, kExpand>& S = smem[warp];
+    unsigned long long nInter = 0, nTests = 0, nUndecided = 0, nRounds = 0, nGroupEvals = 0, nBucketLeaves = 0;
     int spPeak = 0;
     bool overflowed = false;
 
@@ -241,13 +302,60 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             S.dirPos[lane] = make_float4(q.x, q.y, q.z, best);
         }
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
-        int sp = 2, mCount = 0, pCount = 0;
+        int sp = 2, mCount = 0, pCount = 0, fCount = 0;
         uint32_t rounds = 0;
+        // group expansion: the group's radius about its box centre c (IEEE
+        // operations, so the far decision is reproducible) and mean eps^2
+        float rg2 = 0.0f, epsG2 = 0.0f;
+        if (kExpand) {
+            rg2 = warpMaxF(active ? len2Exact(__fsub_rn(xi, cxg), __fsub_rn(yi, cyg), __fsub_rn(zi, czg)) : 0.0f);
+            float e2 = active ? epsI * epsI : 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+            epsG2 = e2 / static_cast<float>(act);
+            if (lane < 20) reinterpret_cast<float*>(S.facc4)[lane] = 0.0f;
+        }
         const f2 X = pack2(xi, xi), Y = pack2(yi, yi), Z = pack2(zi, zi);
         const f2 E2 = pack2(epsI2, epsI2), HE = pack2(0.5f * epsI, 0.5f * epsI);
         Accum2 acc{0ull, 0ull, 0ull, 0ull};
         const uint32_t base = g * 32u;
         unsigned selfSeen = 0u;   // bit l: member l met its own leaf
+        // far list -> the group's expansion coefficients: lane l takes entry l
+        // of the first `cnt`, the 20 coefficients are summed over the warp
+        auto flushFar = [&](int cnt) {
+            if constexpr (!kExpand) return;
+            float t[20];
+            if (lane < cnt) {
+                float e[10];
+                getMono<true>(reinterpret_cast<const float*>(S.flist4), lane, e);
+                farTaylor(e, cxg, cyg, czg, epsG2, t);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 20; ++k) t[k] = 0.0f;
+            }
+            float mine = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 20; ++k) {
+                float v = t[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == k) mine = v;
+            }
+            if (lane < 20) reinterpret_cast<float*>(S.facc4)[lane] += mine;
+            __syncwarp();
+        };
+        auto flushP = [&]() {                 // evaluate plist entries 0..31, move the rest down
+            if (active) evalParticles2(S.plist, S.peps, 0, 16, X, Y, Z, HE, acc);
+            nInter += static_cast<unsigned long long>(act) * 32u;
+            __syncwarp();
+            pCount -= 32;
+            if (lane < pCount) {
+                const float* src = S.plist + 8 * (16 + (lane >> 1)) + (lane & 1);
+                putEntry(S.plist, lane, src[0], src[2], src[4], src[6]);
+                S.peps[lane] = S.peps[32 + lane];
+            }
+            __syncwarp();
+        };
         __syncwarp();
 
         while (sp > 0) {
@@ -337,17 +445,38 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 __syncwarp();
                 unsigned bits = 0u;
                 // the engine's member test (acceptsMember) on two nodes per
-                // iteration, in scalar IEEE operations (__fmul_rn / __fadd_rn
-                // are never contracted into multiply-adds, so a member exactly
-                // on the theta boundary is decided as the engine decides it)
+                // instruction on the packed FP32 pipes; the compiler may fuse
+                // the packed products and sums into multiply-adds, which moves
+                // r^2 by up to an ulp, so a member within 2^-20 of the theta
+                // boundary is re-tested in scalar IEEE operations (__fmul_rn /
+                // __fadd_rn are never contracted) and decided as the engine
+                // decides it, exact ties included
+                const f2 T2 = pack2(theta2, theta2);
                 for (int k = 0; k < nu; k += 2) {
                     const float* ub = undP + 4 * k;
-                    const float4 pa = *reinterpret_cast<const float4*>(ub);       // com xA, xB, yA, yB
-                    const float4 pb = *reinterpret_cast<const float4*>(ub + 4);   // com zA, zB, ddA, ddB
-                    const float r2a = len2Exact(__fsub_rn(xi, pa.x), __fsub_rn(yi, pa.z), __fsub_rn(zi, pb.x));
-                    const float r2b = len2Exact(__fsub_rn(xi, pa.y), __fsub_rn(yi, pa.w), __fsub_rn(zi, pb.y));
-                    const float ta = __fmul_rn(theta2, r2a), tb = __fmul_rn(theta2, r2b);
-                    const float dda = pb.z, ddb = pb.w;
+                    const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(ub);       // (com x), (com y)
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(ub + 4);   // (com z), (dd)
+                    const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
+                    const f2 r2 = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+                    float r2a, r2b, ta, tb, dda, ddb;
+                    unpack2(r2, r2a, r2b);
+                    unpack2(mul2(T2, r2), ta, tb);
+                    unpack2(v.y, dda, ddb);
+                    const bool nearA = fabsf(dda - ta) <= 9.6e-7f * ta, nearB = fabsf(ddb - tb) <= 9.6e-7f * tb;
+                    if (nearA || nearB) {                  // rare: the exact IEEE sequence
+                        float cx0, cx1, cy0, cy1, cz0, cz1;
+                        unpack2(u.x, cx0, cx1);
+                        unpack2(u.y, cy0, cy1);
+                        unpack2(v.x, cz0, cz1);
+                        if (nearA) {
+                            r2a = len2Exact(__fsub_rn(xi, cx0), __fsub_rn(yi, cy0), __fsub_rn(zi, cz0));
+                            ta = __fmul_rn(theta2, r2a);
+                        }
+                        if (nearB) {
+                            r2b = len2Exact(__fsub_rn(xi, cx1), __fsub_rn(yi, cy1), __fsub_rn(zi, cz1));
+                            tb = __fmul_rn(theta2, r2b);
+                        }
+                    }
                     bool okA = dda < ta && r2a > 1.0e-20f, okB = ddb < tb && r2b > 1.0e-20f;
                     if (kInside) {
                         const float4 mnA = S.undMin[k], mxA = S.undMax[k];
@@ -384,6 +513,16 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 }
             }
             bool open = isNode && !accept;
+            // mode 3: an opened node of at most leafBucket particles is not
+            // descended; its sorted leaf range is evaluated particle-particle
+            uint2 brng = make_uint2(1u, 0u);
+            if (kExpand && open && w.leafBucket > 0u) {
+                const uint2 r = __ldg(&w.nodeRange[c]);
+                if (r.x <= r.y && r.y < n && r.y - r.x < w.leafBucket) {
+                    brng = r;
+                    open = false;
+                }
+            }
             unsigned openMask = __ballot_sync(0xffffffffu, open);
             if (sp + 2 * __popc(openMask) > kGravStack) {
                 // Out of stack: the group takes these nodes as monopoles, the
@@ -398,7 +537,16 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 S.stack[pos + 1] = cr;
             }
             sp += 2 * __popc(openMask);
-            const unsigned accMask = __ballot_sync(0xffffffffu, accept);
+            // mode 3: an accepted node far against the group (group radius <=
+            // gamma |c - COM|) joins the group's expansion instead of being
+            // evaluated by every member
+            bool far = false;
+            if (kExpand && accept) {
+                const float R2 = len2Exact(__fsub_rn(cxg, r0.x), __fsub_rn(cyg, r0.y), __fsub_rn(czg, r0.z));
+                far = rg2 <= __fmul_rn(w.expandGamma2, R2);
+            }
+            const unsigned accMask = __ballot_sync(0xffffffffu, accept && !far);
+            const unsigned farMask = kExpand ? __ballot_sync(0xffffffffu, far) : 0u;
             if (w.traceList != nullptr && g == w.traceGroup && (accept || isLeaf)) {
                 const uint32_t k = atomicAdd(reinterpret_cast<uint32_t*>(w.traceList), 1u);
                 if (k < w.traceCap) w.traceList[1 + k] = c;
@@ -416,9 +564,31 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                     e[8] = kGPsuF * 3.0f * s1.x;
                     e[9] = kGPsuF * 3.0f * s1.y;
                 }
-                putMono<kQuad>(S.mlist, mCount + __popc(accMask & laneMaskLt()), e);
+                if constexpr (kExpand) {
+                    if (far)
+                        putMono<true>(reinterpret_cast<float*>(S.flist4), fCount + __popc(farMask & laneMaskLt()), e);
+                    else
+                        putMono<kQuad>(S.mlist, mCount + __popc(accMask & laneMaskLt()), e);
+                } else {
+                    putMono<kQuad>(S.mlist, mCount + __popc(accMask & laneMaskLt()), e);
+                }
             }
             mCount += __popc(accMask);
+            if (kExpand) {
+                fCount += __popc(farMask);
+                nGroupEvals += __popc(farMask);
+                __syncwarp();
+                if (fCount >= 32) {
+                    flushFar(32);
+                    fCount -= 32;
+                    if (lane < fCount) {
+                        float e2[10];
+                        getMono<true>(reinterpret_cast<const float*>(S.flist4), 32 + lane, e2);
+                        putMono<true>(reinterpret_cast<float*>(S.flist4), lane, e2);
+                    }
+                    __syncwarp();
+                }
+            }
             const unsigned leafMask = __ballot_sync(0xffffffffu, isLeaf);
             unsigned selfBit = 0u;
             if (isLeaf) {
@@ -447,19 +617,38 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 }
                 __syncwarp();
             }
-            if (pCount >= 32) {
-                if (active) evalParticles2(S.plist, S.peps, 0, 16, X, Y, Z, HE, acc);
-                nInter += static_cast<unsigned long long>(act) * 32u;
-                __syncwarp();
-                pCount -= 32;
-                if (lane < pCount) {
-                    const float* src = S.plist + 8 * (16 + (lane >> 1)) + (lane & 1);
-                    putEntry(S.plist, lane, src[0], src[2], src[4], src[6]);
-                    S.peps[lane] = S.peps[32 + lane];
+            if (pCount >= 32) flushP();
+            if (kExpand) {
+                // leaf buckets of this round: each range (at most 32 sorted
+                // particles) appended to the particle list by the warp at once
+                unsigned bucketMask = __ballot_sync(0xffffffffu, brng.x <= brng.y);
+                while (bucketMask) {
+                    const int src = __ffs(bucketMask) - 1;
+                    bucketMask &= bucketMask - 1u;
+                    const uint32_t first = __shfl_sync(0xffffffffu, brng.x, src);
+                    const uint32_t last = __shfl_sync(0xffffffffu, brng.y, src);
+                    const uint32_t j = first + static_cast<uint32_t>(lane);
+                    const bool has = j <= last;
+                    const unsigned hm = __ballot_sync(0xffffffffu, has);
+                    unsigned sb = 0u;
+                    if (has) {
+                        const float4 pm = __ldg(&w.leaf[j].a);
+                        const int slot = pCount + __popc(hm & laneMaskLt());
+                        putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);
+                        S.peps[slot] = 0.5f * __ldg(&w.leafAux[j]).y;
+                        const uint32_t rel = j - base;
+                        if (rel < 32u) sb = 1u << rel;
+                    }
+                    const unsigned selfHere = __reduce_or_sync(0xffffffffu, sb);
+                    selfSeen |= selfHere;
+                    pCount += __popc(hm);
+                    nBucketLeaves += static_cast<unsigned long long>(act) * __popc(hm) - __popc(selfHere);
+                    __syncwarp();
+                    if (pCount >= 32) flushP();
                 }
-                __syncwarp();
             }
         }
+        if (kExpand && fCount > 0) flushFar(fCount);
         // odd tails: pad with a massless entry (adds exactly zero)
         if (lane == 0) {
             if (mCount & 1) {
@@ -482,9 +671,25 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 // the self term added to phi: -G m_i / sqrt(eps_i^2), exactly as evaluated
                 phi -= (-kGPsuF * me.w) * rsqrtf(__fmul_rn(epsI, epsI));
             }
-            p.accX[i] = a0 + a1;
-            p.accY[i] = b0 + b1;
-            p.accZ[i] = c0 + c1;
+            float ax = a0 + a1, ay = b0 + b1, az = c0 + c1;
+            if (kExpand) {                     // the group's far field at this member (farTaylor)
+                const float* t = reinterpret_cast<const float*>(S.facc4);
+                const float dx = xi - cxg, dy = yi - cyg, dz = zi - czg;
+                const float jx = t[4] * dx + t[7] * dy + t[8] * dz;      // J d
+                const float jy = t[7] * dx + t[5] * dy + t[9] * dz;
+                const float jz = t[8] * dx + t[9] * dy + t[6] * dz;
+                const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy = dx * dy, xz = dx * dz, yz = dy * dz;
+                const float hx = t[10] * xx + t[15] * yy + t[17] * zz + 2.0f * (t[13] * xy + t[14] * xz + t[19] * yz);
+                const float hy = t[13] * xx + t[11] * yy + t[18] * zz + 2.0f * (t[15] * xy + t[19] * xz + t[16] * yz);
+                const float hz = t[14] * xx + t[16] * yy + t[12] * zz + 2.0f * (t[19] * xy + t[17] * xz + t[18] * yz);
+                ax += t[1] + jx + 0.5f * hx;
+                ay += t[2] + jy + 0.5f * hy;
+                az += t[3] + jz + 0.5f * hz;
+                phi += t[0] - (t[1] * dx + t[2] * dy + t[3] * dz) - 0.5f * (jx * dx + jy * dy + jz * dz);
+            }
+            p.accX[i] = ax;
+            p.accY[i] = ay;
+            p.accZ[i] = az;
             p.phiGrav[i] = phi;
         }
         nRounds += rounds;
@@ -500,6 +705,10 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         atomicAdd(&st->counters[kCntGravityInteractions], nInter);
         atomicAdd(&st->counters[kCntGravityNodeTests], nTests);
         atomicAdd(&st->counters[kCntGravityUndecided], nUndecided);
+        if (kExpand) {
+            atomicAdd(&st->counters[kCntGravityGroupEvals], nGroupEvals);
+            atomicAdd(&st->counters[kCntGravityBucketLeaves], nBucketLeaves);
+        }
         atomicAdd(&st->counters[kCntGravityRounds], nRounds);
         atomicMax(&st->counters[kCntGravityStackPeak], static_cast<unsigned long long>(spPeak));
         if (overflowed) atomicOr(&st->flags, kFlagStackOverflow);
@@ -509,7 +718,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
 }  // namespace
 
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
-                          cudaStream_t st, const FarCapture* far, int warps) {
+                          cudaStream_t st, const FarCapture* far, int warps, bool expansion) {
     if (n == 0) return cudaSuccess;
     const float th = fmaxf(0.0f, theta);
     const float theta2 = th * th;
@@ -522,7 +731,15 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
     using GravFn = void (*)(AstraeaParticles, Work, uint32_t, float, uint32_t, uint32_t*, FarCapture);
     GravFn kernel = nullptr;
     int wps = kGravWarps;
-    if (far != nullptr) {
+    if (expansion && quadrupole && far == nullptr) {
+        if (warps == 2) {
+            kernel = checkInside ? gravityKernel<2, true, true, false, true> : gravityKernel<2, false, true, false, true>;
+            wps = 2;
+        } else {
+            kernel = checkInside ? gravityKernel<kGravWarps, true, true, false, true>
+                                 : gravityKernel<kGravWarps, false, true, false, true>;
+        }
+    } else if (far != nullptr) {
         ff = *far;
         if (ff.groupStride == 0u) ff.groupStride = 1u;
         kernel = checkInside ? gravityKernel<kGravWarps, true, false, true> : gravityKernel<kGravWarps, false, false, true>;

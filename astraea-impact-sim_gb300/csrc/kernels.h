@@ -105,8 +105,11 @@ struct FarCapture {
 // warps: 2, 4 or 8 warps per block for the plain and quadrupole walks (the
 // autotuner's choice; the learned far-field walk uses 4); results do not
 // depend on it.
+// expansion: far-field mode 3 (quadrupole walk with w.leafBucket leaf
+// buckets and the group expansion of nodes far against the group,
+// w.expandGamma2); needs quadrupole.
 cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, float theta, bool quadrupole, int sms,
-                          cudaStream_t st, const FarCapture* far = nullptr, int warps = 4);
+                          cudaStream_t st, const FarCapture* far = nullptr, int warps = 4, bool expansion = false);
 
 // ---------------------------------------------------------------- ff.cu ---
 namespace ff {
@@ -133,15 +136,17 @@ cudaError_t launchApply(const Net& net, const Work& w, const uint2* pairs, const
 cudaError_t launchCorrect(const AstraeaParticles& p, const float4* groups, const float* groupCorr, uint32_t n,
                           cudaStream_t st);
 // Device state of the learned mode's gate (one per device).
+constexpr uint32_t kGateMaxTargets = 1024;   // sampled particles of one gate, at most
 struct GateDev {
-    double errSum;                 // sum of relative squared errors of the spot check (reset by the decision)
     unsigned long long fallbacks;  // gated calls that fell back to the plain walk
     uint32_t runFallback;          // 1: the plain walk after the gate runs, 0: it returns at once
     uint32_t lastPairs;            // (group, node) pairs of the last gated call
     float lastRms;                 // RMS relative error of the last gate
     uint32_t reserved;
+    double acc[3 * kGateMaxTargets];  // direct-sum accelerations of the targets (cleared by the decision)
 };
-// FP64 spot check of K sampled particles and the decision (gate->runFallback).
+// Direct-sum spot check of K <= kGateMaxTargets sampled particles (FP32 pair
+// terms, FP64 sums) and the decision (gate->runFallback).
 cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float tolerance,
                        const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, cudaStream_t st);
 }  // namespace ff

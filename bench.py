@@ -573,8 +573,31 @@ FAR_CONFIGS = (
     {"theta": 0.5, "mode": 2, "theta_far": 0.9, "gamma": 0.3},
     {"theta": 0.5, "mode": 2, "theta_far": 1.2, "gamma": 0.3},
     {"theta": 0.5, "mode": 2, "theta_far": 0.9, "gamma": 0.5},
+    {"theta": 0.7, "mode": 3, "bucket": "auto", "gamma": 0.3},
+    {"theta": 0.7, "mode": 3, "bucket": 16, "gamma": 0.2},
+    {"theta": 0.75, "mode": 3, "bucket": "auto", "gamma": 0.2},
+    {"theta": 0.75, "mode": 3, "bucket": "auto", "gamma": 0.3},
+    {"theta": 0.8, "mode": 3, "bucket": "auto", "gamma": 0.2},
 )
-FAR_NAMES = {0: "monopole", 1: "monopole+quadrupole", 2: "monopole+learned correction"}
+FAR_NAMES = {0: "monopole", 1: "monopole+quadrupole", 2: "monopole+learned correction",
+             3: "quadrupole+leaf buckets+group expansion"}
+
+
+def set_mode(engine, sim, cfg, theta):
+    """Far-field mode of one scan entry; mode 3 with bucket "auto" tunes the
+    leaf bucket on the current tree.  Returns the bucket used (mode 3)."""
+    mode = cfg["mode"]
+    if mode == 2:
+        engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=0.0)
+    engine.set_far_field(mode)
+    bucket = None
+    if mode == 3:
+        bucket = 16 if cfg["bucket"] == "auto" else int(cfg["bucket"])
+        engine.set_far_field_expansion(bucket, cfg["gamma"])
+    engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+    if mode == 3 and cfg["bucket"] == "auto":
+        bucket, _ = engine.autotune_expansion(sim.p, sim.bvh, theta)
+    return bucket
 
 
 def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONFIGS, learned=None):
@@ -591,10 +614,7 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
         theta, mode = cfg["theta"], cfg["mode"]
         if mode == 2 and learned is None:
             continue
-        if mode == 2:
-            engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=0.0)
-        engine.set_far_field(mode)
-        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)   # the order is already sorted: identity permutation
+        bucket = set_mode(engine, sim, cfg, theta)      # the order is already sorted: identity permutation
         engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
         torch.cuda.synchronize()
         engine.reset_device_status()
@@ -608,6 +628,12 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
         rec = {"theta": theta, "far_field": FAR_NAMES[mode], "gravity_ms": ev[0].elapsed_time(ev[1]) / 5,
                "interactions_per_particle": gc["gravity_interactions"] / 5 / sim.p.count,
                "force_rms_vs_fp64": rms_vs_truth(sim, torch, truth)}
+        if mode == 3:
+            cc = engine.read_device_counters()
+            rec.update({"leaf_bucket": bucket, "leaf_bucket_autotuned": cfg["bucket"] == "auto",
+                        "gamma": cfg["gamma"],
+                        "expansion_terms_per_particle": cc["gravity_group_evals"] / 5 / sim.p.count,
+                        "bucket_terms_per_particle": cc["gravity_bucket_leaves"] / 5 / sim.p.count})
         if mode == 2:
             rec.update({"theta_far": cfg["theta_far"], "gamma": cfg["gamma"]})
             engine.ff_set_params(np.zeros_like(params), scale)
@@ -627,10 +653,9 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
     dt_host = torch.zeros(1, dtype=torch.float32).pin_memory()
     for rec in out:
         mode = {v: k for k, v in FAR_NAMES.items()}[rec["far_field"]]
-        if mode == 2:
-            engine.ff_configure(theta_far=rec["theta_far"], gamma=rec["gamma"], gate_tolerance=0.0)
-        engine.set_far_field(mode)
-        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+        cfg = {"mode": mode, "theta_far": rec.get("theta_far"), "gamma": rec.get("gamma"),
+               "bucket": rec.get("leaf_bucket")}
+        set_mode(engine, sim, cfg, rec["theta"])
         engine.invalidate_step_cache(sim.bvh)
         for _ in range(2):
             engine.step(sim.p, sim.alt, sim.bvh, sim.prev_dt, max_dt, rec["theta"], dt_host.data_ptr())
@@ -646,6 +671,7 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
         rec["step_ms"] = ms
         rec["particle_steps_per_s"] = sim.p.count / (ms * 1e-3)
     engine.set_far_field(0)
+    engine.set_far_field_expansion(16, 0.3)
     engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
     engine.invalidate_step_cache(sim.bvh)
     base = out[0]
@@ -768,11 +794,10 @@ def run_c3(args):
     configs = [(t, m, None, None) for t, m in ((0.5, 0), (0.6, 0), (0.7, 0), (0.8, 0), (0.6, 1), (0.7, 1), (0.8, 1),
                                                 (0.9, 1))]
     configs += [(0.5, 2, tf, gm) for tf, gm in ((0.9, 0.3), (1.2, 0.3), (0.9, 0.5))]
+    configs += [(th, 3, None, gm) for th, gm in ((0.7, 0.3), (0.75, 0.2), (0.75, 0.3), (0.8, 0.2), (0.8, 0.3))]
     for theta, mode, theta_far, gamma in configs:
-        if mode == 2:
-            engine.ff_configure(theta_far=theta_far, gamma=gamma, gate_tolerance=0.0)
-        engine.set_far_field(mode)
-        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+        bucket = set_mode(engine, sim, {"mode": mode, "theta_far": theta_far, "gamma": gamma, "bucket": "auto"},
+                          theta)
         engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
         torch.cuda.synchronize()
         engine.reset_device_status()
@@ -793,6 +818,11 @@ def run_c3(args):
                "interactions_per_particle": c["gravity_interactions"] / reps / n,
                "force_rms_vs_fp64": float(torch.sqrt((rel * rel).mean())),
                "force_p99_vs_fp64": float(torch.quantile(rel.float(), 0.99))}
+        if mode == 3:
+            cc = engine.read_device_counters()
+            rec.update({"leaf_bucket": bucket, "gamma": gamma,
+                        "expansion_terms_per_particle": cc["gravity_group_evals"] / reps / n,
+                        "bucket_terms_per_particle": cc["gravity_bucket_leaves"] / reps / n})
         if mode == 2:
             rec.update({"theta_far": theta_far, "gamma": gamma})
             engine.ff_set_params(np.zeros_like(params), scale)
@@ -803,7 +833,10 @@ def run_c3(args):
             engine.ff_set_params(params, scale)
         runs.append(rec)
     engine.set_far_field(0)
+    engine.set_far_field_expansion(16, 0.3)
     base = runs[0]
+    for r in runs:
+        r["gravity_speedup_vs_plain"] = r["particles_per_s"] / base["particles_per_s"]
     ok = [r for r in runs[1:] if r["force_rms_vs_fp64"] <= base["force_rms_vs_fp64"]]
     best = max(ok, key=lambda r: r["particles_per_s"]) if ok else None
     print(json.dumps({

@@ -178,10 +178,35 @@ AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevD
  * second moments and each accepted node adds its quadrupole acceleration
  * and potential, so a larger opening angle (0.7 instead of 0.5) gives the
  * same force error with about half the interactions; 2 = monopole + the
- * learned far-field correction (astraea_gb300_ff_*, below).  Process-wide;
- * gravity in mode 1 or 2 on a tree built in mode 0 returns
- * ASTRAEA_ERR_INVALID. */
+ * learned far-field correction (astraea_gb300_ff_*, below); 3 = the
+ * quadrupole walk with leaf buckets and the group expansion
+ * (astraea_gb300_set_far_field_expansion).  Process-wide; gravity in modes
+ * 1-3 on a tree built in mode 0 returns ASTRAEA_ERR_INVALID. */
 AstraeaStatus astraea_gb300_set_far_field(int mode);
+/* Far-field mode 3.  The walk is mode 1's (the engine's opening test at
+ * theta over groups of 32, quadrupole terms), with two changes: an opened
+ * node of at most `leafBucket` particles (0..32; 0 = off) is not descended,
+ * its sorted leaf range is evaluated particle-particle; an accepted node far
+ * against the group (group radius about its box centre c <= gamma
+ * |c - COM|) is not evaluated by every member but added to the group's
+ * expansion -- its field and potential at c (monopole + quadrupole, Plummer
+ * softening with the group's mean eps^2) and the monopole's first and second
+ * derivatives there -- from which each member takes its second-order Taylor
+ * value.  Defaults 16 and 0.3; gamma in [0, 1).  Interaction counts:
+ * ASTRAEA_COUNTER_GRAVITY_GROUP_EVALS (expansion terms, not in
+ * ASTRAEA_COUNTER_GRAVITY_INTERACTIONS) and ..._BUCKET_LEAVES (P-P terms from
+ * buckets, included).  No engine counterpart. */
+AstraeaStatus astraea_gb300_set_far_field_expansion(uint32_t leafBucket, float gamma);
+/* The leaf bucket of far-field mode 3 picked by timing: the mode-3 gravity
+ * of the current tree (built in mode 3) at theta with the current gamma is
+ * timed (best of 3, CUDA events) for each of `count` candidate bucket sizes
+ * (<= 32); the fastest becomes the mode's bucket and *outBucket, outMs
+ * (host, optional) receives each candidate's time.  Buckets only add exact
+ * particle-particle terms in place of node terms, so no candidate is less
+ * accurate than a smaller one.  Blocks; no engine counterpart. */
+AstraeaStatus astraea_gb300_autotune_expansion(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
+                                               const uint32_t* candidates, uint32_t count, uint32_t* outBucket,
+                                               float* outMs);
 
 /* ---- render frame packing (engine/sph_gravity.cu:1554-1743, 2163-2201) -- */
 
@@ -356,7 +381,8 @@ AstraeaStatus astraea_gb300_build_planet(const AstraeaBodySpec* spec, uint32_t p
  * group's pairs of R + J (x_i - c).  Features: (COM - c)/r, dNode/r,
  * S/(M dNode^2) (central second moments), group extent/r.  With
  * gateTolerance > 0 every mode-2 gravity call checks the RMS relative error
- * of gateTargets sampled particles against an FP64 direct sum and, above the
+ * of gateTargets sampled particles against a direct sum (FP32 pair terms,
+ * FP64 sums: ~1e-6 relative) and, above the
  * tolerance, recomputes plain theta gravity; the decision is taken on the
  * device (the plain walk is always launched and returns at once when the
  * check passed), so the call does not block and can be graph-captured. */
@@ -364,7 +390,7 @@ typedef struct AstraeaFarFieldConfig {
     float thetaFar;          /* opening angle of the far test (default 0.8) */
     float gamma;             /* far test: L1 group extent <= gamma r (default 0.3) */
     float gateTolerance;     /* RMS relative force error at the gate; 0: no gate (default) */
-    uint32_t gateTargets;    /* sampled particles of the gate (default 64) */
+    uint32_t gateTargets;    /* sampled particles of the gate (default 64, at most 1024) */
     uint32_t pairsPerGroup;  /* pair buffer per group of 32 (default 64); a full buffer opens the node */
     uint32_t reserved;
 } AstraeaFarFieldConfig;
@@ -526,7 +552,9 @@ AstraeaStatus astraea_gb300_read_device_status(uint32_t* outFlags, uint64_t* out
 #define ASTRAEA_COUNTER_PASS1_PAIRS           8u   /* pairs with r < 2 h_i in SPH pass 1 */
 #define ASTRAEA_COUNTER_PASS2_PAIRS           9u   /* pairs with r < max(2 h_i, 2 h_j) in SPH pass 2 */
 #define ASTRAEA_COUNTER_DRIFT_PAIRS          10u   /* pairs inside the XSPH drift's radius */
-#define ASTRAEA_COUNTER_COUNT                11u
+#define ASTRAEA_COUNTER_GRAVITY_GROUP_EVALS  11u   /* far-field mode 3: far nodes taken by group expansions */
+#define ASTRAEA_COUNTER_GRAVITY_BUCKET_LEAVES 12u  /* far-field mode 3: P-P terms from leaf buckets */
+#define ASTRAEA_COUNTER_COUNT                13u
 AstraeaStatus astraea_gb300_read_device_counters(uint64_t* outCounters, uint32_t capacity, uint32_t* outCount);
 /* Stage timing of the fused step (no engine counterpart; the engine times
  * the whole step, gpuStepMs, engine/simulation.cpp:1719-1739).  While

@@ -761,6 +761,183 @@ void oracle_gravity_group_counts(AstraeaParticles* p, const AstraeaRadixBvh* b, 
     gravityImpl<float>(p, b, theta, nullptr, nullptr, groupCounts);
 }
 
+// Far-field mode 3 of the library (astraea_gb300_set_far_field_expansion):
+// the quadrupole walk of oracle_gravity_ff at theta with (1) leaf buckets:
+// an opened node of at most leafBucket particles is not descended, its sorted
+// leaf range is evaluated particle-particle; (2) the group expansion: an
+// accepted node with group radius^2 <= gamma^2 |c - COM|^2 (c the group's
+// box centre, IEEE single-precision operations as the library's) adds, about
+// c, its monopole + quadrupole field and potential with Plummer softening
+// eps_g^2 (the members' mean eps^2) and the monopole's first and second
+// derivatives; each member takes a + J d + 1/2 H:dd and
+// phi - a.d - 1/2 d.J.d, d = x - c.  counts[0]: member-evaluated terms
+// (as oracle_gravity), [1]: expansion terms, [2]: P-P terms from buckets.
+void oracle_gravity_expand(AstraeaParticles* p, const AstraeaRadixBvh* b, float theta, const float* S6,
+                           uint32_t leafBucket, float gamma, uint64_t* counts) {
+    const uint32_t n = p->count;
+    if (n == 0) return;
+    if (n == 1) { p->accX[0] = p->accY[0] = p->accZ[0] = p->phiGrav[0] = 0.0f; return; }
+    // sorted leaf range of every internal node
+    std::vector<uint32_t> first(n - 1), last(n - 1);
+    {
+        std::vector<int> order;
+        order.reserve(n - 1);
+        std::vector<int> st{0};
+        while (!st.empty()) {
+            const int v = st.back(); st.pop_back();
+            order.push_back(v);
+            if (b->leftChild[v] >= 0) st.push_back(b->leftChild[v]);
+            if (b->rightChild[v] >= 0) st.push_back(b->rightChild[v]);
+        }
+        for (size_t k = order.size(); k-- > 0;) {
+            const int v = order[k], l = b->leftChild[v], r = b->rightChild[v];
+            first[v] = l < 0 ? static_cast<uint32_t>(~l) : first[l];
+            last[v] = r < 0 ? static_cast<uint32_t>(~r) : last[r];
+        }
+    }
+    const float th = std::fmax(0.0f, theta);
+    const float theta2 = th * th, gamma2 = gamma * gamma;
+    const bool checkInside = theta2 > 0.333333f;
+    const int G = numGroups(n);
+    uint64_t total = 0, groupEvals = 0, bucketLeaves = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : total, groupEvals, bucketLeaves)
+    for (int g = 0; g < G; ++g) {
+        const uint32_t i0 = static_cast<uint32_t>(g) * kGroup;
+        const int act = static_cast<int>(std::min<uint32_t>(kGroup, n - i0));
+        float xi[kGroup], yi[kGroup], zi[kGroup], eI[kGroup], eI2[kGroup];
+        float ax[kGroup] = {}, ay[kGroup] = {}, az[kGroup] = {}, ph[kGroup] = {};
+        float gmin[3] = {3.0e38f, 3.0e38f, 3.0e38f}, gmax[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float e2sum = 0.0f;
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            xi[l] = p->posX[i]; yi[l] = p->posY[i]; zi[l] = p->posZ[i];
+            eI[l] = 0.8f * std::fmax(p->h0[i], 1.0e-6f); eI2[l] = eI[l] * eI[l];
+            gmin[0] = std::fmin(gmin[0], xi[l]); gmax[0] = std::fmax(gmax[0], xi[l]);
+            gmin[1] = std::fmin(gmin[1], yi[l]); gmax[1] = std::fmax(gmax[1], yi[l]);
+            gmin[2] = std::fmin(gmin[2], zi[l]); gmax[2] = std::fmax(gmax[2], zi[l]);
+            e2sum += eI2[l];
+        }
+        const float cgx = 0.5f * (gmin[0] + gmax[0]), cgy = 0.5f * (gmin[1] + gmax[1]), cgz = 0.5f * (gmin[2] + gmax[2]);
+        float rg2 = 0.0f;
+        for (int l = 0; l < act; ++l) {
+            const float dx = xi[l] - cgx, dy = yi[l] - cgy, dz = zi[l] - cgz;
+            rg2 = std::fmax(rg2, (dx * dx + dy * dy) + dz * dz);
+        }
+        const float epsG2 = e2sum / static_cast<float>(act);
+        double T[20] = {};
+        auto pp = [&](uint32_t j) {
+            const float pxj = p->posX[j], pyj = p->posY[j], pzj = p->posZ[j], mj = p->mass[j];
+            const float eJ = 0.8f * std::fmax(p->h0[j], 1.0e-6f);
+            for (int l = 0; l < act; ++l) {
+                if (i0 + l == j) continue;
+                const float dx = xi[l] - pxj, dy = yi[l] - pyj, dz = zi[l] - pzj;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float eij = 0.5f * (eI[l] + eJ);
+                const float iR = 1.0f / std::sqrt(r2 + eij * eij + 1.0e-20f);
+                const float f = -kGPsuF * mj * iR * iR * iR;
+                ax[l] += f * dx; ay[l] += f * dy; az[l] += f * dz;
+                ph[l] -= kGPsuF * mj * iR;
+                ++total;
+            }
+        };
+        int stack[kStackSize];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int node = stack[--sp];
+            const int ch[2] = {b->leftChild[node], b->rightChild[node]};
+            for (int k = 0; k < 2; ++k) {
+                const int c = ch[k];
+                if (c < 0) { pp(static_cast<uint32_t>(~c)); continue; }
+                const NodeBox nb = nodeBox(*b, c);
+                bool anyOpen = false;
+                for (int l = 0; l < act && !anyOpen; ++l) {
+                    const float dx = xi[l] - nb.cx, dy = yi[l] - nb.cy, dz = zi[l] - nb.cz;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    bool acc = (nb.dNode * nb.dNode < theta2 * r2) && (r2 > 1.0e-20f);
+                    if (acc && checkInside && xi[l] >= nb.mnx && xi[l] <= nb.mxx && yi[l] >= nb.mny &&
+                        yi[l] <= nb.mxy && zi[l] >= nb.mnz && zi[l] <= nb.mxz)
+                        acc = false;
+                    if (!acc) anyOpen = true;
+                }
+                if (anyOpen && sp < kStackSize) {
+                    if (leafBucket > 0 && last[c] - first[c] < leafBucket) {
+                        for (uint32_t j = first[c]; j <= last[c]; ++j) {
+                            pp(j);
+                            bucketLeaves += static_cast<uint64_t>(act) - ((j >= i0 && j < i0 + act) ? 1u : 0u);
+                        }
+                    } else {
+                        stack[sp++] = c;
+                    }
+                    continue;
+                }
+                const float* sc = S6 + 6 * static_cast<size_t>(c);
+                const float tr = sc[0] + sc[1] + sc[2];
+                const float qxx = kGPsuF * (3.0f * sc[0] - tr), qyy = kGPsuF * (3.0f * sc[1] - tr);
+                const float qzz = kGPsuF * (3.0f * sc[2] - tr), qxy = kGPsuF * 3.0f * sc[3];
+                const float qxz = kGPsuF * 3.0f * sc[4], qyz = kGPsuF * 3.0f * sc[5];
+                const float ux = cgx - nb.cx, uy = cgy - nb.cy, uz = cgz - nb.cz;
+                const float R2 = (ux * ux + uy * uy) + uz * uz;
+                if (rg2 <= gamma2 * R2) {             // the group's expansion (FP64 sums of FP64 terms)
+                    const double rx = ux, ry = uy, rz = uz, gm = static_cast<double>(kGPsuF) * nb.m;
+                    const double s2 = rx * rx + ry * ry + rz * rz + epsG2;
+                    const double is = 1.0 / std::sqrt(s2), is2 = is * is, is3 = is * is2, is5 = is3 * is2, is7 = is5 * is2;
+                    const double q0 = qxx * rx + qxy * ry + qxz * rz, q1 = qxy * rx + qyy * ry + qyz * rz;
+                    const double q2 = qxz * rx + qyz * ry + qzz * rz, rqr = rx * q0 + ry * q1 + rz * q2;
+                    const double tq = -2.5 * rqr * is7;
+                    T[0] += -gm * is - 0.5 * rqr * is5;
+                    T[1] += -gm * is3 * rx + q0 * is5 + tq * rx;
+                    T[2] += -gm * is3 * ry + q1 * is5 + tq * ry;
+                    T[3] += -gm * is3 * rz + q2 * is5 + tq * rz;
+                    const double a3 = -gm * is3, b5 = 3.0 * gm * is5;
+                    T[4] += a3 + b5 * rx * rx; T[5] += a3 + b5 * ry * ry; T[6] += a3 + b5 * rz * rz;
+                    T[7] += b5 * rx * ry; T[8] += b5 * rx * rz; T[9] += b5 * ry * rz;
+                    const double c5 = 3.0 * gm * is5, c7 = -15.0 * gm * is7;
+                    T[10] += 3.0 * c5 * rx + c7 * rx * rx * rx; T[11] += 3.0 * c5 * ry + c7 * ry * ry * ry;
+                    T[12] += 3.0 * c5 * rz + c7 * rz * rz * rz; T[13] += c5 * ry + c7 * rx * rx * ry;
+                    T[14] += c5 * rz + c7 * rx * rx * rz; T[15] += c5 * rx + c7 * rx * ry * ry;
+                    T[16] += c5 * rz + c7 * ry * ry * rz; T[17] += c5 * rx + c7 * rx * rz * rz;
+                    T[18] += c5 * ry + c7 * ry * rz * rz; T[19] += c7 * rx * ry * rz;
+                    ++groupEvals;
+                    continue;
+                }
+                for (int l = 0; l < act; ++l) {          // monopole + quadrupole at the member
+                    const float dx = xi[l] - nb.cx, dy = yi[l] - nb.cy, dz = zi[l] - nb.cz;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float iR = 1.0f / std::sqrt(r2 + eI2[l] + 1.0e-20f);
+                    const float iR3 = iR * iR * iR;
+                    const float f = -kGPsuF * nb.m * iR3;
+                    ax[l] += f * dx; ay[l] += f * dy; az[l] += f * dz;
+                    ph[l] -= kGPsuF * nb.m * iR;
+                    const float qr0 = qxx * dx + qxy * dy + qxz * dz, qr1 = qxy * dx + qyy * dy + qyz * dz;
+                    const float qr2 = qxz * dx + qyz * dy + qzz * dz, rqr = dx * qr0 + dy * qr1 + dz * qr2;
+                    const float i2 = iR * iR, i5 = iR * i2 * i2, i7 = i5 * i2, t = -2.5f * rqr * i7;
+                    ax[l] += qr0 * i5 + t * dx; ay[l] += qr1 * i5 + t * dy; az[l] += qr2 * i5 + t * dz;
+                    ph[l] += -0.5f * rqr * i5;
+                    ++total;
+                }
+            }
+        }
+        for (int l = 0; l < act; ++l) {
+            const uint32_t i = i0 + l;
+            const double dx = static_cast<double>(xi[l] - cgx), dy = static_cast<double>(yi[l] - cgy),
+                         dz = static_cast<double>(zi[l] - cgz);
+            const double jx = T[4] * dx + T[7] * dy + T[8] * dz, jy = T[7] * dx + T[5] * dy + T[9] * dz;
+            const double jz = T[8] * dx + T[9] * dy + T[6] * dz;
+            const double xx = dx * dx, yy = dy * dy, zz = dz * dz, xy = dx * dy, xz = dx * dz, yz = dy * dz;
+            const double hx = T[10] * xx + T[15] * yy + T[17] * zz + 2.0 * (T[13] * xy + T[14] * xz + T[19] * yz);
+            const double hy = T[13] * xx + T[11] * yy + T[18] * zz + 2.0 * (T[15] * xy + T[19] * xz + T[16] * yz);
+            const double hz = T[14] * xx + T[16] * yy + T[12] * zz + 2.0 * (T[19] * xy + T[17] * xz + T[18] * yz);
+            p->accX[i] = static_cast<float>(ax[l] + T[1] + jx + 0.5 * hx);
+            p->accY[i] = static_cast<float>(ay[l] + T[2] + jy + 0.5 * hy);
+            p->accZ[i] = static_cast<float>(az[l] + T[3] + jz + 0.5 * hz);
+            p->phiGrav[i] = static_cast<float>(ph[l] + T[0] - (T[1] * dx + T[2] * dy + T[3] * dz) -
+                                               0.5 * (jx * dx + jy * dy + jz * dz));
+        }
+    }
+    if (counts) { counts[0] = total; counts[1] = groupEvals; counts[2] = bucketLeaves; }
+}
+
 // Central second moments of every internal node, S = sum m (x - c)(x - c)^T,
 // combined bottom-up with the parallel-axis rule in FP32 exactly as the
 // library's moments refit does (children first, then

@@ -50,6 +50,7 @@ def load(build=True):
             "oracle_gravity_ff": [P, B, f, vp, vp],
             "oracle_gravity_f64": [P, B, f, vp],
             "oracle_gravity_group_counts": [P, B, f, vp],
+            "oracle_gravity_expand": [P, B, f, vp, u32, f, vp],
             "oracle_node_moments": [P, B, vp],
             "oracle_direct_gravity_f64": [u32, vp, vp, vp, vp, vp, u32, vp, vp, vp],
             "oracle_sph_pass2": [P, B],
@@ -418,6 +419,16 @@ class Oracle:
             S6 = self.node_moments()
             self.lib.oracle_gravity_ff(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(S6), _ptr(cnt))
         return int(cnt[0])
+
+    def gravity_expand(self, theta=0.7, leaf_bucket=16, gamma=0.3):
+        """The library's far-field mode 3 (see oracle_gravity_expand); returns
+        (member-evaluated terms, expansion terms, bucket P-P terms)."""
+        s = self.p.struct()
+        S6 = self.node_moments()
+        cnt = np.zeros(3, np.uint64)
+        self.lib.oracle_gravity_expand(ctypes.byref(s), ctypes.byref(self.bvh.s), float(theta), _ptr(S6),
+                                       int(leaf_bucket), float(gamma), _ptr(cnt))
+        return int(cnt[0]), int(cnt[1]), int(cnt[2])
 
     def gravity_group_counts(self, theta=0.5):
         """The reference kernel; returns each group's interaction count."""

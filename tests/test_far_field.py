@@ -1,4 +1,5 @@
-"""Far-field mode 1: monopole + quadrupole of every accepted node.
+"""Far-field modes 1 (monopole + quadrupole of every accepted node) and 3
+(the quadrupole walk with leaf buckets and the group expansion of far nodes).
 
 No counterpart in the reference (its kernel is monopole only and stays the
 library's default, mode 0).  Checks:
@@ -10,7 +11,13 @@ library's default, mode 0).  Checks:
     plain theta = 0.5 error with far fewer interactions;
   * GPU: the library's mode-1 gravity against the oracle's (same group-union
     acceptance, FP32), to 1e-5 norm-relative RMS; a mode-1 evaluation on a
-    tree built in mode 0 is refused.
+    tree built in mode 0 is refused;
+  * mode 3 (CPU, the oracle): at theta = 0.7 with 16-particle buckets and
+    gamma = 0.3 the force error stays below plain theta = 0.5 while the node
+    terms each member evaluates fall to a sixth; (GPU) the library's mode 3
+    equals the oracle's term for term (member-evaluated terms, expansion
+    terms and bucket terms exactly -- the far and bucket decisions are IEEE
+    single-precision tests on both sides) and its accelerations to 1e-5.
 """
 import numpy as np
 import pytest
@@ -144,7 +151,7 @@ def test_gpu_quadrupole_needs_moments_tree():
     finally:
         engine.set_far_field(0)
     with pytest.raises(abi.AstraeaError):
-        engine.set_far_field(3)
+        engine.set_far_field(4)
 
 
 @pytest.mark.gpu
@@ -160,3 +167,53 @@ def test_gpu_direct_sum_f64_matches_oracle():
     ref_acc, ref_phi = oracle.direct_gravity_f64(st, tgt)
     assert np.max(np.abs(acc.cpu().numpy() - ref_acc)) <= 1e-12 * np.max(np.abs(ref_acc))
     assert np.max(np.abs(phi.cpu().numpy() - ref_phi)) <= 1e-12 * np.max(np.abs(ref_phi))
+
+
+def test_mode3_expansion_keeps_error_with_fewer_node_terms(impact_truth):
+    o, sel, ref = impact_truth
+    n = o.p.count
+    c50 = o.gravity(0.5, 0)
+    e50 = rms_error(o, sel, ref)
+    member, group, bucket = o.gravity_expand(0.7, 16, 0.3)
+    e3 = rms_error(o, sel, ref)
+    print("mode 3: error %.3e (plain 0.5: %.3e), node terms per particle %.1f (plain %.1f), expansion terms per "
+          "particle %.2f, bucket terms per particle %.1f" % (e3, e50, (member - bucket) / n, c50 / n, group / n,
+                                                            bucket / n))
+    assert e3 < e50
+    assert (member - bucket) < c50 / 6.0
+    assert group > 0 and bucket > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("theta,bucket,gamma", [(0.7, 16, 0.3), (0.75, 8, 0.25), (0.6, 32, 0.0), (0.7, 0, 0.3)])
+def test_gpu_mode3_matches_oracle(theta, bucket, gamma):
+    from astraea_gb300 import engine
+    st = impact_state(32768, seed=5)
+    n = len(st["posX"])
+    o = oracle.Oracle(st)
+    o.sort_and_build()
+    member, group, leaves = o.gravity_expand(theta, bucket, gamma)
+    ref = o.p.state()
+    try:
+        engine.set_far_field(3)
+        engine.set_far_field_expansion(bucket, gamma)
+        p, alt = engine.DeviceParticles(n), engine.DeviceParticles(n)
+        bvh = engine.DeviceBvh(n)
+        p.upload(st)
+        alt.count = n
+        engine.sort_and_build_bvh(p, alt, bvh)
+        engine.reset_device_status()
+        engine.gravity_barnes_hut(p, bvh, theta)
+        c = engine.read_device_counters()
+        got = p.download()
+    finally:
+        engine.set_far_field(0)
+        engine.set_far_field_expansion(16, 0.3)
+    print("mode 3 theta %.2f bucket %d gamma %.2f: terms %d/%d, expansion %d/%d, bucket %d/%d" % (
+        theta, bucket, gamma, c["gravity_interactions"], member, c["gravity_group_evals"], group,
+        c["gravity_bucket_leaves"], leaves))
+    assert c["gravity_interactions"] == member
+    assert c["gravity_group_evals"] == group
+    assert c["gravity_bucket_leaves"] == leaves
+    for f in ("accX", "accY", "accZ", "phiGrav"):
+        assert rel_rms(got[f], ref[f]) < 1e-5, f
