@@ -402,13 +402,15 @@ __global__ void __launch_bounds__(kLabelWarps * 32) labelKernel(Work w, uint32_t
 }
 
 // The gate's spot check: target k is the k-th of K evenly spaced sorted
-// particles.  Block (s, k) sums the softened pull of sorted particles
-// [s kGateSlice, (s+1) kGateSlice) on target k: the pair terms in FP32 (eps_ij
-// softening, as the walk's leaves), each thread's run of kGateRun terms in
-// FP32, everything above that in FP64, added to gate->acc[3k..3k+2].  The
-// reference sum so formed is within ~1e-6 relative of the exact one -- three
-// orders below any useful gate tolerance -- and costs K n FP32 pair terms
-// spread over every SM.
+// particles.  Block (s, k) sums the softened pull (eps_ij softening, as the
+// walk's leaves) of sorted particles [s kGateSlice, (s+1) kGateSlice) on
+// target k and adds it to gate->acc[3k..3k+2]; K n pair terms spread over
+// every SM.  kF64: pair terms in FP64 (positions widened before the
+// subtraction), the spot check against an FP64 direct sum.  Otherwise FP32
+// pair terms, each thread's run of kGateRun terms in FP32 and everything
+// above in FP64: within ~1e-6 relative of the FP64 sum, three orders below any
+// useful tolerance, at a fraction of the cost (FP64 issues at a small
+// fraction of the FP32 rate on this part).
 constexpr int kGateThreads = 256;
 constexpr int kGateRun = 16;
 constexpr uint32_t kGateSlice = kGateThreads * kGateRun;
@@ -417,26 +419,43 @@ __device__ __forceinline__ uint32_t gateTarget(uint32_t k, uint32_t n, uint32_t 
     return (K > 1u) ? static_cast<uint32_t>((static_cast<uint64_t>(k) * (n - 1u)) / (K - 1u)) : 0u;
 }
 
+template <bool kF64>
 __global__ void __launch_bounds__(kGateThreads) gateSumKernel(Work w, uint32_t n, uint32_t K, GateDev* gate) {
     __shared__ double red[3][kGateThreads / 32];
     const uint32_t k = blockIdx.y;
     const uint32_t t = gateTarget(k, n, K);
     const float4 me = __ldg(&w.leaf[t].a);
     const float ei = __ldg(&w.leafAux[t]).y;
-    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
     const uint32_t j0 = blockIdx.x * kGateSlice + threadIdx.x;
+    if constexpr (kF64) {
+        const double xi = me.x, yi = me.y, zi = me.z, hei = 0.5 * static_cast<double>(ei);
 #pragma unroll 4
-    for (int r = 0; r < kGateRun; ++r) {
-        const uint32_t j = j0 + static_cast<uint32_t>(r) * kGateThreads;
-        if (j >= n || j == t) continue;
-        const float4 pm = __ldg(&w.leaf[j].a);
-        const float e = 0.5f * (ei + __ldg(&w.leafAux[j]).y);
-        const float dx = me.x - pm.x, dy = me.y - pm.y, dz = me.z - pm.z;
-        const float ir = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e * e))));
-        const float f = -kG * pm.w * ir * ir * ir;
-        ax = fmaf(f, dx, ax); ay = fmaf(f, dy, ay); az = fmaf(f, dz, az);
+        for (int r = 0; r < kGateRun; ++r) {
+            const uint32_t j = j0 + static_cast<uint32_t>(r) * kGateThreads;
+            if (j >= n || j == t) continue;
+            const float4 pm = __ldg(&w.leaf[j].a);
+            const double e = hei + 0.5 * static_cast<double>(__ldg(&w.leafAux[j]).y);
+            const double dx = xi - pm.x, dy = yi - pm.y, dz = zi - pm.z;
+            const double ir = rsqrt(dx * dx + dy * dy + dz * dz + e * e);
+            const double f = -static_cast<double>(kG) * pm.w * ir * ir * ir;
+            sx += f * dx; sy += f * dy; sz += f * dz;
+        }
+    } else {
+        float ax = 0.0f, ay = 0.0f, az = 0.0f;
+#pragma unroll 4
+        for (int r = 0; r < kGateRun; ++r) {
+            const uint32_t j = j0 + static_cast<uint32_t>(r) * kGateThreads;
+            if (j >= n || j == t) continue;
+            const float4 pm = __ldg(&w.leaf[j].a);
+            const float e = 0.5f * (ei + __ldg(&w.leafAux[j]).y);
+            const float dx = me.x - pm.x, dy = me.y - pm.y, dz = me.z - pm.z;
+            const float ir = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e * e))));
+            const float f = -kG * pm.w * ir * ir * ir;
+            ax = fmaf(f, dx, ax); ay = fmaf(f, dy, ay); az = fmaf(f, dz, az);
+        }
+        sx = ax; sy = ay; sz = az;
     }
-    double sx = ax, sy = ay, sz = az;
     for (int o = 16; o > 0; o >>= 1) {
         sx += __shfl_xor_sync(0xffffffffu, sx, o);
         sy += __shfl_xor_sync(0xffffffffu, sy, o);
@@ -550,10 +569,13 @@ cudaError_t launchCorrect(const AstraeaParticles& p, const float4* groups, const
 }
 
 cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float tolerance,
-                       const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, cudaStream_t st) {
+                       const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, bool fp32Pairs, cudaStream_t st) {
     if (n == 0u || K == 0u || K > kGateMaxTargets) return cudaErrorInvalidValue;
     const dim3 grid(blocks(n, kGateSlice), K);
-    gateSumKernel<<<grid, kGateThreads, 0, st>>>(w, n, K, gate);
+    if (fp32Pairs)
+        gateSumKernel<false><<<grid, kGateThreads, 0, st>>>(w, n, K, gate);
+    else
+        gateSumKernel<true><<<grid, kGateThreads, 0, st>>>(w, n, K, gate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const unsigned threads = ((K + 31u) / 32u) * 32u;

@@ -445,38 +445,21 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 __syncwarp();
                 unsigned bits = 0u;
                 // the engine's member test (acceptsMember) on two nodes per
-                // instruction on the packed FP32 pipes; the compiler may fuse
-                // the packed products and sums into multiply-adds, which moves
-                // r^2 by up to an ulp, so a member within 2^-20 of the theta
-                // boundary is re-tested in scalar IEEE operations (__fmul_rn /
-                // __fadd_rn are never contracted) and decided as the engine
-                // decides it, exact ties included
-                const f2 T2 = pack2(theta2, theta2);
+                // iteration, in scalar IEEE operations (__fmul_rn / __fadd_rn
+                // are never contracted into multiply-adds, so a member exactly
+                // on the theta boundary is decided as the engine decides it;
+                // the packed f32x2 form is 2 % faster but its products and
+                // sums may be fused, which moved one exact tie of the 1M
+                // impact, and re-testing near ties in scalar costs more than
+                // it saves)
                 for (int k = 0; k < nu; k += 2) {
                     const float* ub = undP + 4 * k;
-                    const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(ub);       // (com x), (com y)
-                    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(ub + 4);   // (com z), (dd)
-                    const f2 dx = sub2(X, u.x), dy = sub2(Y, u.y), dz = sub2(Z, v.x);
-                    const f2 r2 = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
-                    float r2a, r2b, ta, tb, dda, ddb;
-                    unpack2(r2, r2a, r2b);
-                    unpack2(mul2(T2, r2), ta, tb);
-                    unpack2(v.y, dda, ddb);
-                    const bool nearA = fabsf(dda - ta) <= 9.6e-7f * ta, nearB = fabsf(ddb - tb) <= 9.6e-7f * tb;
-                    if (nearA || nearB) {                  // rare: the exact IEEE sequence
-                        float cx0, cx1, cy0, cy1, cz0, cz1;
-                        unpack2(u.x, cx0, cx1);
-                        unpack2(u.y, cy0, cy1);
-                        unpack2(v.x, cz0, cz1);
-                        if (nearA) {
-                            r2a = len2Exact(__fsub_rn(xi, cx0), __fsub_rn(yi, cy0), __fsub_rn(zi, cz0));
-                            ta = __fmul_rn(theta2, r2a);
-                        }
-                        if (nearB) {
-                            r2b = len2Exact(__fsub_rn(xi, cx1), __fsub_rn(yi, cy1), __fsub_rn(zi, cz1));
-                            tb = __fmul_rn(theta2, r2b);
-                        }
-                    }
+                    const float4 pa = *reinterpret_cast<const float4*>(ub);       // com xA, xB, yA, yB
+                    const float4 pb = *reinterpret_cast<const float4*>(ub + 4);   // com zA, zB, ddA, ddB
+                    const float r2a = len2Exact(__fsub_rn(xi, pa.x), __fsub_rn(yi, pa.z), __fsub_rn(zi, pb.x));
+                    const float r2b = len2Exact(__fsub_rn(xi, pa.y), __fsub_rn(yi, pa.w), __fsub_rn(zi, pb.y));
+                    const float ta = __fmul_rn(theta2, r2a), tb = __fmul_rn(theta2, r2b);
+                    const float dda = pb.z, ddb = pb.w;
                     bool okA = dda < ta && r2a > 1.0e-20f, okB = ddb < tb && r2b > 1.0e-20f;
                     if (kInside) {
                         const float4 mnA = S.undMin[k], mxA = S.undMax[k];

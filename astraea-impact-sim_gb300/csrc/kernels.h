@@ -145,10 +145,10 @@ struct GateDev {
     uint32_t reserved;
     double acc[3 * kGateMaxTargets];  // direct-sum accelerations of the targets (cleared by the decision)
 };
-// Direct-sum spot check of K <= kGateMaxTargets sampled particles (FP32 pair
-// terms, FP64 sums) and the decision (gate->runFallback).
+// Direct-sum spot check of K <= kGateMaxTargets sampled particles (FP64 pair
+// terms, or FP32 pair terms with FP64 sums) and the decision (gate->runFallback).
 cudaError_t launchGate(const AstraeaParticles& p, const Work& w, uint32_t n, uint32_t K, float tolerance,
-                       const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, cudaStream_t st);
+                       const uint32_t* pairCount, uint32_t pairCap, GateDev* gate, bool fp32Pairs, cudaStream_t st);
 }  // namespace ff
 
 // -------------------------------------------------------------- sph.cu ---

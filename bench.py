@@ -645,8 +645,13 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
             rec["gravity_parts_ms"] = {k: float(np.median([q[k] for q in parts])) for k in parts[0]}
             engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=1.0, gate_targets=64)
             gated = engine.ff_profile(sim.p, sim.bvh, theta)
+            engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=1.0, gate_targets=64,
+                                gate_fp32_pairs=True)
+            gated32 = engine.ff_profile(sim.p, sim.bvh, theta)
             engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=0.0)
-            rec["gate_ms"] = {"fp64_spot_check_64_targets": gated["gate"], "skipped_fallback_walk": gated["fallback"]}
+            rec["gate_ms"] = {"fp64_spot_check_64_targets": gated["gate"],
+                              "fp32_pairs_spot_check_64_targets": gated32["gate"],
+                              "skipped_fallback_walk": gated["fallback"]}
             engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
         out.append(rec)
     # whole steps (the state advances; e2e re-uploads its own inputs afterwards)
