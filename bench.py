@@ -20,6 +20,10 @@ whole particle set, through the library's fused C-ABI step.
              the FP32 FMA throughput measured in this process
   cpu_baseline  the reference algorithm's FP64 host path (oracle/, OpenMP
              on the host cores): two full steps of the same workload
+  reference_cuda  the reference's own CUDA kernels (compiled for sm_100
+             from its checkout into oracle/_ref) stepping the same initial
+             state on the same GPU, CUDA-event timed, and this library's
+             speed-up over them
 
 --impl reference prints the CPU reference arm on the same workload and
 metric: full FP64 host steps, W untimed and K timed; beside them, in
@@ -84,6 +88,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-planet", action="store_true", help="skip the planet-construction measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default block shape of the tree walks")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip timing the reference's own CUDA kernels (oracle/_ref cubin) beside this library")
     ap.add_argument("--eager", action="store_true",
                     help="time the steps as separate C-ABI calls instead of replaying a captured two-step graph")
     ap.add_argument("--far-field", type=int, default=0, choices=[0, 1],
@@ -332,6 +338,13 @@ def run_gpu(args):
                                "step; the e2e number below is eager calls through the C-ABI)")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(st, args, max_dt)
+    if rank == 0 and world == 1 and args.workload == "c2" and not args.no_reference_cuda:
+        # the reference's own kernels on the same GPU and initial state, after
+        # everything above (their buffers are separate and freed afterwards)
+        ref = reference_cuda(n, st)
+        out["reference_cuda"] = ref
+        if isinstance(ref, dict):
+            out["reference_cuda"]["speedup_of_this_library"] = ref["ms_per_step_median"] / (ms_max / args.steps)
     if rank == 0:
         print(json.dumps(out))
     if dist:

@@ -298,6 +298,17 @@ int numGroups(uint32_t n) { return static_cast<int>((n + kGroup - 1) / kGroup); 
 // Timing sample for the CPU baseline: tree-walking stages visit only groups
 // g with g % g_groupStride == 0 (1 = all groups, the normal checker mode).
 int g_groupStride = 1;
+
+// Rounding of the gravity member test's r^2 (probe of how a compiled kernel
+// evaluates dx*dx + dy*dy + dz*dz): 0 the IEEE sequence (dx^2 + dy^2) + dz^2,
+// 1 fma(dz, dz, fma(dx, dx, dy^2)), 2 fma(dz, dz, fma(dy, dy, dx^2)).  The
+// member test of the gravity walk only; 0 unless a test sets it.
+int g_r2Form = 0;
+inline float memberR2(float dx, float dy, float dz) {
+    if (g_r2Form == 1) return std::fma(dz, dz, std::fma(dx, dx, dy * dy));
+    if (g_r2Form == 2) return std::fma(dz, dz, std::fma(dy, dy, dx * dx));
+    return dx * dx + dy * dy + dz * dz;
+}
 inline bool skipGroup(int g) { return g_groupStride > 1 && (g % g_groupStride) != 0; }
 
 // Depth-first walk shared by the SPH-style traversals: `open(c)` decides
@@ -687,7 +698,7 @@ static void gravityImpl(AstraeaParticles* p, const AstraeaRadixBvh* b, float the
                     bool anyOpen = false;
                     for (int l = 0; l < act; ++l) {
                         const float dx = xi[l] - nb.cx, dy = yi[l] - nb.cy, dz = zi[l] - nb.cz;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float r2 = memberR2(dx, dy, dz);
                         dxs[l] = dx; dys[l] = dy; dzs[l] = dz; r2s[l] = r2;
                         bool acc = (nb.dNode * nb.dNode < theta2 * r2) && (r2 > 1.0e-20f);
                         if (acc && checkInside && xi[l] >= nb.mnx && xi[l] <= nb.mxx && yi[l] >= nb.mny &&
@@ -1650,6 +1661,7 @@ void oracle_telemetry(const AstraeaParticles* p, const AstraeaTelemetryParams* p
 
 int oracle_abi_version(void) { return ASTRAEA_GB300_ABI_VERSION; }
 void oracle_set_group_stride(int k) { g_groupStride = k < 1 ? 1 : k; }
+void oracle_set_r2_form(int k) { g_r2Form = (k >= 0 && k <= 2) ? k : 0; }
 
 }  // extern "C"
 

@@ -78,6 +78,7 @@ def load(build=True):
         _lib.oracle_step_f64.restype = f
         _lib.oracle_pcls_frame.restype = ctypes.c_size_t
         _lib.oracle_set_group_stride.argtypes = [ctypes.c_int]
+        _lib.oracle_set_r2_form.argtypes = [ctypes.c_int]
         _lib.oracle_cold_energy.restype = ctypes.c_double
         _lib.oracle_cold_energy.argtypes = [ctypes.c_int, ctypes.c_double]
     return _lib
@@ -507,6 +508,13 @@ class Oracle:
 def set_group_stride(k):
     """Tree-walking stages visit every k-th group only (CPU timing sample)."""
     load().oracle_set_group_stride(int(k))
+
+
+def set_r2_form(k):
+    """Rounding of r^2 in the gravity member test: 0 the IEEE sequence
+    (default), 1 fma(dz, dz, fma(dx, dx, dy^2)), 2 fma(dz, dz, fma(dy, dy,
+    dx^2)) -- how a compiler that contracts multiply-adds may evaluate it."""
+    load().oracle_set_r2_form(int(k))
 
 
 def eos_batch(mat, rho, u, dmg, reference=False):

@@ -169,14 +169,17 @@ def test_gpu_gate_that_passes_keeps_the_learned_result():
         engine.set_far_field(0)
     stats = engine.ff_stats()
     assert stats["fallbacks"] == before and 0.0 < stats["lastGateRms"] < 10.0
-    # the gate's own RMS against the FP64 direct sum at its 32 evenly spaced
-    # sorted targets: the FP64 spot check equals it to the float the RMS is
-    # reported in; the FP32-pair variant's sum is within ~1e-6 relative
+    # the gate's own RMS against the host's FP64 direct sum at its 32 evenly
+    # spaced sorted targets.  The RMS is of relative errors, so a relative
+    # difference d between the two reference sums moves it by about d: the
+    # device softens with eps = 0.8 h0 rounded to float (the walk's value),
+    # the host in FP64, which leaves d ~ 1e-8 for the FP64 spot check; FP32
+    # pair terms add ~1e-6
     targets = np.array([k * (n - 1) // 31 for k in range(32)], np.uint32)
     sorted_state = {k: gated[k] for k in ("posX", "posY", "posZ", "mass", "h0")}
     host_rms = rms_vs_direct(gated, sorted_state, targets)
     print("gate RMS: device FP64 %.9e, FP64 direct sum %.9e" % (stats["lastGateRms"], host_rms))
-    assert abs(stats["lastGateRms"] - host_rms) <= 1e-6 * host_rms
+    assert abs(stats["lastGateRms"] - host_rms) <= 5e-8
     try:
         engine.set_far_field(2)
         engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=10.0, gate_targets=32, gate_fp32_pairs=True)
@@ -186,7 +189,7 @@ def test_gpu_gate_that_passes_keeps_the_learned_result():
         engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=0.0)
         engine.set_far_field(0)
     print("gate RMS: device FP32 pairs %.9e" % rms32)
-    assert abs(rms32 - host_rms) <= 1e-5 * host_rms
+    assert abs(rms32 - host_rms) <= 2e-6
     engine.gravity_barnes_hut(p, bvh, 0.5)                    # the plain walk (mode 0 tree is the same)
     plain = p.download()
     for f in ("accX", "accY", "accZ"):
