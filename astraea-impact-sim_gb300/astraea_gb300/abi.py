@@ -232,6 +232,7 @@ SIGNATURES = [
     ("astraea_gb300_set_lookback_spin_limit", [_U32], ctypes.c_int),
     ("astraea_gb300_set_far_field", [ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_set_far_field_expansion", [_U32, _F], ctypes.c_int),
+    ("astraea_gb300_set_node_rounding", [ctypes.c_int], ctypes.c_int),
     ("astraea_gb300_autotune_expansion", [_P, _B, _F, _VP, _U32, ctypes.POINTER(_U32), ctypes.POINTER(_F)],
      ctypes.c_int),
     ("astraea_gb300_debug_lookback_probe", [_U32, ctypes.POINTER(_U32)], ctypes.c_int),

@@ -592,6 +592,13 @@ def autotune_expansion(p, bvh, theta, candidates=(8, 16, 24, 32)):
     return out.value, dict(zip(candidates, list(ms)))
 
 
+def set_node_rounding(mode):
+    """0: node masses and COMs from exact moment sums (default); 1: the
+    engine's FP32 bottom-up rounding (its exact node data and opening
+    decisions).  Applies to later builds."""
+    abi.check(lib().astraea_gb300_set_node_rounding(int(mode)))
+
+
 def set_far_field_expansion(leaf_bucket=16, gamma=0.3):
     """Far-field mode 3: leaf bucket size (0..32) and the group-expansion gamma."""
     abi.check(lib().astraea_gb300_set_far_field_expansion(int(leaf_bucket), float(gamma)))

@@ -647,6 +647,64 @@ uint32_t refitLevels(uint32_t nb) {
     return lev;
 }
 
+// Node masses and COMs rounded as the engine rounds them (node rounding 1):
+// the engine's bottom-up FP32 combination (bottomUpBvhMomentsKernel,
+// engine/sph_gravity.cu:531-621) -- m = m_L + m_R, c = (m_L c_L + m_R c_R)
+// (1 / m) with the sum contracted as nvcc contracts it, fma(m_L, c_L, m_R c_R)
+// (on the reference kernels' own build this gives their COMs bit for bit),
+// c = (c_L + c_R) / 2 for a massless pair.  One thread per leaf climbs
+// towards the root; the second child to arrive at a node combines it (the
+// arrival counters were zeroed by the Karras kernel of this build).  Only
+// the mass and COM of the node records and of the descriptor's arrays are
+// replaced; boxes, h extremes and the quadrupole moments stay the refit's.
+__global__ void __launch_bounds__(256) engineNodeMomentsKernel(AstraeaParticles p, AstraeaRadixBvh bvh, Work w,
+                                                                uint32_t n) {
+    const uint32_t leaf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= n || n < 2u) return;
+    auto childRec = [&](int c) {
+        if (c < 0) {
+            const uint32_t j = static_cast<uint32_t>(~c);
+            return make_float4(p.posX[j], p.posY[j], p.posZ[j], p.mass[j]);
+        }
+        return __ldcg(&w.node[4 * static_cast<size_t>(c)]);
+    };
+    int pNode = __ldcg(&bvh.parent[n - 1u + leaf]);
+    __threadfence();
+    uint32_t climbs = 0;
+    while (pNode >= 0 && pNode < static_cast<int>(n) - 1 && ++climbs < 4096u) {
+        if (atomicAdd(&bvh.atomicVisited[pNode], 1u) == 0u) return;   // the sibling's thread combines
+        const float4 L = childRec(__ldcg(&bvh.leftChild[pNode]));
+        const float4 R = childRec(__ldcg(&bvh.rightChild[pNode]));
+        const float m = __fadd_rn(L.w, R.w);
+        float cx, cy, cz;
+        if (m > 0.0f) {
+            const float inv = __fdiv_rn(1.0f, m);
+            cx = __fmul_rn(__fmaf_rn(L.w, L.x, __fmul_rn(R.w, R.x)), inv);
+            cy = __fmul_rn(__fmaf_rn(L.w, L.y, __fmul_rn(R.w, R.y)), inv);
+            cz = __fmul_rn(__fmaf_rn(L.w, L.z, __fmul_rn(R.w, R.z)), inv);
+        } else {
+            cx = __fmul_rn(0.5f, __fadd_rn(L.x, R.x));
+            cy = __fmul_rn(0.5f, __fadd_rn(L.y, R.y));
+            cz = __fmul_rn(0.5f, __fadd_rn(L.z, R.z));
+        }
+        __stcg(&w.node[4 * static_cast<size_t>(pNode)], make_float4(cx, cy, cz, m));
+        if (bvh.aabbMinX != nullptr) {
+            bvh.nodeMass[pNode] = m;
+            bvh.comX[pNode] = cx; bvh.comY[pNode] = cy; bvh.comZ[pNode] = cz;
+        }
+        if (bvh.nodeComMass != nullptr) bvh.nodeComMass[pNode] = AstraeaFloat4{cx, cy, cz, m};
+        __threadfence();
+        pNode = __ldcg(&bvh.parent[pNode]);
+    }
+}
+
+cudaError_t launchEngineNodeMoments(const AstraeaParticles& p, const AstraeaRadixBvh& bvh, const Work& w, uint32_t n,
+                                    cudaStream_t st) {
+    if (n < 2u) return cudaSuccess;
+    engineNodeMomentsKernel<<<gridFor(n, 256), 256, 0, st>>>(p, bvh, w, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, bool moments, cudaStream_t st) {
     if (n < 2u) return cudaSuccess;
     const uint32_t nb = refitBlocks(n);

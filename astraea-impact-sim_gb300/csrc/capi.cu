@@ -28,6 +28,7 @@ namespace {
 thread_local std::string g_lastError;
 std::atomic<cudaStream_t> g_stream{nullptr};
 std::atomic<uint32_t> g_spinLimit{1u << 22};
+std::atomic<int> g_nodeRounding{0};   // 0: exact moment sums, 1: the engine's FP32 bottom-up rounding
 std::atomic<int> g_farField{0};   // 0: monopole (the engine's), 1: + quadrupole, 2: + learned correction,
                                   // 3: quadrupole + leaf buckets + group expansion of far nodes
 std::atomic<uint32_t> g_leafBucket{16};      // mode 3: leaf bucket (particles)
@@ -467,6 +468,7 @@ AstraeaStatus buildTree(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadix
     marks.mark(ASTRAEA_STAGE_REFIT);
     const bool moments = g_farField.load() != 0;
     AG_LAUNCH(launchRefit(kb, w, n, moments, st));
+    if (g_nodeRounding.load() != 0) AG_LAUNCH(launchEngineNodeMoments(*p, kb, w, n, st));
     ws->treeBuilt = true;
     ws->builtN = n;
     ws->momentsBuilt = moments;
@@ -514,6 +516,12 @@ AstraeaStatus astraea_gb300_set_stream(void* s) {
 AstraeaStatus astraea_gb300_set_far_field(int mode) {
     if (mode < 0 || mode > 3) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0, 1, 2 or 3");
     g_farField.store(mode);
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_set_node_rounding(int mode) {
+    if (mode < 0 || mode > 1) return fail(ASTRAEA_ERR_INVALID, "node rounding must be 0 or 1");
+    g_nodeRounding.store(mode);
     return ASTRAEA_OK;
 }
 

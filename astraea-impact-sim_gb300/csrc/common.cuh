@@ -119,6 +119,15 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
 // Squared length with explicit IEEE rounding and no multiply-add fusion:
 // ((dx*dx + dy*dy) + dz*dz).  Range and acceptance tests use this form so a
 // pair's in/out decision is bit-identical to the oracle.
+// |d|^2 rounded as the engine's compiled kernels round dx*dx + dy*dy + dz*dz:
+// nvcc contracts that expression into fma(dz, dz, fma(dx, dx, dy*dy)) (the
+// reference kernels' gravity on the 1M impact takes exactly the opening
+// decisions of this form, and not those of the unfused sum, on the groups
+// where the two differ).  Used wherever the engine decides with it: the
+// gravity member test, the SPH range tests, the dt candidate.
+__device__ __forceinline__ float len2Engine(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+}
 __device__ __forceinline__ float len2Exact(float dx, float dy, float dz) {
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }

@@ -81,12 +81,12 @@ __device__ __forceinline__ uint32_t laneMaskLt() {
     return m;
 }
 
-// The engine's per-member acceptance test (sph_gravity.cu:914-929) with
-// explicit IEEE rounding: dNode^2 < theta^2 r^2, r^2 > 1e-20 and, when
-// checkInside, the member outside the node box.
+// The engine's per-member acceptance test (sph_gravity.cu:914-929) with the
+// engine's rounding (len2Engine): dNode^2 < theta^2 r^2, r^2 > 1e-20 and,
+// when checkInside, the member outside the node box.
 __device__ __forceinline__ bool acceptsMember(float px, float py, float pz, float4 com, float dd, float theta2,
                                               bool checkInside, float4 bmin, float4 bmax) {
-    const float r2 = len2Exact(__fsub_rn(px, com.x), __fsub_rn(py, com.y), __fsub_rn(pz, com.z));
+    const float r2 = len2Engine(__fsub_rn(px, com.x), __fsub_rn(py, com.y), __fsub_rn(pz, com.z));
     bool ok = (dd < __fmul_rn(theta2, r2)) && (r2 > 1.0e-20f);
     if (ok && checkInside && px >= bmin.x && px <= bmax.x && py >= bmin.y && py <= bmax.y && pz >= bmin.z &&
         pz <= bmax.z)
@@ -445,19 +445,16 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 __syncwarp();
                 unsigned bits = 0u;
                 // the engine's member test (acceptsMember) on two nodes per
-                // iteration, in scalar IEEE operations (__fmul_rn / __fadd_rn
-                // are never contracted into multiply-adds, so a member exactly
-                // on the theta boundary is decided as the engine decides it;
-                // the packed f32x2 form is 2 % faster but its products and
-                // sums may be fused, which moved one exact tie of the 1M
-                // impact, and re-testing near ties in scalar costs more than
-                // it saves)
+                // iteration, rounded as the engine rounds it (len2Engine:
+                // explicit __fmaf_rn / __fmul_rn, which the compiler neither
+                // splits nor re-fuses, so a member on the theta boundary is
+                // decided as the engine decides it)
                 for (int k = 0; k < nu; k += 2) {
                     const float* ub = undP + 4 * k;
                     const float4 pa = *reinterpret_cast<const float4*>(ub);       // com xA, xB, yA, yB
                     const float4 pb = *reinterpret_cast<const float4*>(ub + 4);   // com zA, zB, ddA, ddB
-                    const float r2a = len2Exact(__fsub_rn(xi, pa.x), __fsub_rn(yi, pa.z), __fsub_rn(zi, pb.x));
-                    const float r2b = len2Exact(__fsub_rn(xi, pa.y), __fsub_rn(yi, pa.w), __fsub_rn(zi, pb.y));
+                    const float r2a = len2Engine(__fsub_rn(xi, pa.x), __fsub_rn(yi, pa.z), __fsub_rn(zi, pb.x));
+                    const float r2b = len2Engine(__fsub_rn(xi, pa.y), __fsub_rn(yi, pa.w), __fsub_rn(zi, pb.y));
                     const float ta = __fmul_rn(theta2, r2a), tb = __fmul_rn(theta2, r2b);
                     const float dda = pb.z, ddb = pb.w;
                     bool okA = dda < ta && r2a > 1.0e-20f, okB = ddb < tb && r2b > 1.0e-20f;

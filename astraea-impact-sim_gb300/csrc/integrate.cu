@@ -18,19 +18,21 @@ namespace astraea_gb300 {
 namespace {
 
 // Per-particle dt candidate (sph_gravity.cu:1504-1527), each operation an
-// explicit IEEE op so the minimum is bit-identical to the oracle's.
+// explicit IEEE op rounded as the engine's compiled kernel rounds it (its
+// multiply-adds contracted: |v|^2 as len2Engine, 2.2 cs + |v| and
+// u + 0.01 u_scale as one fma each), so the minimum is bit-identical to the
+// engine's and the oracle's.
 __device__ __forceinline__ float dtCandidate(float h, float cs, float vx, float vy, float vz, float ax, float ay,
                                              float az, float u, float duDt, uint8_t mat) {
     const float hi = fmaxf(h, 1.0e-6f);
     const float csI = fmaxf(cs, 0.05f);
-    const float vMag = __fsqrt_rn(len2Exact(vx, vy, vz));
-    const float dtCfl = __fdiv_rn(__fmul_rn(0.25f, hi), __fadd_rn(__fadd_rn(__fmul_rn(2.2f, csI), vMag), 1.0e-6f));
-    const float aMag = __fsqrt_rn(len2Exact(ax, ay, az));
+    const float vMag = __fsqrt_rn(len2Engine(vx, vy, vz));
+    const float dtCfl = __fdiv_rn(__fmul_rn(0.25f, hi), __fadd_rn(__fmaf_rn(2.2f, csI, vMag), 1.0e-6f));
+    const float aMag = __fsqrt_rn(len2Engine(ax, ay, az));
     const float dtAcc = __fmul_rn(0.25f, __fsqrt_rn(__fdiv_rn(hi, __fadd_rn(aMag, 1.0e-8f))));
     const float uI = fmaxf(u, 0.0f);
     const float uScale = fmaxf(uI, c_mat[matIndex(mat)].u0Ref);
-    const float dtTherm =
-        __fdiv_rn(__fmul_rn(0.20f, __fadd_rn(uI, __fmul_rn(0.01f, uScale))), __fadd_rn(fabsf(duDt), 1.0e-8f));
+    const float dtTherm = __fdiv_rn(__fmul_rn(0.20f, __fmaf_rn(0.01f, uScale, uI)), __fadd_rn(fabsf(duDt), 1.0e-8f));
     return fminf(dtCfl, fminf(dtAcc, dtTherm));
 }
 

@@ -58,6 +58,9 @@ cudaError_t launchPermuteLeavesKarras(const AstraeaParticles& p, const AstraeaPa
 cudaError_t launchRefreshLeaves(const AstraeaParticles& p, const Work& w, uint32_t n, bool withVelRho,
                                 cudaStream_t st);
 cudaError_t launchRefit(const AstraeaRadixBvh& bvh, const Work& w, uint32_t n, bool moments, cudaStream_t st);
+// node masses and COMs in the engine's FP32 bottom-up rounding (after launchRefit)
+cudaError_t launchEngineNodeMoments(const AstraeaParticles& p, const AstraeaRadixBvh& bvh, const Work& w, uint32_t n,
+                                    cudaStream_t st);
 // Scratch geometry of the range refit: blocks of 256 leaves, sparse-table levels.
 uint32_t refitBlocks(uint32_t n);
 uint32_t refitLevels(uint32_t nb);

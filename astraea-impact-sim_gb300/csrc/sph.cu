@@ -355,7 +355,7 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
             if (j == i) continue;
             const float4 q = __ldg(&w.leaf[j].a);
             const float R = fmaxf(Hs, __ldg(&w.leafAux[j]).x);
-            if (len2Exact(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z)) < __fmul_rn(R, R)) f(j);
+            if (len2Engine(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z)) < __fmul_rn(R, R)) f(j);
             continue;
         }
         const float4* rec = w.node + 4 * static_cast<size_t>(c2);
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(128, 7) pass1Kernel(AstraeaParticles p, Work w
         forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&w.leaf[j].a); }, [&](uint32_t j, const F8& rj) {
             const float4 q = rj.a;
             const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
-            const float r2 = len2Exact(dx, dy, dz);
+            const float r2 = len2Engine(dx, dy, dz);
             if (!(r2 < Hi2)) return;                       // sph_gravity.cu:713
             ++ngb;
             const float4 vj = rj.b;
@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
                                    [&](uint32_t j, const F8& q01) {
             const float4 b0 = q01.a;
             const float dx = __fsub_rn(xi, b0.x), dy = __fsub_rn(yi, b0.y), dz = __fsub_rn(zi, b0.z);
-            const float r2 = len2Exact(dx, dy, dz);
+            const float r2 = len2Engine(dx, dy, dz);
             const float hj = b0.w, Hj = 2.0f * hj;
             const float Hm = fmaxf(Hi, Hj);
             if (!(r2 < __fmul_rn(Hm, Hm))) return;          // sph_gravity.cu:1071
@@ -666,7 +666,7 @@ __global__ void __launch_bounds__(128) driftKernel(AstraeaParticles p, Work w, u
             forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&w.drift[j].a); }, [&](uint32_t j, const F8& rj) {
                 const float4 q = rj.a;
                 const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
-                const float r2 = len2Exact(dx, dy, dz);
+                const float r2 = len2Engine(dx, dy, dz);
                 const float Hj = q.w;
                 const float Hm = fmaxf(Hi, Hj);
                 if (!(r2 < __fmul_rn(Hm, Hm))) return;

@@ -169,6 +169,18 @@ AstraeaStatus astraea_gb300_leapfrog_drift(AstraeaParticles* p, float dtPsu,
 AstraeaStatus astraea_gb300_reduce_dt_psu(const AstraeaParticles* p, float prevDtPsu,
                                           float maxDtPsu, float* outDtPsu);
 
+/* Rounding of the node masses and COMs of every later tree build (stage
+ * calls and the fused step).  0 (default): from exact fixed-point moment sums
+ * (each node's COM is the correctly rounded quotient of its exact sums; the
+ * engine's FP32 combination can place the COM of coincident particles off
+ * them).  1: the engine's own FP32 bottom-up combination
+ * (bottomUpBvhMomentsKernel, engine/sph_gravity.cu:531-621, with its
+ * multiply-add contracted as nvcc contracts it), bit-identical to the
+ * engine's node data, so the gravity walk takes exactly the engine's opening
+ * decisions.  Boxes, h extremes and quadrupole moments do not depend on it.
+ * Process-wide. */
+AstraeaStatus astraea_gb300_set_node_rounding(int mode);
+
 /* ---- far-field correction (no counterpart in the engine) ---------------- */
 
 /* Far-field model of every later tree build and gravity evaluation (stage

@@ -299,16 +299,21 @@ int numGroups(uint32_t n) { return static_cast<int>((n + kGroup - 1) / kGroup); 
 // g with g % g_groupStride == 0 (1 = all groups, the normal checker mode).
 int g_groupStride = 1;
 
-// Rounding of the gravity member test's r^2 (probe of how a compiled kernel
-// evaluates dx*dx + dy*dy + dz*dz): 0 the IEEE sequence (dx^2 + dy^2) + dz^2,
-// 1 fma(dz, dz, fma(dx, dx, dy^2)), 2 fma(dz, dz, fma(dy, dy, dx^2)).  The
-// member test of the gravity walk only; 0 unless a test sets it.
-int g_r2Form = 0;
-inline float memberR2(float dx, float dy, float dz) {
+// |d|^2 at the engine's decision points (the gravity member test, the SPH
+// range tests, the dt candidate), rounded as the engine's compiled kernels
+// round dx*dx + dy*dy + dz*dz: nvcc contracts it into fma(dz, dz, fma(dx, dx,
+// dy*dy)) (form 1, the default).  Forms 0 (the unfused sequence (dx^2 + dy^2)
+// + dz^2) and 2 (fma(dz, dz, fma(dy, dy, dx^2))) are kept so a test can show
+// which form the reference kernels' results follow: on the 1M impact they
+// take exactly form 1's gravity opening decisions.
+int g_r2Form = 1;
+inline float engineLen2(float dx, float dy, float dz) {
     if (g_r2Form == 1) return std::fma(dz, dz, std::fma(dx, dx, dy * dy));
     if (g_r2Form == 2) return std::fma(dz, dz, std::fma(dy, dy, dx * dx));
     return dx * dx + dy * dy + dz * dz;
 }
+// a*b + c as the engine's compiled kernel rounds it (one fma, form 1 and 2)
+inline float engineMulAdd(float a, float b, float c) { return g_r2Form == 0 ? a * b + c : std::fma(a, b, c); }
 inline bool skipGroup(int g) { return g_groupStride > 1 && (g % g_groupStride) != 0; }
 
 // Depth-first walk shared by the SPH-style traversals: `open(c)` decides
@@ -503,10 +508,12 @@ void oracle_refit(const AstraeaParticles* p, AstraeaRadixBvh* b, uint32_t* livin
         const float ml = b->nodeMass[l], mr = b->nodeMass[r], ms = ml + mr;
         float cx, cy, cz;
         if (ms > 0.0f) {
+            // (ml cl + mr cr) / m as the engine's compiled kernel rounds it:
+            // the sum contracted into fma(ml, cl, mr cr) (engineMulAdd)
             const float im = 1.0f / ms;
-            cx = (ml * b->comX[l] + mr * b->comX[r]) * im;
-            cy = (ml * b->comY[l] + mr * b->comY[r]) * im;
-            cz = (ml * b->comZ[l] + mr * b->comZ[r]) * im;
+            cx = engineMulAdd(ml, b->comX[l], mr * b->comX[r]) * im;
+            cy = engineMulAdd(ml, b->comY[l], mr * b->comY[r]) * im;
+            cz = engineMulAdd(ml, b->comZ[l], mr * b->comZ[r]) * im;
         } else {
             cx = 0.5f * (b->comX[l] + b->comX[r]);
             cy = 0.5f * (b->comY[l] + b->comY[r]);
@@ -583,7 +590,7 @@ static void pass1Impl(AstraeaParticles* p, const AstraeaRadixBvh* b) {
                     for (int l = 0; l < act; ++l) {
                         const uint32_t i = i0 + l;
                         const float dxf = xf[l] - pxj, dyf = yf[l] - pyj, dzf = zf[l] - pzj;
-                        const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+                        const float r2f = engineLen2(dxf, dyf, dzf);
                         if (j == i || !(r2f < Hi2f[l])) continue;
                         ++cnt[l];
                         const R dx = xi[l] - R(pxj), dy = yi[l] - R(pyj), dz = zi[l] - R(pzj);
@@ -698,7 +705,7 @@ static void gravityImpl(AstraeaParticles* p, const AstraeaRadixBvh* b, float the
                     bool anyOpen = false;
                     for (int l = 0; l < act; ++l) {
                         const float dx = xi[l] - nb.cx, dy = yi[l] - nb.cy, dz = zi[l] - nb.cz;
-                        const float r2 = memberR2(dx, dy, dz);
+                        const float r2 = engineLen2(dx, dy, dz);
                         dxs[l] = dx; dys[l] = dy; dzs[l] = dz; r2s[l] = r2;
                         bool acc = (nb.dNode * nb.dNode < theta2 * r2) && (r2 > 1.0e-20f);
                         if (acc && checkInside && xi[l] >= nb.mnx && xi[l] <= nb.mxx && yi[l] >= nb.mny &&
@@ -864,7 +871,7 @@ void oracle_gravity_expand(AstraeaParticles* p, const AstraeaRadixBvh* b, float 
                 bool anyOpen = false;
                 for (int l = 0; l < act && !anyOpen; ++l) {
                     const float dx = xi[l] - nb.cx, dy = yi[l] - nb.cy, dz = zi[l] - nb.cz;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float r2 = engineLen2(dx, dy, dz);
                     bool acc = (nb.dNode * nb.dNode < theta2 * r2) && (r2 > 1.0e-20f);
                     if (acc && checkInside && xi[l] >= nb.mnx && xi[l] <= nb.mxx && yi[l] >= nb.mny &&
                         yi[l] <= nb.mxy && zi[l] >= nb.mnz && zi[l] <= nb.mxz)
@@ -1078,7 +1085,7 @@ static void pass2Impl(AstraeaParticles* p, const AstraeaRadixBvh* b) {
                         const uint32_t i = i0 + l;
                         Lane& q = L[l];
                         const float dxf = q.xf - pxj, dyf = q.yf - pyj, dzf = q.zf - pzj;
-                        const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+                        const float r2f = engineLen2(dxf, dyf, dzf);
                         const float Hmf = std::fmax(q.Hf, Hjf);
                         if (j == i || !(r2f < Hmf * Hmf)) continue;
                         const R dx = q.x - R(pxj), dy = q.y - R(pyj), dz = q.z - R(pzj);
@@ -1305,7 +1312,7 @@ static void driftImpl(AstraeaParticles* p, float dt, const AstraeaRadixBvh* b, i
                     for (int l = 0; l < act; ++l) {
                         if (i0 + l == j) continue;
                         const float dx = xi[l] - pxj, dy = yi[l] - pyj, dz = zi[l] - pzj;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float r2 = engineLen2(dx, dy, dz);
                         const float Hm = std::fmax(Hi[l], Hj);
                         if (!(r2 < Hm * Hm)) continue;
                         const R r = (sizeof(R) == 4) ? R(std::sqrt(r2))
@@ -1347,14 +1354,16 @@ float oracle_reduce_dt(const AstraeaParticles* p, float prevDt, float maxDt, flo
     float mn = 1.0e30f;
     for (uint32_t i = 0; i < n; ++i) {
         const float hi = std::fmax(p->h[i], 1.0e-6f), cs = std::fmax(p->soundSpeed[i], 0.05f);
-        const float v = std::sqrt(p->velX[i] * p->velX[i] + p->velY[i] * p->velY[i] + p->velZ[i] * p->velZ[i]);
-        const float dtC = 0.25f * hi / (2.2f * cs + v + 1.0e-6f);
-        const float a = std::sqrt(p->accX[i] * p->accX[i] + p->accY[i] * p->accY[i] + p->accZ[i] * p->accZ[i]);
+        // the engine's kernel contracts |v|^2, 2.2 cs + |v| and u + 0.01 u_s
+        // into fmas (engineLen2 / engineMulAdd)
+        const float v = std::sqrt(engineLen2(p->velX[i], p->velY[i], p->velZ[i]));
+        const float dtC = 0.25f * hi / (engineMulAdd(2.2f, cs, v) + 1.0e-6f);
+        const float a = std::sqrt(engineLen2(p->accX[i], p->accY[i], p->accZ[i]));
         const float dtA = 0.25f * std::sqrt(hi / (a + 1.0e-8f));
         const int m = matIndex(p->materialId[i]);
         const float uI = std::fmax(p->u[i], 0.0f);
         const float uS = std::fmax(uI, u0RefPsu(m));
-        const float dtT = 0.20f * (uI + 0.01f * uS) / (std::fabs(p->duDt[i]) + 1.0e-8f);
+        const float dtT = 0.20f * engineMulAdd(0.01f, uS, uI) / (std::fabs(p->duDt[i]) + 1.0e-8f);
         const float d = std::fmin(dtC, std::fmin(dtA, dtT));
         if (std::isfinite(d) && d > 0.0f) mn = std::fmin(mn, d);
     }

@@ -511,9 +511,10 @@ def set_group_stride(k):
 
 
 def set_r2_form(k):
-    """Rounding of r^2 in the gravity member test: 0 the IEEE sequence
-    (default), 1 fma(dz, dz, fma(dx, dx, dy^2)), 2 fma(dz, dz, fma(dy, dy,
-    dx^2)) -- how a compiler that contracts multiply-adds may evaluate it."""
+    """Rounding of |d|^2 (and of the dt candidate's multiply-adds) at the
+    engine's decision points: 1 fma(dz, dz, fma(dx, dx, dy^2)), as the
+    engine's compiled kernels round it (the default); 0 the unfused sequence;
+    2 fma(dz, dz, fma(dy, dy, dx^2))."""
     load().oracle_set_r2_form(int(k))
 
 

@@ -13,7 +13,13 @@ before the stage is copied into the oracle), over every particle:
   within 1e-6;
 * integer outputs exact: the EOS phase of every particle, the gravity
   interaction count (the same interaction set), the dt.
+
+Where the reference's own kernels are present (oracle/_ref, compiled from
+the reference checkout for sm_100), the same snapshot also runs through them
+(oracle/ref_gpu.py) and the library is compared with the engine itself.
 """
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -23,6 +29,8 @@ from astraea_gb300 import abi, engine, scenarios
 from conftest import rel_rms
 
 pytestmark = pytest.mark.gpu
+REF_CUBIN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                         "ref_kernels_sm100.cubin")
 N = 1_000_000
 TOL = 1e-5
 MAX_DT = 5.0e-3
@@ -193,3 +201,89 @@ def test_1m_fused_step_from_snapshot(snapshot):
     fields = ["posX", "posY", "posZ", "velX", "velY", "velZ", "rho", "u", "h"]
     e = report("fused-step", {f: g[f][og] for f in fields}, {f: c[f][oc] for f in fields}, fields)
     assert max(e.values()) < TOL
+
+
+@pytest.mark.skipif(not os.path.exists(REF_CUBIN),
+                    reason="the reference kernels' cubin (built from the reference checkout) is absent")
+def test_1m_against_reference_kernels(snapshot):
+    """The snapshot through the reference's own kernels and through the
+    library with the engine's node rounding (astraea_gb300_set_node_rounding):
+    * the tree bit for bit, node masses and COMs included;
+    * pass 1: h bit for bit (the neighbour counts are the engine's: the range
+      test rounds |d|^2 as the engine's compiled kernel does), the other
+      fields within 1e-5;
+    * gravity: the oracle, whose node data and member test are the engine's
+      bit for bit, makes exactly the library's interaction count in every
+      group, and the accelerations agree with the reference kernels' to
+      float summation order in every group;
+    * dt of the reference's state after pass 2: the same float."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(REF_CUBIN), os.pardir))
+    import ref_gpu
+    s1, _ = snapshot
+    e = ref_gpu.RefEngine(N)
+    e.p.upload(s1)
+    e.alt.count = N
+    e.sort_and_build()
+    p, alt, bvh = setup(s1)
+    engine.set_node_rounding(1)
+    try:
+        engine.sort_and_build_bvh(p, alt, bvh)
+    finally:
+        engine.set_node_rounding(0)
+    torch.cuda.synchronize()
+    for name, k in (("mortonCodesSorted", N), ("indicesSorted", N), ("leftChild", N - 1), ("rightChild", N - 1),
+                    ("parent", 2 * N - 1)):
+        assert torch.equal(bvh.t[name][:k], e.bvh.t[name][:k]), name
+    for f in ("aabbMinX", "aabbMinY", "aabbMinZ", "aabbMaxX", "aabbMaxY", "aabbMaxZ", "nodeMaxH", "nodeMass",
+              "comX", "comY", "comZ"):
+        assert torch.equal(bvh.t[f][: 2 * N - 1], e.bvh.t[f][: 2 * N - 1]), f
+    g, r = p.download(), e.p.download()
+    for f in abi.FIELD_NAMES:
+        assert np.array_equal(g[f], r[f]), f
+
+    engine.sph_pass1_neighbors(p, bvh)
+    e.pass1()
+    g, r = p.download(), e.p.download()
+    hdiff = np.flatnonzero(g["h"] != r["h"])
+    print("1M vs reference kernels: pass 1 h differs for %d particles" % hdiff.size)
+    assert hdiff.size == 0, hdiff[:10]
+    err = report("pass1 vs reference kernels", g, r, ["shepardC", "surfFactor", "divV", "curlVX", "curlVY", "curlVZ"])
+    assert max(err.values()) < TOL
+
+    engine.evaluate_eos(p)
+    e.eos()
+    engine.gravity_barnes_hut(p, bvh, 0.5)
+    e.gravity(0.5)
+    gg = engine.gravity_group_counts(p, bvh, 0.5)
+    g, r = p.download(), e.p.download()
+    o = oracle.Oracle(s1)
+    o.sort_and_build()
+    for f in ("nodeMass", "comX", "comY", "comZ"):       # the oracle's own node data is the engine's
+        assert np.array_equal(o.bvh.a[f][: 2 * N - 1], e.bvh.t[f][: 2 * N - 1].cpu().numpy()), f
+    cg = o.gravity_group_counts(0.5)
+    bad = np.flatnonzero(gg != cg)
+    assert bad.size == 0, [(int(k), int(gg[k]), int(cg[k])) for k in bad[:10]]
+    # per particle, against the RMS acceleration (near the bodies' centres
+    # |a| itself goes to zero): float summation order leaves ~1e-7, one
+    # opening decision taken otherwise ~1e-4
+    A = lambda d: np.stack([d["accX"], d["accY"], d["accZ"]], 1).astype(np.float64)
+    ar = A(r)
+    d = np.linalg.norm(A(g) - ar, axis=1) / np.sqrt(np.mean(np.sum(ar * ar, axis=1)))
+    print("1M gravity vs reference kernels: per-particle difference / RMS |a|: median %.2e, p99.99 %.2e, max %.2e; "
+          "interactions %d" % (np.median(d), np.percentile(d, 99.99), d.max(), int(gg.sum())))
+    err = report("gravity vs reference kernels", g, r, ["accX", "accY", "accZ", "phiGrav"])
+    assert max(err.values()) < 1e-6
+    assert d.max() < 2e-5
+
+    engine.sph_pass2_forces(p, bvh)
+    e.pass2()
+    g, r = p.download(), e.p.download()
+    err = report("pass2 vs reference kernels", g, r, ["accX", "accY", "accZ", "drhoDt", "duDt", "radPowerW"])
+    assert max(err.values()) < TOL
+    q = engine.DeviceParticles(N)
+    q.upload(r)
+    dt_l = engine.reduce_dt_psu(q, 0.0, MAX_DT)
+    dt_r = e.reduce_dt(0.0, MAX_DT)
+    print("1M dt on the reference's state after pass 2: library %.9g, reference kernels %.9g" % (dt_l, dt_r))
+    assert dt_l == dt_r

@@ -74,8 +74,11 @@ def test_oracle_matches_reference_kernels(ref):
     check_build(o.state(), b["mortonCodesSorted"], b["indicesSorted"], b["leftChild"], b["rightChild"], b["parent"], ref)
     for f in ("aabbMinX", "aabbMaxX", "nodeMaxH"):
         assert np.array_equal(b[f], ref["build_node_" + f]), f
+    # node masses and COMs bit for bit: the oracle rounds the engine's
+    # (m_L c_L + m_R c_R) / m as nvcc compiles it, the sum contracted into
+    # fma(m_L, c_L, m_R c_R)
     for f in ("nodeMass", "comX", "comY", "comZ"):
-        assert rel_rms(b[f], ref["build_node_" + f]) < 1e-6, f
+        assert np.array_equal(b[f], ref["build_node_" + f]), f
     for stage, fn in (("pass1", o.pass1), ("eos", o.eos), ("gravity", o.gravity), ("pass2", o.pass2)):
         fn()
         check_stage("oracle", o.state(), ref, stage)
@@ -88,6 +91,21 @@ def test_oracle_matches_reference_kernels(ref):
     s = o.state()
     for f in ("posX", "posY", "posZ"):
         assert rel_rms(s[f], ref["drift_" + f]) < 1e-6, f
+
+
+def test_engine_rounding_is_the_contracted_form(ref):
+    """The evidence for the oracle's rounding model: with the unfused sum the
+    node COMs of the same build differ from the reference kernels' in about
+    a third of the nodes; with the contracted form in none (above)."""
+    try:
+        oracle.set_r2_form(0)
+        o = oracle.Oracle(inputs(ref))
+        o.sort_and_build()
+        diff = sum(int(np.sum(o.bvh.a[f] != ref["build_node_" + f])) for f in ("comX", "comY", "comZ"))
+    finally:
+        oracle.set_r2_form(1)
+    print("node COM components differing from the reference with the unfused sum: %d" % diff)
+    assert diff > 100
 
 
 @pytest.mark.gpu
@@ -105,6 +123,8 @@ def test_library_matches_reference_kernels(ref, packed):
     t = lambda name, k, dt=None: bvh.t[name][:k].cpu().numpy().view(dt) if dt else bvh.t[name][:k].cpu().numpy()
     check_build(p.download(), t("mortonCodesSorted", n, np.uint64), t("indicesSorted", n, np.uint32),
                 t("leftChild", n - 1), t("rightChild", n - 1), t("parent", 2 * n - 1), ref)
+    # default node rounding: exact moment sums, within an ulp or so of the
+    # engine's FP32 combination
     for f in ("nodeMass", "comX", "comY", "comZ"):
         assert rel_rms(t(f, 2 * n - 1), ref["build_node_" + f]) < 1e-6, f
     for stage, fn in (("pass1", lambda: engine.sph_pass1_neighbors(p, bvh)), ("eos", lambda: engine.evaluate_eos(p)),
@@ -158,3 +178,27 @@ def test_fused_steps_track_reference_kernels(ref):
                                                           "h", "accX", "accY", "accZ")}
     print("fused-vs-reference-kernels " + " ".join("%s=%.2e" % kv for kv in errs.items()))
     assert max(errs.values()) < 1e-4
+
+
+@pytest.mark.gpu
+def test_engine_node_rounding_gives_reference_node_data(ref):
+    """astraea_gb300_set_node_rounding(1): the library's node masses and COMs
+    equal the reference kernels' bit for bit, and gravity on that tree equals
+    the reference kernels' (the same opening decisions; the pair sums in
+    another order)."""
+    st = inputs(ref)
+    n = len(st["posX"])
+    p, alt = engine.DeviceParticles(n), engine.DeviceParticles(n)
+    p.upload(st)
+    alt.count = n
+    bvh = engine.TorchBvh(n, packed=True)
+    engine.set_node_rounding(1)
+    try:
+        engine.sort_and_build_bvh(p, alt, bvh)
+    finally:
+        engine.set_node_rounding(0)
+    torch.cuda.synchronize()
+    for f in ("nodeMass", "comX", "comY", "comZ"):
+        assert np.array_equal(bvh.t[f][: 2 * n - 1].cpu().numpy(), ref["build_node_" + f]), f
+    engine.gravity_barnes_hut(p, bvh, 0.5)
+    check_stage("gb300 engine-rounded nodes", p.download(), ref, "gravity", tol=1e-6)
