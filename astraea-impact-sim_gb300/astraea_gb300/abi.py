@@ -152,7 +152,7 @@ class PlanetInfo(ctypes.Structure):
 
 class FarFieldConfig(ctypes.Structure):
     _fields_ = [("thetaFar", ctypes.c_float), ("gamma", ctypes.c_float), ("gateTolerance", ctypes.c_float),
-                ("gateTargets", _U32), ("pairsPerGroup", _U32), ("gateFp32Pairs", _U32)]
+                ("gateTargets", _U32), ("pairsPerGroup", _U32), ("gateFp64Pairs", _U32)]
 
 
 class FarFieldStats(ctypes.Structure):

@@ -363,9 +363,9 @@ def build_planet(spec, particle_count, p, offset=0, body_id=0, tracer_grid_res=0
 
 # ------------------------------------------------- learned far field (mode 2)
 def ff_configure(theta_far=0.8, gamma=0.3, gate_tolerance=0.0, gate_targets=64, pairs_per_group=64,
-                 gate_fp32_pairs=False):
+                 gate_fp64_pairs=False):
     cfg = abi.FarFieldConfig(float(theta_far), float(gamma), float(gate_tolerance), int(gate_targets),
-                             int(pairs_per_group), int(bool(gate_fp32_pairs)))
+                             int(pairs_per_group), int(bool(gate_fp64_pairs)))
     abi.check(lib().astraea_gb300_ff_configure(ctypes.byref(cfg)))
 
 

@@ -355,7 +355,7 @@ AstraeaStatus ffWalk(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta
 
 // Gravity of far-field mode 2: walk, network on the recorded pairs,
 // per-member correction, and (gateTolerance > 0) the gate: a direct-sum spot
-// check of gateTargets particles (FP64, or FP32 pair terms with FP64 sums)
+// check of gateTargets particles (FP32 pair terms with FP64 sums, or FP64)
 // decides on the device whether the plain walk at theta that follows runs or
 // returns at once.  No host round trip, so a gated step can be captured in a
 // CUDA graph.
@@ -384,7 +384,7 @@ AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, flo
     if (gate && f->cfg.gateTolerance > 0.0f && n >= 2u) {
         const uint32_t K = std::max<uint32_t>(1u, std::min(f->cfg.gateTargets, n));
         AG_LAUNCH(ff::launchGate(*p, ws->w, n, K, f->cfg.gateTolerance, f->word, f->pairCap, f->gate,
-                                 f->cfg.gateFp32Pairs != 0u, st));
+                                 f->cfg.gateFp64Pairs == 0u, st));
         mark(4);
         Work w = ws->w;
         w.runIf = &f->gate->runFallback;       // the plain walk at theta, run only when the gate failed

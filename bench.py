@@ -656,10 +656,10 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
             # where the time of the mode goes (no gate: spot check and fallback 0)
             parts = [engine.ff_profile(sim.p, sim.bvh, theta) for _ in range(3)]
             rec["gravity_parts_ms"] = {k: float(np.median([q[k] for q in parts])) for k in parts[0]}
-            engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=1.0, gate_targets=64)
-            gated = engine.ff_profile(sim.p, sim.bvh, theta)
             engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=1.0, gate_targets=64,
-                                gate_fp32_pairs=True)
+                                gate_fp64_pairs=True)
+            gated = engine.ff_profile(sim.p, sim.bvh, theta)
+            engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=1.0, gate_targets=64)
             gated32 = engine.ff_profile(sim.p, sim.bvh, theta)
             engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=0.0)
             rec["gate_ms"] = {"fp64_spot_check_64_targets": gated["gate"],

@@ -393,19 +393,19 @@ AstraeaStatus astraea_gb300_build_planet(const AstraeaBodySpec* spec, uint32_t p
  * group's pairs of R + J (x_i - c).  Features: (COM - c)/r, dNode/r,
  * S/(M dNode^2) (central second moments), group extent/r.  With
  * gateTolerance > 0 every mode-2 gravity call checks the RMS relative error
- * of gateTargets sampled particles against a direct sum (gateFp32Pairs 0:
- * FP64 pair terms and sums; 1: FP32 pair terms with FP64 sums, ~1e-6
- * relative and several times cheaper) and, above the tolerance, recomputes
- * plain theta gravity; the decision is taken on the device (the plain walk
- * is always launched and returns at once when the check passed), so the call
- * does not block and can be graph-captured. */
+ * of gateTargets sampled particles against a direct sum (gateFp64Pairs 0:
+ * FP32 pair terms with FP64 sums, ~1e-6 relative of the FP64 sum, the
+ * default; 1: FP64 pair terms, about twenty times the cost on this part) and,
+ * above the tolerance, recomputes plain theta gravity; the decision is taken
+ * on the device (the plain walk is always launched and returns at once when
+ * the check passed), so the call does not block and can be graph-captured. */
 typedef struct AstraeaFarFieldConfig {
     float thetaFar;          /* opening angle of the far test (default 0.8) */
     float gamma;             /* far test: L1 group extent <= gamma r (default 0.3) */
     float gateTolerance;     /* RMS relative force error at the gate; 0: no gate (default) */
     uint32_t gateTargets;    /* sampled particles of the gate (default 64, at most 1024) */
     uint32_t pairsPerGroup;  /* pair buffer per group of 32 (default 64); a full buffer opens the node */
-    uint32_t gateFp32Pairs;  /* 0: FP64 spot check (default); 1: FP32 pair terms, FP64 sums */
+    uint32_t gateFp64Pairs;  /* 0: FP32 pair terms, FP64 sums (default); 1: FP64 pair terms */
 } AstraeaFarFieldConfig;
 
 typedef struct AstraeaFarFieldStats {

@@ -161,7 +161,7 @@ def test_gpu_gate_that_passes_keeps_the_learned_result():
         engine.sort_and_build_bvh(p, alt, bvh)
         engine.gravity_barnes_hut(p, bvh, 0.5)
         ungated = p.download()
-        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=10.0, gate_targets=32)
+        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=10.0, gate_targets=32, gate_fp64_pairs=True)
         engine.gravity_barnes_hut(p, bvh, 0.5)
         gated = p.download()
     finally:
@@ -173,8 +173,8 @@ def test_gpu_gate_that_passes_keeps_the_learned_result():
     # spaced sorted targets.  The RMS is of relative errors, so a relative
     # difference d between the two reference sums moves it by about d: the
     # device softens with eps = 0.8 h0 rounded to float (the walk's value),
-    # the host in FP64, which leaves d ~ 1e-8 for the FP64 spot check; FP32
-    # pair terms add ~1e-6
+    # the host in FP64, which leaves d ~ 1e-8 for the FP64 spot check; the
+    # default FP32 pair terms (FP64 sums) add ~1e-6
     targets = np.array([k * (n - 1) // 31 for k in range(32)], np.uint32)
     sorted_state = {k: gated[k] for k in ("posX", "posY", "posZ", "mass", "h0")}
     host_rms = rms_vs_direct(gated, sorted_state, targets)
@@ -182,7 +182,7 @@ def test_gpu_gate_that_passes_keeps_the_learned_result():
     assert abs(stats["lastGateRms"] - host_rms) <= 5e-8
     try:
         engine.set_far_field(2)
-        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=10.0, gate_targets=32, gate_fp32_pairs=True)
+        engine.ff_configure(theta_far=0.9, gamma=0.3, gate_tolerance=10.0, gate_targets=32)
         engine.gravity_barnes_hut(p, bvh, 0.5)
         rms32 = engine.ff_stats()["lastGateRms"]
     finally:
