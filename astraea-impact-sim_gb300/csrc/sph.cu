@@ -119,32 +119,22 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
         // Superset test r < max(Hs_i, Hs_j) in plain FMA arithmetic, two
         // candidates per instruction: every pass re-tests its own radius
         // exactly, and Hs exceeds those radii by 0.9 %, far more than any
-        // rounding difference.  Tests candidates 0 .. 2 pairs - 1 into a bit
-        // mask first, then appends the hits in candidate order: the stores
-        // run max-hits-per-lane times instead of once per candidate under a
-        // divergent branch.
+        // rounding difference.  Tests candidates 0 .. 2 pairs - 1 in order.
         const f2 X2 = pack2(me.x, me.x), Y2 = pack2(me.y, me.y), Z2 = pack2(me.z, me.z);
         auto flush = [&](int pairs) {
             if (active) {
-                uint32_t hits = 0u;            // bit c: candidate c in range
-#pragma unroll 4
                 for (int k = 0; k < pairs; ++k) {
                     const float* b = S.cand + 8 * k;
                     const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(b);       // (x), (y)
                     const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(b + 4);   // (z), (Hs)
+                    const int2 jj = *reinterpret_cast<const int2*>(S.candIdx + 2 * k);
                     const f2 dx = sub2(X2, u.x), dy = sub2(Y2, u.y), dz = sub2(Z2, v.x);
                     float r2a, r2b, ha, hb;
                     unpack2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))), r2a, r2b);
                     unpack2(v.y, ha, hb);
                     const float Ra = fmaxf(Hs, ha), Rb = fmaxf(Hs, hb);
-                    hits |= ((r2a < Ra * Ra) ? 1u : 0u) << (2 * k);
-                    hits |= ((r2b < Rb * Rb) ? 2u : 0u) << (2 * k);
-                }
-                while (hits != 0u) {
-                    const int c = __ffs(hits) - 1;
-                    hits &= hits - 1u;
-                    const int j = S.candIdx[c];
-                    if (j != static_cast<int>(i)) put(static_cast<uint32_t>(j));
+                    if (r2a < Ra * Ra && jj.x != static_cast<int>(i)) put(static_cast<uint32_t>(jj.x));
+                    if (r2b < Rb * Rb && jj.y != static_cast<int>(i)) put(static_cast<uint32_t>(jj.y));
                 }
             }
         };

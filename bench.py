@@ -278,7 +278,12 @@ def run_gpu(args):
         try:
             with open(tpath) as fh:
                 tr = json.load(fh)
-            traffic = tr.get("bytes_per_particle") and tr["bytes_per_particle"] * n
+            # measured per launch at this N when the capture is of this size,
+            # else scaled by the particle count (the records are read once)
+            if tr.get("n") == n and tr.get("dram_bytes_per_launch"):
+                traffic = float(tr["dram_bytes_per_launch"])
+            else:
+                traffic = tr.get("bytes_per_particle") and tr["bytes_per_particle"] * n
         except ValueError:
             traffic = None
 
