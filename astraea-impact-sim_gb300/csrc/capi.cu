@@ -93,6 +93,30 @@ AstraeaStatus deviceState(DeviceState** out) {
 }
 
 // ------------------------------------------------------------- workspace
+// The per-tree buffers of far-field mode 2: pair records, group centres and
+// corrections, the pair-count word and the gate's device state.  One set
+// per workspace (per BVH), so instances of an ensemble stepping in mode 2
+// on their own streams neither share nor race on them; allocated at a
+// workspace's first mode-2 call (an eager call: before any stream capture).
+struct FfBuffers {
+    uint2* pairs = nullptr;
+    uint32_t pairCap = 0;
+    float4* groups = nullptr;
+    float* groupCorr = nullptr;
+    uint32_t groupCap = 0;
+    uint32_t* word = nullptr;      // [0]: pair count
+    ff::GateDev* gate = nullptr;   // spot-check sums, decision, statistics
+    bool lastCallGated = false;
+    void release() {
+        if (pairs) cudaFree(pairs);
+        if (groups) cudaFree(groups);
+        if (groupCorr) cudaFree(groupCorr);
+        if (word) cudaFree(word);
+        if (gate) cudaFree(gate);
+        *this = FfBuffers{};
+    }
+};
+
 struct Workspace {
     int device = 0;
     Work w{};
@@ -111,6 +135,7 @@ struct Workspace {
     // starts, event kStageCount where the step ends (created on first use)
     cudaEvent_t stageEv[kStageCount + 1] = {};
     bool stageRecorded = false;
+    FfBuffers ff;                  // far-field mode 2 (created on first use)
 };
 std::map<std::pair<int, const void*>, Workspace*> g_work;
 
@@ -212,6 +237,7 @@ void dropWorkspace(const void* leftChild) {
             cudaFree(it->second->block);
             for (cudaEvent_t e : it->second->stageEv)
                 if (e) cudaEventDestroy(e);
+            it->second->ff.release();
             delete it->second;
             g_work.erase(it);
             return;
@@ -279,14 +305,7 @@ struct FfState {
     bool ready = false;            // parameters initialised or loaded
     int adamStep = 0;
     AstraeaFarFieldConfig cfg{0.8f, 0.3f, 0.0f, 64u, 64u, 0u};
-    uint2* pairs = nullptr;
-    uint32_t pairCap = 0;
-    float4* groups = nullptr;
-    float* groupCorr = nullptr;
-    uint32_t groupCap = 0;
-    uint32_t* word = nullptr;      // [0]: pair count
-    ff::GateDev* gate = nullptr;   // the gate's device state (spot-check sum, decision, statistics)
-    bool lastCallGated = false;
+    const FfBuffers* last = nullptr;   // buffers of the last mode-2 gravity call (for ff_stats)
     float* pinned = nullptr;       // 4 floats / words for read-backs
     AstraeaFarFieldStats stats{0ull, 0ull, 0u, 0u, -1.0f, 0.0f};
 };
@@ -301,9 +320,6 @@ AstraeaStatus ffState(FfState** out) {
         AG_CUDA(cudaMalloc(&f.net.adamV, ff::kParams * sizeof(float)));
         AG_CUDA(cudaMalloc(&f.net.outScale, ff::kOut * sizeof(float)));
         AG_CUDA(cudaMalloc(&f.net.loss, sizeof(float)));
-        AG_CUDA(cudaMalloc(&f.word, 4 * sizeof(uint32_t)));
-        AG_CUDA(cudaMalloc(&f.gate, sizeof(ff::GateDev)));
-        AG_CUDA(cudaMemset(f.gate, 0, sizeof(ff::GateDev)));
         AG_CUDA(cudaMallocHost(&f.pinned, 4 * sizeof(float)));
         AG_CUDA(cudaMemset(f.net.params, 0, ff::kParams * sizeof(float)));
         AG_CUDA(cudaMemset(f.net.grads, 0, ff::kParams * sizeof(float)));
@@ -317,37 +333,44 @@ AstraeaStatus ffState(FfState** out) {
     return ASTRAEA_OK;
 }
 
-AstraeaStatus ffCapacity(FfState* f, uint32_t groups) {
+AstraeaStatus ffCapacity(FfBuffers* b, const FfState* f, uint32_t groups) {
+    if (b->word == nullptr) {
+        AG_CUDA(cudaMalloc(&b->word, 4 * sizeof(uint32_t)));
+        AG_CUDA(cudaMalloc(&b->gate, sizeof(ff::GateDev)));
+        AG_CUDA(cudaMemset(b->gate, 0, sizeof(ff::GateDev)));
+    }
     const uint64_t want = static_cast<uint64_t>(groups) * std::max<uint32_t>(1u, f->cfg.pairsPerGroup);
     if (want > 0xFFFFFFFFull) return fail(ASTRAEA_ERR_CAPACITY, "far-field pair buffer above 2^32 entries");
-    if (f->pairCap < want) {
-        if (f->pairs) cudaFree(f->pairs);
-        f->pairs = nullptr;
-        f->pairCap = 0;
-        AG_CUDA(cudaMalloc(&f->pairs, want * sizeof(uint2)));
-        f->pairCap = static_cast<uint32_t>(want);
+    if (b->pairCap < want) {
+        if (b->pairs) cudaFree(b->pairs);
+        b->pairs = nullptr;
+        b->pairCap = 0;
+        AG_CUDA(cudaMalloc(&b->pairs, want * sizeof(uint2)));
+        b->pairCap = static_cast<uint32_t>(want);
     }
-    if (f->groupCap < groups) {
-        if (f->groups) cudaFree(f->groups);
-        if (f->groupCorr) cudaFree(f->groupCorr);
-        f->groups = nullptr;
-        f->groupCorr = nullptr;
-        f->groupCap = 0;
-        AG_CUDA(cudaMalloc(&f->groups, groups * sizeof(float4)));
-        AG_CUDA(cudaMalloc(&f->groupCorr, 12ull * groups * sizeof(float)));
-        f->groupCap = groups;
+    if (b->groupCap < groups) {
+        if (b->groups) cudaFree(b->groups);
+        if (b->groupCorr) cudaFree(b->groupCorr);
+        b->groups = nullptr;
+        b->groupCorr = nullptr;
+        b->groupCap = 0;
+        AG_CUDA(cudaMalloc(&b->groups, groups * sizeof(float4)));
+        AG_CUDA(cudaMalloc(&b->groupCorr, 12ull * groups * sizeof(float)));
+        b->groupCap = groups;
     }
     return ASTRAEA_OK;
 }
 
-// The mode-2 walk: the theta walk plus the far test; records pairs.
+// The mode-2 walk: the theta walk plus the far test; records pairs into the
+// workspace's own buffers.
 AstraeaStatus ffWalk(AstraeaParticles* p, Workspace* ws, uint32_t n, float theta, FfState* f, uint32_t stride) {
     const uint32_t groups = (n + 31u) / 32u;
-    AstraeaStatus s = ffCapacity(f, groups);
+    FfBuffers* b = &ws->ff;
+    AstraeaStatus s = ffCapacity(b, f, groups);
     if (s != ASTRAEA_OK) return s;
     cudaStream_t st = stream();
-    AG_CUDA(cudaMemsetAsync(f->word, 0, sizeof(uint32_t), st));
-    FarCapture cap{f->pairs, f->pairCap, f->word, f->groups, f->cfg.thetaFar * f->cfg.thetaFar,
+    AG_CUDA(cudaMemsetAsync(b->word, 0, sizeof(uint32_t), st));
+    FarCapture cap{b->pairs, b->pairCap, b->word, b->groups, f->cfg.thetaFar * f->cfg.thetaFar,
                    f->cfg.gamma * f->cfg.gamma, std::max<uint32_t>(1u, stride)};
     AG_LAUNCH(launchGravity(*p, ws->w, n, theta, false, smCount(), st, &cap));
     return ASTRAEA_OK;
@@ -374,23 +397,25 @@ AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, flo
     if (s != ASTRAEA_OK) return s;
     const uint32_t groups = (n + 31u) / 32u;
     mark(1);
-    AG_CUDA(cudaMemsetAsync(f->groupCorr, 0, 12ull * groups * sizeof(float), st));
-    AG_LAUNCH(ff::launchApply(f->net, ws->w, f->pairs, f->word, f->pairCap, f->groups, f->groupCorr, smCount(), st));
+    FfBuffers* b = &ws->ff;
+    AG_CUDA(cudaMemsetAsync(b->groupCorr, 0, 12ull * groups * sizeof(float), st));
+    AG_LAUNCH(ff::launchApply(f->net, ws->w, b->pairs, b->word, b->pairCap, b->groups, b->groupCorr, smCount(), st));
     mark(2);
-    AG_LAUNCH(ff::launchCorrect(*p, f->groups, f->groupCorr, n, st));
+    AG_LAUNCH(ff::launchCorrect(*p, b->groups, b->groupCorr, n, st));
     mark(3);
     f->stats.calls++;
-    f->lastCallGated = false;
+    b->lastCallGated = false;
+    f->last = b;
     if (gate && f->cfg.gateTolerance > 0.0f && n >= 2u) {
         const uint32_t K = std::max<uint32_t>(1u, std::min(f->cfg.gateTargets, n));
-        AG_LAUNCH(ff::launchGate(*p, ws->w, n, K, f->cfg.gateTolerance, f->word, f->pairCap, f->gate,
+        AG_LAUNCH(ff::launchGate(*p, ws->w, n, K, f->cfg.gateTolerance, b->word, b->pairCap, b->gate,
                                  f->cfg.gateFp64Pairs == 0u, st));
         mark(4);
         Work w = ws->w;
-        w.runIf = &f->gate->runFallback;       // the plain walk at theta, run only when the gate failed
+        w.runIf = &b->gate->runFallback;       // the plain walk at theta, run only when the gate failed
         AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), st, nullptr,
                                 static_cast<int>(tuningFor(n).gravityWarps)));
-        f->lastCallGated = true;
+        b->lastCallGated = true;
     } else {
         mark(4);
     }
@@ -1025,11 +1050,11 @@ AstraeaStatus astraea_gb300_ff_collect(AstraeaParticles* p, const AstraeaRadixBv
     s = ffWalk(p, ws, n, theta, f, groupStride);
     if (s != ASTRAEA_OK) return s;
     uint32_t recorded = 0;
-    AG_CUDA(cudaMemcpyAsync(f->pinned, f->word, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AG_CUDA(cudaMemcpyAsync(f->pinned, ws->ff.word, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     AG_CUDA(cudaStreamSynchronize(st));
     std::memcpy(&recorded, f->pinned, sizeof(uint32_t));
-    const uint32_t rows = std::min(std::min(recorded, f->pairCap), capacity);
-    AG_LAUNCH(ff::launchLabels(ws->w, n, f->pairs, rows, f->groups, features, labels, st));
+    const uint32_t rows = std::min(std::min(recorded, ws->ff.pairCap), capacity);
+    AG_LAUNCH(ff::launchLabels(ws->w, n, ws->ff.pairs, rows, ws->ff.groups, features, labels, st));
     AG_CUDA(cudaStreamSynchronize(st));
     ws->stepCacheValid = false;
     *outCount = rows;
@@ -1185,12 +1210,27 @@ AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out) {
     FfState* f = nullptr;
     AstraeaStatus s = ffState(&f);
     if (s != ASTRAEA_OK) return s;
-    ff::GateDev g{};
-    AG_CUDA(cudaStreamSynchronize(stream()));
-    AG_CUDA(cudaMemcpy(&g, f->gate, sizeof(g), cudaMemcpyDeviceToHost));
-    f->stats.fallbacks = g.fallbacks;
-    f->stats.lastPairs = g.lastPairs;
-    f->stats.lastGateRms = f->lastCallGated ? g.lastRms : -1.0f;
+    // fallbacks over every workspace of this device; the last gate's values
+    // from the workspace of the last mode-2 call (only compared, never
+    // dereferenced: that workspace may have been released since)
+    AG_CUDA(cudaDeviceSynchronize());
+    uint64_t fallbacks = 0;
+    ff::GateDev lastGate{};
+    bool lastFound = false, lastGated = false;
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        for (const auto& kv : g_work) {
+            const FfBuffers& b = kv.second->ff;
+            if (kv.first.first != currentDevice() || b.gate == nullptr) continue;
+            ff::GateDev g{};
+            AG_CUDA(cudaMemcpy(&g, b.gate, sizeof(g), cudaMemcpyDeviceToHost));
+            fallbacks += g.fallbacks;
+            if (&b == f->last) { lastGate = g; lastFound = true; lastGated = b.lastCallGated; }
+        }
+    }
+    f->stats.fallbacks = fallbacks;
+    f->stats.lastPairs = lastFound ? lastGate.lastPairs : 0u;
+    f->stats.lastGateRms = (lastFound && lastGated) ? lastGate.lastRms : -1.0f;
     *out = f->stats;
     return ASTRAEA_OK;
 }

@@ -408,9 +408,14 @@ typedef struct AstraeaFarFieldConfig {
     uint32_t gateFp64Pairs;  /* 0: FP32 pair terms, FP64 sums (default); 1: FP64 pair terms */
 } AstraeaFarFieldConfig;
 
+/* The pair records, corrections and gate state of mode 2 are kept per BVH
+ * (created by its first mode-2 gravity call, which must come before any
+ * stream capture), so several instances can step in mode 2 concurrently, on
+ * their own streams or as branches of one graph, each gated on its own
+ * spot check.  The network and the configuration are shared. */
 typedef struct AstraeaFarFieldStats {
     uint64_t calls;          /* mode-2 gravity evaluations */
-    uint64_t fallbacks;      /* ... that the gate sent back to the plain walk */
+    uint64_t fallbacks;      /* ... that the gate sent back to the plain walk (all BVHs of the device) */
     uint32_t lastPairs;      /* (group, node) pairs corrected by the last gated call */
     uint32_t reserved;
     float lastGateRms;       /* RMS relative error of the last gate; -1 when no gate ran */
@@ -448,6 +453,8 @@ AstraeaStatus astraea_gb300_ff_predict(const float* features, uint32_t count, fl
 /* Host copies of the 6,288 parameters and the 16 output scales. */
 AstraeaStatus astraea_gb300_ff_get_params(float* params, uint32_t capacity, float* outScale16);
 AstraeaStatus astraea_gb300_ff_set_params(const float* params, uint32_t count, const float* outScale16);
+/* Synchronises the device; lastPairs and lastGateRms are those of the last
+ * mode-2 gravity call's BVH. */
 AstraeaStatus astraea_gb300_ff_stats(AstraeaFarFieldStats* out);
 /* One far-field mode-2 gravity call (current mode must be 2, tree built in
  * it) with CUDA events between its parts; outMs5 (host) receives the times of
