@@ -183,43 +183,27 @@ def load_scenario(cfg, sim=None):
     return sim, out
 
 
-def run_headless(preset="LivingGaiaAsteroidCataclysm", particles=100000, steps=100, dt_max_sec=5.0,
-                 relax_steps=None, verify=True):
-    """engine/headless_main.cpp:162-281: load, step, conservation figures;
-    returns a dict (ok = thresholds met when verify)."""
-    cfg = preset_config(preset, particles, relax_steps)
-    r_t = engine.solve_hydrostatic(cfg["target"])[1]
-    r_i = engine.solve_hydrostatic(cfg["impactor"])[1] if cfg["impactor"].massKg > 0.0 else 0.0
-    m_tot_kg = cfg["target"].massKg + max(0.0, cfg["impactor"].massKg)
-    r_scale = max(r_t + r_i, 1.0)
-    v_esc = math.sqrt(2.0 * G_SI * m_tot_kg / r_scale)
-
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sim, info = load_scenario(cfg)
-    torch.cuda.synchronize()
-    load_s = time.perf_counter() - t0
-    rt, living = info["target_radius_psu"], info["living_body_present"]
-
+def conservation_audit(step, particles, rt, living, steps, m_tot_kg, r_scale, v_esc):
+    """The conservation figures of engine/headless_main.cpp:222-281: the
+    device telemetry before and after `steps` calls of step() (each returns
+    its dt in PSU), radiated energy integrated with the trapezoid rule, energy
+    drift relative to |E0|, |dP| / (M v_esc) and |dL| / max(|L0|, 1e-6 M R
+    v_esc).  particles() gives the device state to reduce (a DeviceParticles
+    of this library or of any stepper that keeps the engine's SoA)."""
     def energy(t):
         return (t["kineticPsu"] + t["potentialPsu"] + t["internalPsu"]) * E_UNIT
 
-    tel0 = engine.reduce_telemetry(sim.p, rt, living)
+    tel0 = engine.reduce_telemetry(particles(), rt, living)
     e0 = energy(tel0)
     p0 = np.array(tel0["momentumPsu"]) * M_UNIT * V_UNIT
     l0 = np.array(tel0["angularMomentumPsu"]) * L_ANG_UNIT
     prev_rad = tel0["radiatedPowerW"]
     e_rad = 0.0
-    max_dt = float(max(1.0e-5, dt_max_sec) / T_UNIT)
     tel = tel0
     finite = math.isfinite(e0)
-    step_s = 0.0
     for _ in range(steps):
-        torch.cuda.synchronize()
-        ts = time.perf_counter()
-        dt = sim.step(max_dt)
-        step_s += time.perf_counter() - ts
-        tel = engine.reduce_telemetry(sim.p, rt, living)
+        dt = step()
+        tel = engine.reduce_telemetry(particles(), rt, living)
         curr = tel["radiatedPowerW"]
         e_rad += 0.5 * (prev_rad + curr) * dt * T_UNIT
         prev_rad = curr
@@ -230,6 +214,51 @@ def run_headless(preset="LivingGaiaAsteroidCataclysm", particles=100000, steps=1
     p_rel = float(np.linalg.norm(dp) / (m_tot_kg * v_esc)) if m_tot_kg * v_esc > 0 else 0.0
     l_ref = max(float(np.linalg.norm(l0)), m_tot_kg * r_scale * v_esc * 1.0e-6)
     l_rel = float(np.linalg.norm(dl) / l_ref)
+    return {"energy_j_t0": e0, "energy_j_t1": energy(tel), "radiated_j": e_rad, "p0": p0, "l0": l0, "tel": tel,
+            "energy_drift_rel": drift, "dp_rel": p_rel, "dl_rel": l_rel, "finite": finite}
+
+
+def scenario_scales(cfg):
+    """Total mass (kg), the length scale R_t + R_i (m) and v_esc over it, as
+    the headless runner forms them for its thresholds."""
+    r_t = engine.solve_hydrostatic(cfg["target"])[1]
+    r_i = engine.solve_hydrostatic(cfg["impactor"])[1] if cfg["impactor"].massKg > 0.0 else 0.0
+    m_tot_kg = cfg["target"].massKg + max(0.0, cfg["impactor"].massKg)
+    r_scale = max(r_t + r_i, 1.0)
+    return m_tot_kg, r_scale, math.sqrt(2.0 * G_SI * m_tot_kg / r_scale)
+
+
+def run_headless(preset="LivingGaiaAsteroidCataclysm", particles=100000, steps=100, dt_max_sec=5.0,
+                 relax_steps=None, verify=True):
+    """engine/headless_main.cpp:162-281: load, step, conservation figures;
+    returns a dict (ok = thresholds met when verify)."""
+    cfg = preset_config(preset, particles, relax_steps)
+    m_tot_kg, r_scale, v_esc = scenario_scales(cfg)
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim, info = load_scenario(cfg)
+    torch.cuda.synchronize()
+    load_s = time.perf_counter() - t0
+    rt, living = info["target_radius_psu"], info["living_body_present"]
+
+    max_dt = float(max(1.0e-5, dt_max_sec) / T_UNIT)
+
+    def step():
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        dt = sim.step(max_dt)
+        step.seconds += time.perf_counter() - ts
+        return dt
+    step.seconds = 0.0
+    a = conservation_audit(step, lambda: sim.p, rt, living, steps, m_tot_kg, r_scale, v_esc)
+    step_s = step.seconds
+    drift, p_rel, l_rel, finite = a["energy_drift_rel"], a["dp_rel"], a["dl_rel"], a["finite"]
+    e0, e_rad, p0, l0, tel = a["energy_j_t0"], a["radiated_j"], a["p0"], a["l0"], a["tel"]
+
+    def energy(t):
+        return (t["kineticPsu"] + t["potentialPsu"] + t["internalPsu"]) * E_UNIT
+
     res = {"preset": preset, "particles": sim.p.count, "tracers": info["tracers"], "steps": steps,
            "energy_j_t0": e0, "energy_j_t1": energy(tel), "radiated_j": e_rad,
            "momentum_t0": p0.tolist(), "momentum_t1": (np.array(tel["momentumPsu"]) * M_UNIT * V_UNIT).tolist(),

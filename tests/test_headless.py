@@ -14,6 +14,7 @@ steps with the device telemetry reduction.
 CPU: the preset table and the Kepler placement's contact speed.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -113,3 +114,49 @@ def test_gpu_tracers_survive_resorts():
         sim.step(5.0e-3)
     t = sim.state(["tracerIndex"])["tracerIndex"]
     assert np.array_equal(np.sort(t[t >= 0]), np.arange(T))
+
+
+REF_CUBIN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                         "ref_kernels_sm100.cubin")
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.path.exists(REF_CUBIN),
+                    reason="the reference kernels' cubin (built from the reference checkout) is absent")
+def test_gpu_conservation_audit_matches_reference_kernels():
+    """AC-5 (EarthTheiaMoonForming, 20,000 particles, 150 steps of at most
+    5 s) from one loaded scenario, stepped by this library and by the
+    reference's own kernels (oracle/ref_gpu.py) on the same GPU; both audited
+    by the same telemetry and formulas: both pass the test's thresholds and
+    the drifts agree within a tenth of each threshold."""
+    import sys
+    import torch
+    from astraea_gb300 import engine
+    sys.path.insert(0, os.path.dirname(os.path.dirname(REF_CUBIN)))
+    import ref_gpu
+    cfg = headless.preset_config("EarthTheiaMoonForming", 20000)
+    m_tot, r_scale, v_esc = headless.scenario_scales(cfg)
+    sim, info = headless.load_scenario(cfg)
+    rt, living = info["target_radius_psu"], info["living_body_present"]
+    state0 = sim.p.download()
+    n = sim.p.count
+    max_dt = 5.0 / headless.T_UNIT
+    ours = headless.conservation_audit(lambda: sim.step(max_dt), lambda: sim.p, rt, living, 150, m_tot, r_scale, v_esc)
+    e = ref_gpu.RefEngine(n)
+    e.p.upload(state0)
+    e.alt.count = n
+    e.initial_forces(0.5)
+    prev = [0.0]
+
+    def ref_step():
+        prev[0] = e.step(prev[0], max_dt, 0.5)
+        return prev[0]
+    ref = headless.conservation_audit(ref_step, lambda: e.p, rt, living, 150, m_tot, r_scale, v_esc)
+    torch.cuda.synchronize()
+    keys = ("energy_drift_rel", "dp_rel", "dl_rel")
+    print("AC-5 drifts (energy, dP, dL): library %s, reference kernels %s"
+          % ([float("%.3e" % ours[k]) for k in keys], [float("%.3e" % ref[k]) for k in keys]))
+    assert abs(ours["energy_j_t0"] - ref["energy_j_t0"]) <= 1e-6 * abs(ref["energy_j_t0"])
+    for k, thr in zip(keys, (0.01, 1e-4, 0.005)):
+        assert abs(ours[k]) < thr and abs(ref[k]) < thr, k
+        assert abs(ours[k] - ref[k]) < 0.1 * thr, k

@@ -287,3 +287,47 @@ def test_1m_against_reference_kernels(snapshot):
     dt_r = e.reduce_dt(0.0, MAX_DT)
     print("1M dt on the reference's state after pass 2: library %.9g, reference kernels %.9g" % (dt_l, dt_r))
     assert dt_l == dt_r
+
+
+@pytest.mark.skipif(not os.path.exists(REF_CUBIN),
+                    reason="the reference kernels' cubin (built from the reference checkout) is absent")
+def test_1m_fused_step_against_reference_step(snapshot):
+    """One fused step of the library (engine node rounding) against one step
+    of the reference's own kernel sequence (engine/simulation.cpp:1721-1732)
+    from the same snapshot: the dt is the same float (it comes from the
+    snapshot's fields), and every field after the step agrees within 1e-5,
+    particle by particle through originalId (the reference's drift reads
+    neighbour positions that other threads are moving, and the sums run in
+    another order)."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(REF_CUBIN), os.pardir))
+    import ref_gpu
+    s1, dt1 = snapshot
+    e = ref_gpu.RefEngine(N)
+    e.p.upload(s1)
+    e.alt.count = N
+    e.sort_and_build()                   # the snapshot's tree, for the opening drift
+    dt_r = e.step(dt1, MAX_DT)
+    r = e.p.download()
+    del e
+    torch.cuda.empty_cache()
+    sim = engine.Simulation(N)
+    sim.p.upload(s1)
+    sim.alt.count = N
+    sim.prev_dt = dt1
+    engine.set_node_rounding(1)
+    try:
+        engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
+        engine.invalidate_step_cache(sim.bvh)
+        dt_g = sim.step(MAX_DT)
+    finally:
+        engine.set_node_rounding(0)
+    g = sim.state()
+    print("1M fused step vs reference step: dt %.9g / %.9g" % (dt_g, dt_r))
+    assert dt_g == dt_r
+    og, orr = np.argsort(g["originalId"]), np.argsort(r["originalId"])
+    assert np.array_equal(g["originalId"][og], r["originalId"][orr])
+    fields = ["posX", "posY", "posZ", "velX", "velY", "velZ", "rho", "u", "h", "accX", "accY", "accZ", "pressure"]
+    err = report("fused step vs reference step", {f: g[f][og] for f in fields}, {f: r[f][orr] for f in fields},
+                 fields)
+    assert max(err.values()) < TOL
