@@ -237,7 +237,10 @@ __device__ __forceinline__ void farTaylor(const float (&e)[10], float cx, float 
 // 1 / |s| for a direction s in {-1, 0, 1}^3 with nz non-zero components.
 __device__ __forceinline__ float invDirNorm(int nz) { return nz == 3 ? 0.57735027f : (nz == 2 ? 0.70710678f : 1.0f); }
 
-template <int kWarps, bool kInside, bool kQuad, bool kLearned, bool kExpand = false>
+// kDebug: the variant that serves the debugging calls (per-group interaction
+// counts, the trace of one group's accepted nodes and leaves); their checks
+// are kept out of the production variants, where they cost 2 % of the walk.
+template <int kWarps, bool kInside, bool kQuad, bool kLearned, bool kExpand = false, bool kDebug = false>
 __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p, Work w, uint32_t n,
                                                                  float theta2, uint32_t numGroups,
                                                                  uint32_t* groupCounter, FarCapture ff) {
@@ -527,7 +530,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             }
             const unsigned accMask = __ballot_sync(0xffffffffu, accept && !far);
             const unsigned farMask = kExpand ? __ballot_sync(0xffffffffu, far) : 0u;
-            if (w.traceList != nullptr && g == w.traceGroup && (accept || isLeaf)) {
+            if (kDebug && w.traceList != nullptr && g == w.traceGroup && (accept || isLeaf)) {
                 const uint32_t k = atomicAdd(reinterpret_cast<uint32_t*>(w.traceList), 1u);
                 if (k < w.traceCap) w.traceList[1 + k] = c;
             }
@@ -676,7 +679,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         nInter += static_cast<unsigned long long>(act) * static_cast<unsigned>(mCount + pCount);
         if (lane == 0) {
             nInter -= static_cast<unsigned long long>(__popc(selfSeen));
-            if (w.groupCounts != nullptr) w.groupCounts[g] = static_cast<uint32_t>(nInter - interBefore);
+            if (kDebug && w.groupCounts != nullptr) w.groupCounts[g] = static_cast<uint32_t>(nInter - interBefore);
         }
         __syncwarp();
     }
@@ -711,7 +714,11 @@ cudaError_t launchGravity(const AstraeaParticles& p, const Work& w, uint32_t n, 
     using GravFn = void (*)(AstraeaParticles, Work, uint32_t, float, uint32_t, uint32_t*, FarCapture);
     GravFn kernel = nullptr;
     int wps = kGravWarps;
-    if (expansion && quadrupole && far == nullptr) {
+    if (w.traceList != nullptr || w.groupCounts != nullptr) {
+        // the debugging calls (monopole walk, 4-warp blocks)
+        kernel = checkInside ? gravityKernel<kGravWarps, true, false, false, false, true>
+                             : gravityKernel<kGravWarps, false, false, false, false, true>;
+    } else if (expansion && quadrupole && far == nullptr) {
         if (warps == 2) {
             kernel = checkInside ? gravityKernel<2, true, true, false, true> : gravityKernel<2, false, true, false, true>;
             wps = 2;
