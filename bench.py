@@ -20,6 +20,9 @@ whole particle set, through the library's fused C-ABI step.
              the FP32 FMA throughput measured in this process
   cpu_baseline  the reference algorithm's FP64 host path (oracle/, OpenMP
              on the host cores): two full steps of the same workload
+  other_configs  the 4M Plummer sphere (gravity only: plain against the
+             far-field modes at their FP64 errors) and the 16M gas-giant
+             impact (full steps), run as --workload c3 / c5 child processes
   reference_cuda  the reference's own CUDA kernels (compiled for sm_100
              from its checkout into oracle/_ref) stepping the same initial
              state on the same GPU, CUDA-event timed, and this library's
@@ -88,6 +91,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-planet", action="store_true", help="skip the planet-construction measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default block shape of the tree walks")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the 4M Plummer (c3) and 16M gas-giant (c5) runs summarised in the c2 line")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's own CUDA kernels (oracle/_ref cubin) beside this library")
     ap.add_argument("--eager", action="store_true",
@@ -343,6 +348,8 @@ def run_gpu(args):
                                "step; the e2e number below is eager calls through the C-ABI)")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(st, args, max_dt)
+    if rank == 0 and world == 1 and args.workload == "c2" and not args.no_other_configs:
+        out["other_configs"] = other_configs(args)
     if rank == 0 and world == 1 and args.workload == "c2" and not args.no_reference_cuda:
         # the reference's own kernels on the same GPU and initial state, after
         # everything above (their buffers are separate and freed afterwards)
@@ -354,6 +361,34 @@ def run_gpu(args):
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def other_configs(args):
+    """The 4M Plummer sphere (gravity only, plain against the far-field
+    modes, errors against the FP64 direct sum) and the 16M gas-giant core
+    impact (full fused steps), each run as `bench.py --workload c3|c5` in a
+    child process after this line's own measurements, summarised here."""
+    res = {}
+    for wl, extra in (("c3", ["--steps", "6", "--warmup", "1"]), ("c5", ["--steps", "5", "--warmup", "3"])):
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--workload", wl] + extra,
+                               capture_output=True, text=True, timeout=900)
+            line = json.loads(r.stdout.strip().splitlines()[-1])
+        except Exception as exc:                # report, never fail the headline line
+            res[wl] = "unavailable: %s" % str(exc).splitlines()[0][:200]
+            continue
+        if wl == "c3":
+            keep = ("theta", "far_field", "gravity_ms", "force_rms_vs_fp64", "gravity_speedup_vs_plain",
+                    "theta_far", "gamma", "leaf_bucket")
+            res[wl] = {"config": line["config"]["workload"],
+                       "runs": [{k: r0[k] for k in keep if k in r0} for r0 in line["runs"]],
+                       "equal_error_choice": line.get("equal_error_choice")}
+        else:
+            res[wl] = {k: line.get(k) for k in ("metric", "value", "unit", "ms_per_step", "force_error_rms_vs_fp64",
+                                                 "clocks")}
+            res[wl]["config"] = line["config"]["workload"]
+            res[wl]["gravity"] = {k: line["roofline"].get(k) for k in ("launch_ms", "achieved", "frac", "unit")}
+    return res
 
 
 def ensemble_run(engine, scenarios, torch, max_dt, theta, replays=25, eager_pairs=4):
