@@ -481,9 +481,12 @@ AstraeaStatus astraea_gb300_ff_profile(AstraeaParticles* p, const AstraeaRadixBv
  * EOS outputs, pass-1 outputs) are not moved, and the step's tree is kept in
  * the library's own node records: the BVH descriptor's node arrays (aabb*,
  * nodeMass, com*, nodeMaxH and the packed float4 arrays) keep the tree of the
- * last astraea_gb300_sort_and_build_bvh.  After writing positions or h from
- * outside the library between steps, call
- * astraea_gb300_invalidate_step_cache. */
+ * last astraea_gb300_sort_and_build_bvh.  After writing fields from outside
+ * the library between steps, call astraea_gb300_invalidate_step_cache: the
+ * next step recomputes its dt and neighbour lists from them on the tree it
+ * keeps.  That tree bounds the positions and h of its build, so positions or
+ * h moved beyond them need astraea_gb300_sort_and_build_bvh first -- as in
+ * the engine, whose drift also walks the tree of the last build. */
 AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, AstraeaRadixBvh* bvh,
                                  float prevDtPsu, float maxDtPsu, float theta, float* outDtPsu);
 /* Forget the neighbour lists and device-side dt kept between fused steps. */
