@@ -278,11 +278,29 @@ def run_gpu(args):
     fp32_peak = max(fp32_scalar, fp32_packed)
     achieved = FLOP_PER_INTERACTION * inter / (grav_ms * 1e-3) / 1e12
     traffic = None
+    issue = None
     tpath = os.path.join(ROOT, "profiles", "gravity_traffic.json")
     if os.path.exists(tpath):
         try:
             with open(tpath) as fh:
                 tr = json.load(fh)
+            ipg = tr.get("warp_instructions_per_group")
+            if ipg:
+                # the bound the kernel actually meets: warp-instruction issue
+                # (4 schedulers per SM, one instruction per clock each)
+                props = torch.cuda.get_device_properties(torch.cuda.current_device())
+                sm_hz = float((clk or {}).get("sm_mhz") or 2070.0) * 1e6
+                peak_issue = props.multi_processor_count * 4 * sm_hz
+                groups = (n + 31) // 32
+                tests_ref = tr.get("node_tests_per_group_at_capture") or 0.0
+                tests_now = gc.get("gravity_node_tests", 0) / reps / groups
+                inst = ipg * groups * ((tests_now / tests_ref) if tests_ref and tests_now else 1.0)
+                issue = {"bound": "instruction issue", "warp_instructions_per_launch": inst,
+                         "achieved": inst / (grav_ms * 1e-3), "peak": peak_issue, "unit": "warp instructions/s",
+                         "frac": inst / (grav_ms * 1e-3) / peak_issue,
+                         "source": "instructions per group from the 262k ncu capture (profiles/gravity_c2_262k.md), "
+                                   "scaled by this run's node tests per group and group count (an estimate); "
+                                   "peak = SMs x 4 schedulers x the sampled SM clock"}
             # measured per launch at this N when the capture is of this size,
             # else scaled by the particle count (the records are read once)
             if tr.get("n") == n and tr.get("dram_bytes_per_launch"):
@@ -327,7 +345,7 @@ def run_gpu(args):
                      "peak_source": "measured in-process: the larger of scalar fmaf (%.1f) and packed "
                                     "fma.rn.f32x2 (%.1f) FMA chains; the bf16/HBM peaks of MEASURED_PEAKS.json "
                                     "do not bound this kernel" % (fp32_scalar, fp32_packed),
-                     "interactions_per_launch": inter, "launch_ms": grav_ms},
+                     "interactions_per_launch": inter, "launch_ms": grav_ms, "issue": issue},
         "step_hbm": step_hbm_roofline(n, ms_max / args.steps),
         "stages": stages,
         "force_error_rms_vs_fp64": err_rms,
