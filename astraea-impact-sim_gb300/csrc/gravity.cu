@@ -40,7 +40,11 @@ constexpr int kGravList = 64;
 // with peps[2k..2k+1] = {eps_jA / 2, eps_jB / 2}.  With the quadrupole
 // (far-field mode 1) an mlist pair block is 20 floats: the 8 above, then
 // G Q_xx, G Q_yy, G Q_zz, G Q_xy, G Q_xz, G Q_yz of both entries, where
-// Q = 3 S - tr(S) I is the node's traceless quadrupole.
+// Q = 3 S - tr(S) I is the node's traceless quadrupole.  Both lists are
+// rings of 64 entries: a round appends at most 32 behind the pending ones
+// (at most 31), and a flush evaluates the 32 oldest, which start at entry 0
+// or 32 (the head toggles), so no entry is ever moved and the evaluation
+// order is the append order.
 // dirPos[k] (k = 9 (sx + 1) + 3 (sy + 1) + (sz + 1), s in {-1, 0, 1}): the
 // member with the largest projection on the unit direction s / |s| (first
 // member on ties) and, in .w, that projection measured from the group-box
@@ -306,6 +310,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         }
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
         int sp = 2, mCount = 0, pCount = 0, fCount = 0;
+        int mHead = 0, pHead = 0;   // first pending entry of each ring list (0 or 32)
         uint32_t rounds = 0;
         // group expansion: the group's radius about its box centre c (IEEE
         // operations, so the far decision is reproducible) and mean eps^2
@@ -347,17 +352,12 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             if (lane < 20) reinterpret_cast<float*>(S.facc4)[lane] += mine;
             __syncwarp();
         };
-        auto flushP = [&]() {                 // evaluate plist entries 0..31, move the rest down
-            if (active) evalParticles2(S.plist, S.peps, 0, 16, X, Y, Z, HE, acc);
+        auto flushP = [&]() {                 // evaluate the 32 entries from pHead
+            if (active) evalParticles2(S.plist, S.peps, pHead >> 1, 16, X, Y, Z, HE, acc);
             nInter += static_cast<unsigned long long>(act) * 32u;
             __syncwarp();
             pCount -= 32;
-            if (lane < pCount) {
-                const float* src = S.plist + 8 * (16 + (lane >> 1)) + (lane & 1);
-                putEntry(S.plist, lane, src[0], src[2], src[4], src[6]);
-                S.peps[lane] = S.peps[32 + lane];
-            }
-            __syncwarp();
+            pHead ^= 32;
         };
         __syncwarp();
 
@@ -551,9 +551,9 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                     if (far)
                         putMono<true>(reinterpret_cast<float*>(S.flist4), fCount + __popc(farMask & laneMaskLt()), e);
                     else
-                        putMono<kQuad>(S.mlist, mCount + __popc(accMask & laneMaskLt()), e);
+                        putMono<kQuad>(S.mlist, (mHead + mCount + __popc(accMask & laneMaskLt())) & 63, e);
                 } else {
-                    putMono<kQuad>(S.mlist, mCount + __popc(accMask & laneMaskLt()), e);
+                    putMono<kQuad>(S.mlist, (mHead + mCount + __popc(accMask & laneMaskLt())) & 63, e);
                 }
             }
             mCount += __popc(accMask);
@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 const int j = ~c;
                 const float4 pm = __ldg(&w.leaf[j].a);
                 const float ej = __ldg(&w.leafAux[j]).y;
-                const int slot = pCount + __popc(leafMask & laneMaskLt());
+                const int slot = (pHead + pCount + __popc(leafMask & laneMaskLt())) & 63;
                 putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);
                 S.peps[slot] = 0.5f * ej;
                 const uint32_t rel = static_cast<uint32_t>(j) - base;
@@ -588,17 +588,12 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             pCount += __popc(leafMask);
             nTests += __popc(__ballot_sync(0xffffffffu, isNode));
             __syncwarp();
-            if (mCount >= 32) {                 // evaluate entries 0..31, move the rest down
-                if (active) evalMonopoles2<kQuad>(S.mlist, 0, 16, X, Y, Z, E2, acc);
+            if (mCount >= 32) {                 // evaluate the 32 entries from mHead
+                if (active) evalMonopoles2<kQuad>(S.mlist, mHead >> 1, 16, X, Y, Z, E2, acc);
                 nInter += static_cast<unsigned long long>(act) * 32u;
                 __syncwarp();
                 mCount -= 32;
-                if (lane < mCount) {
-                    float e[10];
-                    getMono<kQuad>(S.mlist, 32 + lane, e);
-                    putMono<kQuad>(S.mlist, lane, e);
-                }
-                __syncwarp();
+                mHead ^= 32;
             }
             if (pCount >= 32) flushP();
             if (kExpand) {
@@ -616,7 +611,7 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                     unsigned sb = 0u;
                     if (has) {
                         const float4 pm = __ldg(&w.leaf[j].a);
-                        const int slot = pCount + __popc(hm & laneMaskLt());
+                        const int slot = (pHead + pCount + __popc(hm & laneMaskLt())) & 63;
                         putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);
                         S.peps[slot] = 0.5f * __ldg(&w.leafAux[j]).y;
                         const uint32_t rel = j - base;
@@ -636,14 +631,14 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         if (lane == 0) {
             if (mCount & 1) {
                 const float zero[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                putMono<kQuad>(S.mlist, mCount, zero);
+                putMono<kQuad>(S.mlist, mHead + mCount, zero);
             }
-            if (pCount & 1) { putEntry(S.plist, pCount, 0.0f, 0.0f, 0.0f, 0.0f); S.peps[pCount] = 0.0f; }
+            if (pCount & 1) { putEntry(S.plist, pHead + pCount, 0.0f, 0.0f, 0.0f, 0.0f); S.peps[pHead + pCount] = 0.0f; }
         }
         __syncwarp();
         if (active) {
-            evalMonopoles2<kQuad>(S.mlist, 0, (mCount + 1) >> 1, X, Y, Z, E2, acc);
-            evalParticles2(S.plist, S.peps, 0, (pCount + 1) >> 1, X, Y, Z, HE, acc);
+            evalMonopoles2<kQuad>(S.mlist, mHead >> 1, (mCount + 1) >> 1, X, Y, Z, E2, acc);
+            evalParticles2(S.plist, S.peps, pHead >> 1, (pCount + 1) >> 1, X, Y, Z, HE, acc);
             float a0, a1, b0, b1, c0, c1, d0, d1;
             unpack2(acc.ax, a0, a1);
             unpack2(acc.ay, b0, b1);
