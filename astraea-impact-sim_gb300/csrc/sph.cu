@@ -102,7 +102,10 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
         }
         __syncwarp();
         if (lane == 0) { S.stack[0] = rootL; S.stack[1] = rootR; }
-        int sp = 2, cCount = 0;
+        // candidates form a ring of 64 entries: a round appends at most 32
+        // behind the pending ones (at most 31), a flush takes the 32 oldest,
+        // which start at entry 0 or 32 (cHead toggles) -- nothing is moved
+        int sp = 2, cCount = 0, cHead = 0;
         uint32_t cnt = 0, rounds = 0;
         uint32_t* myList = w.nbrList + static_cast<size_t>(g) * maxNbr * 32u + static_cast<uint32_t>(lane);
         __syncwarp();
@@ -123,7 +126,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
         const f2 X2 = pack2(me.x, me.x), Y2 = pack2(me.y, me.y), Z2 = pack2(me.z, me.z);
         auto flush = [&](int pairs) {
             if (active) {
-                for (int k = 0; k < pairs; ++k) {
+                for (int k = cHead >> 1; k < (cHead >> 1) + pairs; ++k) {
                     const float* b = S.cand + 8 * k;
                     const ulonglong2 u = *reinterpret_cast<const ulonglong2*>(b);       // (x), (y)
                     const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(b + 4);   // (z), (Hs)
@@ -138,17 +141,6 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 }
             }
         };
-        // after a flush of entries 0..31: entries 32 .. cCount-1 move down
-        auto shiftDown = [&]() {
-            if (lane < cCount - 32) {
-                const int src = 32 + lane;
-                const float* b = S.cand + 8 * (src >> 1) + (src & 1);
-                const float x = b[0], y = b[2], z = b[4], hs = b[6];
-                const int j = S.candIdx[src];
-                putCand(lane, x, y, z, hs, j);
-            }
-        };
-
         while (sp > 0) {
             if (++rounds > 2u * n + 64u) {     // only reachable on a corrupted tree
                 stackOverflow = true;
@@ -249,16 +241,15 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 keep = dx * dx + dy * dy + dz * dz <= R * R * 1.00001f;
             }
             const unsigned leafMask = __ballot_sync(0xffffffffu, keep);
-            if (keep) putCand(cCount + __popc(leafMask & laneMaskLt()), pm.x, pm.y, pm.z, hsj, ~c);
+            if (keep) putCand((cHead + cCount + __popc(leafMask & laneMaskLt())) & 63, pm.x, pm.y, pm.z, hsj, ~c);
             cCount += __popc(leafMask);
             nCand += __popc(leafMask);
             __syncwarp();
             if (cCount >= 32) {
                 flush(16);
                 __syncwarp();
-                shiftDown();
                 cCount -= 32;
-                __syncwarp();
+                cHead ^= 32;
             }
             while (expandMask) {                // small opened nodes: their particles, lane by lane
                 const int src = __ffs(expandMask) - 1;
@@ -280,22 +271,21 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                     keepJ = dx * dx + dy * dy + dz * dz <= R * R * 1.00001f;
                 }
                 const unsigned km = __ballot_sync(0xffffffffu, keepJ);
-                if (keepJ) putCand(cCount + __popc(km & laneMaskLt()), pj.x, pj.y, pj.z, hj, static_cast<int>(j));
+                if (keepJ) putCand((cHead + cCount + __popc(km & laneMaskLt())) & 63, pj.x, pj.y, pj.z, hj, static_cast<int>(j));
                 cCount += __popc(km);
                 nCand += __popc(km);
                 __syncwarp();
                 if (cCount >= 32) {
                     flush(16);
                     __syncwarp();
-                    shiftDown();
                     cCount -= 32;
-                    __syncwarp();
+                    cHead ^= 32;
                 }
                 }
             }
         }
         if (cCount & 1) {                  // odd tail: a pad entry no member can reach
-            if (lane == 0) putCand(cCount, 3.0e38f, 3.0e38f, 3.0e38f, 0.0f, -1);
+            if (lane == 0) putCand(cHead + cCount, 3.0e38f, 3.0e38f, 3.0e38f, 0.0f, -1);
             __syncwarp();
         }
         flush((cCount + 1) >> 1);
