@@ -12,9 +12,10 @@ sort + tree build, SPH pass 1, EOS, gravity, SPH pass 2, kick, EOS) on the
 whole particle set, through the library's fused C-ABI step.
 
   value      N * steps / device time of the timed steps, inputs resident
-  e2e        same metric through the C-ABI with host buffers: every step
-             uploads the step's input fields from pinned host memory,
-             steps, and reads back the fields the engine's telemetry reads
+  e2e        same metric through the C-ABI with the simulation state on
+             the host: every step uploads the state's input fields from
+             pinned host memory, steps, and reads the state and the fields
+             the engine's telemetry reads back
   roofline   the gravity kernel (dominant): 23 FLOP per evaluated pair
              interaction (device counter) / CUDA-event launch time, against
              the FP32 FMA throughput measured in this process
@@ -771,27 +772,32 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
 
 
 def run_e2e(sim, engine, torch, args, max_dt, world, dist):
-    """The same fused step through the C-ABI with host-resident inputs and
-    outputs.  Every step copies its input fields from pinned host memory into
-    the particle arrays and its result fields (the engine's telemetry fields)
-    and dt back to pinned host memory.  Two device states alternate, so the
-    copies run on their own streams (H2D and D2H in both copy engines) and
-    overlap the kernels of the step on the other state: step k uploads into
-    state k mod 2 while step k-1 computes on the other one, and reads its
-    results back while step k+1 computes."""
+    """The same fused step through the C-ABI with the simulation state held
+    on the host: every step uploads the state's input fields from pinned
+    host memory into the particle arrays, steps, and reads the state back
+    (the input fields and the engine's telemetry fields) together with dt.
+    Two device states alternate, so the copies run on their own streams (H2D
+    and D2H in both copy engines) and overlap the kernels of the step on the
+    other state: step k uploads into state k mod 2 while step k-1 computes
+    on the other one, and reads its results back while step k+1 computes.
+    What a step uploads is what the previous step on that state read back,
+    so the library's tree still bounds it; the step cache is invalidated all
+    the same (the library cannot know that), so every step rebuilds its dt
+    and neighbour lists from the uploaded state."""
     n = sim.p.count
     sims = [sim, engine.Simulation(n)]
     sims[1].load_state(sim.p.download())
     engine.reserve(sims[1].bvh, n)
     sims[1].evaluate_initial_forces(args.theta)
-    host_in = {f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in E2E_IN}
-    host_out = [{f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in E2E_OUT}
-                for _ in range(2)]
-    for f in E2E_IN:
-        host_in[f].copy_(sim.p.arrays[f][:n])
+    fields_out = E2E_IN + [f for f in E2E_OUT if f not in E2E_IN]
+    host = [{f: torch.empty_like(sim.p.arrays[f][:n], device="cpu").pin_memory() for f in fields_out}
+            for _ in range(2)]
+    for b in range(2):
+        for f in fields_out:
+            host[b][f].copy_(sims[b].p.arrays[f][:n])
     dt_host = torch.zeros(2, dtype=torch.float32).pin_memory()
-    bi = sum(t.numel() * t.element_size() for t in host_in.values())
-    bo = sum(t.numel() * t.element_size() for t in host_out[0].values()) + 4
+    bi = sum(host[0][f].numel() * host[0][f].element_size() for f in E2E_IN)
+    bo = sum(host[0][f].numel() * host[0][f].element_size() for f in fields_out) + 4
     comp, h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
     ev = lambda: torch.cuda.Event()
     in_ready, out_ready, out_read = [ev(), ev()], [ev(), ev()], [ev(), ev()]
@@ -808,7 +814,7 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
             if k >= 2:
                 h2d.wait_event(out_read[b])         # state b read back after step k-2
             for f in E2E_IN:
-                sims[b].p.arrays[f][:n].copy_(host_in[f], non_blocking=True)
+                sims[b].p.arrays[f][:n].copy_(host[b][f], non_blocking=True)
             in_ready[b].record(h2d)
 
     upload(0, 0)
@@ -820,12 +826,12 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
         with torch.cuda.stream(comp):
             comp.wait_event(in_ready[b])
             engine.invalidate_step_cache(st.bvh)
-            engine.step(st.p, st.alt, st.bvh, sim.prev_dt, max_dt, args.theta, dt_host[b:].data_ptr())
+            engine.step(st.p, st.alt, st.bvh, st.prev_dt, max_dt, args.theta, dt_host[b:].data_ptr())
             out_ready[b].record(comp)
         with torch.cuda.stream(d2h):
             d2h.wait_event(out_ready[b])
-            for f in E2E_OUT:
-                host_out[b][f].copy_(st.p.arrays[f][:n], non_blocking=True)
+            for f in fields_out:
+                host[b][f].copy_(st.p.arrays[f][:n], non_blocking=True)
             out_read[b].record(d2h)
     comp.wait_stream(d2h)
     e1.record(comp)
@@ -837,10 +843,11 @@ def run_e2e(sim, engine, torch, args, max_dt, world, dist):
     del sims[1], st
     return {"value": rate, "unit": UNIT,
             "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
-            "note": "every step: H2D of the step's input fields from pinned memory into the particle arrays, "
-                    "fused step (step cache invalidated: neighbour lists and dt recomputed from the uploaded "
-                    "state), D2H of the engine telemetry fields and dt; two device states alternate so the "
-                    "copies run on their own streams beside the other state's step"}
+            "note": "the simulation state lives on the host: every step uploads its input fields from pinned "
+                    "memory into the particle arrays, runs the fused step (step cache invalidated: neighbour "
+                    "lists and dt recomputed from the uploaded state) and reads the state and the engine's "
+                    "telemetry fields back with dt; two device states alternate so the copies run on their "
+                    "own streams beside the other state's step"}
 
 
 def run_c3(args):
