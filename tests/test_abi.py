@@ -56,3 +56,17 @@ def test_error_path_without_gpu_is_an_exception():
     rc = lib.astraea_gb300_sph_pass1_neighbors(ctypes.byref(p), ctypes.byref(b))
     assert rc == 3
     assert b"leftChild" in lib.astraea_gb300_last_error()
+
+
+def test_mode_setters_reject_out_of_range_arguments():
+    # process-wide settings are checked before anything touches a device
+    lib = abi.load_library()
+    assert lib.astraea_gb300_set_node_rounding(2) == 3
+    assert b"node rounding" in lib.astraea_gb300_last_error()
+    assert lib.astraea_gb300_set_node_rounding(-1) == 3
+    assert lib.astraea_gb300_set_far_field(4) == 3
+    assert lib.astraea_gb300_set_far_field_expansion(33, 0.3) == 3
+    assert lib.astraea_gb300_set_far_field_expansion(8, 1.0) == 3
+    assert lib.astraea_gb300_set_node_rounding(0) == 0
+    assert lib.astraea_gb300_set_far_field(0) == 0
+    assert lib.astraea_gb300_set_far_field_expansion(16, 0.3) == 0
