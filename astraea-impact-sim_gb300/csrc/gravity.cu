@@ -382,8 +382,12 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             bool farOk = false;
             float dd = 0.0f;
             float4 bmin = make_float4(0.f, 0.f, 0.f, 0.f), bmax = bmin;
-            if (isNode) {
-                const float4* rec = w.node + 4 * static_cast<size_t>(c);
+            {
+                // Evaluated by every lane, the results kept only where isNode (a
+                // lane without a node reads the root's record): as a branch
+                // around the tests the walk was 2.4 % slower at 1M.
+                const int cn = isNode ? c : 0;
+                const float4* rec = w.node + 4 * static_cast<size_t>(cn);
                 r0 = __ldg(&rec[0]);
                 const float4 r1 = __ldg(&rec[1]);
                 cl = __float_as_int(r1.y);
@@ -421,15 +425,14 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 // far test of mode 2: every member passes theta_far (by the
                 // sound bound) and the node is far against the group's size
                 if (kLearned)
-                    farOk = emitFar && boxApart && Lb2 > 2.0e-20f && dd < ff.thetaFar2 * Lb2 * 0.99999f &&
+                    farOk = isNode && emitFar && boxApart && Lb2 > 2.0e-20f && dd < ff.thetaFar2 * Lb2 * 0.99999f &&
                             gExt * gExt <= ff.gamma2 * (ux * ux + uy * uy + uz * uz);
-                if (disjoint && Lb2 > 2.0e-20f && dd < theta2 * Lb2 * 0.99999f) {
-                    accept = true;
-                } else if (!acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax)) {
-                    accept = false;   // (2) the member furthest towards the node opens it
-                } else {
-                    undecided = true; // (3) decided below by the whole group
-                }
+                // (1) accepts; else (2) the member furthest towards the node
+                // opens it; else (3) the whole group decides below
+                const bool boundAccepts = disjoint && Lb2 > 2.0e-20f && dd < theta2 * Lb2 * 0.99999f;
+                const bool extremeAccepts = acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax);
+                accept = isNode && boundAccepts;
+                undecided = isNode && !boundAccepts && extremeAccepts;
             }
             // (3) exact test of each undecided node by all members at once
             const unsigned und = __ballot_sync(0xffffffffu, undecided);

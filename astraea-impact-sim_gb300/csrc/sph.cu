@@ -543,16 +543,21 @@ __global__ void __launch_bounds__(128, 4) pass2Kernel(AstraeaParticles p, Work w
             const float gx = gb * dx, gy = gb * dy, gz = gb * dz;
             const float vDotG = dvx * gx + dvy * gy + dvz * gz;
             drC += volJ * vDotG;                               // continuity (:1114)
-            if (__float_as_int(b4.z) == matI) {                // delta-SPH diffusion (:1115-1119)
+            // The delta-SPH and viscosity terms are evaluated for every pair in
+            // range and kept by a select (the engine's conditions, the same
+            // values): as branches they cost pass 2 11 % at 1M.
+            {                                                  // delta-SPH diffusion (:1115-1119)
                 const float rDotG = -(dx * gx + dy * gy + dz * gz);
                 const float dd = r2 + 0.01f * Hi * Hi;
-                drD += volJ * (2.0f * (rhoJ - rhoI) / dd) * rDotG;
+                const float t = drD + volJ * (2.0f * (rhoJ - rhoI) / dd) * rDotG;
+                drD = (__float_as_int(b4.z) == matI) ? t : drD;
             }
-            float piIJ = 0.0f;                                 // Monaghan AV x Balsara (:1121-1128)
-            if (vDotR < 0.0f) {
+            float piIJ;                                        // Monaghan AV x Balsara (:1121-1128)
+            {
                 const float hB = 0.5f * (hi + hj), cB = 0.5f * (csI + csJ), rB = 0.5f * (rhoI + rhoJ);
                 const float muIJ = __fdividef(hB * vDotR, r2 + 0.01f * hB * hB);
-                piIJ = __fdividef(-1.0f * cB * muIJ + 2.0f * muIJ * muIJ, rB) * (0.5f * (fBalI + fBalJ));
+                const float t = __fdividef(-1.0f * cB * muIJ + 2.0f * muIJ * muIJ, rB) * (0.5f * (fBalI + fBalJ));
+                piIJ = (vDotR < 0.0f) ? t : 0.0f;
             }
             float tens = 0.0f;                                 // tensile correction (:1130-1142)
             const float Rj = b4.w;
