@@ -213,6 +213,7 @@ SIGNATURES = [
     ("astraea_gb300_autotune", [_P, _B, _F, ctypes.POINTER(Tuning)], ctypes.c_int),
     ("astraea_gb300_get_tuning", [_U32, ctypes.POINTER(Tuning)], ctypes.c_int),
     ("astraea_gb300_set_tuning", [_U32, ctypes.POINTER(Tuning)], ctypes.c_int),
+    ("astraea_gb300_get_gravity_warps", [_U32, ctypes.c_int, ctypes.c_float, ctypes.POINTER(_U32)], ctypes.c_int),
     ("astraea_gb300_step", [_P, _P, _B, _F, _F, _F, _VP], ctypes.c_int),
     ("astraea_gb300_invalidate_step_cache", [_B], ctypes.c_int),
     ("astraea_gb300_reserve", [_B, _U32], ctypes.c_int),

@@ -487,7 +487,8 @@ def _tuning_dict(t):
 def autotune(p, bvh, theta=0.5):
     """Chooses the warps per block of the gravity and neighbour walks on the
     current tree (built for p) and keeps the choice for this particle-count
-    bucket; returns it."""
+    bucket; returns it.  The gravity walk tuned is the one the current
+    far-field mode runs at theta; the other walks keep their own shapes."""
     t = abi.Tuning()
     s = p.struct()
     abi.check(lib().astraea_gb300_autotune(ctypes.byref(s), ctypes.byref(bvh.s), float(theta), ctypes.byref(t)))
@@ -503,6 +504,13 @@ def get_tuning(count):
 def set_tuning(count, gravity_warps=4, neighbor_warps=4):
     t = abi.Tuning(int(gravity_warps), int(neighbor_warps), 0.0, 0.0)
     abi.check(lib().astraea_gb300_set_tuning(int(count), ctypes.byref(t)))
+
+
+def get_gravity_warps(count, far_field_mode, theta):
+    """Warps per block of the gravity walk of that far-field mode at theta."""
+    w = ctypes.c_uint32(0)
+    abi.check(lib().astraea_gb300_get_gravity_warps(int(count), int(far_field_mode), float(theta), ctypes.byref(w)))
+    return int(w.value)
 
 
 def invalidate_step_cache(bvh):

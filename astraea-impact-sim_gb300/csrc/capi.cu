@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -283,9 +284,15 @@ AstraeaStatus checkLaunch(cudaError_t e, const char* what) {
 
 // ------------------------------------------------------------ autotuning
 // Warps per block of the two tree walks, per device and power-of-two
-// particle count (bucket floor(log2 n)); {4, 4} until tuned.
+// particle count (bucket floor(log2 n)); {4, 4} until tuned.  The gravity
+// walk is tuned per variant (gravityVariant): its variants differ in
+// registers and work per node, so the best shape of one is not the best of
+// another (1M impact: 8 warps for the monopole walk at theta 0.5, 4 for the
+// quadrupole walk at theta 0.7, 10 % apart).
 std::mutex g_tuneMutex;
 std::map<std::pair<int, int>, AstraeaTuning> g_tuning;
+std::map<std::tuple<int, int, int>, uint32_t> g_gravTuning;
+constexpr int kGravityVariants = 6;
 
 int tuneBucket(uint32_t n) {
     int b = 0;
@@ -297,6 +304,22 @@ AstraeaTuning tuningFor(uint32_t n) {
     std::lock_guard<std::mutex> lock(g_tuneMutex);
     const auto it = g_tuning.find(std::make_pair(currentDevice(), tuneBucket(n)));
     return (it == g_tuning.end()) ? AstraeaTuning{4u, 4u, 0.0f, 0.0f} : it->second;
+}
+
+// The gravity walk a call runs: 2 kind + inside, kind 0 the monopole walk
+// (mode 0, the learned mode's fallback, or no moments built), 1 the
+// quadrupole walk (mode 1), 2 the expansion walk (mode 3); inside = the
+// inside-box rule of theta^2 > 1/3 (the same test as launchGravity).
+int gravityVariant(int mode, bool moments, float theta) {
+    const int kind = (!moments || mode == 0 || mode == 2) ? 0 : (mode == 1 ? 1 : 2);
+    const float th = std::max(0.0f, theta);
+    return 2 * kind + ((th * th > 0.333333f) ? 1 : 0);
+}
+
+uint32_t gravityWarpsFor(uint32_t n, int variant) {
+    std::lock_guard<std::mutex> lock(g_tuneMutex);
+    const auto it = g_gravTuning.find(std::make_tuple(currentDevice(), tuneBucket(n), variant));
+    return (it == g_gravTuning.end()) ? 4u : it->second;
 }
 
 // ------------------------------------------- far-field mode 2 (learned)
@@ -414,7 +437,7 @@ AstraeaStatus learnedGravity(AstraeaParticles* p, Workspace* ws, uint32_t n, flo
         Work w = ws->w;
         w.runIf = &b->gate->runFallback;       // the plain walk at theta, run only when the gate failed
         AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), st, nullptr,
-                                static_cast<int>(tuningFor(n).gravityWarps)));
+                                static_cast<int>(gravityWarpsFor(n, gravityVariant(0, false, theta)))));
         b->lastCallGated = true;
     } else {
         mark(4);
@@ -749,7 +772,7 @@ AstraeaStatus astraea_gb300_gravity_barnes_hut(AstraeaParticles* p, const Astrae
         if (s != ASTRAEA_OK) return s;
     } else {
         AG_LAUNCH(modeGravity(*p, ws->w, n, theta, mode, true, smCount(), stream(),
-                              static_cast<int>(tuningFor(n).gravityWarps)));
+                              static_cast<int>(gravityWarpsFor(n, gravityVariant(mode, true, theta)))));
     }
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
@@ -771,7 +794,7 @@ AstraeaStatus astraea_gb300_debug_gravity_group_trace(AstraeaParticles* p, const
     w.traceGroup = group;
     w.traceCap = capacity;
     AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), stream(), nullptr,
-                            static_cast<int>(tuningFor(n).gravityWarps)));
+                            static_cast<int>(gravityWarpsFor(n, gravityVariant(0, false, theta)))));
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
 }
@@ -789,7 +812,7 @@ AstraeaStatus astraea_gb300_debug_gravity_group_counts(AstraeaParticles* p, cons
     Work w = ws->w;
     w.groupCounts = groupCounts;
     AG_LAUNCH(launchGravity(*p, w, n, theta, false, smCount(), stream(), nullptr,
-                            static_cast<int>(tuningFor(n).gravityWarps)));
+                            static_cast<int>(gravityWarpsFor(n, gravityVariant(0, false, theta)))));
     ws->stepCacheValid = false;
     return ASTRAEA_OK;
 }
@@ -1271,10 +1294,16 @@ AstraeaStatus astraea_gb300_autotune(AstraeaParticles* p, const AstraeaRadixBvh*
         *ms = best;
         return cudaSuccess;
     };
+    // the gravity walk the current far-field mode runs at theta (the learned
+    // mode: its plain fallback walk; its own walk has one shape)
+    const int mode = g_farField.load();
+    const bool moments = ws->momentsBuilt;
+    const int variant = gravityVariant(mode, moments, theta);
+    const int walkMode = (mode == 2) ? 0 : mode;
     AstraeaTuning t{4u, 4u, 3.0e38f, 3.0e38f};
     for (int wv : {2, 4, 8}) {
         float ms = 0.0f;
-        AG_CUDA(best3([&] { return launchGravity(*p, ws->w, n, theta, false, sms, st, nullptr, wv); }, &ms));
+        AG_CUDA(best3([&] { return modeGravity(*p, ws->w, n, theta, walkMode, moments, sms, st, wv); }, &ms));
         if (ms < t.gravityMs) { t.gravityMs = ms; t.gravityWarps = static_cast<uint32_t>(wv); }
     }
     for (int wv : {2, 4, 8}) {
@@ -1285,7 +1314,17 @@ AstraeaStatus astraea_gb300_autotune(AstraeaParticles* p, const AstraeaRadixBvh*
     ws->stepCacheValid = false;
     {
         std::lock_guard<std::mutex> lock(g_tuneMutex);
-        g_tuning[std::make_pair(currentDevice(), tuneBucket(n))] = t;
+        const int dev = currentDevice(), bucket = tuneBucket(n);
+        g_gravTuning[std::make_tuple(dev, bucket, variant)] = t.gravityWarps;
+        const auto it = g_tuning.find(std::make_pair(dev, bucket));
+        AstraeaTuning kept = (it == g_tuning.end()) ? AstraeaTuning{4u, 4u, 0.0f, 0.0f} : it->second;
+        kept.neighborWarps = t.neighborWarps;
+        kept.neighborMs = t.neighborMs;
+        if (variant == 0) {                         // the engine's walk: what get_tuning reports
+            kept.gravityWarps = t.gravityWarps;
+            kept.gravityMs = t.gravityMs;
+        }
+        g_tuning[std::make_pair(dev, bucket)] = kept;
     }
     *out = t;
     return ASTRAEA_OK;
@@ -1313,7 +1352,7 @@ AstraeaStatus astraea_gb300_autotune_expansion(AstraeaParticles* p, const Astrae
         cudaEvent_t a, b;
         ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
     } guard{e0, e1};
-    const int sms = smCount(), warps = static_cast<int>(tuningFor(n).gravityWarps);
+    const int sms = smCount(), warps = static_cast<int>(gravityWarpsFor(n, gravityVariant(3, true, theta)));
     const uint32_t keep = g_leafBucket.load();
     float best = 3.0e38f;
     uint32_t bestBucket = keep;
@@ -1352,7 +1391,16 @@ AstraeaStatus astraea_gb300_set_tuning(uint32_t count, const AstraeaTuning* tuni
     if (!ok(tuning->gravityWarps) || !ok(tuning->neighborWarps))
         return fail(ASTRAEA_ERR_INVALID, "set_tuning: warps per block must be 2, 4 or 8");
     std::lock_guard<std::mutex> lock(g_tuneMutex);
-    g_tuning[std::make_pair(currentDevice(), tuneBucket(count))] = *tuning;
+    const int dev = currentDevice(), bucket = tuneBucket(count);
+    g_tuning[std::make_pair(dev, bucket)] = *tuning;
+    for (int v = 0; v < kGravityVariants; ++v) g_gravTuning[std::make_tuple(dev, bucket, v)] = tuning->gravityWarps;
+    return ASTRAEA_OK;
+}
+
+AstraeaStatus astraea_gb300_get_gravity_warps(uint32_t count, int farFieldMode, float theta, uint32_t* outWarps) {
+    if (outWarps == nullptr) return fail(ASTRAEA_ERR_INVALID, "null argument");
+    if (farFieldMode < 0 || farFieldMode > 3) return fail(ASTRAEA_ERR_INVALID, "far-field mode must be 0, 1, 2 or 3");
+    *outWarps = gravityWarpsFor(count, gravityVariant(farFieldMode, true, theta));
     return ASTRAEA_OK;
 }
 
@@ -1489,8 +1537,9 @@ AstraeaStatus astraea_gb300_step(AstraeaParticles* p, AstraeaParticles* alt, Ast
         s = learnedGravity(p, ws, n, theta, true);
         if (s != ASTRAEA_OK) return s;
     } else {
-        AG_LAUNCH(modeGravity(*p, w, n, theta, g_farField.load(), ws->momentsBuilt, sms, st,
-                              static_cast<int>(tune.gravityWarps)));
+        const int mode = g_farField.load();
+        AG_LAUNCH(modeGravity(*p, w, n, theta, mode, ws->momentsBuilt, sms, st,
+                              static_cast<int>(gravityWarpsFor(n, gravityVariant(mode, ws->momentsBuilt, theta)))));
     }
     marks.mark(ASTRAEA_STAGE_PASS2);
     AG_LAUNCH(launchPass2(*p, w, n, livingPtr(bvh, ws), st));

@@ -382,10 +382,12 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             bool farOk = false;
             float dd = 0.0f;
             float4 bmin = make_float4(0.f, 0.f, 0.f, 0.f), bmax = bmin;
-            {
-                // Evaluated by every lane, the results kept only where isNode (a
-                // lane without a node reads the root's record): as a branch
-                // around the tests the walk was 2.4 % slower at 1M.
+            // Without the inside-box rule the tests run on every lane, the
+            // results kept only where isNode (a lane without a node reads the
+            // root's record): as a branch around them the walk was 2.4 % slower
+            // at 1M.  With the rule (theta^2 > 1/3) the branch stays: there the
+            // masked form needs more registers and was slower.
+            if (kInside ? isNode : true) {
                 const int cn = isNode ? c : 0;
                 const float4* rec = w.node + 4 * static_cast<size_t>(cn);
                 r0 = __ldg(&rec[0]);
@@ -430,9 +432,16 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                 // (1) accepts; else (2) the member furthest towards the node
                 // opens it; else (3) the whole group decides below
                 const bool boundAccepts = disjoint && Lb2 > 2.0e-20f && dd < theta2 * Lb2 * 0.99999f;
-                const bool extremeAccepts = acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax);
-                accept = isNode && boundAccepts;
-                undecided = isNode && !boundAccepts && extremeAccepts;
+                if (kInside) {
+                    if (boundAccepts)
+                        accept = true;
+                    else if (acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax))
+                        undecided = true;
+                } else {
+                    const bool extremeAccepts = acceptsMember(dp.x, dp.y, dp.z, r0, dd, theta2, kInside, bmin, bmax);
+                    accept = isNode && boundAccepts;
+                    undecided = isNode && !boundAccepts && extremeAccepts;
+                }
             }
             // (3) exact test of each undecided node by all members at once
             const unsigned und = __ballot_sync(0xffffffffu, undecided);

@@ -655,9 +655,11 @@ FAR_NAMES = {0: "monopole", 1: "monopole+quadrupole", 2: "monopole+learned corre
              3: "quadrupole+leaf buckets+group expansion"}
 
 
-def set_mode(engine, sim, cfg, theta):
+def set_mode(engine, sim, cfg, theta, tune=False):
     """Far-field mode of one scan entry; mode 3 with bucket "auto" tunes the
-    leaf bucket on the current tree.  Returns the bucket used (mode 3)."""
+    leaf bucket on the current tree; with tune, the block shape of the
+    gravity walk this mode runs at theta is tuned too (each walk variant
+    keeps its own).  Returns the bucket used (mode 3)."""
     mode = cfg["mode"]
     if mode == 2:
         engine.ff_configure(theta_far=cfg["theta_far"], gamma=cfg["gamma"], gate_tolerance=0.0)
@@ -669,6 +671,8 @@ def set_mode(engine, sim, cfg, theta):
     engine.sort_and_build_bvh(sim.p, sim.alt, sim.bvh)
     if mode == 3 and cfg["bucket"] == "auto":
         bucket, _ = engine.autotune_expansion(sim.p, sim.bvh, theta)
+    if tune:
+        engine.autotune(sim.p, sim.bvh, theta)
     return bucket
 
 
@@ -686,7 +690,7 @@ def far_field_scan(sim, engine, torch, np, args, max_dt, truth, configs=FAR_CONF
         theta, mode = cfg["theta"], cfg["mode"]
         if mode == 2 and learned is None:
             continue
-        bucket = set_mode(engine, sim, cfg, theta)      # the order is already sorted: identity permutation
+        bucket = set_mode(engine, sim, cfg, theta, tune=not args.no_autotune)   # sorted already: identity permutation
         engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
         torch.cuda.synchronize()
         engine.reset_device_status()
@@ -880,7 +884,7 @@ def run_c3(args):
     configs += [(th, 3, None, gm) for th, gm in ((0.7, 0.3), (0.75, 0.2), (0.75, 0.3), (0.8, 0.2), (0.8, 0.3))]
     for theta, mode, theta_far, gamma in configs:
         bucket = set_mode(engine, sim, {"mode": mode, "theta_far": theta_far, "gamma": gamma, "bucket": "auto"},
-                          theta)
+                          theta, tune=not args.no_autotune)
         engine.gravity_barnes_hut(sim.p, sim.bvh, theta)
         torch.cuda.synchronize()
         engine.reset_device_status()

@@ -515,18 +515,29 @@ typedef struct AstraeaTuning {
     float neighborMs;        /* best time of the chosen neighbour-walk variant */
 } AstraeaTuning;
 
-/* Times the gravity walk (at theta) and the neighbour-list walk with 2, 4
- * and 8 warps per block on the tree of bvh as built for p (after
+/* Times the gravity walk and the neighbour-list walk with 2, 4 and 8 warps
+ * per block on the tree of bvh as built for p (after
  * astraea_gb300_sort_and_build_bvh), best of three launches each, and keeps
  * the fastest for every later call on this device whose particle count has
- * the same floor(log2 count).  Overwrites p's gravity outputs and the
- * neighbour lists (the next stage calls or step recompute both).  Blocks. */
+ * the same floor(log2 count).  The gravity walk timed is the one the current
+ * far-field mode runs at theta (mode 2: its plain fallback walk), and its
+ * choice is kept for that walk only: the monopole, quadrupole (mode 1) and
+ * expansion (mode 3) walks, each with and without the inside-box rule of
+ * theta^2 > 1/3, are tuned separately (an untuned walk runs 4-warp blocks).
+ * Overwrites p's gravity outputs and the neighbour lists (the next stage
+ * calls or step recompute both).  Blocks. */
 AstraeaStatus astraea_gb300_autotune(AstraeaParticles* p, const AstraeaRadixBvh* bvh, float theta,
                                      AstraeaTuning* out);
-/* The tuning used for `count` particles on this device ({4, 4} untuned). */
+/* The tuning used for `count` particles on this device ({4, 4} untuned):
+ * the neighbour walk's and the monopole gravity walk's at theta^2 <= 1/3
+ * (the engine's walk). */
 AstraeaStatus astraea_gb300_get_tuning(uint32_t count, AstraeaTuning* out);
-/* Sets it by hand (warps 2, 4 or 8), e.g. from a saved autotune result. */
+/* Sets it by hand (warps 2, 4 or 8), e.g. from a saved autotune result; the
+ * gravity shape applies to every gravity walk. */
 AstraeaStatus astraea_gb300_set_tuning(uint32_t count, const AstraeaTuning* tuning);
+/* Warps per block the gravity walk of far-field mode `farFieldMode` (0-3,
+ * on a tree built in that mode) at theta runs for `count` particles. */
+AstraeaStatus astraea_gb300_get_gravity_warps(uint32_t count, int farFieldMode, float theta, uint32_t* outWarps);
 
 /* ---- library primitives and diagnostics --------------------------------- */
 

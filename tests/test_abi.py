@@ -70,3 +70,7 @@ def test_mode_setters_reject_out_of_range_arguments():
     assert lib.astraea_gb300_set_node_rounding(0) == 0
     assert lib.astraea_gb300_set_far_field(0) == 0
     assert lib.astraea_gb300_set_far_field_expansion(16, 0.3) == 0
+    w = ctypes.c_uint32(0)
+    assert lib.astraea_gb300_get_gravity_warps(1024, 4, 0.5, ctypes.byref(w)) == 3
+    assert b"far-field mode" in lib.astraea_gb300_last_error()
+    assert lib.astraea_gb300_get_gravity_warps(1024, 0, 0.5, None) == 3

@@ -4,7 +4,8 @@ The gravity walk and the neighbour-list walk give bit-identical results for
 2, 4 and 8 warps per block (one warp walks one group of 32 particles
 whatever the block size), so the autotuner may pick any of them; the tuned
 choice is kept per power-of-two particle count and used by the stage calls
-and the fused step.
+and the fused step; the gravity walk's choice is kept per walk variant
+(monopole, quadrupole, expansion, each with and without the inside-box rule).
 """
 import numpy as np
 import pytest
@@ -76,3 +77,28 @@ def test_gpu_autotune_records_a_valid_choice():
     with pytest.raises(abi.AstraeaError):
         engine.set_tuning(n, 3, 4)
     engine.set_tuning(n, 4, 4)
+
+
+@pytest.mark.gpu
+def test_gpu_autotune_keeps_each_gravity_walk_its_own_shape():
+    from astraea_gb300 import engine
+    st, _ = scenarios.differentiated_impact(n_total=65536, seed=21)
+    n = len(st["posX"])
+    p, alt, bvh = engine.DeviceParticles(n), engine.DeviceParticles(n), engine.DeviceBvh(n)
+    p.upload(st)
+    alt.count = n
+    engine.set_tuning(n, 2, 2)                   # a hand setting applies to every walk
+    assert all(engine.get_gravity_warps(n, m, th) == 2 for m in (0, 1, 3) for th in (0.5, 0.7))
+    try:
+        engine.set_far_field(1)
+        engine.sort_and_build_bvh(p, alt, bvh)
+        t = engine.autotune(p, bvh, 0.7)             # the quadrupole walk with the inside-box rule
+        assert engine.get_gravity_warps(n, 1, 0.7) == t["gravityWarps"]
+        assert engine.get_gravity_warps(n, 1, 0.5) == 2      # the other walks keep theirs
+        assert engine.get_gravity_warps(n, 0, 0.5) == 2
+        assert engine.get_gravity_warps(n, 0, 0.7) == 2
+        kept = engine.get_tuning(n)
+        assert kept["gravityWarps"] == 2 and kept["neighborWarps"] == t["neighborWarps"]
+    finally:
+        engine.set_far_field(0)
+        engine.set_tuning(n, 4, 4)
