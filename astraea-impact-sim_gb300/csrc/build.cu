@@ -95,9 +95,10 @@ __global__ void __launch_bounds__(256) permuteLeavesKarrasKernel(AstraeaParticle
         const float h0I = fmaxf(__ldg(&p.h0[s]), 1.0e-6f);
         const float Href = 2.0f * hRaw;     // engine leaf nodeMaxH (sph_gravity.cu:446)
         const float Hs = 2.0f * fmaxf(1.09f * hI, 0.351f * h0I);
-        w.leaf[i].a = make_float4(x, y, z, m);
-        w.leafAux[i] = make_float4(Hs, 0.8f * h0I, Href, 0.0f);
-        w.leaf[i].b = make_float4(__ldg(&p.velX[s]), __ldg(&p.velY[s]), __ldg(&p.velZ[s]), __ldg(&p.rho[s]));
+        w.leaf[i].a = make_float4(x, y, z, Hs);
+        w.leafAux[i] = make_float4(Hs, 0.8f * h0I, Href, m);
+        w.leaf[i].b = make_float4(__ldg(&p.velX[s]), __ldg(&p.velY[s]), __ldg(&p.velZ[s]),
+                                  __fdividef(m, fmaxf(__ldg(&p.rho[s]), 1.0e-9f)));
         const uint32_t leaf = (n - 1u) + i;
         if (bvh.aabbMinX != nullptr) {
             bvh.aabbMinX[leaf] = x; bvh.aabbMinY[leaf] = y; bvh.aabbMinZ[leaf] = z;
@@ -163,14 +164,16 @@ __global__ void __launch_bounds__(256) refreshLeavesKernel(AstraeaParticles p, W
     if (i >= n) return;
     const float hI = fmaxf(__ldg(&p.h[i]), 1.0e-6f);
     const float h0I = fmaxf(__ldg(&p.h0[i]), 1.0e-6f);
-    w.leaf[i].a = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), __ldg(&p.mass[i]));
-    w.leafAux[i] = make_float4(2.0f * fmaxf(1.09f * hI, 0.351f * h0I), 0.8f * h0I, 2.0f * __ldg(&p.h[i]), 0.0f);
+    const float m = __ldg(&p.mass[i]);
+    const float Hs = 2.0f * fmaxf(1.09f * hI, 0.351f * h0I);
+    w.leaf[i].a = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), Hs);
+    w.leafAux[i] = make_float4(Hs, 0.8f * h0I, 2.0f * __ldg(&p.h[i]), m);
     const float H = 2.0f * hI;                                      // the drift's 2 max(h, 1e-6)
     w.drift[i].a = make_float4(__ldg(&p.posX[i]), __ldg(&p.posY[i]), __ldg(&p.posZ[i]), H);
     w.driftAux[i] = make_float2(__ldg(&p.mass[i]), wendlandNorm(H));
     if (withVelRho) {
         const float4 vr = make_float4(__ldg(&p.velX[i]), __ldg(&p.velY[i]), __ldg(&p.velZ[i]), __ldg(&p.rho[i]));
-        w.leaf[i].b = vr;
+        w.leaf[i].b = make_float4(vr.x, vr.y, vr.z, __fdividef(m, fmaxf(vr.w, 1.0e-9f)));
         w.drift[i].b = vr;
     }
 }
@@ -408,8 +411,9 @@ __global__ void __launch_bounds__(kRefitBlock) refitBlockKernel(AstraeaRadixBvh 
 #pragma unroll
     for (int k = 0; k < kW; ++k) v[k] = 0;
     if (valid) {
-        const float4 pm = __ldg(&w.leaf[i].a);
+        const float4 pa = __ldg(&w.leaf[i].a);
         const float4 ax = __ldg(&w.leafAux[i]);
+        const float4 pm = make_float4(pa.x, pa.y, pa.z, ax.w);
         e = Ext8{pm.x, pm.y, pm.z, pm.x, pm.y, pm.z, ax.z, ax.x};
         leafTerms<kMoments>(pm, S, v);
     }

@@ -4,8 +4,9 @@
 // the reference kernel they restate (engine/sph_gravity.cu, engine/eos.cu of
 // Ananasjik/astraea-impact-sim).  Data layout (HBM, per particle / per node):
 //
-//   leaf    [N]   32-byte record {x, y, z, m}, {vx, vy, vz, rho}   sorted positions, mass, velocity, density
-//   leafAux [N]   float4 {Hs, eps, 2h, 0}        Hs = search radius (below)
+//   leaf    [N]   32-byte record {x, y, z, Hs}, {vx, vy, vz, m / max(rho, 1e-9)}   sorted positions,
+//                 search radius, velocity, volume (rounded as pass 1 rounds it per pair)
+//   leafAux [N]   float4 {Hs, eps, 2h, m}        Hs = search radius (below)
 //   drift   [N]   32-byte record {x, y, z, H}, {vx, vy, vz, rho}   the next drift's neighbour record
 //   rec2    [6N]  float4 x6 per particle          pass-2 neighbour record
 //   node    [4(N-1)] float4 x4 per internal node:
@@ -528,7 +529,7 @@ struct __align__(32) Rec32 {
 struct Work {
     uint32_t capacity;
     uint32_t maxNbr;
-    Rec32* leaf;           // sorted order: a {x, y, z, m}, b {vx, vy, vz, rho} (permutation / leaf refresh)
+    Rec32* leaf;           // sorted order: a {x, y, z, Hs}, b {vx, vy, vz, m / max(rho, 1e-9)} (permutation / leaf refresh)
     float4* leafAux;
     float4* rec2;          // kRec2Width float4 per particle: the pass-2 record
     float4* node;          // 4 x float4 per internal node

@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(kLabelWarps * 32) labelKernel(Work w, uint32_t
     const double cx = grp.x, cy = grp.y, cz = grp.z;
     double a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (uint32_t j = first + static_cast<uint32_t>(lane); j <= last && j < n; j += 32u) {
-        const float4 pm = __ldg(&w.leaf[j].a);
+        const float4 pa = __ldg(&w.leaf[j].a);
+        const float4 pm = make_float4(pa.x, pa.y, pa.z, __ldg(&w.leafAux[j]).w);
         const double dx = cx - pm.x, dy = cy - pm.y, dz = cz - pm.z;
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (!(r2 > 0.0)) continue;
@@ -434,8 +435,10 @@ __global__ void __launch_bounds__(kGateThreads) gateSumKernel(Work w, uint32_t n
         for (int r = 0; r < kGateRun; ++r) {
             const uint32_t j = j0 + static_cast<uint32_t>(r) * kGateThreads;
             if (j >= n || j == t) continue;
-            const float4 pm = __ldg(&w.leaf[j].a);
-            const double e = hei + 0.5 * static_cast<double>(__ldg(&w.leafAux[j]).y);
+            const float4 pa = __ldg(&w.leaf[j].a);
+            const float4 aux = __ldg(&w.leafAux[j]);
+            const float4 pm = make_float4(pa.x, pa.y, pa.z, aux.w);
+            const double e = hei + 0.5 * static_cast<double>(aux.y);
             const double dx = xi - pm.x, dy = yi - pm.y, dz = zi - pm.z;
             const double ir = rsqrt(dx * dx + dy * dy + dz * dz + e * e);
             const double f = -static_cast<double>(kG) * pm.w * ir * ir * ir;
@@ -447,8 +450,10 @@ __global__ void __launch_bounds__(kGateThreads) gateSumKernel(Work w, uint32_t n
         for (int r = 0; r < kGateRun; ++r) {
             const uint32_t j = j0 + static_cast<uint32_t>(r) * kGateThreads;
             if (j >= n || j == t) continue;
-            const float4 pm = __ldg(&w.leaf[j].a);
-            const float e = 0.5f * (ei + __ldg(&w.leafAux[j]).y);
+            const float4 pa = __ldg(&w.leaf[j].a);
+            const float4 aux = __ldg(&w.leafAux[j]);
+            const float4 pm = make_float4(pa.x, pa.y, pa.z, aux.w);
+            const float e = 0.5f * (ei + aux.y);
             const float dx = me.x - pm.x, dy = me.y - pm.y, dz = me.z - pm.z;
             const float ir = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e * e))));
             const float f = -kG * pm.w * ir * ir * ir;

@@ -279,7 +279,9 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
         float epsI = 0.8e-6f;
         if (active) {
             me = __ldg(&w.leaf[i].a);
-            epsI = __ldg(&w.leafAux[i]).y;
+            const float4 aux = __ldg(&w.leafAux[i]);
+            epsI = aux.y;
+            me.w = aux.w;                                // the mass
         }
         const float xi = me.x, yi = me.y, zi = me.z;
         const float epsI2 = epsI * epsI + 1.0e-20f;
@@ -588,8 +590,10 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
             unsigned selfBit = 0u;
             if (isLeaf) {
                 const int j = ~c;
-                const float4 pm = __ldg(&w.leaf[j].a);
-                const float ej = __ldg(&w.leafAux[j]).y;
+                const float4 pa = __ldg(&w.leaf[j].a);
+                const float4 aux = __ldg(&w.leafAux[j]);
+                const float4 pm = make_float4(pa.x, pa.y, pa.z, aux.w);
+                const float ej = aux.y;
                 const int slot = (pHead + pCount + __popc(leafMask & laneMaskLt())) & 63;
                 putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);
                 S.peps[slot] = 0.5f * ej;
@@ -623,9 +627,10 @@ __global__ void __launch_bounds__(kWarps * 32) gravityKernel(AstraeaParticles p,
                     unsigned sb = 0u;
                     if (has) {
                         const float4 pm = __ldg(&w.leaf[j].a);
+                        const float4 aux = __ldg(&w.leafAux[j]);
                         const int slot = (pHead + pCount + __popc(hm & laneMaskLt())) & 63;
-                        putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * pm.w);
-                        S.peps[slot] = 0.5f * __ldg(&w.leafAux[j]).y;
+                        putEntry(S.plist, slot, pm.x, pm.y, pm.z, -kGPsuF * aux.w);
+                        S.peps[slot] = 0.5f * aux.y;
                         const uint32_t rel = j - base;
                         if (rel < 32u) sb = 1u << rel;
                     }

@@ -10,8 +10,8 @@
 //   * pass 1, pass 2 and the drift run one thread per particle over its own
 //     list, re-applying the engine's exact FP32 range test, so every lane
 //     works on its own pairs;
-//   * neighbour data is read from packed records (pass 1: position + mass
-//     and velocity + density in one 32-byte record; drift: position + H and
+//   * neighbour data is read from packed records (pass 1: position + Hs
+//     and velocity + volume m/rho in one 32-byte record; drift: position + H and
 //     velocity + density; pass 2: a 96-byte record written by the EOS
 //     kernel, read in three 32-byte pieces), one 256-bit load per piece
 //     instead of one gather per field.
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
         float Hs = 0.0f;
         if (active) {
             me = __ldg(&w.leaf[i].a);
-            Hs = __ldg(&w.leafAux[i]).x;
+            Hs = me.w;
         }
         const float gminx = warpMinF(active ? me.x : 3.0e38f), gmaxx = warpMaxF(active ? me.x : -3.0e38f);
         const float gminy = warpMinF(active ? me.y : 3.0e38f), gmaxy = warpMaxF(active ? me.y : -3.0e38f);
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
             bool keep = false;
             if (isLeaf) {
                 pm = __ldg(&w.leaf[~c].a);
-                hsj = __ldg(&w.leafAux[~c]).x;
+                hsj = pm.w;
                 const float dx = fmaxf(0.0f, fmaxf(gminx - pm.x, pm.x - gmaxx));
                 const float dy = fmaxf(0.0f, fmaxf(gminy - pm.y, pm.y - gmaxy));
                 const float dz = fmaxf(0.0f, fmaxf(gminz - pm.z, pm.z - gmaxz));
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kWarps * 32) buildNeighborsKernel(Work w, uint
                 float hj = 0.0f;
                 if (j <= last) {
                     pj = __ldg(&w.leaf[j].a);
-                    hj = __ldg(&w.leafAux[j]).x;
+                    hj = pj.w;
                     const float dx = fmaxf(0.0f, fmaxf(gminx - pj.x, pj.x - gmaxx));
                     const float dy = fmaxf(0.0f, fmaxf(gminy - pj.y, pj.y - gmaxy));
                     const float dz = fmaxf(0.0f, fmaxf(gminz - pj.z, pj.z - gmaxz));
@@ -334,7 +334,7 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
     }
     atomicAdd(&w.status->counters[kCntFallbackWalks], 1ull);
     const float4 me = __ldg(&w.leaf[i].a);
-    const float Hs = __ldg(&w.leafAux[i]).x;
+    const float Hs = me.w;
     int stack[kTreeStack];
     int sp = 0;
     const float4 rootR1 = __ldg(&w.node[1]);
@@ -352,7 +352,7 @@ __device__ __forceinline__ void forEachCandidate(const Work& w, uint32_t i, F&& 
             const uint32_t j = static_cast<uint32_t>(~c2);
             if (j == i) continue;
             const float4 q = __ldg(&w.leaf[j].a);
-            const float R = fmaxf(Hs, __ldg(&w.leafAux[j]).x);
+            const float R = fmaxf(Hs, q.w);
             if (len2Engine(__fsub_rn(me.x, q.x), __fsub_rn(me.y, q.y), __fsub_rn(me.z, q.z)) < __fmul_rn(R, R)) f(j);
             continue;
         }
@@ -428,10 +428,10 @@ __global__ void __launch_bounds__(128, 6) pass1Kernel(AstraeaParticles p, Work w
     if (i >= n) return;
     const F8 rec = ldg256(&w.leaf[i].a);
     const float4 me = rec.a, vr = rec.b;
-    const float mi = me.w;
+    const float mi = __ldg(&p.mass[i]);
     const float hi = fmaxf(__ldg(&p.h[i]), 1.0e-6f);
     const float h0i = fmaxf(__ldg(&p.h0[i]), 1.0e-6f);
-    const float rhoI = fmaxf(vr.w, 1.0e-9f);
+    const float rhoI = fmaxf(__ldg(&p.rho[i]), 1.0e-9f);
     const float Hi = 2.0f * hi;
     const float Hi2 = __fmul_rn(Hi, Hi);
     const float w0 = 21.0f / (2.0f * kPiF * Hi * Hi * Hi);
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(128, 6) pass1Kernel(AstraeaParticles p, Work w
     float nsX = 0.f, nsY = 0.f, nsZ = 0.f;
     float gXX = 0.f, gXY = 0.f, gXZ = 0.f, gYX = 0.f, gYY = 0.f, gYZ = 0.f, gZX = 0.f, gZY = 0.f, gZZ = 0.f;
     if (n >= 2u) {
-        // one 32-byte record per candidate: {x, y, z, m}, {vx, vy, vz, rho}
+        // one 32-byte record per candidate: {x, y, z, Hs}, {vx, vy, vz, m / max(rho, 1e-9)}
         forEachCandidatePrefetched(w, i, [&](uint32_t j) { return ldg256(&w.leaf[j].a); }, [&](uint32_t j, const F8& rj) {
             const float4 q = rj.a;
             const float dx = __fsub_rn(me.x, q.x), dy = __fsub_rn(me.y, q.y), dz = __fsub_rn(me.z, q.z);
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(128, 6) pass1Kernel(AstraeaParticles p, Work w
             ++ngb;
             const float4 vj = rj.b;
             const float r = sqrtf(r2);
-            const float volJ = __fdividef(q.w, fmaxf(vj.w, 1.0e-9f));
+            const float volJ = vj.w;
             const float wij = wendlandC2I(r, Hi, invHi, w0);
             shep += volJ * wij;
             nsX -= volJ * dx * wij;
